@@ -1,0 +1,264 @@
+/*
+ * fdtd_gb300.h -- C ABI of the GB300 (sm_103a) FDTD time-step engine.
+ *
+ * The engine replaces the body of the reference's time loop
+ * (FDTDsimulations/3D/air-AuAntennasSiO2-Si/program.f90:382-607,
+ *  FDTDsimulations/2D/air-nanoAntennas_Si02-Sisubstrate/program.f90:320-471,
+ *  FDTDsimulations/1D/TFSF-air_SLG_SiO2_Sidisp/program.f90:217-308):
+ * the Yee curls (updateD/updateH), the material D->E updates
+ * (ConstantDielectric, Gold Drude+2CP ADE, graphene sheet), the split-field
+ * PML (pmly%updateE / pmly%updateH), the halo exchanges (interchange_E/H,
+ * which become in-memory neighbours of one domain), the soft source and the
+ * running DFT monitors.
+ *
+ * Conventions
+ *  - Every function returns an int status: FDTD_OK (0) or an FDTD_E* code.
+ *    fdtd_last_error() copies a message describing the last failure of the
+ *    calling thread.
+ *  - Device memory belongs to the job handle; the caller only passes host
+ *    pointers.  Calls are asynchronous on the job's CUDA stream; getters and
+ *    fdtd_sync() wait for it and report deferred device errors.
+ *  - One host thread may use a job at a time; different jobs may be driven
+ *    from different threads.
+ *  - Cell indices are 0-based: reference index i maps to i-1.  Arrays passed
+ *    in or out are x-fastest (Fortran column-major, like the reference's).
+ *  - Time step numbers n are 1-based like the reference's `do n=1,Nt`; the
+ *    field time inside step n is t = (n-1)*dt.
+ *  - There is no CPU fallback: without a usable GB300 the calls that need
+ *    the device return FDTD_ENODEV.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  FDTD_OK = 0,
+  FDTD_EINVAL = 1,  /* bad argument or descriptor                       */
+  FDTD_ENOMEM = 2,  /* device or host allocation failed                 */
+  FDTD_ECUDA = 3,   /* a CUDA call or kernel failed                     */
+  FDTD_ESTATE = 4,  /* call not valid in the job's current state        */
+  FDTD_ERANGE = 5,  /* index or size out of range                       */
+  FDTD_ENODEV = 6   /* no usable sm_103a device                         */
+};
+
+/* ---- grid layouts ------------------------------------------------------ */
+enum {
+  FDTD_LAYOUT_1D = 1,    /* Ex, Hz along y: 1D/.../program.f90:42-45          */
+  FDTD_LAYOUT_2D_TE = 2, /* Ex, Ey, Hz in x-y: 2D/.../program.f90:68         */
+  FDTD_LAYOUT_2D_TM = 3, /* Ez, Hx, Hy in x-y: the 3D equations with d/dz=0 */
+  FDTD_LAYOUT_3D = 4     /* Ex..Hz: 3D/.../program.f90:77                   */
+};
+
+enum { FDTD_F32 = 1, FDTD_F64 = 2 };
+
+/* Field components.  The *_INC codes address the 1D total-field/scattered-
+ * field auxiliary incident line (1D/.../program.f90:45). */
+enum {
+  FDTD_EX = 0, FDTD_EY = 1, FDTD_EZ = 2,
+  FDTD_HX = 3, FDTD_HY = 4, FDTD_HZ = 5,
+  FDTD_EX_INC = 6, FDTD_HZ_INC = 7
+};
+
+typedef struct fdtd_grid_desc {
+  int32_t layout;       /* FDTD_LAYOUT_*                                    */
+  int32_t precision;    /* FDTD_F32 or FDTD_F64 storage and arithmetic      */
+  int32_t n[3];         /* cells along x, y, z (1 for unused axes)          */
+  int32_t periodic[3];  /* 1 = periodic wrap on that axis (PBC_x, PBC_z)    */
+  int32_t main_lo[3];   /* inclusive range of the Yee update (locI*range,   */
+  int32_t main_hi[3];   /*   3D/.../include/mympi_func.f90:137-214)         */
+  double ku;            /* Courant factor of the curls (Ku)                 */
+  double dt;            /* time step [s]                                    */
+  double ds;            /* cell size [m]                                    */
+} fdtd_grid_desc;
+
+/* ---- geometry of materials ------------------------------------------- */
+enum {
+  FDTD_REGION_BOX = 0,     /* axis-aligned box (the reference's xinit..zend) */
+  FDTD_REGION_SPHERES = 1, /* union of spheres (3D) or cylinders (2D)        */
+  FDTD_REGION_MASK = 2     /* explicit per-cell mask                          */
+};
+
+typedef struct fdtd_region {
+  int32_t kind;
+  int32_t lo[3], hi[3];          /* BOX: inclusive cell range              */
+  int32_t count;                 /* SPHERES: number of (cx,cy,cz,r) rows   */
+  const double *centers_radii;   /* SPHERES: cell (i,j,k) is inside when
+                                    (i+.5-cx)^2+(j+.5-cy)^2[+(k+.5-cz)^2]
+                                    <= r^2 (z term absent in 2D)           */
+  const uint8_t *mask;           /* MASK: n[0]*n[1]*n[2] bytes, x fastest  */
+} fdtd_region;
+
+/* Drude + two critical points (2D/gold_mod.f90:25-31, 3D/gold_mod.f90:28-34).
+ * Angular frequencies and dampings in rad/s. */
+typedef struct fdtd_drude2cp {
+  double eps_inf;
+  double omega_d, gamma_d;
+  double amp[2], phi[2], omega[2], gamma[2];
+} fdtd_drude2cp;
+
+/* Graphene sheet: intraband Drude surface conductivity from the Fermi level
+ * and relaxation time, plus a Kerr + Raman-delayed third-order response
+ * (1D/graphene633_mod.f90:26-44, 3D/graphene_mod.f90:202-262).  The sheet is
+ * one cell thick; its in-plane E components get the update. */
+typedef struct fdtd_graphene_desc {
+  double fermi_ev;      /* E_F [eV]                                        */
+  double tau;           /* relaxation time [s]                             */
+  double temperature;   /* [K]                                             */
+  double chi3;          /* third-order susceptibility [m^2/V^2]            */
+  double raman_frac;    /* fraction of chi3 that is Raman-delayed          */
+  double raman_freq;    /* Raman line centre [Hz]                          */
+  double raman_tau;     /* Raman damping time [s]                          */
+  double thickness;     /* physical sheet thickness [m] (surface -> bulk)  */
+  double e_scale;       /* V/m per normalised field unit (for chi3 E^2)    */
+} fdtd_graphene_desc;
+
+/* ---- PML ---------------------------------------------------------------- */
+enum {
+  FDTD_PML_REFERENCE = 1, /* the reference's y-slab split-field PML with its
+                             copy-in/copy-out coupling: 1D/BERpmly_ExHz_mod,
+                             2D/BERpmly_HzExEy_mod, 3D/BERpmly_mod            */
+  FDTD_PML_SPLIT = 2      /* split-field PML on any set of faces; the same
+                             graded profiles applied per axis                 */
+};
+
+typedef struct fdtd_pml_desc {
+  int32_t mode;
+  int32_t npml[3][2];  /* thickness per axis, [low, high] side.  REFERENCE:
+                          npml[1][*] = slab thickness (npmly); npml[0][0] and
+                          npml[2][0] = corner profile widths (npmlx, npmlz)  */
+  double eps_lo;       /* relative permittivity of the low-y (REFERENCE) or
+                          of every (SPLIT) PML medium (eplow/ep0)           */
+  double eps_hi;       /* relative permittivity of the high-y slab          */
+  double sigma_max;    /* sigmam [S/m] (3D/.../program.f90:102)            */
+  double order;        /* grading order (3 in the reference)               */
+} fdtd_pml_desc;
+
+/* ---- sources, monitors, probes ------------------------------------------ */
+/* Soft source added to D over a box of cells after the curl update
+ * (3D/.../program.f90:396-406):  g(t) = exp(-0.5((t-t0)/st)^2) sin(w0 t). */
+typedef struct fdtd_source_desc {
+  int32_t component;    /* FDTD_EX..FDTD_EZ, or FDTD_EX_INC (1D TFSF line) */
+  int32_t lo[3], hi[3]; /* inclusive cell box                              */
+  double amp;           /* scale (n_air in 3D/.../program.f90:403)         */
+  double t0, st, w0;
+} fdtd_source_desc;
+
+/* Running DFT over a box of cells (3D/.../program.f90:441-540):
+ *   re += cos(omega_m t) F dt,  im += sin(omega_m t) F dt,  t = (n-1) dt
+ * sampled after the H update of step n, for n_first <= n <= n_last. */
+typedef struct fdtd_monitor_desc {
+  int32_t lo[3], hi[3];  /* inclusive cell box (plane, line or point)      */
+  int32_t comp_mask;     /* bit c = transform component c (FDTD_EX..)      */
+  int32_t n_first, n_last;
+  int32_t nfreq;
+  const double *omega;   /* nfreq angular frequencies (arg(m))             */
+} fdtd_monitor_desc;
+
+/* Per-step samples at one cell (the r*infld/rfld/tfld time series,
+ * 2D/.../program.f90:376-419). */
+typedef struct fdtd_probe_desc {
+  int32_t cell[3];
+  int32_t comp_mask;
+  int32_t n_first, n_last;
+} fdtd_probe_desc;
+
+/* 1D total-field/scattered-field boundary (1D/.../program.f90:221-262). */
+typedef struct fdtd_tfsf1d_desc {
+  int32_t boundary;     /* TFSF_bd, 0-based                                */
+  double eps_lo, eps_hi;/* relative permittivities of the incident line's PML */
+} fdtd_tfsf1d_desc;
+
+typedef struct fdtd_job fdtd_job;
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* Replaces the program's static field arrays and my_mpi_init/set_index
+ * (3D/.../program.f90:77, include/mympi_func.f90:86-214). */
+int fdtd_create(const fdtd_grid_desc *grid, fdtd_job **out);
+int fdtd_destroy(fdtd_job *job);
+int fdtd_last_error(char *buf, size_t len);
+/* Number of sm_103a devices the library can use (0 without a GPU). */
+int fdtd_device_count(int32_t *count);
+
+/* ---- set-up (host side, before fdtd_commit) ------------------------------ */
+/* mat%initialize_material (2D/simpledielectric_mod.f90:150-187,
+ * 3D/simpledielectric_mod.f90:52-103).  Materials paint cells in call order;
+ * a later material overrides an earlier one on shared cells, as the
+ * reference's call order of update_E does (3D/.../program.f90:411-414). */
+int fdtd_add_dielectric(fdtd_job *job, const fdtd_region *region, double eps_r,
+                        int32_t *material_id);
+/* Gold%initialize_material (2D/gold_mod.f90:77-168, 3D/gold_mod.f90:90-195). */
+int fdtd_add_gold(fdtd_job *job, const fdtd_region *region,
+                  const fdtd_drude2cp *params, int32_t *material_id);
+/* Graphene sheet (3D/graphene_mod.f90:59-269, 1D/graphene633_mod.f90:26-105). */
+int fdtd_add_graphene(fdtd_job *job, const fdtd_region *region,
+                      const fdtd_graphene_desc *params, int32_t *material_id);
+/* pmly%initialize (3D/BERpmly_mod.f90:485-508, 2D/BERpmly_HzExEy_mod.f90:229-247,
+ * 1D/BERpmly_ExHz_mod.f90:163-175). */
+int fdtd_add_pml(fdtd_job *job, const fdtd_pml_desc *pml);
+int fdtd_add_tfsf_1d(fdtd_job *job, const fdtd_tfsf1d_desc *tfsf);
+int fdtd_add_source(fdtd_job *job, const fdtd_source_desc *src, int32_t *id);
+int fdtd_add_monitor(fdtd_job *job, const fdtd_monitor_desc *mon, int32_t *id);
+int fdtd_add_probe(fdtd_job *job, const fdtd_probe_desc *probe, int32_t *id);
+/* Builds the per-cell material map and coefficient tables and allocates and
+ * uploads all device state.  No set-up call is accepted afterwards. */
+int fdtd_commit(fdtd_job *job);
+
+/* ---- the time loop ------------------------------------------------------ */
+/* Whole steps n_first .. n_first+n_steps-1, fused (the do-n loop body). */
+int fdtd_step(fdtd_job *job, int32_t n_first, int32_t n_steps);
+
+/* The loop body one procedure group at a time, for a host loop written like
+ * the reference's:
+ *   fdtd_update_DE   = updateD + source + every mat%update_E
+ *                      (3D/.../program.f90:389-414)
+ *   fdtd_pml_update_E = pmly%updateE   (3D/.../program.f90:419)
+ *   fdtd_interchange  = interchange_E / interchange_H (:423, :437); the
+ *                      halo is an in-memory neighbour, so this only checks
+ *                      the call order
+ *   fdtd_update_H    = updateH         (3D/.../program.f90:427-429)
+ *   fdtd_pml_update_H = pmly%updateH   (3D/.../program.f90:433)
+ *   fdtd_sample      = the DFT accumulation and per-step writes (:441-540)
+ */
+int fdtd_update_DE(fdtd_job *job, int32_t n);
+int fdtd_pml_update_E(fdtd_job *job, int32_t n);
+int fdtd_interchange(fdtd_job *job, int32_t which /* 0 = E, 1 = H */);
+int fdtd_update_H(fdtd_job *job, int32_t n);
+int fdtd_pml_update_H(fdtd_job *job, int32_t n);
+int fdtd_sample(fdtd_job *job, int32_t n);
+
+/* ---- results ------------------------------------------------------------- */
+int fdtd_sync(fdtd_job *job);
+/* n[0]*n[1]*n[2] values of one component, x fastest. */
+int fdtd_get_field(fdtd_job *job, int32_t comp, double *host);
+int fdtd_set_field(fdtd_job *job, int32_t comp, const double *host);
+/* DFT sums: for each transformed component (ascending component code), for
+ * each frequency, for each cell of the box (x fastest): re[], im[]. */
+int fdtd_get_monitor(fdtd_job *job, int32_t id, double *re, double *im);
+/* Samples of steps n_first..min(n_last, last stepped n): for each step the
+ * selected components in ascending code order.  *count = steps returned. */
+int fdtd_get_probe(fdtd_job *job, int32_t id, double *host, int32_t *count);
+/* Bytes of device memory the job holds (HBM admission). */
+int fdtd_device_bytes(const fdtd_job *job, uint64_t *bytes);
+
+/* ---- measurement --------------------------------------------------------- */
+/* When enabled, every launch of the job's kernels is bracketed by CUDA events
+ * on the job's stream; fdtd_kernel_time returns the number of launches and
+ * the summed device time of kernel class `kind` since the last reset. */
+enum { FDTD_KERNEL_E = 0, FDTD_KERNEL_H = 1, FDTD_KERNEL_DFT = 2, FDTD_KERNEL_LINE1D = 3,
+       FDTD_KERNEL_PML = 4, FDTD_KERNEL_COUNT = 5 };
+int fdtd_profile(fdtd_job *job, int32_t enable);
+int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms);
+/* Launches of this library's kernels since the job was created. */
+int fdtd_launch_count(const fdtd_job *job, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDTD_GB300_H */
