@@ -1,0 +1,1303 @@
+// fdtd_api.cu -- the C ABI of include/fdtd_gb300.h: job set-up, device
+// state, and the launch sequence of the time loop.
+//
+// The host side does what the reference does once before its time loop
+// (material ranges, PML profiles, gold coefficients: all in FP64, with the
+// reference's formulas and operation order) and then only launches kernels.
+// There is no CPU compute path: without an sm_103 device every call that
+// needs one fails with FDTD_ENODEV.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fdtd_gb300.h"
+#include "fdtd_internal.h"
+
+using namespace fdtd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_err(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return set_err(FDTD_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));  \
+  } while (0)
+
+// Mm/constants_mod.f90:3-7
+struct Consts {
+  double pi, ep0, mu0, c0, z0;
+  Consts() {
+    pi = 4.0 * std::atan(1.0);
+    ep0 = 8.85418781762039e-12;
+    mu0 = pi * 4e-7;
+    c0 = 1.0 / std::sqrt(ep0 * mu0);
+    z0 = std::sqrt(mu0 / ep0);
+  }
+};
+const Consts K;
+
+struct MatRec {
+  int kind;  // MK_*
+  double eps;
+  fdtd_drude2cp gold;
+  fdtd_graphene_desc gr;
+  fdtd_region region;
+  std::vector<double> centers;
+  std::vector<uint8_t> mask;
+};
+
+struct MonRec {
+  fdtd_monitor_desc d;
+  std::vector<double> omega;
+  int ncomp;
+  int comps[6];
+  long long ncell;
+};
+
+struct ProbeRec {
+  fdtd_probe_desc d;
+  int ncomp;
+  int comps[8];
+  double *buf = nullptr;
+  int cap = 0;
+};
+
+int comp_list(int mask, int *out, int maxn) {
+  int n = 0;
+  for (int c = 0; c < 8; ++c)
+    if (mask & (1 << c)) {
+      if (n >= maxn) return -1;
+      out[n++] = c;
+    }
+  return n;
+}
+
+}  // namespace
+
+struct fdtd_job {
+  fdtd_grid_desc g{};
+  int dim = 0;
+  int nx = 1, ny = 1, nz = 1;
+  long long ncell = 0;
+  size_t esz = 8;
+  std::vector<MatRec> mats;
+  bool has_pml = false;
+  fdtd_pml_desc pml{};
+  bool has_tfsf = false;
+  fdtd_tfsf1d_desc tfsf{};
+  std::vector<fdtd_source_desc> srcs;
+  std::vector<MonRec> mons;
+  std::vector<ProbeRec> probes;
+  bool committed = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  uint64_t dev_bytes = 0;
+  // device state
+  void *F[8] = {};  // ex ey ez hx hy hz ex_inc hz_inc
+  uint8_t *d_mat = nullptr;
+  void *d_mc = nullptr, *d_ac = nullptr;
+  int nade = 0, ade_stride = 0;
+  int *d_ade_cell = nullptr;
+  uint8_t *d_ade_mat = nullptr;
+  void *d_ade_state = nullptr;
+  int slo[3] = {0, 0, 0}, shi[3] = {0, 0, 0};
+  void *d_cf[4][3] = {};   // f1 f2 g1 g2 per axis (split PML)
+  void *d_sp[6] = {};
+  int slab_rows = 0, slab_on[2] = {0, 0}, slab_j0[2] = {0, 0};
+  void *d_slab[2][12] = {};
+  void *d_sc[2][12] = {};  // sf1x sf2x sg1x sg2x sf1y sf2y sg1y sg2y sf1z sf2z sg1z sg2z
+  // 1D line slabs [line][side]
+  void *d_lex[2][2] = {}, *d_lhz[2][2] = {}, *d_lc[2][2][4] = {};
+  int ja = -1, jb = -1;
+  // sampling
+  std::vector<Monitor> mon_dev;
+  long long stage_row = 0;
+  void *d_stage = nullptr;
+  long long stage_cap_rows = 0;
+  int stage_fill = 0, stage_n0 = 1;
+  double *d_omega = nullptr, *d_acc_re = nullptr, *d_acc_im = nullptr;
+  long long acc_total = 0;
+  bool gather_fused = true;
+  int dft_blocks = 0;
+  // 1D per-launch source values
+  double *d_srcval = nullptr;
+  long long srcval_cap = 0;
+  int last_n = 0;
+  // profiling
+  bool prof = false;
+  struct EvPair { cudaEvent_t a, b; int kind; };
+  std::vector<EvPair> pending;
+  std::vector<cudaEvent_t> ev_pool;
+  long long kcount[FDTD_KERNEL_COUNT] = {};
+  double kms[FDTD_KERNEL_COUNT] = {};
+  long long launches = 0;
+};
+
+namespace {
+
+int alloc_dev(fdtd_job *J, void **p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  J->allocs.push_back(*p);
+  J->dev_bytes += bytes;
+  e = cudaMemsetAsync(*p, 0, bytes, J->stream);
+  if (e != cudaSuccess) return set_err(FDTD_ECUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+  return FDTD_OK;
+}
+
+template <typename T>
+int upload_vec(fdtd_job *J, void **dst, const std::vector<double> &v) {
+  std::vector<T> t(v.begin(), v.end());
+  int rc = alloc_dev(J, dst, t.size() * sizeof(T));
+  if (rc) return rc;
+  CK(cudaMemcpy(*dst, t.data(), t.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return FDTD_OK;
+}
+
+int check_device(int *dev) {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0)
+    return set_err(FDTD_ENODEV, "no CUDA device (%s); this library has no CPU path",
+                   e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+  int d = 0;
+  CK(cudaGetDevice(&d));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, d));
+  if (prop.major != 10 || prop.minor != 3)
+    return set_err(FDTD_ENODEV, "device %d is sm_%d%d; the kernels are built for sm_103a only", d, prop.major,
+                   prop.minor);
+  *dev = d;
+  return FDTD_OK;
+}
+
+bool inside(const fdtd_job *J, const MatRec &m, int i, int j, int k) {
+  const fdtd_region &r = m.region;
+  switch (r.kind) {
+    case FDTD_REGION_BOX:
+      return i >= r.lo[0] && i <= r.hi[0] && j >= r.lo[1] && j <= r.hi[1] && k >= r.lo[2] && k <= r.hi[2];
+    case FDTD_REGION_SPHERES:
+      for (int q = 0; q < r.count; ++q) {
+        const double *c = m.centers.data() + 4 * q;
+        double dx = i + 0.5 - c[0], dy = j + 0.5 - c[1];
+        double d2 = dx * dx + dy * dy;
+        if (J->dim == 3) {
+          double dz = k + 0.5 - c[2];
+          d2 += dz * dz;
+        }
+        if (d2 <= c[3] * c[3]) return true;
+      }
+      return false;
+    case FDTD_REGION_MASK:
+      return m.mask[(size_t)i + (size_t)J->nx * ((size_t)j + (size_t)J->ny * k)] != 0;
+  }
+  return false;
+}
+
+// bounding box of a region (to paint without a full-grid scan)
+void region_bounds(const fdtd_job *J, const MatRec &m, int lo[3], int hi[3]) {
+  const int n[3] = {J->nx, J->ny, J->nz};
+  for (int a = 0; a < 3; ++a) { lo[a] = 0; hi[a] = n[a] - 1; }
+  if (m.region.kind == FDTD_REGION_BOX) {
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::max(0, m.region.lo[a]);
+      hi[a] = std::min(n[a] - 1, m.region.hi[a]);
+    }
+  } else if (m.region.kind == FDTD_REGION_SPHERES) {
+    for (int a = 0; a < 3; ++a) { lo[a] = n[a]; hi[a] = -1; }
+    for (int q = 0; q < m.region.count; ++q) {
+      const double *c = m.centers.data() + 4 * q;
+      for (int a = 0; a < 3; ++a) {
+        if (a == 2 && J->dim < 3) { lo[2] = 0; hi[2] = n[2] - 1; continue; }
+        lo[a] = std::min(lo[a], std::max(0, (int)std::floor(c[a] - c[3] - 1.0)));
+        hi[a] = std::max(hi[a], std::min(n[a] - 1, (int)std::ceil(c[a] + c[3] + 1.0)));
+      }
+    }
+  }
+}
+
+// ---- PML coefficient tables (FP64, the reference's formulas) -----------
+struct Prof {
+  std::vector<double> f1, f2, g1, g2;
+  void init(int n, double f2d, double g2d) {
+    f1.assign(n, 1.0); f2.assign(n, f2d); g1.assign(n, 1.0); g2.assign(n, g2d);
+  }
+};
+
+// low-side profile over 1-based positions 1..npml stored at index base+pos-1
+// (init_varx1, M3/BERpmly_mod.f90:761-786, and the y low profile :674-692)
+void prof_low(Prof &P, int base, int npml, double ep, double sigmam, double order, double dt, double ds) {
+  const double z0 = std::sqrt(K.mu0 / K.ep0);
+  for (int i = 1; i <= npml; ++i) {
+    const int x = base + i - 1;
+    double sE = ep * sigmam * std::pow(((double)(npml - i) + 0.5) / (double)npml, order);
+    double aE = sE * dt / ep;
+    P.f1[x] = std::exp(-aE);
+    P.f2[x] = (1.0 - P.f1[x]) / (z0 * sE * ds);
+    if (i < npml) {
+      double sH = K.mu0 * sigmam * std::pow(((double)(npml - i)) / (double)npml, order);
+      double aH = sH * dt / K.mu0;
+      P.g1[x] = std::exp(-aH);
+      P.g2[x] = z0 * (1.0 - P.g1[x]) / (sH * ds);
+    }
+  }
+}
+
+// high-side profile: first position stored at index base (ii counts down from npml)
+// (init_varx2, M3/BERpmly_mod.f90:788-815, and the y high profile :695-714)
+void prof_high(Prof &P, int base, int npml, double ep, double sigmam, double order, double dt, double ds) {
+  const double z0 = std::sqrt(K.mu0 / K.ep0);
+  int ii = npml;
+  for (int q = 0; q < npml; ++q) {
+    const int x = base + q;
+    if (ii < npml) {
+      double sE = ep * sigmam * std::pow(((double)(npml - ii)) / (double)npml, order);
+      double aE = sE * dt / ep;
+      P.f1[x] = std::exp(-aE);
+      P.f2[x] = (1.0 - P.f1[x]) / (z0 * sE * ds);
+    }
+    double sH = K.mu0 * sigmam * std::pow(((double)(npml - ii) + 0.5) / (double)npml, order);
+    double aH = sH * dt / K.mu0;
+    P.g1[x] = std::exp(-aH);
+    P.g2[x] = z0 * (1.0 - P.g1[x]) / (sH * ds);
+    ii = ii - 1;
+  }
+}
+
+template <typename T>
+int upload_prof(fdtd_job *J, const Prof &P, void **f1, void **f2, void **g1, void **g2) {
+  int rc;
+  if ((rc = upload_vec<T>(J, f1, P.f1))) return rc;
+  if ((rc = upload_vec<T>(J, f2, P.f2))) return rc;
+  if ((rc = upload_vec<T>(J, g1, P.g1))) return rc;
+  return upload_vec<T>(J, g2, P.g2);
+}
+
+// ---- commit ------------------------------------------------------------
+template <typename T>
+int commit_impl(fdtd_job *J) {
+  int rc;
+  const int nx = J->nx, ny = J->ny, nz = J->nz;
+  const long long N = J->ncell;
+  const bool split = J->has_pml && J->pml.mode == FDTD_PML_SPLIT;
+  const bool ref = J->has_pml && J->pml.mode == FDTD_PML_REFERENCE;
+  // interior box of the split PML; the Yee update and materials run inside it
+  if (split) {
+    const int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+      int lo = J->pml.npml[a][0], hi = J->pml.npml[a][1];
+      if (J->g.periodic[a] || n[a] == 1) lo = hi = 0;
+      J->slo[a] = lo;
+      J->shi[a] = n[a] - 1 - hi;
+      J->g.main_lo[a] = J->slo[a];
+      J->g.main_hi[a] = J->shi[a];
+    }
+  } else {
+    for (int a = 0; a < 3; ++a) { J->slo[a] = 0; J->shi[a] = (a == 0 ? nx : a == 1 ? ny : nz) - 1; }
+  }
+  auto in_shell = [&](int i, int j, int k) {
+    return split && (i < J->slo[0] || i > J->shi[0] || j < J->slo[1] || j > J->shi[1] || k < J->slo[2] || k > J->shi[2]);
+  };
+  // ---- fields ----
+  const bool has[6] = {
+      J->dim != 3 ? (J->g.layout == FDTD_LAYOUT_2D_TE || J->dim == 1) : true,
+      J->dim == 3 || J->g.layout == FDTD_LAYOUT_2D_TE,
+      J->dim == 3 || J->g.layout == FDTD_LAYOUT_2D_TM,
+      J->dim == 3 || J->g.layout == FDTD_LAYOUT_2D_TM,
+      J->dim == 3 || J->g.layout == FDTD_LAYOUT_2D_TM,
+      J->dim == 3 || J->g.layout == FDTD_LAYOUT_2D_TE || J->dim == 1};
+  for (int c = 0; c < 6; ++c)
+    if (has[c] && (rc = alloc_dev(J, &J->F[c], (size_t)N * sizeof(T)))) return rc;
+  if (J->has_tfsf) {
+    if ((rc = alloc_dev(J, &J->F[6], (size_t)N * sizeof(T)))) return rc;
+    if ((rc = alloc_dev(J, &J->F[7], (size_t)N * sizeof(T)))) return rc;
+  }
+  // ---- materials: paint in call order ----
+  std::vector<uint8_t> mat((size_t)N, 0);
+  for (size_t m = 0; m < J->mats.size(); ++m) {
+    int lo[3], hi[3];
+    region_bounds(J, J->mats[m], lo, hi);
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i)
+          if (inside(J, J->mats[m], i, j, k)) mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = (uint8_t)(m + 1);
+  }
+  std::vector<MatCoef<T>> mc(kMaxMat);
+  std::vector<AdeCoef<T>> ac;
+  for (auto &x : mc) { x.kind = MK_NONE; x.ade = -1; x.ca = T(0); x.cs = T(0); }
+  const double Ku = J->g.ku, dt = J->g.dt;
+  for (size_t m = 0; m < J->mats.size(); ++m) {
+    const MatRec &R = J->mats[m];
+    MatCoef<T> &c = mc[m + 1];
+    c.kind = R.kind;
+    if (R.kind == MK_DIEL) {
+      // gax = 1/constant_ep (M2/simpledielectric_mod.f90:176-186)
+      const double gax = R.eps == 0.0 ? 0.0 : 1.0 / R.eps;
+      c.ca = T(Ku * gax);
+      c.cs = T(gax);
+    } else if (R.kind == MK_GOLD) {
+      // M2/gold_mod.f90:129-168 (setexp :160-168)
+      typedef std::complex<double> cd;
+      const fdtd_drude2cp &p = R.gold;
+      cd gb[2], gc[2];
+      for (int q = 0; q < 2; ++q) {
+        cd expi = std::exp(cd(0.0, -p.phi[q]));
+        gb[q] = std::exp(cd(-p.gamma[q] * dt, p.omega[q] * dt));
+        gc[q] = cd(0.0, dt * 2.0 * p.amp[q] * p.omega[q]) * expi;
+      }
+      cd ga = cd(p.eps_inf, 0.0) - gc[0] - gc[1];
+      cd w = 1.0 / ga;
+      AdeCoef<T> a{};
+      a.kind = MK_GOLD;
+      a.normal = -1;
+      a.ha = T(std::exp(-p.gamma_d * dt));
+      a.hb = T((p.omega_d * p.omega_d) * dt / p.gamma_d);
+      a.gb1r = T(gb[0].real()); a.gb1i = T(gb[0].imag());
+      a.gb2r = T(gb[1].real()); a.gb2i = T(gb[1].imag());
+      a.gc1r = T(gc[0].real()); a.gc1i = T(gc[0].imag());
+      a.gc2r = T(gc[1].real()); a.gc2i = T(gc[1].imag());
+      a.wr = T(w.real()); a.wi = T(w.imag());
+      c.ade = (int)ac.size();
+      c.ca = T(Ku);
+      c.cs = T(1);
+      ac.push_back(a);
+    } else if (R.kind == MK_GRAPHENE) {
+      const fdtd_graphene_desc &p = R.gr;
+      const double hbar = 6.62607015e-34 / (2.0 * K.pi), kb = 1.380649e-23, qe = 1.602176634e-19;
+      const double kT = kb * p.temperature, ef = p.fermi_ev * qe;
+      const double sigma_s0 = (2.0 * qe * qe * kT * p.tau / (K.pi * hbar * hbar)) * std::log(2.0 * std::cosh(ef / (2.0 * kT)));
+      const double sigma0 = sigma_s0 / p.thickness;
+      const double gam = 1.0 / p.tau;
+      const double wNL = 2.0 * K.pi * p.raman_freq, dnuNL = 1.0 / p.raman_tau;
+      const double alfaR = 0.5 * dnuNL, betaR = std::sqrt(wNL * wNL - alfaR * alfaR), omegaR = (wNL * wNL) / betaR;
+      const double chi3n = p.chi3 * p.e_scale * p.e_scale;
+      AdeCoef<T> a{};
+      a.kind = MK_GRAPHENE;
+      int normal = -1;
+      const int n3[3] = {nx, ny, nz};
+      for (int ax = 0; ax < 3; ++ax)
+        if (R.region.lo[ax] == R.region.hi[ax] && n3[ax] > 1) { normal = ax; break; }
+      a.normal = normal;
+      a.ha = T(std::exp(-gam * dt));
+      a.hb = T(sigma0 * dt / K.ep0);
+      a.ga = T(1.0);
+      a.r0 = T(p.raman_frac * chi3n * omegaR * dt * std::exp(-alfaR * dt) * std::sin(betaR * dt));
+      a.r1 = T(2.0 * std::exp(-alfaR * dt) * std::cos(betaR * dt));
+      a.r2 = T(-std::exp(-2.0 * alfaR * dt));
+      a.kerr = T((1.0 - p.raman_frac) * chi3n);
+      c.ade = (int)ac.size();
+      c.ca = T(Ku);
+      c.cs = T(1);
+      ac.push_back(a);
+    }
+  }
+  if ((rc = alloc_dev(J, (void **)&J->d_mat, (size_t)N))) return rc;
+  CK(cudaMemcpy(J->d_mat, mat.data(), (size_t)N, cudaMemcpyHostToDevice));
+  if ((rc = alloc_dev(J, &J->d_mc, sizeof(MatCoef<T>) * kMaxMat))) return rc;
+  CK(cudaMemcpy(J->d_mc, mc.data(), sizeof(MatCoef<T>) * kMaxMat, cudaMemcpyHostToDevice));
+  if ((rc = alloc_dev(J, &J->d_ac, sizeof(AdeCoef<T>) * std::max<size_t>(1, ac.size())))) return rc;
+  if (!ac.empty()) CK(cudaMemcpy(J->d_ac, ac.data(), sizeof(AdeCoef<T>) * ac.size(), cudaMemcpyHostToDevice));
+  // ---- ADE slots (dispersive cells) ----
+  std::vector<int> ade_cell;
+  std::vector<uint8_t> ade_mat;
+  for (long long c = 0; c < N; ++c) {
+    const uint8_t id = mat[(size_t)c];
+    if (!id || (mc[id].kind != MK_GOLD && mc[id].kind != MK_GRAPHENE)) continue;
+    const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((long long)nx * ny));
+    if (in_shell(i, j, k)) continue;
+    if (!(i >= J->g.main_lo[0] && i <= J->g.main_hi[0] && j >= J->g.main_lo[1] && j <= J->g.main_hi[1] &&
+          k >= J->g.main_lo[2] && k <= J->g.main_hi[2]))
+      return set_err(FDTD_EINVAL, "dispersive cell (%d,%d,%d) lies outside the Yee update range", i, j, k);
+    ade_cell.push_back((int)c);
+    ade_mat.push_back(id);
+  }
+  J->nade = (int)ade_cell.size();
+  J->ade_stride = ((J->nade + 31) / 32) * 32;
+  if ((rc = alloc_dev(J, (void **)&J->d_ade_cell, sizeof(int) * std::max(1, J->nade)))) return rc;
+  if ((rc = alloc_dev(J, (void **)&J->d_ade_mat, std::max(1, J->nade)))) return rc;
+  if (J->nade) {
+    CK(cudaMemcpy(J->d_ade_cell, ade_cell.data(), sizeof(int) * J->nade, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(J->d_ade_mat, ade_mat.data(), J->nade, cudaMemcpyHostToDevice));
+  }
+  if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)kAdeFields * 3 * std::max(32, J->ade_stride)))) return rc;
+  // ---- PML ----
+  const double Kpml = dt * K.c0 / J->g.ds;  // dt*c0/ds (M3/BERpmly_mod.f90:506)
+  if (split) {
+    const fdtd_pml_desc &p = J->pml;
+    const double ep = p.eps_lo * K.ep0, epr = ep / K.ep0;
+    const int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+      Prof P;
+      P.init(n[a], Kpml / epr, Kpml);
+      int lo = p.npml[a][0], hi = p.npml[a][1];
+      if (J->g.periodic[a] || n[a] == 1) lo = hi = 0;
+      if (lo > 0) prof_low(P, 0, lo, ep, p.sigma_max, p.order, dt, J->g.ds);
+      if (hi > 0) prof_high(P, n[a] - hi, hi, ep, p.sigma_max, p.order, dt, J->g.ds);
+      if ((rc = upload_prof<T>(J, P, &J->d_cf[0][a], &J->d_cf[1][a], &J->d_cf[2][a], &J->d_cf[3][a]))) return rc;
+    }
+    const int nsp = J->dim == 3 ? 6 : 1;
+    for (int q = 0; q < nsp; ++q)
+      if ((rc = alloc_dev(J, &J->d_sp[q], (size_t)N * sizeof(T)))) return rc;
+    if (J->dim == 2) J->d_sp[3] = J->d_sp[0];  // unused alias keeps pointers valid
+  }
+  if (ref && J->dim >= 2) {
+    const fdtd_pml_desc &p = J->pml;
+    const int rows = p.npml[1][0];
+    J->slab_rows = rows;
+    if (rows > 0) {
+      const double eps_side[2] = {p.eps_lo, p.eps_hi};
+      for (int side = 0; side < 2; ++side) {
+        J->slab_on[side] = 1;
+        J->slab_j0[side] = side == 0 ? 0 : ny - rows;
+        const double ep = eps_side[side] * K.ep0, epr = ep / K.ep0;
+        // x (corner) profile
+        Prof X; X.init(nx, Kpml / epr, Kpml);
+        int nlo = p.npml[0][0], nhi = p.npml[0][1] > 0 ? p.npml[0][1] : p.npml[0][0];
+        if (nlo > 0) {
+          prof_low(X, 0, nlo, ep, p.sigma_max, p.order, dt, J->g.ds);
+          prof_high(X, nx - nhi, nhi, ep, p.sigma_max, p.order, dt, J->g.ds);
+        }
+        Prof Y; Y.init(rows, Kpml / epr, Kpml);
+        if (side == 0) prof_low(Y, 0, rows, ep, p.sigma_max, p.order, dt, J->g.ds);
+        else prof_high(Y, 0, rows, ep, p.sigma_max, p.order, dt, J->g.ds);
+        Prof Z; Z.init(nz, Kpml / epr, Kpml);
+        int zlo = p.npml[2][0], zhi = p.npml[2][1] > 0 ? p.npml[2][1] : p.npml[2][0];
+        if (J->dim == 3 && zlo > 0) {
+          prof_low(Z, 0, zlo, ep, p.sigma_max, p.order, dt, J->g.ds);
+          prof_high(Z, nz - zhi, zhi, ep, p.sigma_max, p.order, dt, J->g.ds);
+        }
+        void **sc = J->d_sc[side];
+        if ((rc = upload_prof<T>(J, X, &sc[0], &sc[1], &sc[2], &sc[3]))) return rc;
+        if ((rc = upload_prof<T>(J, Y, &sc[4], &sc[5], &sc[6], &sc[7]))) return rc;
+        if ((rc = upload_prof<T>(J, Z, &sc[8], &sc[9], &sc[10], &sc[11]))) return rc;
+        const int nf = J->dim == 3 ? 12 : 4;
+        for (int q = 0; q < nf; ++q)
+          if ((rc = alloc_dev(J, &J->d_slab[side][q], (size_t)nx * rows * nz * sizeof(T)))) return rc;
+      }
+    }
+  }
+  if (ref && J->dim == 1) {
+    const fdtd_pml_desc &p = J->pml;
+    const int rows = p.npml[1][0];
+    J->ja = rows - 1;
+    J->jb = ny - rows;
+    if (rows > 0) {
+      for (int line = 0; line < (J->has_tfsf ? 2 : 1); ++line) {
+        const double eps_side[2] = {line ? J->tfsf.eps_lo : p.eps_lo, line ? J->tfsf.eps_hi : p.eps_hi};
+        for (int side = 0; side < 2; ++side) {
+          J->slab_on[side] = 1;
+          const double ep = eps_side[side] * K.ep0, epr = ep / K.ep0;
+          Prof Y; Y.init(rows + 2, Kpml / epr, Kpml);
+          if (side == 0) prof_low(Y, 1, rows, ep, p.sigma_max, p.order, dt, J->g.ds);
+          else prof_high(Y, 1, rows, ep, p.sigma_max, p.order, dt, J->g.ds);
+          void **lc = J->d_lc[line][side];
+          if ((rc = upload_prof<T>(J, Y, &lc[0], &lc[1], &lc[2], &lc[3]))) return rc;
+          if ((rc = alloc_dev(J, &J->d_lex[line][side], (size_t)(rows + 2) * sizeof(T)))) return rc;
+          if ((rc = alloc_dev(J, &J->d_lhz[line][side], (size_t)(rows + 2) * sizeof(T)))) return rc;
+        }
+      }
+    }
+  }
+  // ---- monitors ----
+  long long base = 0, acc = 0;
+  int foff = 0;
+  std::vector<double> omega;
+  bool touches_slab = false;
+  for (auto &M : J->mons) {
+    Monitor m{};
+    for (int a = 0; a < 3; ++a) { m.lo[a] = M.d.lo[a]; m.hi[a] = M.d.hi[a]; }
+    m.ncomp = M.ncomp;
+    for (int u = 0; u < M.ncomp; ++u) m.comps[u] = M.comps[u];
+    m.ncell = (int)M.ncell;
+    m.base = base;
+    m.n_first = M.d.n_first;
+    m.n_last = M.d.n_last;
+    m.nfreq = M.d.nfreq;
+    m.acc = acc;
+    m.freq_off = foff;
+    base += (long long)M.ncomp * M.ncell;
+    acc += (long long)M.ncomp * M.d.nfreq * M.ncell;
+    foff += M.d.nfreq;
+    omega.insert(omega.end(), M.omega.begin(), M.omega.end());
+    J->mon_dev.push_back(m);
+    if (ref && J->dim == 3 && J->slab_rows > 0 &&
+        (m.lo[1] <= J->slab_rows - 1 || m.hi[1] >= ny - J->slab_rows))
+      touches_slab = true;
+  }
+  for (auto &P : J->probes)
+    if (ref && J->dim == 3 && J->slab_rows > 0 && (P.d.cell[1] <= J->slab_rows - 1 || P.d.cell[1] >= ny - J->slab_rows))
+      touches_slab = true;
+  J->gather_fused = !touches_slab;
+  J->stage_row = base;
+  J->acc_total = acc;
+  if (!omega.empty()) {
+    if ((rc = alloc_dev(J, (void **)&J->d_omega, omega.size() * sizeof(double)))) return rc;
+    CK(cudaMemcpy(J->d_omega, omega.data(), omega.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if ((rc = alloc_dev(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
+  if ((rc = alloc_dev(J, (void **)&J->d_acc_im, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
+  J->stage_cap_rows = J->dim == 1 ? 4096 : kStageSteps;
+  if ((rc = alloc_dev(J, &J->d_stage, (size_t)std::max(1LL, base) * J->stage_cap_rows * sizeof(T)))) return rc;
+  int blocks = 0;
+  for (auto &m : J->mon_dev)
+    blocks += ((m.ncomp * m.ncell + 255) / 256) * ((m.nfreq + 7) / 8);
+  J->dft_blocks = blocks;
+  CK(cudaStreamSynchronize(J->stream));
+  J->committed = true;
+  return FDTD_OK;
+}
+
+// ---- stepping ------------------------------------------------------------
+double gauss_t(const fdtd_source_desc &s, double t) {
+  // dexp(-0.5d0*((t-t0)/st)**2)*dsin(w0*t)   (2D/.../program.f90:337)
+  const double a = (t - s.t0) / s.st;
+  return std::exp(-0.5 * (a * a)) * std::sin(s.w0 * t);
+}
+
+template <typename T>
+void fill_common(fdtd_job *J, StepParams<T> &p) {
+  memset(&p, 0, sizeof p);
+  p.layout = J->g.layout;
+  p.nx = J->nx; p.ny = J->ny; p.nz = J->nz;
+  for (int a = 0; a < 3; ++a) {
+    p.per[a] = J->g.periodic[a];
+    p.mlo[a] = J->g.main_lo[a];
+    p.mhi[a] = J->g.main_hi[a];
+    p.slo[a] = J->slo[a];
+    p.shi[a] = J->shi[a];
+  }
+  p.ku = T(J->g.ku);
+  p.ex = (T *)J->F[0]; p.ey = (T *)J->F[1]; p.ez = (T *)J->F[2];
+  p.hx = (T *)J->F[3]; p.hy = (T *)J->F[4]; p.hz = (T *)J->F[5];
+  p.mat = J->d_mat;
+  p.mc = (const MatCoef<T> *)J->d_mc;
+  p.nade = J->nade;
+  p.ade_cell = J->d_ade_cell;
+  p.ade_mat = J->d_ade_mat;
+  p.ac = (const AdeCoef<T> *)J->d_ac;
+  p.ade_state = (T *)J->d_ade_state;
+  p.ade_stride = J->ade_stride;
+  p.pml_mode = J->has_pml ? J->pml.mode : 0;
+  for (int a = 0; a < 3; ++a) {
+    p.cf1[a] = (const T *)J->d_cf[0][a]; p.cf2[a] = (const T *)J->d_cf[1][a];
+    p.cg1[a] = (const T *)J->d_cf[2][a]; p.cg2[a] = (const T *)J->d_cf[3][a];
+  }
+  for (int q = 0; q < 6; ++q) p.sp[q] = (T *)J->d_sp[q];
+  p.slab_rows = J->slab_rows;
+  for (int s = 0; s < 2; ++s) {
+    p.slab_on[s] = J->slab_on[s];
+    p.slab_j0[s] = J->slab_j0[s];
+    for (int q = 0; q < 12; ++q) p.slab[s][q] = (T *)J->d_slab[s][q];
+    void *const *sc = J->d_sc[s];
+    p.sf1x[s] = (const T *)sc[0]; p.sf2x[s] = (const T *)sc[1]; p.sg1x[s] = (const T *)sc[2]; p.sg2x[s] = (const T *)sc[3];
+    p.sf1y[s] = (const T *)sc[4]; p.sf2y[s] = (const T *)sc[5]; p.sg1y[s] = (const T *)sc[6]; p.sg2y[s] = (const T *)sc[7];
+    p.sf1z[s] = (const T *)sc[8]; p.sf2z[s] = (const T *)sc[9]; p.sg1z[s] = (const T *)sc[10]; p.sg2z[s] = (const T *)sc[11];
+  }
+  if (J->dim == 2) {
+    p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 31) / 32; p.tiles_z = 1;
+  } else {
+    p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 7) / 8; p.tiles_z = (J->nz + 15) / 16;
+  }
+  p.ntile_blocks = p.tiles_x * p.tiles_y * p.tiles_z;
+  p.nslab_blocks = (J->dim == 3 && J->slab_rows > 0) ? (2 * J->nx * J->slab_rows * J->nz + 255) / 256 : 0;
+  p.nade_blocks = (J->nade + 255) / 256;
+  p.nmon = (int)J->mon_dev.size();
+  for (int q = 0; q < p.nmon; ++q) p.mon[q] = J->mon_dev[q];
+  p.stage = (T *)J->d_stage;
+  p.stage_row = J->stage_row;
+  p.nprobe = (int)J->probes.size();
+  for (int q = 0; q < p.nprobe; ++q) {
+    const ProbeRec &P = J->probes[q];
+    Probe &d = p.probe[q];
+    for (int a = 0; a < 3; ++a) d.cell[a] = P.d.cell[a];
+    d.ncomp = P.ncomp;
+    for (int u = 0; u < P.ncomp; ++u) d.comps[u] = P.comps[u];
+    d.n_first = P.d.n_first;
+    d.n_last = P.d.n_last;
+    d.buf = P.buf;
+    d.cap = P.cap;
+  }
+}
+
+template <typename T>
+void set_sources(fdtd_job *J, StepParams<T> &p, int n) {
+  const double t = (double)(n - 1) * J->g.dt;
+  p.nsrc = 0;
+  for (auto &s : J->srcs) {
+    if (s.component == FDTD_EX_INC) continue;
+    Source &d = p.src[p.nsrc];
+    d.comp = s.component;
+    for (int a = 0; a < 3; ++a) {
+      d.lo[a] = std::max(s.lo[a], J->g.main_lo[a]);
+      d.hi[a] = std::min(s.hi[a], J->g.main_hi[a]);
+    }
+    d.amp = s.amp;
+    p.srcval[p.nsrc] = gauss_t(s, t) * s.amp;
+    ++p.nsrc;
+  }
+}
+
+void ev_record(fdtd_job *J, int kind, bool begin) {
+  if (!J->prof) return;
+  cudaEvent_t e;
+  if (J->ev_pool.empty()) cudaEventCreate(&e);
+  else { e = J->ev_pool.back(); J->ev_pool.pop_back(); }
+  cudaEventRecord(e, J->stream);
+  if (begin) J->pending.push_back({e, nullptr, kind});
+  else J->pending.back().b = e;
+}
+
+int ensure_probe_cap(fdtd_job *J, int n_max) {
+  for (auto &P : J->probes) {
+    long long need = (long long)std::min(P.d.n_last, n_max) - P.d.n_first + 1;
+    if (need <= P.cap) continue;
+    long long cap = std::max<long long>(need, 2LL * P.cap);
+    cap = std::max<long long>(cap, 1024);
+    double *nb = nullptr;
+    cudaError_t e = cudaMalloc(&nb, (size_t)cap * P.ncomp * sizeof(double));
+    if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "probe buffer: %s", cudaGetErrorString(e));
+    CK(cudaMemsetAsync(nb, 0, (size_t)cap * P.ncomp * sizeof(double), J->stream));
+    if (P.buf) {
+      CK(cudaMemcpyAsync(nb, P.buf, (size_t)P.cap * P.ncomp * sizeof(double), cudaMemcpyDeviceToDevice, J->stream));
+      CK(cudaStreamSynchronize(J->stream));
+      cudaFree(P.buf);
+      J->dev_bytes -= (uint64_t)P.cap * P.ncomp * sizeof(double);
+    }
+    P.buf = nb;
+    P.cap = (int)cap;
+    J->dev_bytes += (uint64_t)cap * P.ncomp * sizeof(double);
+  }
+  return FDTD_OK;
+}
+
+template <typename T>
+int dft_fold(fdtd_job *J) {
+  if (J->stage_fill == 0) return FDTD_OK;
+  if (!J->mon_dev.empty()) {
+    DftParams d{};
+    d.nmon = (int)J->mon_dev.size();
+    for (int q = 0; q < d.nmon; ++q) d.mon[q] = J->mon_dev[q];
+    d.omega = J->d_omega;
+    d.acc_re = J->d_acc_re;
+    d.acc_im = J->d_acc_im;
+    d.dt = J->g.dt;
+    d.stage_row = J->stage_row;
+    d.total_work_blocks = J->dft_blocks;
+    // fold in rings of kStageSteps rows (the 1D stage holds many rings)
+    for (int r0 = 0; r0 < J->stage_fill; r0 += kStageSteps) {
+      d.nslots = std::min(kStageSteps, J->stage_fill - r0);
+      d.n0 = J->stage_n0 + r0;
+      ev_record(J, FDTD_KERNEL_DFT, true);
+      launch_dft<T>(d, (const T *)J->d_stage + (size_t)r0 * J->stage_row, J->stream);
+      ev_record(J, FDTD_KERNEL_DFT, false);
+      J->launches++;
+    }
+    CK(cudaGetLastError());
+  }
+  J->stage_n0 += J->stage_fill;
+  J->stage_fill = 0;
+  return FDTD_OK;
+}
+
+enum { ST_E = 1, ST_H = 2, ST_SAMPLE = 4 };
+
+// 2D / 3D: one half step (or a role subset of it)
+template <typename T>
+int half_e(fdtd_job *J, int n, int roles) {
+  StepParams<T> p;
+  fill_common<T>(J, p);
+  set_sources<T>(J, p, n);
+  p.roles = roles;
+  p.n = n;
+  int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
+  ev_record(J, FDTD_KERNEL_E, true);
+  if (J->dim == 2) launch_e2d<T>(p, blocks, J->stream);
+  else launch_e3d<T>(p, blocks, J->stream);
+  ev_record(J, FDTD_KERNEL_E, false);
+  J->launches++;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+template <typename T>
+int half_h(fdtd_job *J, int n, int roles, bool gather) {
+  StepParams<T> p;
+  fill_common<T>(J, p);
+  p.roles = roles;
+  p.n = n;
+  p.gather = gather ? 1 : 0;
+  p.slot = J->stage_fill;
+  int blocks = p.ntile_blocks + p.nslab_blocks;
+  ev_record(J, FDTD_KERNEL_H, true);
+  if (J->dim == 2) launch_h2d<T>(p, blocks, J->stream);
+  else launch_h3d<T>(p, blocks, J->stream);
+  ev_record(J, FDTD_KERNEL_H, false);
+  J->launches++;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+template <typename T>
+int sample_sep(fdtd_job *J, int n) {
+  StepParams<T> p;
+  fill_common<T>(J, p);
+  p.n = n;
+  p.slot = J->stage_fill;
+  launch_gather<T>(p, J->stream);
+  J->launches++;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+template <typename T>
+int after_sample(fdtd_job *J, int n) {
+  if (J->stage_fill == 0) J->stage_n0 = n;
+  J->stage_fill++;
+  J->last_n = n;
+  if (J->stage_fill == kStageSteps) return dft_fold<T>(J);
+  return FDTD_OK;
+}
+
+// 1D: the persistent line kernel over a chunk of steps
+template <typename T>
+int line_run(fdtd_job *J, int n_first, int n_steps, int stages) {
+  LineParams<T> p;
+  memset(&p, 0, sizeof p);
+  p.N = J->ny;
+  p.mlo = J->g.main_lo[1];
+  p.mhi = J->g.main_hi[1];
+  p.ku = T(J->g.ku);
+  p.ex = (T *)J->F[0];
+  p.hz = (T *)J->F[5];
+  p.exi = (T *)J->F[6];
+  p.hzi = (T *)J->F[7];
+  p.tfsf_bd = J->has_tfsf ? J->tfsf.boundary : -1;
+  p.mat = J->d_mat;
+  p.mc = (const MatCoef<T> *)J->d_mc;
+  p.ac = (const AdeCoef<T> *)J->d_ac;
+  p.nade = J->nade;
+  p.ade_cell = J->d_ade_cell;
+  p.ade_mat = J->d_ade_mat;
+  p.ade_state = (T *)J->d_ade_state;
+  p.ade_stride = J->ade_stride;
+  p.ja = J->ja;
+  p.jb = J->jb;
+  for (int s = 0; s < 2; ++s) {
+    p.slab_on[s] = J->slab_on[s];
+    for (int line = 0; line < 2; ++line) {
+      p.pex[line][s] = (T *)J->d_lex[line][s];
+      p.phz[line][s] = (T *)J->d_lhz[line][s];
+      p.f1[line][s] = (const T *)J->d_lc[line][s][0];
+      p.f2[line][s] = (const T *)J->d_lc[line][s][1];
+      p.g1[line][s] = (const T *)J->d_lc[line][s][2];
+      p.g2[line][s] = (const T *)J->d_lc[line][s][3];
+    }
+  }
+  // sources: values for every step of the chunk
+  p.nsrc = 0;
+  for (auto &s : J->srcs) {
+    Source &d = p.src[p.nsrc];
+    d.comp = s.component;
+    for (int a = 0; a < 3; ++a) { d.lo[a] = s.lo[a]; d.hi[a] = s.hi[a]; }
+    if (s.component != FDTD_EX_INC) {
+      d.lo[1] = std::max(d.lo[1], J->g.main_lo[1]);
+      d.hi[1] = std::min(d.hi[1], J->g.main_hi[1]);
+    }
+    d.amp = s.amp;
+    ++p.nsrc;
+  }
+  if (p.nsrc) {
+    std::vector<double> v((size_t)n_steps * p.nsrc);
+    for (int st = 0; st < n_steps; ++st) {
+      const double t = (double)(n_first + st - 1) * J->g.dt;
+      int q = 0;
+      for (auto &s : J->srcs) {
+        const double g = gauss_t(s, t);
+        v[(size_t)st * p.nsrc + q] = s.component == FDTD_EX_INC ? g : g * s.amp;
+        ++q;
+      }
+    }
+    if ((long long)v.size() > J->srcval_cap) {
+      if (J->d_srcval) { cudaFree(J->d_srcval); J->dev_bytes -= J->srcval_cap * sizeof(double); }
+      J->srcval_cap = std::max<long long>((long long)v.size(), 4096);
+      CK(cudaMalloc(&J->d_srcval, J->srcval_cap * sizeof(double)));
+      J->dev_bytes += J->srcval_cap * sizeof(double);
+    }
+    CK(cudaMemcpyAsync(J->d_srcval, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, J->stream));
+    CK(cudaStreamSynchronize(J->stream));  // v is a temporary
+  }
+  p.srcval = J->d_srcval;
+  p.nmon = (int)J->mon_dev.size();
+  for (int q = 0; q < p.nmon; ++q) p.mon[q] = J->mon_dev[q];
+  p.nprobe = (int)J->probes.size();
+  for (int q = 0; q < p.nprobe; ++q) {
+    const ProbeRec &P = J->probes[q];
+    Probe &d = p.probe[q];
+    for (int a = 0; a < 3; ++a) d.cell[a] = P.d.cell[a];
+    d.ncomp = P.ncomp;
+    for (int u = 0; u < P.ncomp; ++u) d.comps[u] = P.comps[u];
+    d.n_first = P.d.n_first;
+    d.n_last = P.d.n_last;
+    d.buf = P.buf;
+    d.cap = P.cap;
+  }
+  p.dt = J->g.dt;
+  p.n_first = n_first;
+  p.n_steps = n_steps;
+  p.stages = stages;
+  T *stage = (T *)J->d_stage + (size_t)J->stage_fill * J->stage_row;
+  ev_record(J, FDTD_KERNEL_LINE1D, true);
+  launch_line1d_stage<T>(p, stage, J->stage_row, J->stream);
+  ev_record(J, FDTD_KERNEL_LINE1D, false);
+  J->launches++;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+template <typename T>
+int step_impl(fdtd_job *J, int n_first, int n_steps) {
+  int rc;
+  if ((rc = ensure_probe_cap(J, n_first + n_steps - 1))) return rc;
+  if (J->dim == 1) {
+    int n = n_first, left = n_steps;
+    while (left > 0) {
+      if (J->stage_fill == 0) J->stage_n0 = n;
+      int chunk = (int)std::min<long long>(left, J->stage_cap_rows - J->stage_fill);
+      if ((rc = line_run<T>(J, n, chunk, ST_E | ST_H | ST_SAMPLE))) return rc;
+      J->stage_fill += chunk;
+      n += chunk;
+      left -= chunk;
+      J->last_n = n - 1;
+      if (J->stage_fill >= J->stage_cap_rows)
+        if ((rc = dft_fold<T>(J))) return rc;
+    }
+    return FDTD_OK;
+  }
+  const int all = ROLE_MAIN | ROLE_PML | ROLE_ADE;
+  for (int n = n_first; n < n_first + n_steps; ++n) {
+    if ((rc = half_e<T>(J, n, all))) return rc;
+    if ((rc = half_h<T>(J, n, ROLE_MAIN | ROLE_PML, J->gather_fused))) return rc;
+    if (!J->gather_fused && (rc = sample_sep<T>(J, n))) return rc;
+    if ((rc = after_sample<T>(J, n))) return rc;
+  }
+  return FDTD_OK;
+}
+
+#define DISPATCH(J, call) ((J)->g.precision == FDTD_F32 ? call<float> : call<double>)
+
+int check_job(fdtd_job *J, bool need_commit) {
+  if (!J) return set_err(FDTD_EINVAL, "null job");
+  if (need_commit && !J->committed) return set_err(FDTD_ESTATE, "job not committed");
+  if (!need_commit && J->committed) return set_err(FDTD_ESTATE, "job already committed");
+  return FDTD_OK;
+}
+
+}  // namespace
+
+template <typename T>
+static int proc_call(fdtd_job *J, int n, int what) {
+  int rc = ensure_probe_cap(J, n);
+  if (rc) return rc;
+  if (J->dim == 1) {
+    if (what == 0) { if (J->stage_fill == 0) J->stage_n0 = n; return line_run<T>(J, n, 1, ST_E); }
+    if (what == 2) return line_run<T>(J, n, 1, ST_H);
+    if (what == 4) {
+      if (J->stage_fill == 0) J->stage_n0 = n;
+      if ((rc = line_run<T>(J, n, 1, ST_SAMPLE))) return rc;
+      J->stage_fill++;
+      J->last_n = n;
+      if (J->stage_fill >= J->stage_cap_rows) return dft_fold<T>(J);
+    }
+    return FDTD_OK;
+  }
+  switch (what) {
+    case 0: return half_e<T>(J, n, ROLE_MAIN | ROLE_ADE);
+    case 1: return half_e<T>(J, n, ROLE_PML);
+    case 2: return half_h<T>(J, n, ROLE_MAIN, false);
+    case 3: return half_h<T>(J, n, ROLE_PML, false);
+    case 4:
+      if ((rc = sample_sep<T>(J, n))) return rc;
+      return after_sample<T>(J, n);
+  }
+  return FDTD_OK;
+}
+
+template <typename T>
+static int get_field_impl(fdtd_job *J, int comp, double *host) {
+  if (comp < 0 || comp > 7 || !J->F[comp]) return set_err(FDTD_EINVAL, "component %d not in this layout", comp);
+  std::vector<T> tmp((size_t)J->ncell);
+  CK(cudaMemcpyAsync(tmp.data(), J->F[comp], (size_t)J->ncell * sizeof(T), cudaMemcpyDeviceToHost, J->stream));
+  CK(cudaStreamSynchronize(J->stream));
+  for (long long c = 0; c < J->ncell; ++c) host[c] = (double)tmp[(size_t)c];
+  return FDTD_OK;
+}
+
+template <typename T>
+static int set_field_impl(fdtd_job *J, int comp, const double *host) {
+  if (comp < 0 || comp > 7 || !J->F[comp]) return set_err(FDTD_EINVAL, "component %d not in this layout", comp);
+  std::vector<T> tmp(host, host + J->ncell);
+  CK(cudaMemcpyAsync(J->F[comp], tmp.data(), (size_t)J->ncell * sizeof(T), cudaMemcpyHostToDevice, J->stream));
+  CK(cudaStreamSynchronize(J->stream));
+  return FDTD_OK;
+}
+
+// =========================================================================
+extern "C" {
+
+int fdtd_last_error(char *buf, size_t len) {
+  if (buf && len) {
+    snprintf(buf, len, "%s", g_last_error.c_str());
+  }
+  return FDTD_OK;
+}
+
+int fdtd_device_count(int32_t *count) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+  int usable = 0;
+  for (int d = 0; d < n; ++d) {
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, d) == cudaSuccess && prop.major == 10 && prop.minor == 3) ++usable;
+  }
+  if (count) *count = usable;
+  return FDTD_OK;
+}
+
+int fdtd_create(const fdtd_grid_desc *g, fdtd_job **out) {
+  if (!g || !out) return set_err(FDTD_EINVAL, "null argument");
+  *out = nullptr;
+  int dim;
+  switch (g->layout) {
+    case FDTD_LAYOUT_1D: dim = 1; break;
+    case FDTD_LAYOUT_2D_TE: case FDTD_LAYOUT_2D_TM: dim = 2; break;
+    case FDTD_LAYOUT_3D: dim = 3; break;
+    default: return set_err(FDTD_EINVAL, "bad layout %d", g->layout);
+  }
+  if (g->precision != FDTD_F32 && g->precision != FDTD_F64) return set_err(FDTD_EINVAL, "bad precision");
+  for (int a = 0; a < 3; ++a)
+    if (g->n[a] < 1) return set_err(FDTD_EINVAL, "n[%d] < 1", a);
+  if (dim == 1 && (g->n[0] != 1 || g->n[2] != 1)) return set_err(FDTD_EINVAL, "1D runs along y: n = (1, N, 1)");
+  if (dim == 2 && g->n[2] != 1) return set_err(FDTD_EINVAL, "2D needs n[2] = 1");
+  const long long N = (long long)g->n[0] * g->n[1] * g->n[2];
+  if (N >= (1LL << 31)) return set_err(FDTD_ERANGE, "grid of %lld cells exceeds 2^31", N);
+  if (g->dt <= 0 || g->ds <= 0) return set_err(FDTD_EINVAL, "dt and ds must be positive");
+  int dev = 0, rc = check_device(&dev);
+  if (rc) return rc;
+  fdtd_job *J = new fdtd_job();
+  J->g = *g;
+  J->dim = dim;
+  J->nx = g->n[0]; J->ny = g->n[1]; J->nz = g->n[2];
+  J->ncell = N;
+  J->esz = g->precision == FDTD_F32 ? 4 : 8;
+  J->device = dev;
+  for (int a = 0; a < 3; ++a) {
+    J->g.main_lo[a] = std::max(0, g->main_lo[a]);
+    J->g.main_hi[a] = std::min(g->n[a] - 1, g->main_hi[a]);
+  }
+  if (cudaStreamCreateWithFlags(&J->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete J;
+    return set_err(FDTD_ECUDA, "cudaStreamCreate failed");
+  }
+  *out = J;
+  return FDTD_OK;
+}
+
+int fdtd_destroy(fdtd_job *J) {
+  if (!J) return FDTD_OK;
+  if (J->stream) cudaStreamSynchronize(J->stream);
+  for (void *p : J->allocs) cudaFree(p);
+  for (auto &P : J->probes) if (P.buf) cudaFree(P.buf);
+  if (J->d_srcval) cudaFree(J->d_srcval);
+  for (auto &e : J->pending) { cudaEventDestroy(e.a); if (e.b) cudaEventDestroy(e.b); }
+  for (auto e : J->ev_pool) cudaEventDestroy(e);
+  if (J->stream) cudaStreamDestroy(J->stream);
+  delete J;
+  return FDTD_OK;
+}
+
+static int add_mat(fdtd_job *J, const fdtd_region *r, MatRec &m, int32_t *id) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (!r) return set_err(FDTD_EINVAL, "null region");
+  if (J->mats.size() >= (size_t)(kMaxMat - 1)) return set_err(FDTD_ERANGE, "too many materials");
+  m.region = *r;
+  if (r->kind == FDTD_REGION_SPHERES) {
+    if (r->count < 0 || (r->count > 0 && !r->centers_radii)) return set_err(FDTD_EINVAL, "bad spheres");
+    m.centers.assign(r->centers_radii, r->centers_radii + 4 * (size_t)r->count);
+    m.region.centers_radii = nullptr;
+  } else if (r->kind == FDTD_REGION_MASK) {
+    if (!r->mask) return set_err(FDTD_EINVAL, "null mask");
+    m.mask.assign(r->mask, r->mask + J->ncell);
+    m.region.mask = nullptr;
+  } else if (r->kind != FDTD_REGION_BOX) {
+    return set_err(FDTD_EINVAL, "bad region kind %d", r->kind);
+  }
+  J->mats.push_back(m);
+  if (id) *id = (int32_t)J->mats.size();
+  return FDTD_OK;
+}
+
+int fdtd_add_dielectric(fdtd_job *J, const fdtd_region *r, double eps, int32_t *id) {
+  MatRec m{};
+  m.kind = MK_DIEL;
+  m.eps = eps;
+  return add_mat(J, r, m, id);
+}
+
+int fdtd_add_gold(fdtd_job *J, const fdtd_region *r, const fdtd_drude2cp *p, int32_t *id) {
+  if (!p) return set_err(FDTD_EINVAL, "null gold parameters");
+  if (p->gamma_d <= 0) return set_err(FDTD_EINVAL, "gamma_d must be positive");
+  MatRec m{};
+  m.kind = MK_GOLD;
+  m.gold = *p;
+  return add_mat(J, r, m, id);
+}
+
+int fdtd_add_graphene(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_desc *p, int32_t *id) {
+  if (!p || !r) return set_err(FDTD_EINVAL, "null argument");
+  if (r->kind != FDTD_REGION_BOX) return set_err(FDTD_EINVAL, "graphene needs a one-cell-thick box");
+  bool thin = false;
+  for (int a = 0; a < 3; ++a) if (r->lo[a] == r->hi[a] && J && J->g.n[a] > 1) thin = true;
+  if (!thin) return set_err(FDTD_EINVAL, "graphene box must be one cell thick");
+  if (p->tau <= 0 || p->thickness <= 0 || p->raman_tau <= 0) return set_err(FDTD_EINVAL, "bad graphene parameters");
+  MatRec m{};
+  m.kind = MK_GRAPHENE;
+  m.gr = *p;
+  return add_mat(J, r, m, id);
+}
+
+int fdtd_add_pml(fdtd_job *J, const fdtd_pml_desc *p) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (!p) return set_err(FDTD_EINVAL, "null pml");
+  if (p->mode != FDTD_PML_REFERENCE && p->mode != FDTD_PML_SPLIT) return set_err(FDTD_EINVAL, "bad pml mode");
+  if (p->mode == FDTD_PML_SPLIT && J->dim == 1) return set_err(FDTD_EINVAL, "1D uses the reference PML");
+  if (p->mode == FDTD_PML_REFERENCE && J->g.layout == FDTD_LAYOUT_2D_TM)
+    return set_err(FDTD_EINVAL, "2D TM uses the split PML");
+  const int n[3] = {J->nx, J->ny, J->nz};
+  for (int a = 0; a < 3; ++a)
+    for (int s = 0; s < 2; ++s)
+      if (p->npml[a][s] < 0 || 2 * p->npml[a][s] >= n[a] + (n[a] == 1 ? 2 : 0))
+        return set_err(FDTD_EINVAL, "npml[%d][%d] = %d does not fit the grid", a, s, p->npml[a][s]);
+  if (p->mode == FDTD_PML_REFERENCE && p->npml[1][0] != p->npml[1][1])
+    return set_err(FDTD_EINVAL, "reference PML: both y slabs have npmly cells");
+  J->has_pml = true;
+  J->pml = *p;
+  return FDTD_OK;
+}
+
+int fdtd_add_tfsf_1d(fdtd_job *J, const fdtd_tfsf1d_desc *t) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (!t) return set_err(FDTD_EINVAL, "null tfsf");
+  if (J->dim != 1) return set_err(FDTD_EINVAL, "TFSF line is 1D only");
+  if (t->boundary < 1 || t->boundary >= J->ny) return set_err(FDTD_ERANGE, "TFSF boundary out of range");
+  J->has_tfsf = true;
+  J->tfsf = *t;
+  return FDTD_OK;
+}
+
+int fdtd_add_source(fdtd_job *J, const fdtd_source_desc *s, int32_t *id) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (!s) return set_err(FDTD_EINVAL, "null source");
+  if (J->srcs.size() >= (size_t)kMaxSrc) return set_err(FDTD_ERANGE, "too many sources");
+  if (!(s->component >= FDTD_EX && s->component <= FDTD_EZ) && s->component != FDTD_EX_INC)
+    return set_err(FDTD_EINVAL, "source drives an E component");
+  if (s->st == 0) return set_err(FDTD_EINVAL, "source width st = 0");
+  J->srcs.push_back(*s);
+  if (id) *id = (int32_t)J->srcs.size() - 1;
+  return FDTD_OK;
+}
+
+int fdtd_add_monitor(fdtd_job *J, const fdtd_monitor_desc *m, int32_t *id) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (!m || (m->nfreq > 0 && !m->omega)) return set_err(FDTD_EINVAL, "null monitor");
+  if (J->mons.size() >= (size_t)kMaxMon) return set_err(FDTD_ERANGE, "too many monitors");
+  const int n[3] = {J->nx, J->ny, J->nz};
+  for (int a = 0; a < 3; ++a)
+    if (m->lo[a] < 0 || m->hi[a] >= n[a] || m->lo[a] > m->hi[a]) return set_err(FDTD_ERANGE, "monitor box out of grid");
+  if (m->nfreq < 1) return set_err(FDTD_EINVAL, "monitor needs frequencies");
+  MonRec R;
+  R.d = *m;
+  R.omega.assign(m->omega, m->omega + m->nfreq);
+  R.d.omega = nullptr;
+  R.ncomp = comp_list(m->comp_mask, R.comps, 6);
+  if (R.ncomp <= 0) return set_err(FDTD_EINVAL, "monitor needs 1..6 components");
+  for (int u = 0; u < R.ncomp; ++u)
+    if ((R.comps[u] >= FDTD_EX_INC) != (J->dim == 1 && R.comps[u] >= FDTD_EX_INC) ||
+        (R.comps[u] >= FDTD_EX_INC && !J->has_tfsf))
+      return set_err(FDTD_EINVAL, "component %d not available", R.comps[u]);
+  R.ncell = (long long)(m->hi[0] - m->lo[0] + 1) * (m->hi[1] - m->lo[1] + 1) * (m->hi[2] - m->lo[2] + 1);
+  J->mons.push_back(R);
+  if (id) *id = (int32_t)J->mons.size() - 1;
+  return FDTD_OK;
+}
+
+int fdtd_add_probe(fdtd_job *J, const fdtd_probe_desc *p, int32_t *id) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (!p) return set_err(FDTD_EINVAL, "null probe");
+  if (J->probes.size() >= (size_t)kMaxProbe) return set_err(FDTD_ERANGE, "too many probes");
+  const int n[3] = {J->nx, J->ny, J->nz};
+  for (int a = 0; a < 3; ++a)
+    if (p->cell[a] < 0 || p->cell[a] >= n[a]) return set_err(FDTD_ERANGE, "probe cell out of grid");
+  ProbeRec R;
+  R.d = *p;
+  R.ncomp = comp_list(p->comp_mask, R.comps, 8);
+  if (R.ncomp <= 0) return set_err(FDTD_EINVAL, "probe needs components");
+  J->probes.push_back(R);
+  if (id) *id = (int32_t)J->probes.size() - 1;
+  return FDTD_OK;
+}
+
+int fdtd_commit(fdtd_job *J) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (J->dim == 1 && J->has_pml && J->pml.npml[1][0] < 1) return set_err(FDTD_EINVAL, "1D PML needs npmly >= 1");
+  return DISPATCH(J, commit_impl)(J);
+}
+
+int fdtd_step(fdtd_job *J, int32_t n_first, int32_t n_steps) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (n_steps < 0 || n_first < 1) return set_err(FDTD_EINVAL, "bad step range");
+  if (n_steps == 0) return FDTD_OK;
+  return DISPATCH(J, step_impl)(J, n_first, n_steps);
+}
+
+int fdtd_update_DE(fdtd_job *J, int32_t n) {
+  int rc = check_job(J, true);
+  return rc ? rc : DISPATCH(J, proc_call)(J, n, 0);
+}
+int fdtd_pml_update_E(fdtd_job *J, int32_t n) {
+  int rc = check_job(J, true);
+  return rc ? rc : DISPATCH(J, proc_call)(J, n, 1);
+}
+int fdtd_interchange(fdtd_job *J, int32_t which) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (which != 0 && which != 1) return set_err(FDTD_EINVAL, "interchange: 0 = E, 1 = H");
+  return FDTD_OK;  // one domain: the halo is the neighbouring cell
+}
+int fdtd_update_H(fdtd_job *J, int32_t n) {
+  int rc = check_job(J, true);
+  return rc ? rc : DISPATCH(J, proc_call)(J, n, 2);
+}
+int fdtd_pml_update_H(fdtd_job *J, int32_t n) {
+  int rc = check_job(J, true);
+  return rc ? rc : DISPATCH(J, proc_call)(J, n, 3);
+}
+int fdtd_sample(fdtd_job *J, int32_t n) {
+  int rc = check_job(J, true);
+  return rc ? rc : DISPATCH(J, proc_call)(J, n, 4);
+}
+
+int fdtd_sync(fdtd_job *J) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if ((rc = DISPATCH(J, dft_fold)(J))) return rc;
+  CK(cudaStreamSynchronize(J->stream));
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+int fdtd_get_field(fdtd_job *J, int32_t comp, double *host) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (!host) return set_err(FDTD_EINVAL, "null buffer");
+  return DISPATCH(J, get_field_impl)(J, comp, host);
+}
+
+int fdtd_set_field(fdtd_job *J, int32_t comp, const double *host) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (!host) return set_err(FDTD_EINVAL, "null buffer");
+  return DISPATCH(J, set_field_impl)(J, comp, host);
+}
+
+int fdtd_get_monitor(fdtd_job *J, int32_t id, double *re, double *im) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (id < 0 || id >= (int)J->mons.size()) return set_err(FDTD_ERANGE, "bad monitor id");
+  if ((rc = fdtd_sync(J))) return rc;
+  const Monitor &m = J->mon_dev[id];
+  const size_t n = (size_t)m.ncomp * m.nfreq * m.ncell;
+  if (re) CK(cudaMemcpy(re, J->d_acc_re + m.acc, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (im) CK(cudaMemcpy(im, J->d_acc_im + m.acc, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return FDTD_OK;
+}
+
+int fdtd_get_probe(fdtd_job *J, int32_t id, double *host, int32_t *count) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (id < 0 || id >= (int)J->probes.size()) return set_err(FDTD_ERANGE, "bad probe id");
+  CK(cudaStreamSynchronize(J->stream));
+  const ProbeRec &P = J->probes[id];
+  long long cnt = (long long)std::min(P.d.n_last, J->last_n) - P.d.n_first + 1;
+  cnt = std::max(0LL, std::min<long long>(cnt, P.cap));
+  if (count) *count = (int32_t)cnt;
+  if (host && cnt > 0) CK(cudaMemcpy(host, P.buf, (size_t)cnt * P.ncomp * sizeof(double), cudaMemcpyDeviceToHost));
+  return FDTD_OK;
+}
+
+int fdtd_device_bytes(const fdtd_job *J, uint64_t *bytes) {
+  if (!J || !bytes) return set_err(FDTD_EINVAL, "null argument");
+  *bytes = J->dev_bytes;
+  return FDTD_OK;
+}
+
+int fdtd_profile(fdtd_job *J, int32_t enable) {
+  if (!J) return set_err(FDTD_EINVAL, "null job");
+  J->prof = enable != 0;
+  return FDTD_OK;
+}
+
+int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
+  if (!J) return set_err(FDTD_EINVAL, "null job");
+  if (kind < 0 || kind >= FDTD_KERNEL_COUNT) return set_err(FDTD_EINVAL, "bad kernel kind");
+  CK(cudaStreamSynchronize(J->stream));
+  for (auto &e : J->pending) {
+    if (!e.b) continue;
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e.a, e.b);
+    J->kms[e.kind] += t;
+    J->kcount[e.kind] += 1;
+    J->ev_pool.push_back(e.a);
+    J->ev_pool.push_back(e.b);
+  }
+  J->pending.clear();
+  if (launches) *launches = J->kcount[kind];
+  if (ms) *ms = J->kms[kind];
+  return FDTD_OK;
+}
+
+int fdtd_launch_count(const fdtd_job *J, int64_t *launches) {
+  if (!J || !launches) return set_err(FDTD_EINVAL, "null argument");
+  *launches = J->launches;
+  return FDTD_OK;
+}
+
+}  // extern "C"

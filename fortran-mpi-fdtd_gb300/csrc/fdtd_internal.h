@@ -1,0 +1,204 @@
+// fdtd_internal.h -- device-side parameter blocks shared by the kernels and
+// the host job manager (fdtd_api.cu).  Not part of the public ABI.
+//
+// Data layout in HBM (per job, T = float or double):
+//   * main fields: one array per component, nx*ny*nz values, x fastest, no
+//     halo cells: neighbours across a periodic face are read by index wrap,
+//     across a non-periodic face they are zero.  The MPI slabs of the
+//     reference are one array, so interchange_E/H need no copies.
+//   * material id map: one byte per cell (0 = no material).
+//   * dispersive (ADE) cells: a compact slot list (cell index, material id)
+//     with structure-of-arrays state per slot and component.
+//   * PML: reference y-slabs (split arrays over npml rows only) or, for the
+//     split-field PML on any faces, one stored sub-field per split component
+//     (the other part is the total minus the stored part) over the full grid
+//     (only shell cells are touched).
+//   * DFT: samples of the monitored cells are staged per step in a ring of
+//     kStageSteps slots and folded into FP64 accumulators once per ring.
+#pragma once
+#include <cstdint>
+
+namespace fdtd {
+
+constexpr int kMaxMat = 256;
+constexpr int kMaxSrc = 8;
+constexpr int kMaxMon = 16;
+constexpr int kMaxProbe = 16;
+constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
+
+enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3 };
+
+// per material id, in the job's precision
+template <typename T>
+struct MatCoef {
+  int kind;
+  int ade;      // index into the ADE coefficient table (gold/graphene), -1 otherwise
+  T ca;         // Ku * (1/eps): E += ca * curl
+  T cs;         // 1/eps: E += cs * source
+};
+
+// Drude + 2 critical points (and the graphene Drude + Raman/Kerr variant)
+template <typename T>
+struct AdeCoef {
+  int kind;
+  int normal;              // graphene sheet normal axis (in-plane comps updated)
+  T ha, hb;                // Drude: S = ha*S + hb*E, Q -= hb*E
+  T gb1r, gb1i, gb2r, gb2i;// CP recursion factors
+  T gc1r, gc1i, gc2r, gc2i;// CP drive
+  T wr, wi;                // 1/ga (E = Re(num * (wr + i wi)))
+  T r0, r1, r2, kerr, ga;  // graphene Raman recursion, Kerr, eps
+};
+
+struct Source {
+  int comp;                // 0..2 (E component) or 6 (1D incident line)
+  int lo[3], hi[3];
+  double amp;
+};
+
+struct Monitor {
+  int lo[3], hi[3];
+  int ncomp, comps[6];
+  int ncell;
+  long long base;          // first index of this monitor in the stage row
+  int n_first, n_last;
+  int nfreq;
+  long long acc;           // offset of this monitor's accumulators
+  int freq_off;            // offset into the omega table
+};
+
+struct Probe {
+  int cell[3];
+  int ncomp, comps[8];
+  int n_first, n_last;
+  double *buf;             // device buffer: [step - n_first][comp]
+  int cap;                 // steps of capacity
+};
+
+// Everything a step kernel needs, passed by value.
+template <typename T>
+struct StepParams {
+  // geometry
+  int layout;              // FDTD_LAYOUT_*
+  int nx, ny, nz;
+  int per[3];
+  int mlo[3], mhi[3];      // main (Yee) range
+  T ku;
+  // fields (E/H components; null when the layout lacks them)
+  T *ex, *ey, *ez, *hx, *hy, *hz;
+  const uint8_t *mat;
+  const MatCoef<T> *mc;
+  // ADE slots
+  int nade;
+  const int *ade_cell;     // linear cell index
+  const uint8_t *ade_mat;  // material id
+  const AdeCoef<T> *ac;
+  T *ade_state;            // [field][comp][slot], see AdeState
+  int ade_stride;          // = padded nade
+  // sources active this step
+  int nsrc;
+  Source src[kMaxSrc];
+  double srcval[kMaxSrc];  // amp * g(t) for this step
+  // PML
+  int pml_mode;            // 0 none, 1 reference slabs, 2 split
+  // split-field PML on any faces: shell = outside [slo, shi]
+  int slo[3], shi[3];
+  const T *cf1[3], *cf2[3], *cg1[3], *cg2[3];   // per-axis tables (len n[a])
+  T *sp[6];                // stored sub-fields (3D: Exy Eyz Ezx Hxy Hyz Hzx;
+                           // 2D TM: Ezx; 2D TE: Hzx)
+  // reference y-slabs (2D: Ex Ey Hzx Hzy; 3D: 12 split arrays) per side
+  int slab_on[2];
+  int slab_j0[2];          // first 0-based row of the slab
+  int slab_rows;           // npmly
+  T *slab[2][12];
+  const T *sf1x[2], *sf2x[2], *sg1x[2], *sg2x[2];  // per side, len nx
+  const T *sf1y[2], *sf2y[2], *sg1y[2], *sg2y[2];  // per side, len rows
+  const T *sf1z[2], *sf2z[2], *sg1z[2], *sg2z[2];  // per side, len nz
+  // work split of one launch
+  int roles;               // ROLE_* bits
+  int tiles_x, tiles_y, tiles_z, ntile_blocks;
+  int nslab_blocks, nade_blocks;
+  // sampling fused into the H kernel
+  int gather;              // 1: tile threads write the stage row / probes
+  int nmon;
+  Monitor mon[kMaxMon];
+  T *stage;                // [slot][sample]
+  long long stage_row;     // samples per step
+  int slot;                // ring slot of this step
+  int nprobe;
+  Probe probe[kMaxProbe];
+  int n;                   // step number
+};
+
+enum Role : int {
+  ROLE_MAIN = 1,  // Yee update + materials on main cells
+  ROLE_PML = 2,   // PML (slabs or shell)
+  ROLE_ADE = 4,   // dispersive slots
+};
+
+// ADE state layout: state[(f*3 + comp)*stride + slot] with fields
+// 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:SRm1 3:SRm2 4:E_prev)
+constexpr int kAdeFields = 6;
+
+// launchers (defined in k2d.cu / k3d.cu / k1d.cu / kdft.cu)
+template <typename T> void launch_e2d(const StepParams<T> &p, int blocks, void *stream);
+template <typename T> void launch_h2d(const StepParams<T> &p, int blocks, void *stream);
+template <typename T> void launch_e3d(const StepParams<T> &p, int blocks, void *stream);
+template <typename T> void launch_h3d(const StepParams<T> &p, int blocks, void *stream);
+
+// separate gather (per-procedure API, or monitors inside reference slabs)
+template <typename T> void launch_gather(const StepParams<T> &p, void *stream);
+
+// DFT fold: acc += sum over valid ring slots of e^{i w t} * sample * dt
+struct DftParams {
+  int nmon;
+  Monitor mon[kMaxMon];
+  const double *omega;     // all monitors' frequencies
+  double *acc_re, *acc_im; // FP64 accumulators
+  int nslots;              // valid slots in this fold (0..kStageSteps)
+  int n0;                  // step number of slot 0
+  double dt;
+  long long stage_row;
+  int total_work_blocks;
+};
+template <typename T> void launch_dft(const DftParams &d, const T *stage, void *stream);
+
+// 1D line: persistent single-block kernel running many steps
+template <typename T>
+struct LineParams {
+  int N;                   // cells
+  int mlo, mhi;            // main range
+  T ku;
+  T *ex, *hz, *dx;         // main line (dx only used for ADE cells)
+  T *exi, *hzi;            // incident line (TFSF) or null
+  int tfsf_bd;             // 0-based TFSF boundary cell (-1 none)
+  const uint8_t *mat;
+  const MatCoef<T> *mc;
+  const AdeCoef<T> *ac;
+  int nade;
+  const int *ade_cell;
+  const uint8_t *ade_mat;
+  T *ade_state;
+  int ade_stride;
+  // reference PML, per side and line (0 main, 1 incident)
+  int slab_on[2];
+  int ja, jb;              // 0-based: low slab rows [0, ja], high [jb, N-1]
+  T *pex[2][2], *phz[2][2];      // [line][side] slab arrays incl. coupling row
+  const T *f1[2][2], *f2[2][2], *g1[2][2], *g2[2][2];
+  // sources: values for every step of the launch
+  int nsrc;
+  Source src[kMaxSrc];
+  const double *srcval;    // [step][src]
+  // sampling
+  int nmon;
+  Monitor mon[kMaxMon];
+  const double *omega;
+  double *acc_re, *acc_im;
+  int nprobe;
+  Probe probe[kMaxProbe];
+  double dt;
+  int n_first, n_steps;
+  int stages;              // bit0: E half, bit1: H half, bit2: sample
+};
+template <typename T> void launch_line1d_stage(const LineParams<T> &p, T *stage, long long stage_row, void *stream);
+
+}  // namespace fdtd

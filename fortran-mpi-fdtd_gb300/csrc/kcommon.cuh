@@ -1,0 +1,144 @@
+// kcommon.cuh -- device helpers shared by the 2D and 3D half-step kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fdtd_internal.h"
+
+namespace fdtd {
+
+// Neighbour loads across a face of the domain: wrapped when the axis is
+// periodic (the reference's interchange_E/H with PBC), zero otherwise (the
+// halo cells the reference never writes).
+template <typename T>
+__device__ __forceinline__ T ld_x(const T *a, int i, int j, int nx, int per) {
+  if (i < 0) return per ? a[(long long)j * nx + (nx - 1)] : T(0);
+  if (i >= nx) return per ? a[(long long)j * nx] : T(0);
+  return a[(long long)j * nx + i];
+}
+template <typename T>
+__device__ __forceinline__ T ld_y(const T *a, int i, int j, int nx, int ny, int per) {
+  if (j < 0) return per ? a[(long long)(ny - 1) * nx + i] : T(0);
+  if (j >= ny) return per ? a[i] : T(0);
+  return a[(long long)j * nx + i];
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_left(T v, int lane) {
+  return __shfl_up_sync(0xffffffffu, v, 1);
+}
+template <typename T>
+__device__ __forceinline__ T shfl_right(T v, int lane) {
+  return __shfl_down_sync(0xffffffffu, v, 1);
+}
+
+template <typename T>
+__device__ __forceinline__ bool in_shell2(const StepParams<T> &p, int i, int j) {
+  return i < p.slo[0] || i > p.shi[0] || j < p.slo[1] || j > p.shi[1];
+}
+template <typename T>
+__device__ __forceinline__ bool in_shell3(const StepParams<T> &p, int i, int j, int k) {
+  return i < p.slo[0] || i > p.shi[0] || j < p.slo[1] || j > p.shi[1] || k < p.slo[2] || k > p.shi[2];
+}
+template <typename T>
+__device__ __forceinline__ bool in_main2(const StepParams<T> &p, int i, int j) {
+  return i >= p.mlo[0] && i <= p.mhi[0] && j >= p.mlo[1] && j <= p.mhi[1];
+}
+template <typename T>
+__device__ __forceinline__ bool in_main3(const StepParams<T> &p, int i, int j, int k) {
+  return i >= p.mlo[0] && i <= p.mhi[0] && j >= p.mlo[1] && j <= p.mhi[1] && k >= p.mlo[2] && k <= p.mhi[2];
+}
+
+// Sum of this step's soft-source values driving component `comp` at a cell
+// (3D/.../program.f90:396-406: D += gauss_t*n_air on the source plane).
+template <typename T>
+__device__ __forceinline__ T src_sum(const StepParams<T> &p, int comp, int i, int j, int k) {
+  T s = T(0);
+  for (int q = 0; q < p.nsrc; ++q) {
+    const Source &sr = p.src[q];
+    if (sr.comp == comp && i >= sr.lo[0] && i <= sr.hi[0] && j >= sr.lo[1] && j <= sr.hi[1] &&
+        k >= sr.lo[2] && k <= sr.hi[2])
+      s += T(p.srcval[q]);
+  }
+  return s;
+}
+
+// One E component of a dispersive cell.  `inc` is this step's D increment
+// (Ku*curl + source).  Gold (2D/gold_mod.f90:57-71, 3D/gold_mod.f90:61-82):
+//   E = Re[(D - I + ha S + gb1 g1 + gb2 g2) / ga];  I += hb E;
+//   S = ha S + hb E;  g_p = gb_p g_p + gc_p E
+// with Q = D - I kept instead of D and I (Q += inc - hb E).
+// Graphene sheet (1D/graphene633_mod.f90:33-41, 3D/graphene_mod.f90:70-76):
+//   E = (Q + ha S + 2 kerr E^3) / (ga + S_R + 3 kerr E^2), Raman recursion.
+template <typename T>
+__device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int comp, const AdeCoef<T> &a,
+                                               T inc, T eold) {
+  T *q_ = st + (0 * 3 + comp) * (long long)stride + slot;
+  T *s_ = st + (1 * 3 + comp) * (long long)stride + slot;
+  T *f2 = st + (2 * 3 + comp) * (long long)stride + slot;
+  T *f3 = st + (3 * 3 + comp) * (long long)stride + slot;
+  T Q = *q_ + inc;
+  T S = *s_;
+  if (a.kind == MK_GOLD) {
+    T *f4 = st + (4 * 3 + comp) * (long long)stride + slot;
+    T *f5 = st + (5 * 3 + comp) * (long long)stride + slot;
+    const T g1r = *f2, g1i = *f3, g2r = *f4, g2i = *f5;
+    const T p1r = a.gb1r * g1r - a.gb1i * g1i, p1i = a.gb1r * g1i + a.gb1i * g1r;
+    const T p2r = a.gb2r * g2r - a.gb2i * g2i, p2i = a.gb2r * g2i + a.gb2i * g2r;
+    const T nre = ((Q + a.ha * S) + p1r) + p2r;
+    const T nim = p1i + p2i;
+    const T e = nre * a.wr - nim * a.wi;
+    *q_ = Q - a.hb * e;
+    *s_ = a.ha * S + a.hb * e;
+    *f2 = p1r + a.gc1r * e;
+    *f3 = p1i + a.gc1i * e;
+    *f4 = p2r + a.gc2r * e;
+    *f5 = p2i + a.gc2i * e;
+    return e;
+  }
+  // graphene
+  if (comp == a.normal) {  // out-of-plane component: vacuum, E = D
+    *q_ = Q;
+    return eold + inc;
+  }
+  const T srm1 = *f2, srm2 = *f3;
+  const T num = (Q + a.ha * S) + T(2) * a.kerr * (eold * eold * eold);
+  const T den = (a.ga + srm1) + T(3) * a.kerr * (eold * eold);
+  const T e = num / den;
+  const T sr = a.r1 * srm1 + a.r2 * srm2 + a.r0 * (e * e);
+  *f3 = srm1;
+  *f2 = sr;
+  *q_ = Q - a.hb * e;
+  *s_ = a.ha * S + a.hb * e;
+  return e;
+}
+
+template <typename T>
+__device__ __forceinline__ T ade_update(const StepParams<T> &p, const AdeCoef<T> &a, int slot, int comp, T inc,
+                                         T eold) {
+  return ade_update_state<T>(p.ade_state, p.ade_stride, slot, comp, a, inc, eold);
+}
+
+// Fused sampling: write the monitored components of cell (i,j,k) into this
+// step's stage row, and probe samples.  vals[c] = value of component c.
+template <typename T>
+__device__ __forceinline__ void gather_cell(const StepParams<T> &p, int i, int j, int k, const T *vals) {
+  for (int q = 0; q < p.nmon; ++q) {
+    const Monitor &m = p.mon[q];
+    if (i < m.lo[0] || i > m.hi[0] || j < m.lo[1] || j > m.hi[1] || k < m.lo[2] || k > m.hi[2]) continue;
+    const int wx = m.hi[0] - m.lo[0] + 1, wy = m.hi[1] - m.lo[1] + 1;
+    const long long idx = (long long)(i - m.lo[0]) + (long long)wx * ((j - m.lo[1]) + (long long)wy * (k - m.lo[2]));
+    T *row = p.stage + (long long)p.slot * p.stage_row + m.base;
+    for (int u = 0; u < m.ncomp; ++u) row[(long long)u * m.ncell + idx] = vals[m.comps[u]];
+  }
+  for (int q = 0; q < p.nprobe; ++q) {
+    const Probe &pr = p.probe[q];
+    if (i != pr.cell[0] || j != pr.cell[1] || k != pr.cell[2]) continue;
+    if (p.n < pr.n_first || p.n > pr.n_last) continue;
+    const long long st = p.n - pr.n_first;
+    if (st >= pr.cap) continue;
+    double *out = pr.buf + st * pr.ncomp;
+    for (int u = 0; u < pr.ncomp; ++u) out[u] = (double)vals[pr.comps[u]];
+  }
+}
+
+}  // namespace fdtd

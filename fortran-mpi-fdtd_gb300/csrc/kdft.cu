@@ -1,0 +1,134 @@
+// kdft.cu -- running DFT of the monitored cells and the stand-alone gather.
+//
+// The reference accumulates, every step and for every monitored cell and
+// frequency (2D/.../program.f90:383-391, 3D/.../program.f90:456-472):
+//   re += cos(arg(m) t) F dt,  im += sin(arg(m) t) F dt,  t = (n-1) dt.
+// Here the half-step kernels stage F for kStageSteps steps and this kernel
+// folds the whole ring at once: each thread owns one (component, cell)
+// sample, holds its kStageSteps values in registers, and for a chunk of
+// frequencies adds sum_s cos(w t_s) F_s (and sin) into the FP64
+// accumulators.  Phases are computed in FP64 (sincos of w*t); the products
+// and the ring sum run in the job's precision; the accumulators are FP64.
+// Slots outside a monitor's [n_first, n_last] get zero weight.
+#include <cuda_runtime.h>
+
+#include "fdtd_internal.h"
+
+namespace fdtd {
+
+constexpr int kDftThreads = 256;
+constexpr int kFreqChunk = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kDftThreads) dft_kernel(const __grid_constant__ DftParams d, const T *__restrict__ stage) {
+  __shared__ T cw[kFreqChunk][kStageSteps];
+  __shared__ T sw[kFreqChunk][kStageSteps];
+  // locate (monitor, freq chunk, sample block) of this block
+  int b = blockIdx.x, q = 0, sblocks = 0, fchunks = 0;
+  for (q = 0; q < d.nmon; ++q) {
+    const Monitor &m = d.mon[q];
+    sblocks = (m.ncomp * m.ncell + kDftThreads - 1) / kDftThreads;
+    fchunks = (m.nfreq + kFreqChunk - 1) / kFreqChunk;
+    if (b < sblocks * fchunks) break;
+    b -= sblocks * fchunks;
+  }
+  if (q >= d.nmon) return;
+  const Monitor &m = d.mon[q];
+  // skip the fold when no slot of it lies in the monitor's step window
+  const int nlast = d.n0 + d.nslots - 1;
+  if (nlast < m.n_first || d.n0 > m.n_last) return;
+  const int fc = b / sblocks, sb = b % sblocks;
+  const int f0 = fc * kFreqChunk;
+  for (int t = threadIdx.x; t < kFreqChunk * kStageSteps; t += kDftThreads) {
+    const int f = t / kStageSteps, s = t % kStageSteps;
+    double c = 0.0, sn = 0.0;
+    const int n = d.n0 + s;
+    if (f0 + f < m.nfreq && s < d.nslots && n >= m.n_first && n <= m.n_last) {
+      const double tt = (double)(n - 1) * d.dt;          // t=real(n-1,8)*dt
+      sincos(d.omega[m.freq_off + f0 + f] * tt, &sn, &c);
+    }
+    cw[f][s] = T(c);
+    sw[f][s] = T(sn);
+  }
+  __syncthreads();
+  const long long p = (long long)sb * kDftThreads + threadIdx.x;
+  const long long nsamp = (long long)m.ncomp * m.ncell;
+  if (p >= nsamp) return;
+  T v[kStageSteps];
+#pragma unroll
+  for (int s = 0; s < kStageSteps; ++s) v[s] = s < d.nslots ? stage[(long long)s * d.stage_row + m.base + p] : T(0);
+  const int u = (int)(p / m.ncell);
+  const long long cell = p % m.ncell;
+  const int nf = min(kFreqChunk, m.nfreq - f0);
+  for (int f = 0; f < nf; ++f) {
+    T sr = T(0), si = T(0);
+#pragma unroll
+    for (int s = 0; s < kStageSteps; ++s) {
+      sr += cw[f][s] * v[s];
+      si += sw[f][s] * v[s];
+    }
+    const long long a = m.acc + ((long long)u * m.nfreq + (f0 + f)) * m.ncell + cell;
+    d.acc_re[a] += (double)sr * d.dt;
+    d.acc_im[a] += (double)si * d.dt;
+  }
+}
+
+template <typename T>
+void launch_dft(const DftParams &d, const T *stage, void *stream) {
+  if (d.total_work_blocks <= 0 || d.nslots <= 0) return;
+  dft_kernel<T><<<d.total_work_blocks, kDftThreads, 0, (cudaStream_t)stream>>>(d, stage);
+}
+
+template void launch_dft<float>(const DftParams &, const float *, void *);
+template void launch_dft<double>(const DftParams &, const double *, void *);
+
+// Stand-alone gather of the monitored cells and probes after the H update:
+// one thread per monitored (component, cell) sample, plus one per probe.
+template <typename T>
+__global__ void gather_kernel(const __grid_constant__ StepParams<T> p) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const T *F[6] = {p.ex, p.ey, p.ez, p.hx, p.hy, p.hz};
+  for (int q = 0; q < p.nmon; ++q) {
+    const Monitor &m = p.mon[q];
+    const long long ns = (long long)m.ncomp * m.ncell;
+    if (t < ns) {
+      const int u = (int)(t / m.ncell);
+      const long long c = t % m.ncell;
+      const int wx = m.hi[0] - m.lo[0] + 1, wy = m.hi[1] - m.lo[1] + 1;
+      const int i = m.lo[0] + (int)(c % wx);
+      const int j = m.lo[1] + (int)((c / wx) % wy);
+      const int k = m.lo[2] + (int)(c / ((long long)wx * wy));
+      const long long cell = (long long)i + (long long)p.nx * (j + (long long)p.ny * k);
+      const T *f = F[m.comps[u]];
+      p.stage[(long long)p.slot * p.stage_row + m.base + t] = f ? f[cell] : T(0);
+      return;
+    }
+    t -= ns;
+  }
+  if (t < p.nprobe) {
+    const Probe &pr = p.probe[t];
+    if (p.n < pr.n_first || p.n > pr.n_last) return;
+    const long long st = p.n - pr.n_first;
+    if (st >= pr.cap) return;
+    const long long cell = (long long)pr.cell[0] + (long long)p.nx * (pr.cell[1] + (long long)p.ny * pr.cell[2]);
+    for (int u = 0; u < pr.ncomp; ++u) {
+      const T *f = F[pr.comps[u]];
+      pr.buf[st * pr.ncomp + u] = f ? (double)f[cell] : 0.0;
+    }
+  }
+}
+
+template <typename T>
+void launch_gather(const StepParams<T> &p, void *stream) {
+  long long total = p.nprobe;
+  for (int q = 0; q < p.nmon; ++q) total += (long long)p.mon[q].ncomp * p.mon[q].ncell;
+  if (total <= 0) return;
+  const int threads = 256;
+  const long long blocks = (total + threads - 1) / threads;
+  gather_kernel<T><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(p);
+}
+
+template void launch_gather<float>(const StepParams<float> &, void *);
+template void launch_gather<double>(const StepParams<double> &, void *);
+
+}  // namespace fdtd

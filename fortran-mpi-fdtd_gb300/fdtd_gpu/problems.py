@@ -354,13 +354,16 @@ def config_2d_tmz(precision=abi.F32, n=2048, steps=10000, ncyl=40, nfreq=100, np
                    name="config_2d_tmz")
     spec.add_dielectric(box((0, 0, 0), (n - 1, n - 1, 0)), 1.0)
     scale = n / 2048.0
-    cyl = cylinders_2d(n=n, count=ncyl, ylo=int(200 * scale), yhi=int(1948 * scale), pml=npml,
+    cyl = cylinders_2d(n=n, count=ncyl, ylo=max(int(200 * scale), npml + 12), yhi=min(int(1948 * scale), n - npml - 4), pml=npml,
                        rmin=max(2, int(10 * scale)), rmax=max(3, int(40 * scale))) if ncyl else []
     if cyl:
         spec.add_gold(spheres(cyl), GOLD_CONFIG)
     spec.pml = dict(mode=abi.PML_SPLIT, npml=((npml, npml), (npml, npml), (0, 0)),
                     eps_lo=1.0, sigma_max=sigmam, order=order)
-    ys, yin, yt = int(100 * scale), int(200 * scale), int(1948 * scale)
+    # positions of the 2048^2 layout, scaled; at reduced sizes kept clear of the PML
+    ys = max(int(100 * scale), npml + 4)
+    yin = max(int(200 * scale), ys + 8)
+    yt = min(int(1948 * scale), n - npml - 4)
     spec.sources.append(dict(component=abi.EZ, lo=(0, ys, 0), hi=(n - 1, ys, 0), amp=1.0, **_pulse(600e-9)))
     arg = dft_omegas(500e-9, 800e-9, nfreq)
     dist = ds * float(yin + 8 - ys) + 4.5 * 600e-9
@@ -385,7 +388,7 @@ def config_3d_sphere(precision=abi.F32, n=512, steps=8000, nfreq=64, npml=16, ra
     c = n / 2.0
     spec.add_gold(spheres([(c, c, c, radius * n / 512.0)]), GOLD_CONFIG)
     spec.pml = dict(mode=abi.PML_SPLIT, npml=((npml, npml),) * 3, eps_lo=1.0, sigma_max=sigmam, order=order)
-    zs = int(40 * n / 512)
+    zs = max(int(40 * n / 512), npml + 4)
     spec.sources.append(dict(component=abi.EX, lo=(0, 0, zs), hi=(n - 1, n - 1, zs), amp=1.0, **_pulse(600e-9)))
     arg = dft_omegas(500e-9, 800e-9, nfreq)
     h = int(half * n / 512)

@@ -733,7 +733,7 @@ static void apply_sources(ora_job *J, int n, int incident) {
     for (int k = s->lo[2]; k <= s->hi[2]; k++)
       for (int j = s->lo[1]; j <= s->hi[1]; j++)
         for (int i = s->lo[0]; i <= s->hi[0]; i++) {
-          if (!inc && J->pml_mode == FDTD_PML_SPLIT && !in_main(J, i, j, k)) continue;
+          if (!inc && !in_main(J, i, j, k)) continue;   /* D is only updated on main cells */
           int64_t c = cell_ix(J, i, j, k);
           if (inc) D[c] = D[c] + g;                  /* ex_inc=ex_inc+gauss_t (P1/program.f90:229) */
           else D[c] = D[c] + g * s->amp;             /* Dx=Dx+gauss_t*n_air (P3/program.f90:403) */

@@ -1,0 +1,201 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle and
+against the reference's own shipped 2D outputs.
+
+FP64 plain path: relative L2 <= 1e-10 on fields, DFT sums and spectra.
+FP32 path: DFT spectra relative L2 <= 1e-4 against the FP64 oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from fdtd_gpu import abi, problems
+
+pytestmark = pytest.mark.gpu
+
+NTH = os.cpu_count() or 1
+TOL64 = 1e-10
+TOL32_DFT = 1e-4
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from fdtd_gpu import build, job
+    build.build()
+    if job.device_count() < 1:
+        pytest.skip("no sm_103a device")
+    return job
+
+
+def golden():
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_2d_ref.npz"))
+
+
+# ---------------------------------------------------------------------------
+# 2D reference program: full 13696-step run against the shipped outputs
+# ---------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def run2d_gpu(gpu):
+    spec, meta = problems.reference_2d()
+    J = gpu.Job(spec)
+    ic = meta["ic"] - 1
+    liney = np.zeros((20, meta["ny"], 2))
+    maps = {}
+    n = 0
+    for f in range(1, 21):
+        target = f * meta["dn"]
+        J.step(n + 1, target - n)
+        n = target
+        ex = J.get_field(abi.EX)[0]
+        hz = J.get_field(abi.HZ)[0]
+        liney[f - 1, :, 0] = ex[:, ic]
+        liney[f - 1, :, 1] = hz[:, ic]
+        if f in (1, 20):
+            maps[f] = hz.copy()
+    J.step(n + 1, meta["Nt"] - n)
+    out = dict(meta=meta, liney=liney, maps=maps, job=J)
+    out["mon"] = [J.get_monitor(q) for q in range(3)]
+    out["probe"] = [J.get_probe(q) for q in range(3)]
+    return out
+
+
+def test_2d_reference_spectra_match_shipped_outputs(run2d_gpu):
+    g = golden()
+    ds = run2d_gpu["meta"]["ds"]
+    for q, key in enumerate(("syin", "syr", "syt")):
+        sy = problems.poynting_2d_te(*run2d_gpu["mon"][q], ds)
+        assert rel_l2(sy, g[key][:, 1]) <= TOL64, key
+    sy = [problems.poynting_2d_te(*run2d_gpu["mon"][q], ds) for q in range(3)]
+    rta = np.stack([-sy[1] / sy[0], sy[2] / sy[0]], 1)
+    assert np.max(np.abs(rta - g["rta"][:, 1:3])) <= 1e-10
+
+
+def test_2d_reference_fields_match_shipped_outputs(run2d_gpu):
+    g = golden()
+    for f in range(20):
+        assert rel_l2(run2d_gpu["liney"][f], g["liney"][f]) <= TOL64, f
+    for q, f in enumerate(g["map_frames"]):
+        assert rel_l2(run2d_gpu["maps"][int(f)], g["maps"][q]) <= TOL64
+    assert rel_l2(run2d_gpu["probe"][0], g["infld"][:, 1:]) <= TOL64
+    assert rel_l2(run2d_gpu["probe"][2], g["tfld"][:, 1:]) <= TOL64
+    assert rel_l2(run2d_gpu["probe"][1], g["rfld"][:, 1:]) <= 1e-9  # F30.19 print precision
+
+
+def test_2d_per_procedure_path_equals_fused(gpu):
+    spec, meta = problems.reference_2d()
+    a, b = gpu.Job(spec), gpu.Job(spec)
+    a.step(1, 700)
+    for n in range(1, 701):
+        b.step_procedures(n)
+    for c in (abi.EX, abi.EY, abi.HZ):
+        np.testing.assert_array_equal(a.get_field(c), b.get_field(c))
+    for q in range(3):
+        for x, y in zip(a.get_monitor(q), b.get_monitor(q)):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_2d_reference_deterministic(gpu):
+    spec, _ = problems.reference_2d()
+    a, b = gpu.Job(spec), gpu.Job(spec)
+    a.step(1, 1500)
+    b.step(1, 1500)
+    np.testing.assert_array_equal(a.get_field(abi.HZ), b.get_field(abi.HZ))
+    np.testing.assert_array_equal(a.get_monitor(0)[0], b.get_monitor(0)[0])
+
+
+# ---------------------------------------------------------------------------
+# 3D and 1D reference programs against the oracle
+# ---------------------------------------------------------------------------
+def test_3d_reference_vs_oracle(gpu, oracle_lib):
+    spec, meta = problems.reference_3d()
+    steps = 700
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec, nthreads=NTH)
+    J.step(1, steps)
+    O.step(1, steps)
+    for c in (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ):
+        assert rel_l2(J.get_field(c), O.get_field(c)) <= TOL64, c
+    for q in (0, 2):
+        for x, y in zip(J.get_monitor(q), O.get_monitor(q)):
+            assert rel_l2(x, y) <= TOL64
+    for q in range(2):
+        assert rel_l2(J.get_probe(q), O.get_probe(q)) <= TOL64
+
+
+def test_1d_reference_vs_oracle(gpu, oracle_lib):
+    spec, meta = problems.reference_1d()
+    steps = 12000
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec)
+    J.step(1, steps)
+    O.step(1, steps)
+    for c in (abi.EX, abi.HZ, abi.EX_INC, abi.HZ_INC):
+        assert rel_l2(J.get_field(c), O.get_field(c)) <= TOL64, c
+    for q in range(2):
+        for x, y in zip(J.get_monitor(q), O.get_monitor(q)):
+            assert rel_l2(x, y) <= TOL64
+        assert rel_l2(J.get_probe(q), O.get_probe(q)) <= TOL64
+
+
+# ---------------------------------------------------------------------------
+# benchmark workloads at reduced size: FP64 plain and FP32 against the oracle
+# ---------------------------------------------------------------------------
+def _dft_err(J, O, nmon):
+    errs = []
+    for q in range(nmon):
+        (jr, ji), (orr, oi) = J.get_monitor(q), O.get_monitor(q)
+        errs.append(rel_l2(np.concatenate([jr.ravel(), ji.ravel()]), np.concatenate([orr.ravel(), oi.ravel()])))
+    return max(errs)
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+def test_2d_tmz_cylinders_vs_oracle(gpu, oracle_lib, prec):
+    spec, meta = problems.config_2d_tmz(precision=prec, n=384, ncyl=8, nfreq=24)
+    steps = 2500
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64))
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, 3)
+    if prec == abi.F64:
+        assert err <= TOL64
+        for c in (abi.EZ, abi.HX, abi.HY):
+            assert rel_l2(J.get_field(c), O.get_field(c)) <= TOL64, c
+    else:
+        assert err <= TOL32_DFT
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+def test_3d_sphere_vs_oracle(gpu, oracle_lib, prec):
+    spec, meta = problems.config_3d_sphere(precision=prec, n=96, nfreq=8, npml=8, radius=40.0, half=20)
+    steps = 600
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, 6)
+    if prec == abi.F64:
+        assert err <= TOL64
+        for c in (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ):
+            assert rel_l2(J.get_field(c), O.get_field(c)) <= TOL64, c
+    else:
+        assert err <= TOL32_DFT
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+def test_1d_gold_slab_vs_oracle(gpu, oracle_lib, prec):
+    spec, meta = problems.config_1d_gold(precision=prec)
+    steps = 20000
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64))
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, 3)
+    assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)
