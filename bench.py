@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""Benchmark of the FDTD time-step engine on the 2D TMz workload.
+
+Workload (default): 2D TMz, 2048 x 2048 cells, dx = 1 nm, Courant 0.5,
+32-cell split-field PML on all faces, 40 seeded gold cylinders (Drude +
+2 critical points), Ez line source at y=100 (600 nm pulse), line DFT monitors
+of Ez and Hx at y=200 (incident / reflected, gated) and y=1948 (transmitted)
+with 100 frequencies, 10000 time steps.  Synthetic, seeded geometry.
+
+One bench "step" is one whole job of that workload (10000 time steps from
+a fresh state) with its inputs already resident in HBM.  The headline value
+is Mcell-updates/s of the FP32 path (FP64 DFT accumulation); the FP64 plain
+path, the FP32/FP64 ratio and the FP32 DFT error against the FP64 path are
+reported beside it, with the dominant kernel's roofline, an end-to-end
+figure through the C ABI with host buffers, and a CPU baseline (the FP64
+oracle on the host cores).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fortran-mpi-fdtd_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mcell-updates/s FP32 vs FP64 plain at <=1e-4 DFT rel err; serve p50/p99 latency"
+UNIT = "Mcell-updates/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nt", type=int, default=10000, help="time steps per job")
+    ap.add_argument("--n", type=int, default=2048, help="grid cells per side")
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload(n, nt, precision):
+    from fdtd_gpu import problems
+    spec, meta = problems.config_2d_tmz(precision=precision, n=n, steps=nt)
+    return spec, meta
+
+
+def workload_name(n, nt):
+    return f"2d_tmz_{n}x{n}_40cyl_splitpml32_{nt}steps"
+
+
+# ---- bytes each kernel must move per cell (FP32 / FP64 word size w) --------
+# E kernel: read Hx, Hy, Ez, material id; write Ez        -> 4w + 1
+# H kernel: read Ez, Hx, Hy; write Hx, Hy                  -> 5w
+# whole step, each field read and written once (+ id)      -> 6w + 1
+def alg_bytes(kind, w):
+    return {"E": 4 * w + 1, "H": 5 * w, "step": 6 * w + 1}[kind]
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """dram bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_2d_tmz.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None, None
+    m = re.search(r"traffic_bytes_per_full_launch:\s*([0-9.eE+]+)", txt)
+    return (float(m.group(1)) if m else None), os.path.relpath(path, ROOT)
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(n, seconds, nthreads=None):
+    """The FP64 oracle (reference algorithm on the CPU) on the host cores over a
+    bounded sample of the same workload: chunks of time steps until `seconds`."""
+    from fdtd_gpu import abi
+    from oracle.pyoracle import OracleJob, build
+    build()
+    nth = nthreads or os.cpu_count() or 1
+    spec, meta = workload(n, 10000, abi.F64)
+    O = OracleJob(spec, nthreads=nth)
+    O.step(1, 4)  # touch memory
+    done, t0 = 0, time.perf_counter()
+    while True:
+        O.step(5 + done, 10)
+        done += 10
+        el = time.perf_counter() - t0
+        if el >= seconds or done >= 2000:
+            break
+    value = spec.cells() * done / el / 1e6
+    return {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"FP64 oracle, {done} time steps of the {n}x{n} workload on {nth} host threads ({el:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from fdtd_gpu import abi
+    from oracle.pyoracle import OracleJob, build
+    build()
+    nth = os.cpu_count() or 1
+    spec, meta = workload(args.n, 10000, abi.F64)
+    O = OracleJob(spec, nthreads=nth)
+    per_step = 20  # time steps of the workload per bench step (bounded sample)
+    n = 1
+    for _ in range(args.warmup):
+        O.step(n, per_step)
+        n += per_step
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.step(n, per_step)
+        times.append(time.perf_counter() - t0)
+        n += per_step
+    tot = sum(times)
+    value = spec.cells() * per_step * args.steps / tot / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": workload_name(args.n, per_step),
+                                            "note": f"each bench step = {per_step} time steps of the workload"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": f"FP64 oracle (the reference's algorithm restated in C; the Fortran/MPI "
+                                       f"reference needs gfortran+MPI, absent on this box), {per_step} time steps "
+                                       f"per bench step on {nth} host threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+    from fdtd_gpu import abi
+    from fdtd_gpu import job as gj
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed_jobs(precision, k, warm):
+        spec, meta = workload(args.n, args.nt, precision)
+        jobs = [gj.Job(spec) for _ in range(warm + k)]
+        for j in jobs:
+            j.set_stream(stream.cuda_stream)
+        for j in jobs[:warm]:
+            flush.zero_()
+            j.step(1, args.nt)
+            j.sync()
+        for j in jobs[warm:]:
+            j.profile(True)
+        barrier()
+        torch.cuda.synchronize()
+        evs = []
+        launches0 = sum(j.launch_count() for j in jobs[warm:])
+        clk = Clocks(local)
+        clk.start()
+        for j in jobs[warm:]:
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            j.step(1, args.nt)
+            j.sync()  # folds the last DFT ring
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        clocks = clk.stop()
+        barrier()
+        ms = [a.elapsed_time(b) for a, b in evs]
+        launches = sum(j.launch_count() for j in jobs[warm:]) - launches0
+        kt = {}
+        for kind, name in ((abi.KERNEL_E, "E"), (abi.KERNEL_H, "H"), (abi.KERNEL_DFT, "DFT")):
+            cnt, tot = 0, 0.0
+            for j in jobs[warm:]:
+                c, t = j.kernel_time(kind)
+                cnt += c
+                tot += t
+            kt[name] = (cnt, tot)
+        return spec, meta, jobs[warm:], ms, launches, kt, clocks
+
+    # ---- FP32 (headline) ----
+    spec32, meta, jobs32, ms32, launches, kt32, clocks = timed_jobs(abi.F32, args.steps, args.warmup)
+    t_step = max(ms32) if False else sum(ms32) / len(ms32)
+    if world > 1:
+        t = torch.tensor([t_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    cells = spec32.cells()
+    value = world * cells * args.nt / (t_step / 1e3) / 1e6
+
+    # ---- FP64 plain ----
+    spec64, _, jobs64, ms64, _, kt64, _ = timed_jobs(abi.F64, args.fp64_steps, 1)
+    t64 = sum(ms64) / len(ms64)
+    value64 = world * cells * args.nt / (t64 / 1e3) / 1e6
+
+    # ---- DFT error FP32 vs FP64 (same job, same steps) ----
+    num = den = 0.0
+    for q in range(len(spec32.monitors)):
+        r32, i32 = jobs32[0].get_monitor(q)
+        r64, i64 = jobs64[0].get_monitor(q)
+        num += float(np.sum((r32 - r64) ** 2) + np.sum((i32 - i64) ** 2))
+        den += float(np.sum(r64 ** 2) + np.sum(i64 ** 2))
+    dft_err = math.sqrt(num / den) if den > 0 else float("nan")
+
+    # ---- roofline of the dominant kernel (FP32) ----
+    dom = "E" if kt32["E"][1] >= kt32["H"][1] else "H"
+    cnt, tot = kt32[dom]
+    avg_s = (tot / cnt) / 1e3
+    bpl = cells * alg_bytes(dom, 4)
+    achieved = bpl / avg_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic, tr_src = profile_traffic(dom)
+    roof = {"bound": "hbm", "kernel": f"{dom.lower()}2d_kernel<float,TM>", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+            "alg_bytes_per_launch": bpl, "avg_launch_us": avg_s * 1e6,
+            "note": "algorithmic bytes = cells x (4w+1) for E, 5w for H; working set ~0.1 GB is L2-resident "
+                    "(129 MB L2), so the frac can exceed 1 against HBM"}
+    if tr_src:
+        roof["traffic_source"] = tr_src
+    step_bw = cells * alg_bytes("step", 4) / (t_step / 1e3 / args.nt) / 1e9
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_runs = 2
+    t_e2e, h2d, d2h = [], 0, 0
+    for _ in range(e2e_runs):
+        torch.cuda.synchronize()
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J = gj.Job(spec32)              # host geometry -> device
+        J.step(1, args.nt)
+        outs = [J.get_monitor(q) for q in range(len(spec32.monitors))]  # spectra -> host
+        t_e2e.append(time.perf_counter() - t0)
+        h2d, d2h = J.transfer_bytes()
+        J.close()
+    e2e_value = world * cells * args.nt / (sum(t_e2e) / len(t_e2e)) / 1e6
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(args.n, args.nt), "cells": cells, "time_steps_per_job": args.nt,
+                   "bench_step": "one job of the workload from a fresh state",
+                   "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed jobs",
+                   "parallelism": f"replicas x{world}"},
+        "fp64_plain": {"value": value64, "ms_per_step": t64, "steps": len(ms64)},
+        "fp32_over_fp64": value / value64,
+        "dft_rel_err_fp32_vs_fp64": dft_err,
+        "step_bandwidth_gbs": step_bw,
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "clock": "host wall clock around create+commit, all time steps and the spectra download"},
+        "gpu_launches": launches,
+        "kernel_ms_fp32": {k: {"launches": v[0], "ms": v[1]} for k, v in kt32.items()},
+        "kernel_ms_fp64": {k: {"launches": v[0], "ms": v[1]} for k, v in kt64.items()},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -122,7 +122,7 @@ struct fdtd_job {
   void *d_ade_state = nullptr;
   int slo[3] = {0, 0, 0}, shi[3] = {0, 0, 0};
   void *d_cf[4][3] = {};   // f1 f2 g1 g2 per axis (split PML)
-  void *d_sp[6] = {};
+  void *d_sp[12] = {};
   int slab_rows = 0, slab_on[2] = {0, 0}, slab_j0[2] = {0, 0};
   void *d_slab[2][12] = {};
   void *d_sc[2][12] = {};  // sf1x sf2x sg1x sg2x sf1y sf2y sg1y sg2y sf1z sf2z sg1z sg2z
@@ -151,6 +151,8 @@ struct fdtd_job {
   long long kcount[FDTD_KERNEL_COUNT] = {};
   double kms[FDTD_KERNEL_COUNT] = {};
   long long launches = 0;
+  cudaStream_t own_stream = nullptr;
+  uint64_t h2d = 0, d2h = 0;
 };
 
 namespace {
@@ -172,6 +174,7 @@ int upload_vec(fdtd_job *J, void **dst, const std::vector<double> &v) {
   int rc = alloc_dev(J, dst, t.size() * sizeof(T));
   if (rc) return rc;
   CK(cudaMemcpy(*dst, t.data(), t.size() * sizeof(T), cudaMemcpyHostToDevice));
+  J->h2d += t.size() * sizeof(T);
   return FDTD_OK;
 }
 
@@ -414,8 +417,10 @@ int commit_impl(fdtd_job *J) {
   }
   if ((rc = alloc_dev(J, (void **)&J->d_mat, (size_t)N))) return rc;
   CK(cudaMemcpy(J->d_mat, mat.data(), (size_t)N, cudaMemcpyHostToDevice));
+  J->h2d += (uint64_t)N;
   if ((rc = alloc_dev(J, &J->d_mc, sizeof(MatCoef<T>) * kMaxMat))) return rc;
   CK(cudaMemcpy(J->d_mc, mc.data(), sizeof(MatCoef<T>) * kMaxMat, cudaMemcpyHostToDevice));
+  J->h2d += sizeof(MatCoef<T>) * kMaxMat + sizeof(AdeCoef<T>) * ac.size();
   if ((rc = alloc_dev(J, &J->d_ac, sizeof(AdeCoef<T>) * std::max<size_t>(1, ac.size())))) return rc;
   if (!ac.empty()) CK(cudaMemcpy(J->d_ac, ac.data(), sizeof(AdeCoef<T>) * ac.size(), cudaMemcpyHostToDevice));
   // ---- ADE slots (dispersive cells) ----
@@ -439,6 +444,7 @@ int commit_impl(fdtd_job *J) {
   if (J->nade) {
     CK(cudaMemcpy(J->d_ade_cell, ade_cell.data(), sizeof(int) * J->nade, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(J->d_ade_mat, ade_mat.data(), J->nade, cudaMemcpyHostToDevice));
+    J->h2d += (uint64_t)J->nade * (sizeof(int) + 1);
   }
   if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)kAdeFields * 3 * std::max(32, J->ade_stride)))) return rc;
   // ---- PML ----
@@ -457,9 +463,11 @@ int commit_impl(fdtd_job *J) {
       if ((rc = upload_prof<T>(J, P, &J->d_cf[0][a], &J->d_cf[1][a], &J->d_cf[2][a], &J->d_cf[3][a]))) return rc;
     }
     const int nsp = J->dim == 3 ? 6 : 1;
-    for (int q = 0; q < nsp; ++q)
+    const bool two = sizeof(T) == 8;
+    for (int q = 0; q < nsp; ++q) {
       if ((rc = alloc_dev(J, &J->d_sp[q], (size_t)N * sizeof(T)))) return rc;
-    if (J->dim == 2) J->d_sp[3] = J->d_sp[0];  // unused alias keeps pointers valid
+      if (two && (rc = alloc_dev(J, &J->d_sp[6 + q], (size_t)N * sizeof(T)))) return rc;
+    }
   }
   if (ref && J->dim >= 2) {
     const fdtd_pml_desc &p = J->pml;
@@ -554,6 +562,7 @@ int commit_impl(fdtd_job *J) {
   if (!omega.empty()) {
     if ((rc = alloc_dev(J, (void **)&J->d_omega, omega.size() * sizeof(double)))) return rc;
     CK(cudaMemcpy(J->d_omega, omega.data(), omega.size() * sizeof(double), cudaMemcpyHostToDevice));
+    J->h2d += omega.size() * sizeof(double);
   }
   if ((rc = alloc_dev(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
   if ((rc = alloc_dev(J, (void **)&J->d_acc_im, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
@@ -603,7 +612,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.cf1[a] = (const T *)J->d_cf[0][a]; p.cf2[a] = (const T *)J->d_cf[1][a];
     p.cg1[a] = (const T *)J->d_cf[2][a]; p.cg2[a] = (const T *)J->d_cf[3][a];
   }
-  for (int q = 0; q < 6; ++q) p.sp[q] = (T *)J->d_sp[q];
+  for (int q = 0; q < 12; ++q) p.sp[q] = (T *)J->d_sp[q];
   p.slab_rows = J->slab_rows;
   for (int s = 0; s < 2; ++s) {
     p.slab_on[s] = J->slab_on[s];
@@ -950,6 +959,7 @@ static int get_field_impl(fdtd_job *J, int comp, double *host) {
   CK(cudaMemcpyAsync(tmp.data(), J->F[comp], (size_t)J->ncell * sizeof(T), cudaMemcpyDeviceToHost, J->stream));
   CK(cudaStreamSynchronize(J->stream));
   for (long long c = 0; c < J->ncell; ++c) host[c] = (double)tmp[(size_t)c];
+  J->d2h += (uint64_t)J->ncell * sizeof(T);
   return FDTD_OK;
 }
 
@@ -959,6 +969,7 @@ static int set_field_impl(fdtd_job *J, int comp, const double *host) {
   std::vector<T> tmp(host, host + J->ncell);
   CK(cudaMemcpyAsync(J->F[comp], tmp.data(), (size_t)J->ncell * sizeof(T), cudaMemcpyHostToDevice, J->stream));
   CK(cudaStreamSynchronize(J->stream));
+  J->h2d += (uint64_t)J->ncell * sizeof(T);
   return FDTD_OK;
 }
 
@@ -1019,6 +1030,7 @@ int fdtd_create(const fdtd_grid_desc *g, fdtd_job **out) {
     delete J;
     return set_err(FDTD_ECUDA, "cudaStreamCreate failed");
   }
+  J->own_stream = J->stream;
   *out = J;
   return FDTD_OK;
 }
@@ -1031,7 +1043,7 @@ int fdtd_destroy(fdtd_job *J) {
   if (J->d_srcval) cudaFree(J->d_srcval);
   for (auto &e : J->pending) { cudaEventDestroy(e.a); if (e.b) cudaEventDestroy(e.b); }
   for (auto e : J->ev_pool) cudaEventDestroy(e);
-  if (J->stream) cudaStreamDestroy(J->stream);
+  if (J->own_stream) cudaStreamDestroy(J->own_stream);
   delete J;
   return FDTD_OK;
 }
@@ -1247,6 +1259,7 @@ int fdtd_get_monitor(fdtd_job *J, int32_t id, double *re, double *im) {
   const size_t n = (size_t)m.ncomp * m.nfreq * m.ncell;
   if (re) CK(cudaMemcpy(re, J->d_acc_re + m.acc, n * sizeof(double), cudaMemcpyDeviceToHost));
   if (im) CK(cudaMemcpy(im, J->d_acc_im + m.acc, n * sizeof(double), cudaMemcpyDeviceToHost));
+  J->d2h += (uint64_t)((re ? 1 : 0) + (im ? 1 : 0)) * n * sizeof(double);
   return FDTD_OK;
 }
 
@@ -1259,7 +1272,10 @@ int fdtd_get_probe(fdtd_job *J, int32_t id, double *host, int32_t *count) {
   long long cnt = (long long)std::min(P.d.n_last, J->last_n) - P.d.n_first + 1;
   cnt = std::max(0LL, std::min<long long>(cnt, P.cap));
   if (count) *count = (int32_t)cnt;
-  if (host && cnt > 0) CK(cudaMemcpy(host, P.buf, (size_t)cnt * P.ncomp * sizeof(double), cudaMemcpyDeviceToHost));
+  if (host && cnt > 0) {
+    CK(cudaMemcpy(host, P.buf, (size_t)cnt * P.ncomp * sizeof(double), cudaMemcpyDeviceToHost));
+    J->d2h += (uint64_t)cnt * P.ncomp * sizeof(double);
+  }
   return FDTD_OK;
 }
 
@@ -1297,6 +1313,21 @@ int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
 int fdtd_launch_count(const fdtd_job *J, int64_t *launches) {
   if (!J || !launches) return set_err(FDTD_EINVAL, "null argument");
   *launches = J->launches;
+  return FDTD_OK;
+}
+
+int fdtd_set_stream(fdtd_job *J, void *cuda_stream) {
+  if (!J) return set_err(FDTD_EINVAL, "null job");
+  // finish what is queued on the old stream before switching
+  CK(cudaStreamSynchronize(J->stream));
+  J->stream = cuda_stream ? (cudaStream_t)cuda_stream : J->own_stream;
+  return FDTD_OK;
+}
+
+int fdtd_transfer_bytes(const fdtd_job *J, uint64_t *h2d, uint64_t *d2h) {
+  if (!J) return set_err(FDTD_EINVAL, "null job");
+  if (h2d) *h2d = J->h2d;
+  if (d2h) *d2h = J->d2h;
   return FDTD_OK;
 }
 

@@ -103,8 +103,10 @@ struct StepParams {
   // split-field PML on any faces: shell = outside [slo, shi]
   int slo[3], shi[3];
   const T *cf1[3], *cf2[3], *cg1[3], *cg2[3];   // per-axis tables (len n[a])
-  T *sp[6];                // stored sub-fields (3D: Exy Eyz Ezx Hxy Hyz Hzx;
-                           // 2D TM: Ezx; 2D TE: Hzx)
+  T *sp[12];               // stored sub-fields (3D: Exy Eyz Ezx Hxy Hyz Hzx;
+                           // 2D TM: Ezx; 2D TE: Hzx).  FP64 also stores the
+                           // other parts in sp[6+q] (Exz Eyx Ezy Hxz Hyx Hzy /
+                           // Ezy / Hzy); FP32 takes them as total - part.
   // reference y-slabs (2D: Ex Ey Hzx Hzy; 3D: 12 split arrays) per side
   int slab_on[2];
   int slab_j0[2];          // first 0-based row of the slab

@@ -53,10 +53,11 @@ struct K2 {
           if (p.roles & ROLE_PML) {
             // Ez = Ezx + Ezy, Ezx stored (3D/BERpmly_mod.f90:151,153 with d/dz = 0)
             const T ezx = p.sp[0][c];
-            const T ezy = p.ez[c] - ezx;
+            const T ezy = kTwoParts<T> ? p.sp[6][c] : p.ez[c] - ezx;
             const T nezx = p.cf1[0][i] * ezx + p.cf2[0][i] * dxpart;
             const T nezy = p.cf1[1][j] * ezy + p.cf2[1][j] * dypart;
             p.sp[0][c] = nezx;
+            if (kTwoParts<T>) p.sp[6][c] = nezy;
             p.ez[c] = nezx + nezy;
           }
         } else if ((p.roles & ROLE_MAIN) && in_main2(p, i, j)) {
@@ -187,10 +188,11 @@ struct K2 {
         if (p.pml_mode == 2 && in_shell2(p, i, j)) {
           if (p.roles & ROLE_PML) {
             T hzx = p.sp[0][c];
-            T hzy = p.hz[c] - hzx;
+            T hzy = kTwoParts<T> ? p.sp[6][c] : p.hz[c] - hzx;
             hzy = p.cg1[1][j] * hzy + p.cg2[1][j] * (up - exc);
             hzx = p.cg1[0][i] * hzx + p.cg2[0][i] * (-eyr + eyc);
             p.sp[0][c] = hzx;
+            if (kTwoParts<T>) p.sp[6][c] = hzy;
             hz = hzy + hzx;
             p.hz[c] = hz;
             wrote = true;

@@ -76,7 +76,9 @@ __device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b) {
         const T f1x = p.cf1[0][i], f2x = p.cf2[0][i], f1y = p.cf1[1][j], f2y = p.cf2[1][j];
         const T f1z = p.cf1[2][k], f2z = p.cf2[2][k];
         T exy = p.sp[0][c], eyz = p.sp[1][c], ezx = p.sp[2][c];
-        T exz = p.ex[c] - exy, eyx = p.ey[c] - eyz, ezy = p.ez[c] - ezx;
+        T exz, eyx, ezy;
+        if (kTwoParts<T>) { exz = p.sp[6][c]; eyx = p.sp[7][c]; ezy = p.sp[8][c]; }
+        else { exz = p.ex[c] - exy; eyx = p.ey[c] - eyz; ezy = p.ez[c] - ezx; }
         exy = f1y * exy + f2y * curlhzy;
         exz = f1z * exz + f2z * curlhyz;
         eyz = f1z * eyz + f2z * curlhxz;
@@ -84,6 +86,7 @@ __device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b) {
         ezx = f1x * ezx + f2x * curlhyx;
         ezy = f1y * ezy + f2y * curlhxy;
         p.sp[0][c] = exy; p.sp[1][c] = eyz; p.sp[2][c] = ezx;
+        if (kTwoParts<T>) { p.sp[6][c] = exz; p.sp[7][c] = eyx; p.sp[8][c] = ezy; }
         p.ex[c] = exy + exz; p.ey[c] = eyz + eyx; p.ez[c] = ezx + ezy;
       }
       continue;
@@ -140,7 +143,9 @@ __device__ __forceinline__ void tile_h3(const StepParams<T> &p, int b) {
         const T g1x = p.cg1[0][i], g2x = p.cg2[0][i], g1y = p.cg1[1][j], g2y = p.cg2[1][j];
         const T g1z = p.cg1[2][k], g2z = p.cg2[2][k];
         T hxy = p.sp[3][c], hyz = p.sp[4][c], hzx = p.sp[5][c];
-        T hxz = p.hx[c] - hxy, hyx = p.hy[c] - hyz, hzy = p.hz[c] - hzx;
+        T hxz, hyx, hzy;
+        if (kTwoParts<T>) { hxz = p.sp[9][c]; hyx = p.sp[10][c]; hzy = p.sp[11][c]; }
+        else { hxz = p.hx[c] - hxy; hyx = p.hy[c] - hyz; hzy = p.hz[c] - hzx; }
         hxy = g1y * hxy + g2y * curlezy;
         hxz = g1z * hxz + g2z * curleyz;
         hyz = g1z * hyz + g2z * curlexz;
@@ -148,6 +153,7 @@ __device__ __forceinline__ void tile_h3(const StepParams<T> &p, int b) {
         hzx = g1x * hzx + g2x * curleyx;
         hzy = g1y * hzy + g2y * curlexy;
         p.sp[3][c] = hxy; p.sp[4][c] = hyz; p.sp[5][c] = hzx;
+        if (kTwoParts<T>) { p.sp[9][c] = hxz; p.sp[10][c] = hyx; p.sp[11][c] = hzy; }
         hx = hxy + hxz; hy = hyz + hyx; hz = hzx + hzy;
         p.hx[c] = hx; p.hy[c] = hy; p.hz[c] = hz;
         wrote = true;

@@ -6,6 +6,11 @@
 
 namespace fdtd {
 
+// The FP64 plain path keeps both parts of every split PML field (as the
+// reference does); FP32 stores one part and takes the other as total - part.
+template <typename T>
+constexpr bool kTwoParts = sizeof(T) == 8;
+
 // Neighbour loads across a face of the domain: wrapped when the axis is
 // periodic (the reference's interchange_E/H with PBC), zero otherwise (the
 // halo cells the reference never writes).

@@ -23,7 +23,7 @@ EXPORTS = [
     "fdtd_step", "fdtd_update_DE", "fdtd_pml_update_E", "fdtd_interchange", "fdtd_update_H",
     "fdtd_pml_update_H", "fdtd_sample", "fdtd_sync", "fdtd_get_field", "fdtd_set_field",
     "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_profile",
-    "fdtd_kernel_time", "fdtd_launch_count",
+    "fdtd_kernel_time", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
 ]
 
 
@@ -57,6 +57,8 @@ def lib(path=None):
             "fdtd_device_bytes": [vp, C.POINTER(C.c_uint64)], "fdtd_profile": [vp, i32],
             "fdtd_kernel_time": [vp, i32, C.POINTER(C.c_int64), C.POINTER(dbl)],
             "fdtd_launch_count": [vp, C.POINTER(C.c_int64)],
+            "fdtd_set_stream": [vp, vp],
+            "fdtd_transfer_bytes": [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -195,6 +197,15 @@ class Job:
         n = C.c_int64()
         check(lib().fdtd_launch_count(self.h, C.byref(n)))
         return n.value
+
+    def set_stream(self, cuda_stream):
+        """Queue the job's work on a caller-owned CUDA stream (an int handle)."""
+        check(lib().fdtd_set_stream(self.h, C.c_void_p(cuda_stream)))
+
+    def transfer_bytes(self):
+        h, d = C.c_uint64(), C.c_uint64()
+        check(lib().fdtd_transfer_bytes(self.h, C.byref(h), C.byref(d)))
+        return h.value, d.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -257,6 +257,12 @@ int fdtd_profile(fdtd_job *job, int32_t enable);
 int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms);
 /* Launches of this library's kernels since the job was created. */
 int fdtd_launch_count(const fdtd_job *job, int64_t *launches);
+/* Run the job's work on a caller-owned cudaStream_t (NULL: the job's own
+ * stream), so a host program can order it with its other GPU work. */
+int fdtd_set_stream(fdtd_job *job, void *cuda_stream);
+/* Host->device and device->host bytes moved by set-up, getters and setters
+ * since the job was created. */
+int fdtd_transfer_bytes(const fdtd_job *job, uint64_t *h2d, uint64_t *d2h);
 
 #ifdef __cplusplus
 }

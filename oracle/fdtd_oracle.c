@@ -134,6 +134,7 @@ struct ora_job {
   oslab islab[2];
   int committed;
   int last_n;
+  int nth;
 };
 
 static int in_shell(const struct ora_job *J, int i0, int j0, int k0);
@@ -674,12 +675,14 @@ static void materials_update_E(ora_job *J) {
     omat *M = &J->mat[m];
     if (M->kind == MAT_DIEL) {
       /* E = D*gax (M2/simpledielectric_mod.f90:141-146) */
+#pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
       for (int64_t q = 0; q < M->ncell; q++) {
         int64_t c = M->cells[q];
         for (int u = 0; u < nc; u++) { int a = ncomp_list[u]; E[a][c] = D[a][c] * M->gax; }
       }
     } else if (M->kind == MAT_GOLD) {
       /* M2/gold_mod.f90:57-71, M3/gold_mod.f90:61-82 */
+#pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
       for (int64_t q = 0; q < M->ncell; q++) {
         int64_t c = M->cells[q];
         for (int u = 0; u < nc; u++) {
@@ -748,6 +751,7 @@ static void te2d_updateD(ora_job *J) {
   double Ku = J->g.ku;
   /* the reference loops i-outer; every cell is independent, so the
      cache-friendly order gives the same values */
+#pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
   for (int j = J->g.main_lo[1] + 1; j <= J->g.main_hi[1] + 1; j++)
     for (int i = J->g.main_lo[0] + 1; i <= J->g.main_hi[0] + 1; i++) {
       double curlhx = hz[IX(J, i, j, 0)] - hz[IX(J, i - 1, j, 0)];
@@ -761,6 +765,7 @@ static void te2d_updateH(ora_job *J) {
   /* P2/include/myfdtd_2Dfunc.f90:34-44 */
   double *hz = J->F[HZ], *ex = J->F[EX], *ey = J->F[EY];
   double Ku = J->g.ku;
+#pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
   for (int j = J->g.main_lo[1] + 1; j <= J->g.main_hi[1] + 1; j++)
     for (int i = J->g.main_lo[0] + 1; i <= J->g.main_hi[0] + 1; i++) {
       double curlE = ey[IX(J, i + 1, j, 0)] - ey[IX(J, i, j, 0)] - ex[IX(J, i, j + 1, 0)] + ex[IX(J, i, j, 0)];
@@ -875,6 +880,7 @@ static void wrap_z_low(ora_job *J, double *f) {
 static void tm2d_updateD(ora_job *J) {
   double *hx = J->F[HX], *hy = J->F[HY], *dz = J->F[DZ];
   double Ku = J->g.ku;
+#pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
   for (int j = J->g.main_lo[1] + 1; j <= J->g.main_hi[1] + 1; j++)
     for (int i = J->g.main_lo[0] + 1; i <= J->g.main_hi[0] + 1; i++) {
       double curlhyx = hy[IX(J, i, j, 0)] - hy[IX(J, i - 1, j, 0)];
@@ -885,6 +891,7 @@ static void tm2d_updateD(ora_job *J) {
 static void tm2d_updateH(ora_job *J) {
   double *hx = J->F[HX], *hy = J->F[HY], *ez = J->F[EZ];
   double Ku = J->g.ku;
+#pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
   for (int j = J->g.main_lo[1] + 1; j <= J->g.main_hi[1] + 1; j++)
     for (int i = J->g.main_lo[0] + 1; i <= J->g.main_hi[0] + 1; i++) {
       double curlezy = -ez[IX(J, i, j + 1, 0)] + ez[IX(J, i, j, 0)];
@@ -907,6 +914,7 @@ static void split_E(ora_job *J) {
   double *ex = J->F[EX], *ey = J->F[EY], *ez = J->F[EZ], *hx = J->F[HX], *hy = J->F[HY], *hz = J->F[HZ];
   int L = J->g.layout;
   for (int k0 = 0; k0 < J->nz; k0++)
+  #pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
     for (int j0 = 0; j0 < J->ny; j0++)
       for (int i0 = 0; i0 < J->nx; i0++) {
         if (!in_shell(J, i0, j0, k0)) continue;
@@ -941,6 +949,7 @@ static void split_H(ora_job *J) {
   double *ex = J->F[EX], *ey = J->F[EY], *ez = J->F[EZ], *hx = J->F[HX], *hy = J->F[HY], *hz = J->F[HZ];
   int L = J->g.layout;
   for (int k0 = 0; k0 < J->nz; k0++)
+  #pragma omp parallel for num_threads(J->nth) schedule(static) if (J->nth > 1)
     for (int j0 = 0; j0 < J->ny; j0++)
       for (int i0 = 0; i0 < J->nx; i0++) {
         if (!in_shell(J, i0, j0, k0)) continue;
@@ -1220,6 +1229,7 @@ static void sample(ora_job *J, int n, int nth) {
 /* ---- the loop body --------------------------------------------------------------- */
 int ora_step(ora_job *J, int n_first, int n_steps, int nth) {
   if (!J->committed) FAIL("commit first");
+  J->nth = nth > 1 ? nth : 1;
   int L = J->g.layout;
   for (int n = n_first; n < n_first + n_steps; n++) {
     if (L == FDTD_LAYOUT_1D) {
