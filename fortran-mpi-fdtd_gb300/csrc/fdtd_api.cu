@@ -240,6 +240,12 @@ void region_bounds(const fdtd_job *J, const MatRec &m, int lo[3], int hi[3]) {
   }
 }
 
+// exp(x + i y) - 1 without cancellation
+std::complex<double> expm1c(double x, double y) {
+  const double sh = std::sin(0.5 * y);
+  return std::complex<double>(std::expm1(x) * std::cos(y) - 2.0 * sh * sh, std::exp(x) * std::sin(y));
+}
+
 // ---- PML coefficient tables (FP64, the reference's formulas) -----------
 struct Prof {
   std::vector<double> f1, f2, g1, g2;
@@ -376,8 +382,11 @@ int commit_impl(fdtd_job *J) {
       a.normal = -1;
       a.ha = T(std::exp(-p.gamma_d * dt));
       a.hb = T((p.omega_d * p.omega_d) * dt / p.gamma_d);
-      a.gb1r = T(gb[0].real()); a.gb1i = T(gb[0].imag());
-      a.gb2r = T(gb[1].real()); a.gb2i = T(gb[1].imag());
+      a.dha = T(-std::expm1(-p.gamma_d * dt));
+      const cd d1 = expm1c(-p.gamma[0] * dt, p.omega[0] * dt), d2 = expm1c(-p.gamma[1] * dt, p.omega[1] * dt);
+      a.d1r = T(d1.real()); a.d1i = T(d1.imag());
+      a.d2r = T(d2.real()); a.d2i = T(d2.imag());
+      (void)gb;
       a.gc1r = T(gc[0].real()); a.gc1i = T(gc[0].imag());
       a.gc2r = T(gc[1].real()); a.gc2i = T(gc[1].imag());
       a.wr = T(w.real()); a.wi = T(w.imag());
@@ -404,10 +413,15 @@ int commit_impl(fdtd_job *J) {
       a.normal = normal;
       a.ha = T(std::exp(-gam * dt));
       a.hb = T(sigma0 * dt / K.ep0);
+      a.dha = T(-std::expm1(-gam * dt));
       a.ga = T(1.0);
       a.r0 = T(p.raman_frac * chi3n * omegaR * dt * std::exp(-alfaR * dt) * std::sin(betaR * dt));
-      a.r1 = T(2.0 * std::exp(-alfaR * dt) * std::cos(betaR * dt));
-      a.r2 = T(-std::exp(-2.0 * alfaR * dt));
+      // r1 = 2 e^{-a} cos b, r2 = -e^{-2a}; c1 = r1 - 2, c2 = 1 + r2, without cancellation
+      const double sb = std::sin(0.5 * betaR * dt);
+      const double c1 = 2.0 * (std::expm1(-alfaR * dt) * std::cos(betaR * dt) - 2.0 * sb * sb);
+      const double c2 = -std::expm1(-2.0 * alfaR * dt);
+      a.rv = T(1.0 - c2);
+      a.rs = T(c1 + c2);
       a.kerr = T((1.0 - p.raman_frac) * chi3n);
       c.ade = (int)ac.size();
       c.ca = T(Ku);

@@ -38,15 +38,19 @@ struct MatCoef {
 };
 
 // Drude + 2 critical points (and the graphene Drude + Raman/Kerr variant)
+// The recursions are carried in delta form, with the small deltas computed
+// once in FP64 on the host: a decay factor ha = exp(-g dt) ~ 1 - 3.6e-4
+// rounded to FP32 would perturb its decay rate 1 - ha by ~1e-4.
 template <typename T>
 struct AdeCoef {
   int kind;
   int normal;              // graphene sheet normal axis (in-plane comps updated)
-  T ha, hb;                // Drude: S = ha*S + hb*E, Q -= hb*E
-  T gb1r, gb1i, gb2r, gb2i;// CP recursion factors
+  T ha, hb, dha;           // Drude: S += hb*E - dha*S (dha = 1-ha), Q -= hb*E
+  T d1r, d1i, d2r, d2i;    // CP: g += (gb-1)*g + gc*E, d = gb-1
   T gc1r, gc1i, gc2r, gc2i;// CP drive
   T wr, wi;                // 1/ga (E = Re(num * (wr + i wi)))
-  T r0, r1, r2, kerr, ga;  // graphene Raman recursion, Kerr, eps
+  T r0, rv, rs, kerr, ga;  // graphene Raman in velocity form: V = rv*V + rs*SR + r0*E^2,
+                           // SR += V (rv = 1-(1+r2), rs = (r1-2)+(1+r2)); Kerr; eps
 };
 
 struct Source {
@@ -138,7 +142,7 @@ enum Role : int {
 };
 
 // ADE state layout: state[(f*3 + comp)*stride + slot] with fields
-// 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:SRm1 3:SRm2 4:E_prev)
+// 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:S_R 3:V = S_R(n)-S_R(n-1))
 constexpr int kAdeFields = 6;
 
 // launchers (defined in k2d.cu / k3d.cu / k1d.cu / kdft.cu)

@@ -71,9 +71,11 @@ __device__ __forceinline__ T src_sum(const StepParams<T> &p, int comp, int i, in
 // (Ku*curl + source).  Gold (2D/gold_mod.f90:57-71, 3D/gold_mod.f90:61-82):
 //   E = Re[(D - I + ha S + gb1 g1 + gb2 g2) / ga];  I += hb E;
 //   S = ha S + hb E;  g_p = gb_p g_p + gc_p E
-// with Q = D - I kept instead of D and I (Q += inc - hb E).
+// with Q = D - I kept instead of D and I (Q += inc - hb E) and the
+// recursions in delta form (S += hb E - (1-ha) S, g += (gb-1) g + gc E).
 // Graphene sheet (1D/graphene633_mod.f90:33-41, 3D/graphene_mod.f90:70-76):
-//   E = (Q + ha S + 2 kerr E^3) / (ga + S_R + 3 kerr E^2), Raman recursion.
+//   E = (Q + ha S + 2 kerr E^3) / (ga + S_R + 3 kerr E^2) with the Raman
+//   recursion S_R(n) = r1 S_R(n-1) + r2 S_R(n-2) + r0 E^2 in velocity form.
 template <typename T>
 __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int comp, const AdeCoef<T> &a,
                                                T inc, T eold) {
@@ -87,13 +89,14 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
     T *f4 = st + (4 * 3 + comp) * (long long)stride + slot;
     T *f5 = st + (5 * 3 + comp) * (long long)stride + slot;
     const T g1r = *f2, g1i = *f3, g2r = *f4, g2i = *f5;
-    const T p1r = a.gb1r * g1r - a.gb1i * g1i, p1i = a.gb1r * g1i + a.gb1i * g1r;
-    const T p2r = a.gb2r * g2r - a.gb2i * g2i, p2i = a.gb2r * g2i + a.gb2i * g2r;
+    // gb*g = g + (gb-1)*g
+    const T p1r = g1r + (a.d1r * g1r - a.d1i * g1i), p1i = g1i + (a.d1r * g1i + a.d1i * g1r);
+    const T p2r = g2r + (a.d2r * g2r - a.d2i * g2i), p2i = g2i + (a.d2r * g2i + a.d2i * g2r);
     const T nre = ((Q + a.ha * S) + p1r) + p2r;
     const T nim = p1i + p2i;
     const T e = nre * a.wr - nim * a.wi;
     *q_ = Q - a.hb * e;
-    *s_ = a.ha * S + a.hb * e;
+    *s_ = S + (a.hb * e - a.dha * S);
     *f2 = p1r + a.gc1r * e;
     *f3 = p1i + a.gc1i * e;
     *f4 = p2r + a.gc2r * e;
@@ -105,15 +108,15 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
     *q_ = Q;
     return eold + inc;
   }
-  const T srm1 = *f2, srm2 = *f3;
+  const T sr = *f2, v = *f3;
   const T num = (Q + a.ha * S) + T(2) * a.kerr * (eold * eold * eold);
-  const T den = (a.ga + srm1) + T(3) * a.kerr * (eold * eold);
+  const T den = (a.ga + sr) + T(3) * a.kerr * (eold * eold);
   const T e = num / den;
-  const T sr = a.r1 * srm1 + a.r2 * srm2 + a.r0 * (e * e);
-  *f3 = srm1;
-  *f2 = sr;
+  const T nv = a.rv * v + a.rs * sr + a.r0 * (e * e);
+  *f3 = nv;
+  *f2 = sr + nv;
   *q_ = Q - a.hb * e;
-  *s_ = a.ha * S + a.hb * e;
+  *s_ = S + (a.hb * e - a.dha * S);
   return e;
 }
 
