@@ -239,8 +239,6 @@ def main():
             flush.zero_()
             j.step(1, args.nt)
             j.sync()
-        for j in jobs[warm:]:
-            j.profile(True)
         barrier()
         torch.cuda.synchronize()
         evs = []
@@ -260,14 +258,18 @@ def main():
         barrier()
         ms = [a.elapsed_time(b) for a, b in evs]
         launches = sum(j.launch_count() for j in jobs[warm:]) - launches0
+        # per-kernel device time: the same job once more with an event pair
+        # around every launch (eager launches; the timed jobs replay graphs)
+        pj = gj.Job(spec)
+        pj.set_stream(stream.cuda_stream)
+        pj.profile(True)
+        flush.zero_()
+        pj.step(1, args.nt)
+        pj.sync()
         kt = {}
         for kind, name in ((abi.KERNEL_E, "E"), (abi.KERNEL_H, "H"), (abi.KERNEL_DFT, "DFT")):
-            cnt, tot = 0, 0.0
-            for j in jobs[warm:]:
-                c, t = j.kernel_time(kind)
-                cnt += c
-                tot += t
-            kt[name] = (cnt, tot)
+            kt[name] = pj.kernel_time(kind)
+        pj.close()
         return spec, meta, jobs[warm:], ms, launches, kt, clocks
 
     # ---- FP32 (headline) ----
@@ -333,6 +335,7 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload_name(args.n, args.nt), "cells": cells, "time_steps_per_job": args.nt,
                    "bench_step": "one job of the workload from a fresh state",
+                   "launch": "CUDA graph per 32-step ring (E, H and DFT fold kernels)",
                    "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed jobs",
                    "parallelism": f"replicas x{world}"},
         "fp64_plain": {"value": value64, "ms_per_step": t64, "steps": len(ms64)},

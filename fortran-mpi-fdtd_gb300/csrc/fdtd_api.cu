@@ -13,6 +13,7 @@
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -142,6 +143,17 @@ struct fdtd_job {
   // 1D per-launch source values
   double *d_srcval = nullptr;
   long long srcval_cap = 0;
+  // 2D/3D: amp*g(t) of every step, [(n-1)*nsrc + q], on the device
+  std::vector<double> srctab;
+  double *d_srctab = nullptr;
+  long long srctab_steps = 0, srctab_cap_steps = 0;
+  int nsrc_dev = 0;
+  // CUDA graph of one ring of kStageSteps steps + its DFT fold
+  int *d_base = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_kernels = 0;
+  bool use_graph = true;
   int last_n = 0;
   // profiling
   bool prof = false;
@@ -638,7 +650,9 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.sf1z[s] = (const T *)sc[8]; p.sf2z[s] = (const T *)sc[9]; p.sg1z[s] = (const T *)sc[10]; p.sg2z[s] = (const T *)sc[11];
   }
   if (J->dim == 2) {
-    p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 31) / 32; p.tiles_z = 1;
+    const int vw = sizeof(T) == 4 ? 4 : 2;  // float4 / double2 rows when aligned
+    p.vec = (J->nx % vw == 0) ? vw : 1;
+    p.tiles_x = (J->nx + 32 * p.vec - 1) / (32 * p.vec); p.tiles_y = (J->ny + 31) / 32; p.tiles_z = 1;
   } else {
     p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 7) / 8; p.tiles_z = (J->nz + 15) / 16;
   }
@@ -664,8 +678,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
 }
 
 template <typename T>
-void set_sources(fdtd_job *J, StepParams<T> &p, int n) {
-  const double t = (double)(n - 1) * J->g.dt;
+void set_sources(fdtd_job *J, StepParams<T> &p) {
   p.nsrc = 0;
   for (auto &s : J->srcs) {
     if (s.component == FDTD_EX_INC) continue;
@@ -676,9 +689,50 @@ void set_sources(fdtd_job *J, StepParams<T> &p, int n) {
       d.hi[a] = std::min(s.hi[a], J->g.main_hi[a]);
     }
     d.amp = s.amp;
-    p.srcval[p.nsrc] = gauss_t(s, t) * s.amp;
     ++p.nsrc;
   }
+  p.srcval_tab = J->d_srctab;
+}
+
+void destroy_graph(fdtd_job *J) {
+  if (J->graph_exec) cudaGraphExecDestroy(J->graph_exec);
+  if (J->graph) cudaGraphDestroy(J->graph);
+  J->graph_exec = nullptr;
+  J->graph = nullptr;
+}
+
+// amp*g(t) for steps 1..n_max of the 2D/3D sources, kept on the device
+int ensure_srctab(fdtd_job *J, int n_max) {
+  int nsrc = 0;
+  for (auto &s : J->srcs) if (s.component != FDTD_EX_INC) ++nsrc;
+  J->nsrc_dev = nsrc;
+  if (nsrc == 0 || n_max <= J->srctab_steps) return FDTD_OK;
+  const long long old_steps = J->srctab_steps;
+  for (long long n = old_steps + 1; n <= n_max; ++n) {
+    const double t = (double)(n - 1) * J->g.dt;           // t=real(n-1,8)*dt
+    for (auto &s : J->srcs)
+      if (s.component != FDTD_EX_INC) J->srctab.push_back(gauss_t(s, t) * s.amp);
+  }
+  J->srctab_steps = n_max;
+  if (n_max > J->srctab_cap_steps) {
+    long long cap = std::max<long long>(2 * J->srctab_cap_steps, std::max(n_max, 4096));
+    double *nb = nullptr;
+    cudaError_t e = cudaMalloc(&nb, (size_t)cap * nsrc * sizeof(double));
+    if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "source table: %s", cudaGetErrorString(e));
+    CK(cudaStreamSynchronize(J->stream));
+    if (J->d_srctab) { cudaFree(J->d_srctab); J->dev_bytes -= (uint64_t)J->srctab_cap_steps * nsrc * sizeof(double); }
+    J->d_srctab = nb;
+    J->srctab_cap_steps = cap;
+    J->dev_bytes += (uint64_t)cap * nsrc * sizeof(double);
+    destroy_graph(J);  // the captured launches hold the old pointer
+    CK(cudaMemcpy(J->d_srctab, J->srctab.data(), (size_t)n_max * nsrc * sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    CK(cudaMemcpyAsync(J->d_srctab + (size_t)old_steps * nsrc, J->srctab.data() + (size_t)old_steps * nsrc,
+                       (size_t)(n_max - old_steps) * nsrc * sizeof(double), cudaMemcpyHostToDevice, J->stream));
+    CK(cudaStreamSynchronize(J->stream));  // the host vector may grow again
+  }
+  J->h2d += (uint64_t)(n_max - old_steps) * nsrc * sizeof(double);
+  return FDTD_OK;
 }
 
 void ev_record(fdtd_job *J, int kind, bool begin) {
@@ -710,6 +764,7 @@ int ensure_probe_cap(fdtd_job *J, int n_max) {
     P.buf = nb;
     P.cap = (int)cap;
     J->dev_bytes += (uint64_t)cap * P.ncomp * sizeof(double);
+    destroy_graph(J);  // the captured launches hold the old buffer
   }
   return FDTD_OK;
 }
@@ -745,48 +800,53 @@ int dft_fold(fdtd_job *J) {
 
 enum { ST_E = 1, ST_H = 2, ST_SAMPLE = 4 };
 
-// 2D / 3D: one half step (or a role subset of it)
+// 2D / 3D: one half step (or a role subset of it).  In graph mode the step
+// number comes from the device-side ring base (d_base) plus the ring slot.
 template <typename T>
-int half_e(fdtd_job *J, int n, int roles) {
+int half_e(fdtd_job *J, int n, int roles, int slot = 0, bool graph = false) {
   StepParams<T> p;
   fill_common<T>(J, p);
-  set_sources<T>(J, p, n);
+  set_sources<T>(J, p);
   p.roles = roles;
   p.n = n;
+  p.slot = slot;
+  p.d_base = graph ? J->d_base : nullptr;
   int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
-  ev_record(J, FDTD_KERNEL_E, true);
+  if (!graph) ev_record(J, FDTD_KERNEL_E, true);
   if (J->dim == 2) launch_e2d<T>(p, blocks, J->stream);
   else launch_e3d<T>(p, blocks, J->stream);
-  ev_record(J, FDTD_KERNEL_E, false);
+  if (!graph) ev_record(J, FDTD_KERNEL_E, false);
   J->launches++;
   CK(cudaGetLastError());
   return FDTD_OK;
 }
 
 template <typename T>
-int half_h(fdtd_job *J, int n, int roles, bool gather) {
+int half_h(fdtd_job *J, int n, int roles, bool gather, int slot = -1, bool graph = false) {
   StepParams<T> p;
   fill_common<T>(J, p);
   p.roles = roles;
   p.n = n;
   p.gather = gather ? 1 : 0;
-  p.slot = J->stage_fill;
+  p.slot = slot >= 0 ? slot : J->stage_fill;
+  p.d_base = graph ? J->d_base : nullptr;
   int blocks = p.ntile_blocks + p.nslab_blocks;
-  ev_record(J, FDTD_KERNEL_H, true);
+  if (!graph) ev_record(J, FDTD_KERNEL_H, true);
   if (J->dim == 2) launch_h2d<T>(p, blocks, J->stream);
   else launch_h3d<T>(p, blocks, J->stream);
-  ev_record(J, FDTD_KERNEL_H, false);
+  if (!graph) ev_record(J, FDTD_KERNEL_H, false);
   J->launches++;
   CK(cudaGetLastError());
   return FDTD_OK;
 }
 
 template <typename T>
-int sample_sep(fdtd_job *J, int n) {
+int sample_sep(fdtd_job *J, int n, int slot = -1, bool graph = false) {
   StepParams<T> p;
   fill_common<T>(J, p);
   p.n = n;
-  p.slot = J->stage_fill;
+  p.slot = slot >= 0 ? slot : J->stage_fill;
+  p.d_base = graph ? J->d_base : nullptr;
   launch_gather<T>(p, J->stream);
   J->launches++;
   CK(cudaGetLastError());
@@ -799,6 +859,73 @@ int after_sample(fdtd_job *J, int n) {
   J->stage_fill++;
   J->last_n = n;
   if (J->stage_fill == kStageSteps) return dft_fold<T>(J);
+  return FDTD_OK;
+}
+
+template <typename T>
+int eager_step(fdtd_job *J, int n) {
+  int rc;
+  if ((rc = half_e<T>(J, n, ROLE_MAIN | ROLE_PML | ROLE_ADE))) return rc;
+  if ((rc = half_h<T>(J, n, ROLE_MAIN | ROLE_PML, J->gather_fused))) return rc;
+  if (!J->gather_fused && (rc = sample_sep<T>(J, n))) return rc;
+  return after_sample<T>(J, n);
+}
+
+__global__ void set_base_kernel(int *base, int v) { *base = v; }
+
+// Capture one ring (kStageSteps steps and the DFT fold of the ring) as a CUDA
+// graph; every replay reads its first step number from d_base.
+template <typename T>
+int ring_graph(fdtd_job *J) {
+  int rc;
+  if (J->graph_exec) return FDTD_OK;
+  if (!J->d_base && (rc = alloc_dev(J, (void **)&J->d_base, sizeof(int)))) return rc;
+  CK(cudaStreamSynchronize(J->stream));
+  const long long launches0 = J->launches;
+  CK(cudaStreamBeginCapture(J->stream, cudaStreamCaptureModeThreadLocal));
+  int bad = FDTD_OK;
+  for (int s = 0; s < kStageSteps && !bad; ++s) {
+    bad = half_e<T>(J, 0, ROLE_MAIN | ROLE_PML | ROLE_ADE, s, true);
+    if (!bad) bad = half_h<T>(J, 0, ROLE_MAIN | ROLE_PML, J->gather_fused, s, true);
+    if (!bad && !J->gather_fused) bad = sample_sep<T>(J, 0, s, true);
+  }
+  if (!bad && !J->mon_dev.empty() && J->dft_blocks > 0) {
+    DftParams d{};
+    d.nmon = (int)J->mon_dev.size();
+    for (int q = 0; q < d.nmon; ++q) d.mon[q] = J->mon_dev[q];
+    d.omega = J->d_omega;
+    d.acc_re = J->d_acc_re;
+    d.acc_im = J->d_acc_im;
+    d.dt = J->g.dt;
+    d.stage_row = J->stage_row;
+    d.total_work_blocks = J->dft_blocks;
+    d.nslots = kStageSteps;
+    d.d_base = J->d_base;
+    launch_dft<T>(d, (const T *)J->d_stage, J->stream);
+    J->launches++;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(J->stream, &g);
+  J->graph_kernels = (int)(J->launches - launches0);
+  J->launches = launches0;
+  if (bad) { if (g) cudaGraphDestroy(g); return bad; }
+  if (e != cudaSuccess) return set_err(FDTD_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+  J->graph = g;
+  e = cudaGraphInstantiate(&J->graph_exec, J->graph, 0);
+  if (e != cudaSuccess) { destroy_graph(J); return set_err(FDTD_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+  return FDTD_OK;
+}
+
+template <typename T>
+int replay_ring(fdtd_job *J, int n0) {
+  int rc = ring_graph<T>(J);
+  if (rc) return rc;
+  set_base_kernel<<<1, 1, 0, J->stream>>>(J->d_base, n0);
+  CK(cudaGetLastError());
+  CK(cudaGraphLaunch(J->graph_exec, J->stream));
+  J->launches += 1 + J->graph_kernels;
+  J->stage_n0 = n0 + kStageSteps;
+  J->last_n = n0 + kStageSteps - 1;
   return FDTD_OK;
 }
 
@@ -917,13 +1044,21 @@ int step_impl(fdtd_job *J, int n_first, int n_steps) {
     }
     return FDTD_OK;
   }
-  const int all = ROLE_MAIN | ROLE_PML | ROLE_ADE;
-  for (int n = n_first; n < n_first + n_steps; ++n) {
-    if ((rc = half_e<T>(J, n, all))) return rc;
-    if ((rc = half_h<T>(J, n, ROLE_MAIN | ROLE_PML, J->gather_fused))) return rc;
-    if (!J->gather_fused && (rc = sample_sep<T>(J, n))) return rc;
-    if ((rc = after_sample<T>(J, n))) return rc;
+  const int end = n_first + n_steps;
+  if ((rc = ensure_srctab(J, end - 1))) return rc;
+  int n = n_first;
+  // finish a partly filled ring eagerly, replay whole rings from the graph,
+  // run the tail eagerly (the per-launch events of fdtd_profile need eager)
+  while (n < end && J->stage_fill != 0)
+    if ((rc = eager_step<T>(J, n++))) return rc;
+  if (J->use_graph && !J->prof) {
+    while (end - n >= kStageSteps) {
+      if ((rc = replay_ring<T>(J, n))) return rc;
+      n += kStageSteps;
+    }
   }
+  while (n < end)
+    if ((rc = eager_step<T>(J, n++))) return rc;
   return FDTD_OK;
 }
 
@@ -942,6 +1077,7 @@ template <typename T>
 static int proc_call(fdtd_job *J, int n, int what) {
   int rc = ensure_probe_cap(J, n);
   if (rc) return rc;
+  if (J->dim >= 2 && (rc = ensure_srctab(J, n))) return rc;
   if (J->dim == 1) {
     if (what == 0) { if (J->stage_fill == 0) J->stage_n0 = n; return line_run<T>(J, n, 1, ST_E); }
     if (what == 2) return line_run<T>(J, n, 1, ST_H);
@@ -1045,6 +1181,8 @@ int fdtd_create(const fdtd_grid_desc *g, fdtd_job **out) {
     return set_err(FDTD_ECUDA, "cudaStreamCreate failed");
   }
   J->own_stream = J->stream;
+  const char *ng = getenv("FDTD_NO_GRAPH");
+  J->use_graph = !(ng && ng[0] == '1');
   *out = J;
   return FDTD_OK;
 }
@@ -1055,6 +1193,8 @@ int fdtd_destroy(fdtd_job *J) {
   for (void *p : J->allocs) cudaFree(p);
   for (auto &P : J->probes) if (P.buf) cudaFree(P.buf);
   if (J->d_srcval) cudaFree(J->d_srcval);
+  if (J->d_srctab) cudaFree(J->d_srctab);
+  destroy_graph(J);
   for (auto &e : J->pending) { cudaEventDestroy(e.a); if (e.b) cudaEventDestroy(e.b); }
   for (auto e : J->ev_pool) cudaEventDestroy(e);
   if (J->own_stream) cudaStreamDestroy(J->own_stream);

@@ -98,10 +98,10 @@ struct StepParams {
   const AdeCoef<T> *ac;
   T *ade_state;            // [field][comp][slot], see AdeState
   int ade_stride;          // = padded nade
-  // sources active this step
+  // sources: boxes, and amp*g(t) of every step in a device table
   int nsrc;
   Source src[kMaxSrc];
-  double srcval[kMaxSrc];  // amp * g(t) for this step
+  const double *srcval_tab;  // [(n-1)*nsrc + q]
   // PML
   int pml_mode;            // 0 none, 1 reference slabs, 2 split
   // split-field PML on any faces: shell = outside [slo, shi]
@@ -132,7 +132,10 @@ struct StepParams {
   int slot;                // ring slot of this step
   int nprobe;
   Probe probe[kMaxProbe];
-  int n;                   // step number
+  int n;                   // step number (eager launches)
+  const int *d_base;       // graph replays: step number of ring slot 0 on the
+                           // device; then n = *d_base + slot
+  int vec;                 // cells per thread along x in the 2D tile path
 };
 
 enum Role : int {
@@ -161,7 +164,8 @@ struct DftParams {
   const double *omega;     // all monitors' frequencies
   double *acc_re, *acc_im; // FP64 accumulators
   int nslots;              // valid slots in this fold (0..kStageSteps)
-  int n0;                  // step number of slot 0
+  int n0;                  // step number of slot 0 (eager launches)
+  const int *d_base;       // graph replays: slot-0 step number on the device
   double dt;
   long long stage_row;
   int total_work_blocks;

@@ -45,7 +45,7 @@ struct F3 {
 };
 
 template <typename T>
-__device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b) {
+__device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b, int n) {
   const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
   const int tx = b % p.tiles_x, t2 = b / p.tiles_x;
   const int ty = t2 % p.tiles_y, tz = t2 / p.tiles_y;
@@ -98,7 +98,7 @@ __device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b) {
         T ey = p.ey[c] + mc.ca * (curlhxz + curlhzx);
         T ez = p.ez[c] + mc.ca * (curlhyx + curlhxy);
         if (p.nsrc) {
-          const T sx = src_sum<T>(p, 0, i, j, k), sy = src_sum<T>(p, 1, i, j, k), sz = src_sum<T>(p, 2, i, j, k);
+          const T sx = src_sum<T>(p, n, 0, i, j, k), sy = src_sum<T>(p, n, 1, i, j, k), sz = src_sum<T>(p, n, 2, i, j, k);
           if (sx != T(0)) ex += mc.cs * sx;
           if (sy != T(0)) ey += mc.cs * sy;
           if (sz != T(0)) ez += mc.cs * sz;
@@ -110,7 +110,7 @@ __device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b) {
 }
 
 template <typename T>
-__device__ __forceinline__ void tile_h3(const StepParams<T> &p, int b) {
+__device__ __forceinline__ void tile_h3(const StepParams<T> &p, int b, int n) {
   const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
   const int tx = b % p.tiles_x, t2 = b / p.tiles_x;
   const int ty = t2 % p.tiles_y, tz = t2 / p.tiles_y;
@@ -168,7 +168,7 @@ __device__ __forceinline__ void tile_h3(const StepParams<T> &p, int b) {
     if (p.gather) {
       if (!wrote) { hx = p.hx[c]; hy = p.hy[c]; hz = p.hz[c]; }
       const T vals[6] = {ex0, ey0, ezc, hx, hy, hz};
-      gather_cell<T>(p, i, j, k, vals);
+      gather_cell<T>(p, n, i, j, k, vals);
     }
   }
 }
@@ -290,7 +290,7 @@ __device__ __forceinline__ void slab_h3(const StepParams<T> &p, int t) {
 }
 
 template <typename T>
-__device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s) {
+__device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
   const int cell = p.ade_cell[s];
   const int nx = p.nx, ny = p.ny;
   const int i = cell % nx, j = (cell / nx) % ny, k = cell / (nx * ny);
@@ -301,9 +301,9 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s) {
   const T curlhzy = hzc - f.ly(p.hz, i, j - 1, k), curlhyz = -hyc + f.lz(p.hy, i, j, k - 1);
   const T curlhxz = hxc - f.lz(p.hx, i, j, k - 1), curlhzx = -hzc + f.lx(p.hz, i - 1, j, k);
   const T curlhyx = hyc - f.lx(p.hy, i - 1, j, k), curlhxy = -hxc + f.ly(p.hx, i, j - 1, k);
-  const T ix_ = p.ku * (curlhzy + curlhyz) + src_sum<T>(p, 0, i, j, k);
-  const T iy_ = p.ku * (curlhxz + curlhzx) + src_sum<T>(p, 1, i, j, k);
-  const T iz_ = p.ku * (curlhyx + curlhxy) + src_sum<T>(p, 2, i, j, k);
+  const T ix_ = p.ku * (curlhzy + curlhyz) + src_sum<T>(p, n, 0, i, j, k);
+  const T iy_ = p.ku * (curlhxz + curlhzx) + src_sum<T>(p, n, 1, i, j, k);
+  const T iz_ = p.ku * (curlhyx + curlhxy) + src_sum<T>(p, n, 2, i, j, k);
   p.ex[cell] = ade_update<T>(p, a, s, 0, ix_, p.ex[cell]);
   p.ey[cell] = ade_update<T>(p, a, s, 1, iy_, p.ey[cell]);
   p.ez[cell] = ade_update<T>(p, a, s, 2, iz_, p.ez[cell]);
@@ -311,9 +311,10 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s) {
 
 template <typename T>
 __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepParams<T> p) {
+  const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
-    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_e3<T>(p, b);
+    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_e3<T>(p, b, n);
     return;
   }
   b -= p.ntile_blocks;
@@ -324,15 +325,16 @@ __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepPa
   b -= p.nslab_blocks;
   if (p.roles & ROLE_ADE) {
     const int s = b * 256 + threadIdx.x;
-    if (s < p.nade) ade_e3<T>(p, s);
+    if (s < p.nade) ade_e3<T>(p, s, n);
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) h3d_kernel(const __grid_constant__ StepParams<T> p) {
+  const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
-    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_h3<T>(p, b);
+    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_h3<T>(p, b, n);
     return;
   }
   b -= p.ntile_blocks;

@@ -11,6 +11,52 @@ namespace fdtd {
 template <typename T>
 constexpr bool kTwoParts = sizeof(T) == 8;
 
+// ---- vector access of V consecutive cells along x ------------------------
+template <typename T, int V> struct VecOf;
+template <> struct VecOf<float, 1> { typedef float t; };
+template <> struct VecOf<float, 2> { typedef float2 t; };
+template <> struct VecOf<float, 4> { typedef float4 t; };
+template <> struct VecOf<double, 1> { typedef double t; };
+template <> struct VecOf<double, 2> { typedef double2 t; };
+template <int V> struct ByteVec;
+template <> struct ByteVec<1> { typedef unsigned char t; };
+template <> struct ByteVec<2> { typedef uchar2 t; };
+template <> struct ByteVec<4> { typedef uchar4 t; };
+
+template <typename T, int V>
+__device__ __forceinline__ void vld_ro(const T *a, T (&v)[V]) {  // read-only path
+  typedef typename VecOf<T, V>::t VT;
+  const VT x = __ldg(reinterpret_cast<const VT *>(a));
+  const T *e = reinterpret_cast<const T *>(&x);
+#pragma unroll
+  for (int q = 0; q < V; ++q) v[q] = e[q];
+}
+template <typename T, int V>
+__device__ __forceinline__ void vld(const T *a, T (&v)[V]) {
+  typedef typename VecOf<T, V>::t VT;
+  const VT x = *reinterpret_cast<const VT *>(a);
+  const T *e = reinterpret_cast<const T *>(&x);
+#pragma unroll
+  for (int q = 0; q < V; ++q) v[q] = e[q];
+}
+template <typename T, int V>
+__device__ __forceinline__ void vst(T *a, const T (&v)[V]) {
+  typedef typename VecOf<T, V>::t VT;
+  VT x;
+  T *e = reinterpret_cast<T *>(&x);
+#pragma unroll
+  for (int q = 0; q < V; ++q) e[q] = v[q];
+  *reinterpret_cast<VT *>(a) = x;
+}
+template <int V>
+__device__ __forceinline__ void vld_ids(const uint8_t *a, uint8_t (&v)[V]) {
+  typedef typename ByteVec<V>::t BT;
+  const BT x = __ldg(reinterpret_cast<const BT *>(a));
+  const uint8_t *e = reinterpret_cast<const uint8_t *>(&x);
+#pragma unroll
+  for (int q = 0; q < V; ++q) v[q] = e[q];
+}
+
 // Neighbour loads across a face of the domain: wrapped when the axis is
 // periodic (the reference's interchange_E/H with PBC), zero otherwise (the
 // halo cells the reference never writes).
@@ -53,18 +99,45 @@ __device__ __forceinline__ bool in_main3(const StepParams<T> &p, int i, int j, i
   return i >= p.mlo[0] && i <= p.mhi[0] && j >= p.mlo[1] && j <= p.mhi[1] && k >= p.mlo[2] && k <= p.mhi[2];
 }
 
+// Step number of this launch: a kernel parameter for eager launches, the
+// device-side ring base + slot when the step is replayed from a CUDA graph.
+template <typename T>
+__device__ __forceinline__ int step_n(const StepParams<T> &p) {
+  return p.d_base ? *p.d_base + p.slot : p.n;
+}
+
 // Sum of this step's soft-source values driving component `comp` at a cell
 // (3D/.../program.f90:396-406: D += gauss_t*n_air on the source plane).
 template <typename T>
-__device__ __forceinline__ T src_sum(const StepParams<T> &p, int comp, int i, int j, int k) {
+__device__ __forceinline__ T src_sum(const StepParams<T> &p, int n, int comp, int i, int j, int k) {
   T s = T(0);
   for (int q = 0; q < p.nsrc; ++q) {
     const Source &sr = p.src[q];
     if (sr.comp == comp && i >= sr.lo[0] && i <= sr.hi[0] && j >= sr.lo[1] && j <= sr.hi[1] &&
         k >= sr.lo[2] && k <= sr.hi[2])
-      s += T(p.srcval[q]);
+      s += T(p.srcval_tab[(long long)(n - 1) * p.nsrc + q]);
   }
   return s;
+}
+
+// Does any source drive component `comp` on row j (plane k)?
+template <typename T>
+__device__ __forceinline__ bool src_row(const StepParams<T> &p, int comp, int j, int k) {
+  for (int q = 0; q < p.nsrc; ++q) {
+    const Source &sr = p.src[q];
+    if (sr.comp == comp && j >= sr.lo[1] && j <= sr.hi[1] && k >= sr.lo[2] && k <= sr.hi[2]) return true;
+  }
+  return false;
+}
+
+// Does any monitor or probe sample row j (plane k)?
+template <typename T>
+__device__ __forceinline__ bool sample_row(const StepParams<T> &p, int j, int k) {
+  for (int q = 0; q < p.nmon; ++q)
+    if (j >= p.mon[q].lo[1] && j <= p.mon[q].hi[1] && k >= p.mon[q].lo[2] && k <= p.mon[q].hi[2]) return true;
+  for (int q = 0; q < p.nprobe; ++q)
+    if (j == p.probe[q].cell[1] && k == p.probe[q].cell[2]) return true;
+  return false;
 }
 
 // One E component of a dispersive cell.  `inc` is this step's D increment
@@ -129,7 +202,7 @@ __device__ __forceinline__ T ade_update(const StepParams<T> &p, const AdeCoef<T>
 // Fused sampling: write the monitored components of cell (i,j,k) into this
 // step's stage row, and probe samples.  vals[c] = value of component c.
 template <typename T>
-__device__ __forceinline__ void gather_cell(const StepParams<T> &p, int i, int j, int k, const T *vals) {
+__device__ __forceinline__ void gather_cell(const StepParams<T> &p, int n, int i, int j, int k, const T *vals) {
   for (int q = 0; q < p.nmon; ++q) {
     const Monitor &m = p.mon[q];
     if (i < m.lo[0] || i > m.hi[0] || j < m.lo[1] || j > m.hi[1] || k < m.lo[2] || k > m.hi[2]) continue;
@@ -141,8 +214,8 @@ __device__ __forceinline__ void gather_cell(const StepParams<T> &p, int i, int j
   for (int q = 0; q < p.nprobe; ++q) {
     const Probe &pr = p.probe[q];
     if (i != pr.cell[0] || j != pr.cell[1] || k != pr.cell[2]) continue;
-    if (p.n < pr.n_first || p.n > pr.n_last) continue;
-    const long long st = p.n - pr.n_first;
+    if (n < pr.n_first || n > pr.n_last) continue;
+    const long long st = n - pr.n_first;
     if (st >= pr.cap) continue;
     double *out = pr.buf + st * pr.ncomp;
     for (int u = 0; u < pr.ncomp; ++u) out[u] = (double)vals[pr.comps[u]];

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.h"
+#include "kcommon.cuh"
 
 namespace fdtd {
 
@@ -35,14 +36,15 @@ __global__ void __launch_bounds__(kDftThreads) dft_kernel(const __grid_constant_
   if (q >= d.nmon) return;
   const Monitor &m = d.mon[q];
   // skip the fold when no slot of it lies in the monitor's step window
-  const int nlast = d.n0 + d.nslots - 1;
-  if (nlast < m.n_first || d.n0 > m.n_last) return;
+  const int n0 = d.d_base ? *d.d_base : d.n0;
+  const int nlast = n0 + d.nslots - 1;
+  if (nlast < m.n_first || n0 > m.n_last) return;
   const int fc = b / sblocks, sb = b % sblocks;
   const int f0 = fc * kFreqChunk;
   for (int t = threadIdx.x; t < kFreqChunk * kStageSteps; t += kDftThreads) {
     const int f = t / kStageSteps, s = t % kStageSteps;
     double c = 0.0, sn = 0.0;
-    const int n = d.n0 + s;
+    const int n = n0 + s;
     if (f0 + f < m.nfreq && s < d.nslots && n >= m.n_first && n <= m.n_last) {
       const double tt = (double)(n - 1) * d.dt;          // t=real(n-1,8)*dt
       sincos(d.omega[m.freq_off + f0 + f] * tt, &sn, &c);
@@ -86,6 +88,7 @@ template void launch_dft<double>(const DftParams &, const double *, void *);
 // one thread per monitored (component, cell) sample, plus one per probe.
 template <typename T>
 __global__ void gather_kernel(const __grid_constant__ StepParams<T> p) {
+  const int n = step_n(p);
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const T *F[6] = {p.ex, p.ey, p.ez, p.hx, p.hy, p.hz};
   for (int q = 0; q < p.nmon; ++q) {
@@ -107,8 +110,8 @@ __global__ void gather_kernel(const __grid_constant__ StepParams<T> p) {
   }
   if (t < p.nprobe) {
     const Probe &pr = p.probe[t];
-    if (p.n < pr.n_first || p.n > pr.n_last) return;
-    const long long st = p.n - pr.n_first;
+    if (n < pr.n_first || n > pr.n_last) return;
+    const long long st = n - pr.n_first;
     if (st >= pr.cap) return;
     const long long cell = (long long)pr.cell[0] + (long long)p.nx * (pr.cell[1] + (long long)p.ny * pr.cell[2]);
     for (int u = 0; u < pr.ncomp; ++u) {
