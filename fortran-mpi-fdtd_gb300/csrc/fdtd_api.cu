@@ -116,7 +116,8 @@ struct fdtd_job {
   // device state
   void *F[8] = {};  // ex ey ez hx hy hz ex_inc hz_inc
   uint8_t *d_mat = nullptr;
-  void *d_mc = nullptr, *d_ac = nullptr;
+  void *d_mc = nullptr, *d_ac = nullptr, *d_mca = nullptr, *d_mcs = nullptr;
+  uint8_t *d_rowflag = nullptr;
   int nade = 0, ade_stride = 0;
   int *d_ade_cell = nullptr;
   uint8_t *d_ade_mat = nullptr;
@@ -354,7 +355,15 @@ int commit_impl(fdtd_job *J) {
     if ((rc = alloc_dev(J, &J->F[6], (size_t)N * sizeof(T)))) return rc;
     if ((rc = alloc_dev(J, &J->F[7], (size_t)N * sizeof(T)))) return rc;
   }
-  // ---- materials: paint in call order ----
+  // ---- materials: device ids (constant dielectrics 1..127, dispersive
+  // materials kAdeId..255), painted in call order ----
+  std::vector<int> mid(J->mats.size());
+  int ndiel = 0, nadem = 0;
+  for (size_t m = 0; m < J->mats.size(); ++m) {
+    const bool ade = J->mats[m].kind == MK_GOLD || J->mats[m].kind == MK_GRAPHENE;
+    mid[m] = ade ? kAdeId + nadem++ : 1 + ndiel++;
+    if (ndiel >= kAdeId || nadem > 255 - kAdeId) return set_err(FDTD_ERANGE, "too many materials of one kind");
+  }
   std::vector<uint8_t> mat((size_t)N, 0);
   for (size_t m = 0; m < J->mats.size(); ++m) {
     int lo[3], hi[3];
@@ -362,7 +371,7 @@ int commit_impl(fdtd_job *J) {
     for (int k = lo[2]; k <= hi[2]; ++k)
       for (int j = lo[1]; j <= hi[1]; ++j)
         for (int i = lo[0]; i <= hi[0]; ++i)
-          if (inside(J, J->mats[m], i, j, k)) mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = (uint8_t)(m + 1);
+          if (inside(J, J->mats[m], i, j, k)) mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = (uint8_t)mid[m];
   }
   std::vector<MatCoef<T>> mc(kMaxMat);
   std::vector<AdeCoef<T>> ac;
@@ -370,7 +379,7 @@ int commit_impl(fdtd_job *J) {
   const double Ku = J->g.ku, dt = J->g.dt;
   for (size_t m = 0; m < J->mats.size(); ++m) {
     const MatRec &R = J->mats[m];
-    MatCoef<T> &c = mc[m + 1];
+    MatCoef<T> &c = mc[mid[m]];
     c.kind = R.kind;
     if (R.kind == MK_DIEL) {
       // gax = 1/constant_ep (M2/simpledielectric_mod.f90:176-186)
@@ -447,6 +456,13 @@ int commit_impl(fdtd_job *J) {
   if ((rc = alloc_dev(J, &J->d_mc, sizeof(MatCoef<T>) * kMaxMat))) return rc;
   CK(cudaMemcpy(J->d_mc, mc.data(), sizeof(MatCoef<T>) * kMaxMat, cudaMemcpyHostToDevice));
   J->h2d += sizeof(MatCoef<T>) * kMaxMat + sizeof(AdeCoef<T>) * ac.size();
+  {
+    std::vector<double> ca(kMaxMat, 0.0), cs(kMaxMat, 0.0);
+    for (int t = 0; t < kMaxMat; ++t)
+      if (mc[t].kind == MK_DIEL) { ca[t] = (double)mc[t].ca; cs[t] = (double)mc[t].cs; }
+    if ((rc = upload_vec<T>(J, &J->d_mca, ca))) return rc;
+    if ((rc = upload_vec<T>(J, &J->d_mcs, cs))) return rc;
+  }
   if ((rc = alloc_dev(J, &J->d_ac, sizeof(AdeCoef<T>) * std::max<size_t>(1, ac.size())))) return rc;
   if (!ac.empty()) CK(cudaMemcpy(J->d_ac, ac.data(), sizeof(AdeCoef<T>) * ac.size(), cudaMemcpyHostToDevice));
   // ---- ADE slots (dispersive cells) ----
@@ -583,6 +599,22 @@ int commit_impl(fdtd_job *J) {
     if (ref && J->dim == 3 && J->slab_rows > 0 && (P.d.cell[1] <= J->slab_rows - 1 || P.d.cell[1] >= ny - J->slab_rows))
       touches_slab = true;
   J->gather_fused = !touches_slab;
+  if (J->dim == 2) {
+    std::vector<uint8_t> rf((size_t)ny, 0);
+    for (auto &sr : J->srcs) {
+      if (sr.component == FDTD_EX_INC) continue;
+      for (int j = std::max(sr.lo[1], J->g.main_lo[1]); j <= std::min(sr.hi[1], J->g.main_hi[1]); ++j) rf[j] |= ROW_SRC;
+    }
+    for (auto &M : J->mons)
+      for (int j = M.d.lo[1]; j <= M.d.hi[1]; ++j) rf[j] |= ROW_SAMPLE;
+    for (auto &P : J->probes) rf[P.d.cell[1]] |= ROW_SAMPLE;
+    if (ref && J->slab_rows > 0)
+      for (int j = 0; j < ny; ++j)
+        if (j < J->slab_rows || j >= ny - J->slab_rows) rf[j] |= ROW_SLAB;
+    if ((rc = alloc_dev(J, (void **)&J->d_rowflag, (size_t)ny))) return rc;
+    CK(cudaMemcpy(J->d_rowflag, rf.data(), (size_t)ny, cudaMemcpyHostToDevice));
+    J->h2d += (uint64_t)ny;
+  }
   J->stage_row = base;
   J->acc_total = acc;
   if (!omega.empty()) {
@@ -627,6 +659,9 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   p.hx = (T *)J->F[3]; p.hy = (T *)J->F[4]; p.hz = (T *)J->F[5];
   p.mat = J->d_mat;
   p.mc = (const MatCoef<T> *)J->d_mc;
+  p.mca = (const T *)J->d_mca;
+  p.mcs = (const T *)J->d_mcs;
+  p.rowflag = J->d_rowflag;
   p.nade = J->nade;
   p.ade_cell = J->d_ade_cell;
   p.ade_mat = J->d_ade_mat;

@@ -89,8 +89,11 @@ struct StepParams {
   T ku;
   // fields (E/H components; null when the layout lacks them)
   T *ex, *ey, *ez, *hx, *hy, *hz;
-  const uint8_t *mat;
+  const uint8_t *mat;      // material id per cell: 0 none, 1..127 constant
+                           // dielectric, 128..255 dispersive (ADE slots)
   const MatCoef<T> *mc;
+  const T *mca, *mcs;      // per id: Ku/eps and 1/eps (0 for none and ADE ids)
+  const uint8_t *rowflag;  // 2D: per row, ROW_* bits
   // ADE slots
   int nade;
   const int *ade_cell;     // linear cell index
@@ -137,6 +140,10 @@ struct StepParams {
                            // device; then n = *d_base + slot
   int vec;                 // cells per thread along x in the 2D tile path
 };
+
+// per-row flags of the 2D tile path (precomputed from the job's set-up)
+enum RowFlag : int { ROW_SRC = 1, ROW_SAMPLE = 2, ROW_SLAB = 4 };
+constexpr int kAdeId = 128;  // material ids >= kAdeId are dispersive
 
 enum Role : int {
   ROLE_MAIN = 1,  // Yee update + materials on main cells

@@ -26,48 +26,19 @@ namespace fdtd {
 
 constexpr int kRows = 4;  // rows per warp
 
-template <typename T>
-struct Smem {
-  T ca[kMaxMat];
-  T cs[kMaxMat];
-  unsigned ade[kMaxMat / 32];
-};
-
-template <typename T>
-__device__ __forceinline__ void load_smem(const StepParams<T> &p, Smem<T> &sm) {
-  for (int t = threadIdx.x; t < kMaxMat; t += blockDim.x) {
-    const MatCoef<T> mc = p.mc[t];
-    sm.ca[t] = mc.kind == MK_DIEL ? mc.ca : T(0);
-    sm.cs[t] = mc.kind == MK_DIEL ? mc.cs : T(0);
-  }
-  if (threadIdx.x < kMaxMat / 32) {
-    unsigned m = 0;
-    for (int b = 0; b < 32; ++b) {
-      const int k = p.mc[threadIdx.x * 32 + b].kind;
-      if (k == MK_GOLD || k == MK_GRAPHENE) m |= 1u << b;
-    }
-    sm.ade[threadIdx.x] = m;
-  }
-  __syncthreads();
-}
-
-template <typename T>
-__device__ __forceinline__ bool is_ade(const Smem<T> &sm, uint8_t id) {
-  return (sm.ade[id >> 5] >> (id & 31)) & 1u;
-}
-
 // store V values, skipping cells whose E belongs to an ADE thread
+// (material ids >= kAdeId)
 template <typename T, int V>
-__device__ __forceinline__ void st_guard(T *a, const T (&v)[V], const uint8_t (&id)[V], const Smem<T> &sm) {
+__device__ __forceinline__ void st_guard(T *a, const T (&v)[V], const uint8_t (&id)[V]) {
   bool any = false;
 #pragma unroll
-  for (int q = 0; q < V; ++q) any |= is_ade(sm, id[q]);
+  for (int q = 0; q < V; ++q) any |= id[q] >= kAdeId;
   if (!any) {
     vst<T, V>(a, v);
   } else {
 #pragma unroll
     for (int q = 0; q < V; ++q)
-      if (!is_ade(sm, id[q])) a[q] = v[q];
+      if (id[q] < kAdeId) a[q] = v[q];
   }
 }
 
@@ -122,12 +93,8 @@ struct K2 {
     return true;
   }
 
-  static __device__ __forceinline__ bool slab_row(const StepParams<T> &p, int j) {
-    return p.pml_mode == 1 && ((p.slab_on[0] && j < p.slab_rows) || (p.slab_on[1] && j >= p.slab_j0[1]));
-  }
-
   // ---- E half step ------------------------------------------------------
-  static __device__ __forceinline__ void tile_e(const StepParams<T> &p, int bx, const Smem<T> &sm, int n) {
+  static __device__ __forceinline__ void tile_e(const StepParams<T> &p, int bx, int n) {
     const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
     const int tx = bx % p.tiles_x, ty = bx / p.tiles_x;
     const int i0 = (tx * 32 + lane) * V;
@@ -136,137 +103,153 @@ struct K2 {
     if (j0 >= ny) return;  // whole warp
     const bool inx = i0 < nx;
     const bool do_main = p.roles & ROLE_MAIN, do_pml = p.roles & ROLE_PML;
-    const bool shell_x = p.pml_mode == 2 && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
+    const bool split = p.pml_mode == 2;
+    const bool shell_x = split && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
     const bool main_x = i0 >= p.mlo[0] && i0 + V - 1 <= p.mhi[0];
-    // the y-derivative component one row below
-    const T *ydc = L == 3 ? p.hx : p.hz;
-    T prev[V];
+    const int nr = min(kRows, ny - j0);
+    // ---- prefetch the rows of this thread (and the row below) ----
+    const T *ydc = L == 3 ? p.hx : p.hz;  // component with the y derivative
+    T prev[V], a0[kRows][V], a1[kRows][V], e0[kRows][V], e1[kRows][V];
+    uint8_t id[kRows][V];
+    uint8_t rf[kRows];
 #pragma unroll
     for (int q = 0; q < V; ++q) prev[q] = T(0);
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+#pragma unroll
+      for (int q = 0; q < V; ++q) { a0[r][q] = a1[r][q] = e0[r][q] = e1[r][q] = T(0); id[r][q] = 0; }
+      rf[r] = 0;
+    }
     if (inx) {
       if (j0 > 0) vld_ro<T, V>(ydc + (long long)(j0 - 1) * nx + i0, prev);
       else if (p.per[1]) vld_ro<T, V>(ydc + (long long)(ny - 1) * nx + i0, prev);
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        if (r >= nr) break;
+        const long long c = (long long)(j0 + r) * nx + i0;
+        if (L == 3) {
+          vld_ro<T, V>(p.hy + c, a0[r]);
+          vld_ro<T, V>(p.hx + c, a1[r]);
+          vld<T, V>(p.ez + c, e0[r]);
+        } else {
+          vld_ro<T, V>(p.hz + c, a0[r]);
+          vld<T, V>(p.ex + c, e0[r]);
+          vld<T, V>(p.ey + c, e1[r]);
+        }
+        vld_ids<V>(p.mat + c, id[r]);
+        rf[r] = __ldg(p.rowflag + j0 + r);
+      }
     }
+    // x neighbour at the left edge of each vector
+    T left[kRows];
+#pragma unroll
     for (int r = 0; r < kRows; ++r) {
+      left[r] = shfl_left(a0[r][V - 1], lane);
+      if (lane == 0 && inx && r < nr) left[r] = ld_x(L == 3 ? p.hy : p.hz, i0 - 1, j0 + r, nx, p.per[0]);
+    }
+    if (!inx) return;
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      if (r >= nr) break;
       const int j = j0 + r;
-      if (j >= ny) break;
       const long long c = (long long)j * nx + i0;
-      const bool shell_y = p.pml_mode == 2 && (j < p.slo[1] || j > p.shi[1]);
+      const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
       const bool main_y = j >= p.mlo[1] && j <= p.mhi[1];
       if (L == 3) {
         // TM: Ez += Ku/eps ((Hy(i)-Hy(i-1)) + (-Hx(j)+Hx(j-1)))
-        T hy[V], hx[V];
-#pragma unroll
-        for (int q = 0; q < V; ++q) { hy[q] = T(0); hx[q] = T(0); }
-        if (inx) { vld_ro<T, V>(p.hy + c, hy); vld_ro<T, V>(p.hx + c, hx); }
-        T hyl = shfl_left(hy[V - 1], lane);
-        if (lane == 0 && inx) hyl = ld_x(p.hy, i0 - 1, j, nx, p.per[0]);
         T dxp[V], dyp[V];
 #pragma unroll
         for (int q = 0; q < V; ++q) {
-          dxp[q] = hy[q] - (q ? hy[q - 1] : hyl);  // curlhyx
-          dyp[q] = -hx[q] + prev[q];             // curlhxy
-          prev[q] = hx[q];
+          dxp[q] = a0[r][q] - (q ? a0[r][q - 1] : left[r]);  // curlhyx
+          dyp[q] = -a1[r][q] + prev[q];                      // curlhxy
+          prev[q] = a1[r][q];
         }
-        if (!inx) continue;
-        if (shell_x || shell_y) {
-          // split-field shell cells (and the main cells of this vector)
-          T ez[V];
-          uint8_t id[V];
-          vld<T, V>(p.ez + c, ez);
-          vld_ids<V>(p.mat + c, id);
-          bool wrote = false;
+        T (&ez)[V] = e0[r];
+        if (!shell_x && !shell_y && main_x && main_y && !(rf[r] & ROW_SRC)) {
+          if (do_main) {
 #pragma unroll
-          for (int q = 0; q < V; ++q) {
-            const int i = i0 + q;
-            if (i < p.slo[0] || i > p.shi[0] || shell_y) {
-              if (do_pml) {
-                const long long cc = c + q;
-                const T ezx = p.sp[0][cc];
-                const T ezy = kTwoParts<T> ? p.sp[6][cc] : ez[q] - ezx;
-                const T nezx = p.cf1[0][i] * ezx + p.cf2[0][i] * dxp[q];
-                const T nezy = p.cf1[1][j] * ezy + p.cf2[1][j] * dyp[q];
-                p.sp[0][cc] = nezx;
-                if (kTwoParts<T>) p.sp[6][cc] = nezy;
-                ez[q] = nezx + nezy;
-                wrote = true;
-              }
-            } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-              ez[q] = ez[q] + sm.ca[id[q]] * (dxp[q] + dyp[q]);
-              if (p.nsrc) {
-                const T s = src_sum<T>(p, n, 2, i, j, 0);
-                if (s != T(0)) ez[q] += sm.cs[id[q]] * s;
-              }
-              wrote = true;
-            }
+            for (int q = 0; q < V; ++q) ez[q] = ez[q] + __ldg(p.mca + id[r][q]) * (dxp[q] + dyp[q]);
+            st_guard<T, V>(p.ez + c, ez, id[r]);
           }
-          if (wrote) st_guard<T, V>(p.ez + c, ez, id, sm);
-        } else if (do_main && main_y) {
-          T ez[V];
-          uint8_t id[V];
-          vld<T, V>(p.ez + c, ez);
-          vld_ids<V>(p.mat + c, id);
-          const bool srow = p.nsrc && src_row(p, 2, j, 0);
-#pragma unroll
-          for (int q = 0; q < V; ++q) {
-            const int i = i0 + q;
-            if (main_x || (i >= p.mlo[0] && i <= p.mhi[0])) {
-              ez[q] = ez[q] + sm.ca[id[q]] * (dxp[q] + dyp[q]);
-              if (srow) {
-                const T s = src_sum<T>(p, n, 2, i, j, 0);
-                if (s != T(0)) ez[q] += sm.cs[id[q]] * s;
-              }
-            }
-          }
-          st_guard<T, V>(p.ez + c, ez, id, sm);
+          continue;
         }
-      } else {
-        // TE: Ex += Ku/eps (Hz(j)-Hz(j-1)), Ey -= Ku/eps (Hz(i)-Hz(i-1))
-        T hz[V];
-#pragma unroll
-        for (int q = 0; q < V; ++q) hz[q] = T(0);
-        if (inx) vld_ro<T, V>(p.hz + c, hz);
-        T hzl = shfl_left(hz[V - 1], lane);
-        if (lane == 0 && inx) hzl = ld_x(p.hz, i0 - 1, j, nx, p.per[0]);
-        T chx[V], chy[V], left[V];
+        bool wrote = false;
 #pragma unroll
         for (int q = 0; q < V; ++q) {
-          left[q] = q ? hz[q - 1] : hzl;
-          chx[q] = hz[q] - left[q];              // curlhx
-          chy[q] = hz[q] - prev[q];              // curlhy
+          const int i = i0 + q;
+          if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
+            if (do_pml) {
+              // Ez = Ezx + Ezy (3D/BERpmly_mod.f90:151,153 with d/dz = 0)
+              const long long cc = c + q;
+              const T ezx = p.sp[0][cc];
+              const T ezy = kTwoParts<T> ? p.sp[6][cc] : ez[q] - ezx;
+              const T nezx = p.cf1[0][i] * ezx + p.cf2[0][i] * dxp[q];
+              const T nezy = p.cf1[1][j] * ezy + p.cf2[1][j] * dyp[q];
+              p.sp[0][cc] = nezx;
+              if (kTwoParts<T>) p.sp[6][cc] = nezy;
+              ez[q] = nezx + nezy;
+              wrote = true;
+            }
+          } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+            ez[q] = ez[q] + __ldg(p.mca + id[r][q]) * (dxp[q] + dyp[q]);
+            if (rf[r] & ROW_SRC) {
+              const T sv = src_sum<T>(p, n, 2, i, j, 0);
+              if (sv != T(0)) ez[q] += __ldg(p.mcs + id[r][q]) * sv;
+            }
+            wrote = true;
+          }
+        }
+        if (wrote) st_guard<T, V>(p.ez + c, ez, id[r]);
+      } else {
+        // TE: Ex += Ku/eps (Hz(j)-Hz(j-1)), Ey -= Ku/eps (Hz(i)-Hz(i-1))
+        const T *hz = a0[r];
+        T chx[V], chy[V], lft[V];
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          lft[q] = q ? hz[q - 1] : left[r];
+          chx[q] = hz[q] - lft[q];   // curlhx
+          chy[q] = hz[q] - prev[q];  // curlhy
           prev[q] = hz[q];
         }
-        if (!inx) continue;
-        const bool srow = p.nsrc && (src_row(p, 0, j, 0) || src_row(p, 1, j, 0));
+        T (&ex)[V] = e0[r];
+        T (&ey)[V] = e1[r];
+        if (!shell_x && !shell_y && main_x && main_y && !(rf[r] & (ROW_SRC | ROW_SLAB))) {
+          if (do_main) {
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+              const T ca = __ldg(p.mca + id[r][q]);
+              ex[q] = ex[q] + ca * chy[q];
+              ey[q] = ey[q] - ca * chx[q];
+            }
+            st_guard<T, V>(p.ex + c, ex, id[r]);
+            st_guard<T, V>(p.ey + c, ey, id[r]);
+          }
+          continue;
+        }
         if (shell_x || shell_y || (do_main && main_y)) {
-          T ex[V], ey[V];
-          uint8_t id[V];
-          vld<T, V>(p.ex + c, ex);
-          vld<T, V>(p.ey + c, ey);
-          vld_ids<V>(p.mat + c, id);
 #pragma unroll
           for (int q = 0; q < V; ++q) {
             const int i = i0 + q;
-            if (p.pml_mode == 2 && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
+            if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
               if (do_pml) {
                 ex[q] = p.cf1[1][j] * ex[q] + p.cf2[1][j] * chy[q];
-                ey[q] = p.cf1[0][i] * ey[q] + p.cf2[0][i] * (-hz[q] + left[q]);
+                ey[q] = p.cf1[0][i] * ey[q] + p.cf2[0][i] * (-hz[q] + lft[q]);
               }
             } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-              const T ca = sm.ca[id[q]];
+              const T ca = __ldg(p.mca + id[r][q]);
               ex[q] = ex[q] + ca * chy[q];
               ey[q] = ey[q] - ca * chx[q];
-              if (srow) {
+              if (rf[r] & ROW_SRC) {
                 const T sx = src_sum<T>(p, n, 0, i, j, 0), sy = src_sum<T>(p, n, 1, i, j, 0);
-                if (sx != T(0)) ex[q] += sm.cs[id[q]] * sx;
-                if (sy != T(0)) ey[q] += sm.cs[id[q]] * sy;
+                if (sx != T(0)) ex[q] += __ldg(p.mcs + id[r][q]) * sx;
+                if (sy != T(0)) ey[q] += __ldg(p.mcs + id[r][q]) * sy;
               }
             }
           }
-          st_guard<T, V>(p.ex + c, ex, id, sm);
-          st_guard<T, V>(p.ey + c, ey, id, sm);
+          st_guard<T, V>(p.ex + c, ex, id[r]);
+          st_guard<T, V>(p.ey + c, ey, id[r]);
         }
-        if (do_pml && slab_row(p, j)) {
+        if (do_pml && (rf[r] & ROW_SLAB)) {
 #pragma unroll
           for (int q = 0; q < V; ++q) ref_slab_e(p, i0 + q, j);
         }
@@ -284,116 +267,157 @@ struct K2 {
     if (j0 >= ny) return;
     const bool inx = i0 < nx;
     const bool do_main = p.roles & ROLE_MAIN, do_pml = p.roles & ROLE_PML;
-    const bool shell_x = p.pml_mode == 2 && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
-    const T *ydc = L == 3 ? p.ez : p.ex;   // E component with a y derivative
-    T cur[V];
+    const bool split = p.pml_mode == 2;
+    const bool shell_x = split && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
+    const bool main_x = i0 >= p.mlo[0] && i0 + V - 1 <= p.mhi[0];
+    const int nr = min(kRows, ny - j0);
+    const T *ydc = L == 3 ? p.ez : p.ex;  // E component with a y derivative
+    // rows j0..j0+nr of ydc (one more above), the other E (TE: Ey) and H
+    T ey_[kRows + 1][V], eo[kRows][V], h0[kRows][V], h1[kRows][V];
+    uint8_t rf[kRows];
 #pragma unroll
-    for (int q = 0; q < V; ++q) cur[q] = T(0);
-    if (inx) vld_ro<T, V>(ydc + (long long)j0 * nx + i0, cur);
+    for (int r = 0; r <= kRows; ++r)
+#pragma unroll
+      for (int q = 0; q < V; ++q) ey_[r][q] = T(0);
+#pragma unroll
     for (int r = 0; r < kRows; ++r) {
-      const int j = j0 + r;
-      if (j >= ny) break;
-      const long long c = (long long)j * nx + i0;
-      T up[V];
 #pragma unroll
-      for (int q = 0; q < V; ++q) up[q] = T(0);
-      if (inx) {
-        if (j + 1 < ny) vld_ro<T, V>(ydc + c + nx, up);
-        else if (p.per[1]) vld_ro<T, V>(ydc + i0, up);
+      for (int q = 0; q < V; ++q) eo[r][q] = h0[r][q] = h1[r][q] = T(0);
+      rf[r] = 0;
+    }
+    if (inx) {
+#pragma unroll
+      for (int r = 0; r <= kRows; ++r) {
+        if (r > nr) break;
+        const int j = j0 + r;
+        if (j < ny) vld_ro<T, V>(ydc + (long long)j * nx + i0, ey_[r]);
+        else if (p.per[1]) vld_ro<T, V>(ydc + i0, ey_[r]);
       }
-      const bool shell_y = p.pml_mode == 2 && (j < p.slo[1] || j > p.shi[1]);
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        if (r >= nr) break;
+        const long long c = (long long)(j0 + r) * nx + i0;
+        if (L == 3) {
+          vld<T, V>(p.hx + c, h0[r]);
+          vld<T, V>(p.hy + c, h1[r]);
+        } else {
+          vld_ro<T, V>(p.ey + c, eo[r]);
+          vld<T, V>(p.hz + c, h0[r]);
+        }
+        rf[r] = __ldg(p.rowflag + j0 + r);
+      }
+    }
+    // x neighbour at the right edge of each vector (the x-derivative component)
+    T right[kRows];
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      const T first = L == 3 ? ey_[r][0] : eo[r][0];
+      right[r] = shfl_right(first, lane);
+      if ((lane == 31 || i0 + V >= nx) && inx && r < nr) right[r] = ld_x(L == 3 ? p.ez : p.ey, i0 + V, j0 + r, nx, p.per[0]);
+    }
+    if (!inx) return;
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      if (r >= nr) break;
+      const int j = j0 + r;
+      const long long c = (long long)j * nx + i0;
+      const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
       const bool main_y = j >= p.mlo[1] && j <= p.mhi[1];
-      const bool srow = p.gather && sample_row(p, j, 0);
+      const bool srow = p.gather && (rf[r] & ROW_SAMPLE);
+      const T *cur = ey_[r], *up = ey_[r + 1];
       if (L == 3) {
-        T ez[V];
-#pragma unroll
-        for (int q = 0; q < V; ++q) ez[q] = cur[q];
-        T ezr = shfl_right(ez[0], lane);
-        if ((lane == 31 || i0 + V >= nx) && inx) ezr = ld_x(p.ez, i0 + V, j, nx, p.per[0]);
-#pragma unroll
-        for (int q = 0; q < V; ++q) cur[q] = up[q];
-        if (!inx) continue;
-        if (shell_x || shell_y || (do_main && main_y) || srow) {
-          T hx[V], hy[V];
-          vld<T, V>(p.hx + c, hx);
-          vld<T, V>(p.hy + c, hy);
-          bool wrote = false;
-#pragma unroll
-          for (int q = 0; q < V; ++q) {
-            const int i = i0 + q;
-            const T right = q < V - 1 ? ez[q + 1] : ezr;
-            if (p.pml_mode == 2 && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
-              if (do_pml) {
-                hx[q] = p.cg1[1][j] * hx[q] + p.cg2[1][j] * (-up[q] + ez[q]);
-                hy[q] = p.cg1[0][i] * hy[q] + p.cg2[0][i] * (right - ez[q]);
-                wrote = true;
-              }
-            } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-              hx[q] = hx[q] + p.ku * (-up[q] + ez[q]);
-              hy[q] = hy[q] + p.ku * (right - ez[q]);
-              wrote = true;
-            }
-          }
-          if (wrote) { vst<T, V>(p.hx + c, hx); vst<T, V>(p.hy + c, hy); }
-          if (srow) {
+        T (&hx)[V] = h0[r];
+        T (&hy)[V] = h1[r];
+        if (!shell_x && !shell_y && main_x && main_y && !srow) {
+          if (do_main) {
 #pragma unroll
             for (int q = 0; q < V; ++q) {
-              const T vals[6] = {T(0), T(0), ez[q], hx[q], hy[q], T(0)};
-              gather_cell<T>(p, n, i0 + q, j, 0, vals);
+              const T rgt = q < V - 1 ? cur[q + 1] : right[r];
+              hx[q] = hx[q] + p.ku * (-up[q] + cur[q]);
+              hy[q] = hy[q] + p.ku * (rgt - cur[q]);
             }
+            vst<T, V>(p.hx + c, hx);
+            vst<T, V>(p.hy + c, hy);
+          }
+          continue;
+        }
+        bool wrote = false;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const int i = i0 + q;
+          const T rgt = q < V - 1 ? cur[q + 1] : right[r];
+          if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
+            if (do_pml) {
+              hx[q] = p.cg1[1][j] * hx[q] + p.cg2[1][j] * (-up[q] + cur[q]);
+              hy[q] = p.cg1[0][i] * hy[q] + p.cg2[0][i] * (rgt - cur[q]);
+              wrote = true;
+            }
+          } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+            hx[q] = hx[q] + p.ku * (-up[q] + cur[q]);
+            hy[q] = hy[q] + p.ku * (rgt - cur[q]);
+            wrote = true;
+          }
+        }
+        if (wrote) { vst<T, V>(p.hx + c, hx); vst<T, V>(p.hy + c, hy); }
+        if (srow) {
+#pragma unroll
+          for (int q = 0; q < V; ++q) {
+            const T vals[6] = {T(0), T(0), cur[q], hx[q], hy[q], T(0)};
+            gather_cell<T>(p, n, i0 + q, j, 0, vals);
           }
         }
       } else {
-        T ex[V], ey[V];
+        T (&hz)[V] = h0[r];
+        const T *ex = cur, *ey = eo[r];
+        const bool slab = do_pml && (rf[r] & ROW_SLAB);
+        if (!shell_x && !shell_y && main_x && main_y && !srow && !slab) {
+          if (do_main) {
 #pragma unroll
-        for (int q = 0; q < V; ++q) { ex[q] = cur[q]; ey[q] = T(0); }
-        if (inx) vld_ro<T, V>(p.ey + c, ey);
-        T eyr = shfl_right(ey[0], lane);
-        if ((lane == 31 || i0 + V >= nx) && inx) eyr = ld_x(p.ey, i0 + V, j, nx, p.per[0]);
-#pragma unroll
-        for (int q = 0; q < V; ++q) cur[q] = up[q];
-        if (!inx) continue;
-        const bool slab = do_pml && slab_row(p, j);
-        if (shell_x || shell_y || (do_main && main_y) || srow || slab) {
-          T hz[V];
-          vld<T, V>(p.hz + c, hz);
-          bool wrote = false;
-#pragma unroll
-          for (int q = 0; q < V; ++q) {
-            const int i = i0 + q;
-            const T right = q < V - 1 ? ey[q + 1] : eyr;
-            if (p.pml_mode == 2 && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
-              if (do_pml) {
-                const long long cc = c + q;
-                T hzx = p.sp[0][cc];
-                T hzy = kTwoParts<T> ? p.sp[6][cc] : hz[q] - hzx;
-                hzy = p.cg1[1][j] * hzy + p.cg2[1][j] * (up[q] - ex[q]);
-                hzx = p.cg1[0][i] * hzx + p.cg2[0][i] * (-right + ey[q]);
-                p.sp[0][cc] = hzx;
-                if (kTwoParts<T>) p.sp[6][cc] = hzy;
-                hz[q] = hzy + hzx;
-                wrote = true;
-              }
-            } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-              const T curlE = ((right - ey[q]) - up[q]) + ex[q];
+            for (int q = 0; q < V; ++q) {
+              const T rgt = q < V - 1 ? ey[q + 1] : right[r];
+              const T curlE = ((rgt - ey[q]) - up[q]) + ex[q];
               hz[q] = hz[q] - p.ku * curlE;
+            }
+            vst<T, V>(p.hz + c, hz);
+          }
+          continue;
+        }
+        bool wrote = false;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const int i = i0 + q;
+          const T rgt = q < V - 1 ? ey[q + 1] : right[r];
+          if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
+            if (do_pml) {
+              const long long cc = c + q;
+              T hzx = p.sp[0][cc];
+              T hzy = kTwoParts<T> ? p.sp[6][cc] : hz[q] - hzx;
+              hzy = p.cg1[1][j] * hzy + p.cg2[1][j] * (up[q] - ex[q]);
+              hzx = p.cg1[0][i] * hzx + p.cg2[0][i] * (-rgt + ey[q]);
+              p.sp[0][cc] = hzx;
+              if (kTwoParts<T>) p.sp[6][cc] = hzy;
+              hz[q] = hzy + hzx;
               wrote = true;
             }
+          } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+            const T curlE = ((rgt - ey[q]) - up[q]) + ex[q];
+            hz[q] = hz[q] - p.ku * curlE;
+            wrote = true;
           }
-          if (wrote) vst<T, V>(p.hz + c, hz);
-          if (slab) {
+        }
+        if (wrote) vst<T, V>(p.hz + c, hz);
+        if (slab) {
 #pragma unroll
-            for (int q = 0; q < V; ++q) {
-              T v;
-              if (ref_slab_h(p, i0 + q, j, &v)) hz[q] = v;
-            }
+          for (int q = 0; q < V; ++q) {
+            T v;
+            if (ref_slab_h(p, i0 + q, j, &v)) hz[q] = v;
           }
-          if (srow) {
+        }
+        if (srow) {
 #pragma unroll
-            for (int q = 0; q < V; ++q) {
-              const T vals[6] = {ex[q], ey[q], T(0), T(0), T(0), hz[q]};
-              gather_cell<T>(p, n, i0 + q, j, 0, vals);
-            }
+          for (int q = 0; q < V; ++q) {
+            const T vals[6] = {ex[q], ey[q], T(0), T(0), T(0), hz[q]};
+            gather_cell<T>(p, n, i0 + q, j, 0, vals);
           }
         }
       }
@@ -430,10 +454,7 @@ __global__ void __launch_bounds__(256) e2d_kernel(const __grid_constant__ StepPa
   const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
-    if (!(p.roles & (ROLE_MAIN | ROLE_PML))) return;
-    __shared__ Smem<T> sm;
-    load_smem(p, sm);
-    K2<T, L, V>::tile_e(p, b, sm, n);
+    if (p.roles & (ROLE_MAIN | ROLE_PML)) K2<T, L, V>::tile_e(p, b, n);
     return;
   }
   b -= p.ntile_blocks;
