@@ -110,6 +110,7 @@ struct fdtd_job {
   std::vector<ProbeRec> probes;
   bool committed = false;
   int device = 0;
+  int num_sms = 152;
   cudaStream_t stream = nullptr;
   std::vector<void *> allocs;
   uint64_t dev_bytes = 0;
@@ -687,11 +688,14 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   if (J->dim == 2) {
     const int vw = sizeof(T) == 4 ? 4 : 2;  // float4 / double2 rows when aligned
     p.vec = (J->nx % vw == 0) ? vw : 1;
-    p.tiles_x = (J->nx + 32 * p.vec - 1) / (32 * p.vec); p.tiles_y = (J->ny + 31) / 32; p.tiles_z = 1;
+    // grid-stride over (row, vector) units: up to 8 blocks of 256 per SM
+    const long long units = (long long)(J->nx / p.vec) * J->ny;
+    p.tiles_x = p.tiles_y = p.tiles_z = 0;
+    p.ntile_blocks = (int)std::min<long long>((units + 255) / 256, (long long)J->num_sms * 8);
   } else {
     p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 7) / 8; p.tiles_z = (J->nz + 15) / 16;
+    p.ntile_blocks = p.tiles_x * p.tiles_y * p.tiles_z;
   }
-  p.ntile_blocks = p.tiles_x * p.tiles_y * p.tiles_z;
   p.nslab_blocks = (J->dim == 3 && J->slab_rows > 0) ? (2 * J->nx * J->slab_rows * J->nz + 255) / 256 : 0;
   p.nade_blocks = (J->nade + 255) / 256;
   p.nmon = (int)J->mon_dev.size();
@@ -1207,6 +1211,7 @@ int fdtd_create(const fdtd_grid_desc *g, fdtd_job **out) {
   J->ncell = N;
   J->esz = g->precision == FDTD_F32 ? 4 : 8;
   J->device = dev;
+  cudaDeviceGetAttribute(&J->num_sms, cudaDevAttrMultiProcessorCount, dev);
   for (int a = 0; a < 3; ++a) {
     J->g.main_lo[a] = std::max(0, g->main_lo[a]);
     J->g.main_hi[a] = std::min(g->n[a] - 1, g->main_hi[a]);

@@ -1,12 +1,10 @@
 // k2d.cu -- 2D half-step kernels (TE: Ex, Ey, Hz; TM: Ez, Hx, Hy).
 //
 // One launch per half step; blockIdx selects the work:
-//   tile blocks : 32*V x 32 cells.  A warp owns a 32*V-cell row segment and
-//                 walks 4 rows, each thread V consecutive cells (float4 /
-//                 double2 loads when the row length allows).  The row's
-//                 inputs are loaded up front through the read-only path; the
-//                 x neighbour at a vector edge comes from a warp shuffle and
-//                 the previous row's value from registers.  Main cells do the
+//   grid-stride blocks : each thread takes (row, V-cell vector) units in
+//                 turn (float4 / double2 when the row length allows); inputs
+//                 come through the read-only path, the neighbour row and the
+//                 neighbour cell at the vector edge from L1.  Main cells do the
 //                 Yee update with the constant-dielectric material folded in
 //                 (E += Ku/eps * curl: the reference's D update and E = D*gax,
 //                 2D/.../myfdtd_2Dfunc.f90:16-44, 2D/simpledielectric_mod.f90:
@@ -23,8 +21,6 @@
 #include "kcommon.cuh"
 
 namespace fdtd {
-
-constexpr int kRows = 4;  // rows per warp
 
 // store V values, skipping cells whose E belongs to an ADE thread
 // (material ids >= kAdeId)
@@ -93,332 +89,252 @@ struct K2 {
     return true;
   }
 
-  // ---- E half step ------------------------------------------------------
-  static __device__ __forceinline__ void tile_e(const StepParams<T> &p, int bx, int n) {
-    const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
-    const int tx = bx % p.tiles_x, ty = bx / p.tiles_x;
-    const int i0 = (tx * 32 + lane) * V;
-    const int j0 = ty * (8 * kRows) + wy * kRows;
+  // ---- E half step: one (row, V-cell vector) unit ------------------------
+  static __device__ __forceinline__ void unit_e(const StepParams<T> &p, long long t, int n) {
+    const int nvec = p.nx / V;
+    const int j = (int)(t / nvec), i0 = (int)(t % nvec) * V;
     const int nx = p.nx, ny = p.ny;
-    if (j0 >= ny) return;  // whole warp
-    const bool inx = i0 < nx;
+    const long long c = (long long)j * nx + i0;
     const bool do_main = p.roles & ROLE_MAIN, do_pml = p.roles & ROLE_PML;
     const bool split = p.pml_mode == 2;
-    const bool shell_x = split && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
+    const bool shell = split && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0] || j < p.slo[1] || j > p.shi[1]);
+    const bool main_y = j >= p.mlo[1] && j <= p.mhi[1];
     const bool main_x = i0 >= p.mlo[0] && i0 + V - 1 <= p.mhi[0];
-    const int nr = min(kRows, ny - j0);
-    // ---- prefetch the rows of this thread (and the row below) ----
+    const int rf = __ldg(p.rowflag + j);
     const T *ydc = L == 3 ? p.hx : p.hz;  // component with the y derivative
-    T prev[V], a0[kRows][V], a1[kRows][V], e0[kRows][V], e1[kRows][V];
-    uint8_t id[kRows][V];
-    uint8_t rf[kRows];
+    const T *xdc = L == 3 ? p.hy : p.hz;  // component with the x derivative
+    T below[V], a0[V], a1[V], e0[V], e1[V];
+    uint8_t id[V];
 #pragma unroll
-    for (int q = 0; q < V; ++q) prev[q] = T(0);
+    for (int q = 0; q < V; ++q) below[q] = T(0);
+    if (j > 0) vld_ro<T, V>(ydc + c - nx, below);
+    else if (p.per[1]) vld_ro<T, V>(ydc + (long long)(ny - 1) * nx + i0, below);
+    vld_ro<T, V>(xdc + c, a0);
+    const T left = i0 > 0 ? __ldg(xdc + c - 1) : (p.per[0] ? __ldg(xdc + c + nx - 1) : T(0));
+    vld_ids<V>(p.mat + c, id);
+    if (L == 3) {
+      vld_ro<T, V>(p.hx + c, a1);
+      vld<T, V>(p.ez + c, e0);
+      // TM: Ez += Ku/eps ((Hy(i)-Hy(i-1)) + (-Hx(j)+Hx(j-1)))
+      T dxp[V], dyp[V];
 #pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-#pragma unroll
-      for (int q = 0; q < V; ++q) { a0[r][q] = a1[r][q] = e0[r][q] = e1[r][q] = T(0); id[r][q] = 0; }
-      rf[r] = 0;
-    }
-    if (inx) {
-      if (j0 > 0) vld_ro<T, V>(ydc + (long long)(j0 - 1) * nx + i0, prev);
-      else if (p.per[1]) vld_ro<T, V>(ydc + (long long)(ny - 1) * nx + i0, prev);
-#pragma unroll
-      for (int r = 0; r < kRows; ++r) {
-        if (r >= nr) break;
-        const long long c = (long long)(j0 + r) * nx + i0;
-        if (L == 3) {
-          vld_ro<T, V>(p.hy + c, a0[r]);
-          vld_ro<T, V>(p.hx + c, a1[r]);
-          vld<T, V>(p.ez + c, e0[r]);
-        } else {
-          vld_ro<T, V>(p.hz + c, a0[r]);
-          vld<T, V>(p.ex + c, e0[r]);
-          vld<T, V>(p.ey + c, e1[r]);
-        }
-        vld_ids<V>(p.mat + c, id[r]);
-        rf[r] = __ldg(p.rowflag + j0 + r);
+      for (int q = 0; q < V; ++q) {
+        dxp[q] = a0[q] - (q ? a0[q - 1] : left);  // curlhyx
+        dyp[q] = -a1[q] + below[q];              // curlhxy
       }
-    }
-    // x neighbour at the left edge of each vector
-    T left[kRows];
+      if (!shell && main_x && main_y && !(rf & ROW_SRC)) {
+        if (do_main) {
 #pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      left[r] = shfl_left(a0[r][V - 1], lane);
-      if (lane == 0 && inx && r < nr) left[r] = ld_x(L == 3 ? p.hy : p.hz, i0 - 1, j0 + r, nx, p.per[0]);
-    }
-    if (!inx) return;
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      if (r >= nr) break;
-      const int j = j0 + r;
-      const long long c = (long long)j * nx + i0;
+          for (int q = 0; q < V; ++q) e0[q] = e0[q] + __ldg(p.mca + id[q]) * (dxp[q] + dyp[q]);
+          st_guard<T, V>(p.ez + c, e0, id);
+        }
+        return;
+      }
       const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
-      const bool main_y = j >= p.mlo[1] && j <= p.mhi[1];
-      if (L == 3) {
-        // TM: Ez += Ku/eps ((Hy(i)-Hy(i-1)) + (-Hx(j)+Hx(j-1)))
-        T dxp[V], dyp[V];
+      bool wrote = false;
 #pragma unroll
-        for (int q = 0; q < V; ++q) {
-          dxp[q] = a0[r][q] - (q ? a0[r][q - 1] : left[r]);  // curlhyx
-          dyp[q] = -a1[r][q] + prev[q];                      // curlhxy
-          prev[q] = a1[r][q];
-        }
-        T (&ez)[V] = e0[r];
-        if (!shell_x && !shell_y && main_x && main_y && !(rf[r] & ROW_SRC)) {
-          if (do_main) {
-#pragma unroll
-            for (int q = 0; q < V; ++q) ez[q] = ez[q] + __ldg(p.mca + id[r][q]) * (dxp[q] + dyp[q]);
-            st_guard<T, V>(p.ez + c, ez, id[r]);
+      for (int q = 0; q < V; ++q) {
+        const int i = i0 + q;
+        if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
+          if (do_pml) {
+            // Ez = Ezx + Ezy (3D/BERpmly_mod.f90:151,153 with d/dz = 0)
+            const long long cc = c + q;
+            const T ezx = p.sp[0][cc];
+            const T ezy = kTwoParts<T> ? p.sp[6][cc] : e0[q] - ezx;
+            const T nezx = p.cf1[0][i] * ezx + p.cf2[0][i] * dxp[q];
+            const T nezy = p.cf1[1][j] * ezy + p.cf2[1][j] * dyp[q];
+            p.sp[0][cc] = nezx;
+            if (kTwoParts<T>) p.sp[6][cc] = nezy;
+            e0[q] = nezx + nezy;
+            wrote = true;
           }
-          continue;
+        } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+          e0[q] = e0[q] + __ldg(p.mca + id[q]) * (dxp[q] + dyp[q]);
+          if (rf & ROW_SRC) {
+            const T sv = src_sum<T>(p, n, 2, i, j, 0);
+            if (sv != T(0)) e0[q] += __ldg(p.mcs + id[q]) * sv;
+          }
+          wrote = true;
         }
-        bool wrote = false;
+      }
+      if (wrote) st_guard<T, V>(p.ez + c, e0, id);
+    } else {
+      vld<T, V>(p.ex + c, e0);
+      vld<T, V>(p.ey + c, e1);
+      // TE: Ex += Ku/eps (Hz(j)-Hz(j-1)), Ey -= Ku/eps (Hz(i)-Hz(i-1))
+      T chx[V], chy[V], lft[V];
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        lft[q] = q ? a0[q - 1] : left;
+        chx[q] = a0[q] - lft[q];    // curlhx
+        chy[q] = a0[q] - below[q];  // curlhy
+      }
+      if (!shell && main_x && main_y && !(rf & (ROW_SRC | ROW_SLAB))) {
+        if (do_main) {
+#pragma unroll
+          for (int q = 0; q < V; ++q) {
+            const T ca = __ldg(p.mca + id[q]);
+            e0[q] = e0[q] + ca * chy[q];
+            e1[q] = e1[q] - ca * chx[q];
+          }
+          st_guard<T, V>(p.ex + c, e0, id);
+          st_guard<T, V>(p.ey + c, e1, id);
+        }
+        return;
+      }
+      const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
+      if (shell || (do_main && main_y)) {
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const int i = i0 + q;
           if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
             if (do_pml) {
-              // Ez = Ezx + Ezy (3D/BERpmly_mod.f90:151,153 with d/dz = 0)
-              const long long cc = c + q;
-              const T ezx = p.sp[0][cc];
-              const T ezy = kTwoParts<T> ? p.sp[6][cc] : ez[q] - ezx;
-              const T nezx = p.cf1[0][i] * ezx + p.cf2[0][i] * dxp[q];
-              const T nezy = p.cf1[1][j] * ezy + p.cf2[1][j] * dyp[q];
-              p.sp[0][cc] = nezx;
-              if (kTwoParts<T>) p.sp[6][cc] = nezy;
-              ez[q] = nezx + nezy;
-              wrote = true;
+              e0[q] = p.cf1[1][j] * e0[q] + p.cf2[1][j] * chy[q];
+              e1[q] = p.cf1[0][i] * e1[q] + p.cf2[0][i] * (-a0[q] + lft[q]);
             }
           } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-            ez[q] = ez[q] + __ldg(p.mca + id[r][q]) * (dxp[q] + dyp[q]);
-            if (rf[r] & ROW_SRC) {
-              const T sv = src_sum<T>(p, n, 2, i, j, 0);
-              if (sv != T(0)) ez[q] += __ldg(p.mcs + id[r][q]) * sv;
-            }
-            wrote = true;
-          }
-        }
-        if (wrote) st_guard<T, V>(p.ez + c, ez, id[r]);
-      } else {
-        // TE: Ex += Ku/eps (Hz(j)-Hz(j-1)), Ey -= Ku/eps (Hz(i)-Hz(i-1))
-        const T *hz = a0[r];
-        T chx[V], chy[V], lft[V];
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-          lft[q] = q ? hz[q - 1] : left[r];
-          chx[q] = hz[q] - lft[q];   // curlhx
-          chy[q] = hz[q] - prev[q];  // curlhy
-          prev[q] = hz[q];
-        }
-        T (&ex)[V] = e0[r];
-        T (&ey)[V] = e1[r];
-        if (!shell_x && !shell_y && main_x && main_y && !(rf[r] & (ROW_SRC | ROW_SLAB))) {
-          if (do_main) {
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-              const T ca = __ldg(p.mca + id[r][q]);
-              ex[q] = ex[q] + ca * chy[q];
-              ey[q] = ey[q] - ca * chx[q];
-            }
-            st_guard<T, V>(p.ex + c, ex, id[r]);
-            st_guard<T, V>(p.ey + c, ey, id[r]);
-          }
-          continue;
-        }
-        if (shell_x || shell_y || (do_main && main_y)) {
-#pragma unroll
-          for (int q = 0; q < V; ++q) {
-            const int i = i0 + q;
-            if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
-              if (do_pml) {
-                ex[q] = p.cf1[1][j] * ex[q] + p.cf2[1][j] * chy[q];
-                ey[q] = p.cf1[0][i] * ey[q] + p.cf2[0][i] * (-hz[q] + lft[q]);
-              }
-            } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-              const T ca = __ldg(p.mca + id[r][q]);
-              ex[q] = ex[q] + ca * chy[q];
-              ey[q] = ey[q] - ca * chx[q];
-              if (rf[r] & ROW_SRC) {
-                const T sx = src_sum<T>(p, n, 0, i, j, 0), sy = src_sum<T>(p, n, 1, i, j, 0);
-                if (sx != T(0)) ex[q] += __ldg(p.mcs + id[r][q]) * sx;
-                if (sy != T(0)) ey[q] += __ldg(p.mcs + id[r][q]) * sy;
-              }
+            const T ca = __ldg(p.mca + id[q]);
+            e0[q] = e0[q] + ca * chy[q];
+            e1[q] = e1[q] - ca * chx[q];
+            if (rf & ROW_SRC) {
+              const T sx = src_sum<T>(p, n, 0, i, j, 0), sy = src_sum<T>(p, n, 1, i, j, 0);
+              if (sx != T(0)) e0[q] += __ldg(p.mcs + id[q]) * sx;
+              if (sy != T(0)) e1[q] += __ldg(p.mcs + id[q]) * sy;
             }
           }
-          st_guard<T, V>(p.ex + c, ex, id[r]);
-          st_guard<T, V>(p.ey + c, ey, id[r]);
         }
-        if (do_pml && (rf[r] & ROW_SLAB)) {
+        st_guard<T, V>(p.ex + c, e0, id);
+        st_guard<T, V>(p.ey + c, e1, id);
+      }
+      if (do_pml && (rf & ROW_SLAB)) {
 #pragma unroll
-          for (int q = 0; q < V; ++q) ref_slab_e(p, i0 + q, j);
-        }
+        for (int q = 0; q < V; ++q) ref_slab_e(p, i0 + q, j);
       }
     }
   }
 
-  // ---- H half step ------------------------------------------------------
-  static __device__ __forceinline__ void tile_h(const StepParams<T> &p, int bx, int n) {
-    const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
-    const int tx = bx % p.tiles_x, ty = bx / p.tiles_x;
-    const int i0 = (tx * 32 + lane) * V;
-    const int j0 = ty * (8 * kRows) + wy * kRows;
+  // ---- H half step: one (row, V-cell vector) unit ------------------------
+  static __device__ __forceinline__ void unit_h(const StepParams<T> &p, long long t, int n) {
+    const int nvec = p.nx / V;
+    const int j = (int)(t / nvec), i0 = (int)(t % nvec) * V;
     const int nx = p.nx, ny = p.ny;
-    if (j0 >= ny) return;
-    const bool inx = i0 < nx;
+    const long long c = (long long)j * nx + i0;
     const bool do_main = p.roles & ROLE_MAIN, do_pml = p.roles & ROLE_PML;
     const bool split = p.pml_mode == 2;
-    const bool shell_x = split && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
+    const bool shell = split && (i0 < p.slo[0] || i0 + V - 1 > p.shi[0] || j < p.slo[1] || j > p.shi[1]);
+    const bool main_y = j >= p.mlo[1] && j <= p.mhi[1];
     const bool main_x = i0 >= p.mlo[0] && i0 + V - 1 <= p.mhi[0];
-    const int nr = min(kRows, ny - j0);
+    const int rf = __ldg(p.rowflag + j);
+    const bool srow = p.gather && (rf & ROW_SAMPLE);
     const T *ydc = L == 3 ? p.ez : p.ex;  // E component with a y derivative
-    // rows j0..j0+nr of ydc (one more above), the other E (TE: Ey) and H
-    T ey_[kRows + 1][V], eo[kRows][V], h0[kRows][V], h1[kRows][V];
-    uint8_t rf[kRows];
+    const T *xdc = L == 3 ? p.ez : p.ey;  // E component with an x derivative
+    T cur[V], up[V], xe[V], h0[V], h1[V];
 #pragma unroll
-    for (int r = 0; r <= kRows; ++r)
+    for (int q = 0; q < V; ++q) up[q] = T(0);
+    vld_ro<T, V>(ydc + c, cur);
+    if (j + 1 < ny) vld_ro<T, V>(ydc + c + nx, up);
+    else if (p.per[1]) vld_ro<T, V>(ydc + i0, up);
+    if (L == 3) {
 #pragma unroll
-      for (int q = 0; q < V; ++q) ey_[r][q] = T(0);
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-#pragma unroll
-      for (int q = 0; q < V; ++q) eo[r][q] = h0[r][q] = h1[r][q] = T(0);
-      rf[r] = 0;
+      for (int q = 0; q < V; ++q) xe[q] = cur[q];
+    } else {
+      vld_ro<T, V>(p.ey + c, xe);
     }
-    if (inx) {
+    const T right = i0 + V < nx ? __ldg(xdc + c + V) : (p.per[0] ? __ldg(xdc + c + V - nx) : T(0));
+    if (L == 3) {
+      vld<T, V>(p.hx + c, h0);
+      vld<T, V>(p.hy + c, h1);
+      if (!shell && main_x && main_y && !srow) {
+        if (do_main) {
 #pragma unroll
-      for (int r = 0; r <= kRows; ++r) {
-        if (r > nr) break;
-        const int j = j0 + r;
-        if (j < ny) vld_ro<T, V>(ydc + (long long)j * nx + i0, ey_[r]);
-        else if (p.per[1]) vld_ro<T, V>(ydc + i0, ey_[r]);
-      }
-#pragma unroll
-      for (int r = 0; r < kRows; ++r) {
-        if (r >= nr) break;
-        const long long c = (long long)(j0 + r) * nx + i0;
-        if (L == 3) {
-          vld<T, V>(p.hx + c, h0[r]);
-          vld<T, V>(p.hy + c, h1[r]);
-        } else {
-          vld_ro<T, V>(p.ey + c, eo[r]);
-          vld<T, V>(p.hz + c, h0[r]);
+          for (int q = 0; q < V; ++q) {
+            const T rgt = q < V - 1 ? cur[q + 1] : right;
+            h0[q] = h0[q] + p.ku * (-up[q] + cur[q]);
+            h1[q] = h1[q] + p.ku * (rgt - cur[q]);
+          }
+          vst<T, V>(p.hx + c, h0);
+          vst<T, V>(p.hy + c, h1);
         }
-        rf[r] = __ldg(p.rowflag + j0 + r);
+        return;
       }
-    }
-    // x neighbour at the right edge of each vector (the x-derivative component)
-    T right[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      const T first = L == 3 ? ey_[r][0] : eo[r][0];
-      right[r] = shfl_right(first, lane);
-      if ((lane == 31 || i0 + V >= nx) && inx && r < nr) right[r] = ld_x(L == 3 ? p.ez : p.ey, i0 + V, j0 + r, nx, p.per[0]);
-    }
-    if (!inx) return;
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-      if (r >= nr) break;
-      const int j = j0 + r;
-      const long long c = (long long)j * nx + i0;
       const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
-      const bool main_y = j >= p.mlo[1] && j <= p.mhi[1];
-      const bool srow = p.gather && (rf[r] & ROW_SAMPLE);
-      const T *cur = ey_[r], *up = ey_[r + 1];
-      if (L == 3) {
-        T (&hx)[V] = h0[r];
-        T (&hy)[V] = h1[r];
-        if (!shell_x && !shell_y && main_x && main_y && !srow) {
-          if (do_main) {
+      bool wrote = false;
 #pragma unroll
-            for (int q = 0; q < V; ++q) {
-              const T rgt = q < V - 1 ? cur[q + 1] : right[r];
-              hx[q] = hx[q] + p.ku * (-up[q] + cur[q]);
-              hy[q] = hy[q] + p.ku * (rgt - cur[q]);
-            }
-            vst<T, V>(p.hx + c, hx);
-            vst<T, V>(p.hy + c, hy);
-          }
-          continue;
-        }
-        bool wrote = false;
-#pragma unroll
-        for (int q = 0; q < V; ++q) {
-          const int i = i0 + q;
-          const T rgt = q < V - 1 ? cur[q + 1] : right[r];
-          if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
-            if (do_pml) {
-              hx[q] = p.cg1[1][j] * hx[q] + p.cg2[1][j] * (-up[q] + cur[q]);
-              hy[q] = p.cg1[0][i] * hy[q] + p.cg2[0][i] * (rgt - cur[q]);
-              wrote = true;
-            }
-          } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-            hx[q] = hx[q] + p.ku * (-up[q] + cur[q]);
-            hy[q] = hy[q] + p.ku * (rgt - cur[q]);
+      for (int q = 0; q < V; ++q) {
+        const int i = i0 + q;
+        const T rgt = q < V - 1 ? cur[q + 1] : right;
+        if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
+          if (do_pml) {
+            h0[q] = p.cg1[1][j] * h0[q] + p.cg2[1][j] * (-up[q] + cur[q]);
+            h1[q] = p.cg1[0][i] * h1[q] + p.cg2[0][i] * (rgt - cur[q]);
             wrote = true;
           }
+        } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+          h0[q] = h0[q] + p.ku * (-up[q] + cur[q]);
+          h1[q] = h1[q] + p.ku * (rgt - cur[q]);
+          wrote = true;
         }
-        if (wrote) { vst<T, V>(p.hx + c, hx); vst<T, V>(p.hy + c, hy); }
-        if (srow) {
-#pragma unroll
-          for (int q = 0; q < V; ++q) {
-            const T vals[6] = {T(0), T(0), cur[q], hx[q], hy[q], T(0)};
-            gather_cell<T>(p, n, i0 + q, j, 0, vals);
-          }
-        }
-      } else {
-        T (&hz)[V] = h0[r];
-        const T *ex = cur, *ey = eo[r];
-        const bool slab = do_pml && (rf[r] & ROW_SLAB);
-        if (!shell_x && !shell_y && main_x && main_y && !srow && !slab) {
-          if (do_main) {
-#pragma unroll
-            for (int q = 0; q < V; ++q) {
-              const T rgt = q < V - 1 ? ey[q + 1] : right[r];
-              const T curlE = ((rgt - ey[q]) - up[q]) + ex[q];
-              hz[q] = hz[q] - p.ku * curlE;
-            }
-            vst<T, V>(p.hz + c, hz);
-          }
-          continue;
-        }
-        bool wrote = false;
+      }
+      if (wrote) { vst<T, V>(p.hx + c, h0); vst<T, V>(p.hy + c, h1); }
+      if (srow) {
 #pragma unroll
         for (int q = 0; q < V; ++q) {
-          const int i = i0 + q;
-          const T rgt = q < V - 1 ? ey[q + 1] : right[r];
-          if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
-            if (do_pml) {
-              const long long cc = c + q;
-              T hzx = p.sp[0][cc];
-              T hzy = kTwoParts<T> ? p.sp[6][cc] : hz[q] - hzx;
-              hzy = p.cg1[1][j] * hzy + p.cg2[1][j] * (up[q] - ex[q]);
-              hzx = p.cg1[0][i] * hzx + p.cg2[0][i] * (-rgt + ey[q]);
-              p.sp[0][cc] = hzx;
-              if (kTwoParts<T>) p.sp[6][cc] = hzy;
-              hz[q] = hzy + hzx;
-              wrote = true;
-            }
-          } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-            const T curlE = ((rgt - ey[q]) - up[q]) + ex[q];
-            hz[q] = hz[q] - p.ku * curlE;
+          const T vals[6] = {T(0), T(0), cur[q], h0[q], h1[q], T(0)};
+          gather_cell<T>(p, n, i0 + q, j, 0, vals);
+        }
+      }
+    } else {
+      vld<T, V>(p.hz + c, h0);
+      const bool slab = do_pml && (rf & ROW_SLAB);
+      if (!shell && main_x && main_y && !srow && !slab) {
+        if (do_main) {
+#pragma unroll
+          for (int q = 0; q < V; ++q) {
+            const T rgt = q < V - 1 ? xe[q + 1] : right;
+            const T curlE = ((rgt - xe[q]) - up[q]) + cur[q];
+            h0[q] = h0[q] - p.ku * curlE;
+          }
+          vst<T, V>(p.hz + c, h0);
+        }
+        return;
+      }
+      const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
+      bool wrote = false;
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        const int i = i0 + q;
+        const T rgt = q < V - 1 ? xe[q + 1] : right;
+        if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
+          if (do_pml) {
+            const long long cc = c + q;
+            T hzx = p.sp[0][cc];
+            T hzy = kTwoParts<T> ? p.sp[6][cc] : h0[q] - hzx;
+            hzy = p.cg1[1][j] * hzy + p.cg2[1][j] * (up[q] - cur[q]);
+            hzx = p.cg1[0][i] * hzx + p.cg2[0][i] * (-rgt + xe[q]);
+            p.sp[0][cc] = hzx;
+            if (kTwoParts<T>) p.sp[6][cc] = hzy;
+            h0[q] = hzy + hzx;
             wrote = true;
           }
+        } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+          const T curlE = ((rgt - xe[q]) - up[q]) + cur[q];
+          h0[q] = h0[q] - p.ku * curlE;
+          wrote = true;
         }
-        if (wrote) vst<T, V>(p.hz + c, hz);
-        if (slab) {
+      }
+      if (wrote) vst<T, V>(p.hz + c, h0);
+      if (slab) {
 #pragma unroll
-          for (int q = 0; q < V; ++q) {
-            T v;
-            if (ref_slab_h(p, i0 + q, j, &v)) hz[q] = v;
-          }
+        for (int q = 0; q < V; ++q) {
+          T v;
+          if (ref_slab_h(p, i0 + q, j, &v)) h0[q] = v;
         }
-        if (srow) {
+      }
+      if (srow) {
 #pragma unroll
-          for (int q = 0; q < V; ++q) {
-            const T vals[6] = {ex[q], ey[q], T(0), T(0), T(0), hz[q]};
-            gather_cell<T>(p, n, i0 + q, j, 0, vals);
-          }
+        for (int q = 0; q < V; ++q) {
+          const T vals[6] = {cur[q], xe[q], T(0), T(0), T(0), h0[q]};
+          gather_cell<T>(p, n, i0 + q, j, 0, vals);
         }
       }
     }
@@ -449,24 +365,32 @@ __device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
   }
 }
 
+// Block layout of a launch: the ADE blocks first (their dependent loads start
+// early), then the grid-stride blocks over (row, vector) units.
 template <typename T, int L, int V>
 __global__ void __launch_bounds__(256) e2d_kernel(const __grid_constant__ StepParams<T> p) {
   const int n = step_n(p);
   int b = blockIdx.x;
-  if (b < p.ntile_blocks) {
-    if (p.roles & (ROLE_MAIN | ROLE_PML)) K2<T, L, V>::tile_e(p, b, n);
+  if (b < p.nade_blocks) {
+    if (p.roles & ROLE_ADE) {
+      const int s = b * 256 + threadIdx.x;
+      if (s < p.nade) ade_e2<T, L>(p, s, n);
+    }
     return;
   }
-  b -= p.ntile_blocks;
-  if (p.roles & ROLE_ADE) {
-    const int s = b * 256 + threadIdx.x;
-    if (s < p.nade) ade_e2<T, L>(p, s, n);
-  }
+  if (!(p.roles & (ROLE_MAIN | ROLE_PML))) return;
+  b -= p.nade_blocks;
+  const long long units = (long long)(p.nx / V) * p.ny;
+  for (long long t = (long long)b * 256 + threadIdx.x; t < units; t += (long long)p.ntile_blocks * 256)
+    K2<T, L, V>::unit_e(p, t, n);
 }
 
 template <typename T, int L, int V>
 __global__ void __launch_bounds__(256) h2d_kernel(const __grid_constant__ StepParams<T> p) {
-  if ((int)blockIdx.x < p.ntile_blocks) K2<T, L, V>::tile_h(p, blockIdx.x, step_n(p));
+  const int n = step_n(p);
+  const long long units = (long long)(p.nx / V) * p.ny;
+  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < units; t += (long long)p.ntile_blocks * 256)
+    K2<T, L, V>::unit_h(p, t, n);
 }
 
 // V: cells per thread along x; 4 (float) / 2 (double) when the row length
