@@ -119,7 +119,9 @@ struct fdtd_job {
   uint8_t *d_mat = nullptr;
   void *d_mc = nullptr, *d_ac = nullptr, *d_mca = nullptr, *d_mcs = nullptr;
   uint8_t *d_rowflag = nullptr;
-  int nade = 0, ade_stride = 0;
+  int nade = 0, ade_stride = 0, id0 = 0;
+  int *d_ade_slot = nullptr;
+  std::vector<double> mca_host;
   int *d_ade_cell = nullptr;
   uint8_t *d_ade_mat = nullptr;
   void *d_ade_state = nullptr;
@@ -462,6 +464,7 @@ int commit_impl(fdtd_job *J) {
     for (int t = 0; t < kMaxMat; ++t)
       if (mc[t].kind == MK_DIEL) { ca[t] = (double)mc[t].ca; cs[t] = (double)mc[t].cs; }
     if ((rc = upload_vec<T>(J, &J->d_mca, ca))) return rc;
+    J->mca_host = ca;
     if ((rc = upload_vec<T>(J, &J->d_mcs, cs))) return rc;
   }
   if ((rc = alloc_dev(J, &J->d_ac, sizeof(AdeCoef<T>) * std::max<size_t>(1, ac.size())))) return rc;
@@ -490,6 +493,22 @@ int commit_impl(fdtd_job *J) {
     J->h2d += (uint64_t)J->nade * (sizeof(int) + 1);
   }
   if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)kAdeFields * 3 * std::max(32, J->ade_stride)))) return rc;
+  if (J->dim == 2 && J->nade) {
+    // cell -> ADE slot, read by the 2D units for dispersive cells only
+    std::vector<int> slot((size_t)N, -1);
+    for (int q = 0; q < J->nade; ++q) slot[(size_t)ade_cell[q]] = q;
+    if ((rc = alloc_dev(J, (void **)&J->d_ade_slot, (size_t)N * sizeof(int)))) return rc;
+    CK(cudaMemcpy(J->d_ade_slot, slot.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice));
+    J->h2d += (uint64_t)N * sizeof(int);
+  }
+  {
+    // most common constant-dielectric material: its Ku/eps is a kernel parameter
+    std::vector<long long> cnt(kMaxMat, 0);
+    for (long long c2 = 0; c2 < N; ++c2) cnt[mat[(size_t)c2]]++;
+    int best = 0;
+    for (int t = 1; t < kAdeId; ++t) if (cnt[t] > cnt[best]) best = t;
+    J->id0 = best;
+  }
   // ---- PML ----
   const double Kpml = dt * K.c0 / J->g.ds;  // dt*c0/ds (M3/BERpmly_mod.f90:506)
   if (split) {
@@ -663,6 +682,9 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   p.mca = (const T *)J->d_mca;
   p.mcs = (const T *)J->d_mcs;
   p.rowflag = J->d_rowflag;
+  p.ade_slot = J->d_ade_slot;
+  p.id0 = J->id0;
+  p.ca0 = J->mca_host.empty() ? T(0) : T(J->mca_host[J->id0]);
   p.nade = J->nade;
   p.ade_cell = J->d_ade_cell;
   p.ade_mat = J->d_ade_mat;
@@ -697,7 +719,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.ntile_blocks = p.tiles_x * p.tiles_y * p.tiles_z;
   }
   p.nslab_blocks = (J->dim == 3 && J->slab_rows > 0) ? (2 * J->nx * J->slab_rows * J->nz + 255) / 256 : 0;
-  p.nade_blocks = (J->nade + 255) / 256;
+  p.nade_blocks = J->dim == 2 ? 0 : (J->nade + 255) / 256;  // 2D: done by the units
   p.nmon = (int)J->mon_dev.size();
   for (int q = 0; q < p.nmon; ++q) p.mon[q] = J->mon_dev[q];
   p.stage = (T *)J->d_stage;

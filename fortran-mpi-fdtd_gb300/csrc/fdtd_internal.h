@@ -93,6 +93,9 @@ struct StepParams {
                            // dielectric, 128..255 dispersive (ADE slots)
   const MatCoef<T> *mc;
   const T *mca, *mcs;      // per id: Ku/eps and 1/eps (0 for none and ADE ids)
+  int id0;                 // most common material id of the main cells and
+  T ca0;                   //   its Ku/eps (no table lookup for it)
+  const int *ade_slot;     // 2D: per cell, its ADE slot (read for ids >= kAdeId)
   const uint8_t *rowflag;  // 2D: per row, ROW_* bits
   // ADE slots
   int nade;
