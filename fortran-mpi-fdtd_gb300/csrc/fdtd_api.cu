@@ -120,8 +120,8 @@ struct fdtd_job {
   void *d_mc = nullptr, *d_ac = nullptr, *d_mca = nullptr, *d_mcs = nullptr;
   uint8_t *d_rowflag = nullptr;
   int nade = 0, ade_stride = 0, id0 = 0;
-  int *d_ade_slot = nullptr;
   std::vector<double> mca_host;
+  std::vector<char> ac_host;  // AdeCoef<T> table, host copy
   int *d_ade_cell = nullptr;
   uint8_t *d_ade_mat = nullptr;
   void *d_ade_state = nullptr;
@@ -469,6 +469,7 @@ int commit_impl(fdtd_job *J) {
   }
   if ((rc = alloc_dev(J, &J->d_ac, sizeof(AdeCoef<T>) * std::max<size_t>(1, ac.size())))) return rc;
   if (!ac.empty()) CK(cudaMemcpy(J->d_ac, ac.data(), sizeof(AdeCoef<T>) * ac.size(), cudaMemcpyHostToDevice));
+  J->ac_host.assign((const char *)ac.data(), (const char *)ac.data() + sizeof(AdeCoef<T>) * ac.size());
   // ---- ADE slots (dispersive cells) ----
   std::vector<int> ade_cell;
   std::vector<uint8_t> ade_mat;
@@ -493,14 +494,6 @@ int commit_impl(fdtd_job *J) {
     J->h2d += (uint64_t)J->nade * (sizeof(int) + 1);
   }
   if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)kAdeFields * 3 * std::max(32, J->ade_stride)))) return rc;
-  if (J->dim == 2 && J->nade) {
-    // cell -> ADE slot, read by the 2D units for dispersive cells only
-    std::vector<int> slot((size_t)N, -1);
-    for (int q = 0; q < J->nade; ++q) slot[(size_t)ade_cell[q]] = q;
-    if ((rc = alloc_dev(J, (void **)&J->d_ade_slot, (size_t)N * sizeof(int)))) return rc;
-    CK(cudaMemcpy(J->d_ade_slot, slot.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice));
-    J->h2d += (uint64_t)N * sizeof(int);
-  }
   {
     // most common constant-dielectric material: its Ku/eps is a kernel parameter
     std::vector<long long> cnt(kMaxMat, 0);
@@ -682,13 +675,14 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   p.mca = (const T *)J->d_mca;
   p.mcs = (const T *)J->d_mcs;
   p.rowflag = J->d_rowflag;
-  p.ade_slot = J->d_ade_slot;
   p.id0 = J->id0;
   p.ca0 = J->mca_host.empty() ? T(0) : T(J->mca_host[J->id0]);
   p.nade = J->nade;
   p.ade_cell = J->d_ade_cell;
   p.ade_mat = J->d_ade_mat;
   p.ac = (const AdeCoef<T> *)J->d_ac;
+  for (size_t q = 0; q < J->ac_host.size() && q < (size_t)kAdeParam; ++q)
+    memcpy(&p.acp[q], J->ac_host.data() + q * sizeof(AdeCoef<T>), sizeof(AdeCoef<T>));
   p.ade_state = (T *)J->d_ade_state;
   p.ade_stride = J->ade_stride;
   p.pml_mode = J->has_pml ? J->pml.mode : 0;
@@ -719,7 +713,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.ntile_blocks = p.tiles_x * p.tiles_y * p.tiles_z;
   }
   p.nslab_blocks = (J->dim == 3 && J->slab_rows > 0) ? (2 * J->nx * J->slab_rows * J->nz + 255) / 256 : 0;
-  p.nade_blocks = J->dim == 2 ? 0 : (J->nade + 255) / 256;  // 2D: done by the units
+  p.nade_blocks = (J->nade + 255) / 256;
   p.nmon = (int)J->mon_dev.size();
   for (int q = 0; q < p.nmon; ++q) p.mon[q] = J->mon_dev[q];
   p.stage = (T *)J->d_stage;

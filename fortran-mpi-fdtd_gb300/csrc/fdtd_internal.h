@@ -95,13 +95,13 @@ struct StepParams {
   const T *mca, *mcs;      // per id: Ku/eps and 1/eps (0 for none and ADE ids)
   int id0;                 // most common material id of the main cells and
   T ca0;                   //   its Ku/eps (no table lookup for it)
-  const int *ade_slot;     // 2D: per cell, its ADE slot (read for ids >= kAdeId)
   const uint8_t *rowflag;  // 2D: per row, ROW_* bits
   // ADE slots
   int nade;
   const int *ade_cell;     // linear cell index
   const uint8_t *ade_mat;  // material id
   const AdeCoef<T> *ac;
+  AdeCoef<T> acp[4];       // the first dispersive materials' coefficients
   T *ade_state;            // [field][comp][slot], see AdeState
   int ade_stride;          // = padded nade
   // sources: boxes, and amp*g(t) of every step in a device table
@@ -146,7 +146,9 @@ struct StepParams {
 
 // per-row flags of the 2D tile path (precomputed from the job's set-up)
 enum RowFlag : int { ROW_SRC = 1, ROW_SAMPLE = 2, ROW_SLAB = 4 };
-constexpr int kAdeId = 128;  // material ids >= kAdeId are dispersive
+constexpr int kAdeId = 128;  // material ids >= kAdeId are dispersive;
+                             // id - kAdeId indexes the ADE coefficient table
+constexpr int kAdeParam = 4; // ADE coefficient sets passed as kernel parameters
 
 enum Role : int {
   ROLE_MAIN = 1,  // Yee update + materials on main cells

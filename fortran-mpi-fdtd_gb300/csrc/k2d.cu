@@ -13,8 +13,8 @@
 //                 reference PML; monitored rows stage their samples.
 //                 Sources, shells, slabs and samples are tested per row (warp
 //                 uniform) before any per-cell test.
-//   dispersive cells (gold Drude+2CP, 2D/gold_mod.f90:47-75) are updated by
-//   the unit that holds them, their state found through a cell -> slot map.
+//   ADE blocks  : one thread per dispersive cell (gold Drude+2CP,
+//                 2D/gold_mod.f90:47-75); tile threads never store E there.
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.h"
@@ -42,13 +42,6 @@ __device__ __forceinline__ void st_guard(T *a, const T (&v)[V], const uint8_t (&
 template <typename T>
 __device__ __forceinline__ T coef_ca(const StepParams<T> &p, uint8_t id) {
   return id == p.id0 ? p.ca0 : __ldg(p.mca + id);
-}
-
-// store V values; dispersive cells only when this launch owns them (ROLE_ADE)
-template <typename T, int V>
-__device__ __forceinline__ void st_guard_roles(const StepParams<T> &p, T *a, const T (&v)[V], const uint8_t (&id)[V]) {
-  if (p.roles & ROLE_ADE) vst<T, V>(a, v);
-  else st_guard<T, V>(a, v, id);
 }
 
 template <typename T, int L, int V>
@@ -135,10 +128,7 @@ struct K2 {
         dxp[q] = a0[q] - (q ? a0[q - 1] : left);  // curlhyx
         dyp[q] = -a1[q] + below[q];              // curlhxy
       }
-      bool anyade = false;
-#pragma unroll
-      for (int q = 0; q < V; ++q) anyade |= id[q] >= kAdeId;
-      if (!shell && main_x && main_y && !(rf & ROW_SRC) && !anyade) {
+      if (!shell && main_x && main_y && !(rf & ROW_SRC)) {
         if (do_main) {
           bool uni = true;
 #pragma unroll
@@ -146,11 +136,12 @@ struct K2 {
           if (uni) {
 #pragma unroll
             for (int q = 0; q < V; ++q) e0[q] = e0[q] + p.ca0 * (dxp[q] + dyp[q]);
+            vst<T, V>(p.ez + c, e0);
           } else {
 #pragma unroll
             for (int q = 0; q < V; ++q) e0[q] = e0[q] + coef_ca(p, id[q]) * (dxp[q] + dyp[q]);
+            st_guard<T, V>(p.ez + c, e0, id);
           }
-          vst<T, V>(p.ez + c, e0);
         }
         return;
       }
@@ -172,24 +163,16 @@ struct K2 {
             e0[q] = nezx + nezy;
             wrote = true;
           }
-        } else if (main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-          const T sv = (rf & ROW_SRC) ? src_sum<T>(p, n, 2, i, j, 0) : T(0);
-          if (id[q] >= kAdeId) {
-            // dispersive cell: its ADE update (2D/gold_mod.f90:47-75)
-            if (p.roles & ROLE_ADE) {
-              const int sl = __ldg(p.ade_slot + c + q);
-              const AdeCoef<T> &a = p.ac[p.mc[id[q]].ade];
-              e0[q] = ade_update<T>(p, a, sl, 0, p.ku * (dxp[q] + dyp[q]) + sv, e0[q]);
-              wrote = true;
-            }
-          } else if (do_main) {
-            e0[q] = e0[q] + coef_ca(p, id[q]) * (dxp[q] + dyp[q]);
+        } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+          e0[q] = e0[q] + coef_ca(p, id[q]) * (dxp[q] + dyp[q]);
+          if (rf & ROW_SRC) {
+            const T sv = src_sum<T>(p, n, 2, i, j, 0);
             if (sv != T(0)) e0[q] += __ldg(p.mcs + id[q]) * sv;
-            wrote = true;
           }
+          wrote = true;
         }
       }
-      if (wrote) st_guard_roles<T, V>(p, p.ez + c, e0, id);
+      if (wrote) st_guard<T, V>(p.ez + c, e0, id);
     } else {
       vld<T, V>(p.ex + c, e0);
       vld<T, V>(p.ey + c, e1);
@@ -201,10 +184,7 @@ struct K2 {
         chx[q] = a0[q] - lft[q];    // curlhx
         chy[q] = a0[q] - below[q];  // curlhy
       }
-      bool anyade = false;
-#pragma unroll
-      for (int q = 0; q < V; ++q) anyade |= id[q] >= kAdeId;
-      if (!shell && main_x && main_y && !(rf & (ROW_SRC | ROW_SLAB)) && !anyade) {
+      if (!shell && main_x && main_y && !(rf & (ROW_SRC | ROW_SLAB))) {
         if (do_main) {
 #pragma unroll
           for (int q = 0; q < V; ++q) {
@@ -212,13 +192,13 @@ struct K2 {
             e0[q] = e0[q] + ca * chy[q];
             e1[q] = e1[q] - ca * chx[q];
           }
-          vst<T, V>(p.ex + c, e0);
-          vst<T, V>(p.ey + c, e1);
+          st_guard<T, V>(p.ex + c, e0, id);
+          st_guard<T, V>(p.ey + c, e1, id);
         }
         return;
       }
       const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
-      if (shell || main_y) {
+      if (shell || (do_main && main_y)) {
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const int i = i0 + q;
@@ -227,27 +207,19 @@ struct K2 {
               e0[q] = p.cf1[1][j] * e0[q] + p.cf2[1][j] * chy[q];
               e1[q] = p.cf1[0][i] * e1[q] + p.cf2[0][i] * (-a0[q] + lft[q]);
             }
-          } else if (main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
-            T sx = T(0), sy = T(0);
-            if (rf & ROW_SRC) { sx = src_sum<T>(p, n, 0, i, j, 0); sy = src_sum<T>(p, n, 1, i, j, 0); }
-            if (id[q] >= kAdeId) {
-              if (p.roles & ROLE_ADE) {
-                const int sl = __ldg(p.ade_slot + c + q);
-                const AdeCoef<T> &a = p.ac[p.mc[id[q]].ade];
-                e0[q] = ade_update<T>(p, a, sl, 0, p.ku * chy[q] + sx, e0[q]);
-                e1[q] = ade_update<T>(p, a, sl, 1, -(p.ku * chx[q]) + sy, e1[q]);
-              }
-            } else if (do_main) {
-              const T ca = coef_ca(p, id[q]);
-              e0[q] = e0[q] + ca * chy[q];
-              e1[q] = e1[q] - ca * chx[q];
+          } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
+            const T ca = coef_ca(p, id[q]);
+            e0[q] = e0[q] + ca * chy[q];
+            e1[q] = e1[q] - ca * chx[q];
+            if (rf & ROW_SRC) {
+              const T sx = src_sum<T>(p, n, 0, i, j, 0), sy = src_sum<T>(p, n, 1, i, j, 0);
               if (sx != T(0)) e0[q] += __ldg(p.mcs + id[q]) * sx;
               if (sy != T(0)) e1[q] += __ldg(p.mcs + id[q]) * sy;
             }
           }
         }
-        st_guard_roles<T, V>(p, p.ex + c, e0, id);
-        st_guard_roles<T, V>(p, p.ey + c, e1, id);
+        st_guard<T, V>(p.ex + c, e0, id);
+        st_guard<T, V>(p.ey + c, e1, id);
       }
       if (do_pml && (rf & ROW_SLAB)) {
 #pragma unroll
@@ -384,12 +356,44 @@ struct K2 {
   }
 };
 
-// Grid-stride blocks over (row, vector) units; dispersive cells are updated
-// by the unit that holds them (through the cell -> ADE slot map).
+// ---- dispersive cells ------------------------------------------------------
+template <typename T, int L>
+__device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
+  const int cell = p.ade_cell[s];
+  const int nx = p.nx, ny = p.ny;
+  const int i = cell % nx, j = cell / nx;
+  const AdeCoef<T> a = ade_coef(p, p.ade_mat[s]);
+  if (L == 3) {
+    T curl = (p.hy[cell] - ld_x(p.hy, i - 1, j, nx, p.per[0])) +
+             (-p.hx[cell] + ld_y(p.hx, i, j - 1, nx, ny, p.per[1]));
+    T inc = p.ku * curl + src_sum<T>(p, n, 2, i, j, 0);
+    p.ez[cell] = ade_update<T>(p, a, s, 0, inc, p.ez[cell]);
+  } else {
+    T hzc = p.hz[cell];
+    T curlhx = hzc - ld_x(p.hz, i - 1, j, nx, p.per[0]);
+    T curlhy = hzc - ld_y(p.hz, i, j - 1, nx, ny, p.per[1]);
+    T incx = p.ku * curlhy + src_sum<T>(p, n, 0, i, j, 0);
+    T incy = -(p.ku * curlhx) + src_sum<T>(p, n, 1, i, j, 0);
+    p.ex[cell] = ade_update<T>(p, a, s, 0, incx, p.ex[cell]);
+    p.ey[cell] = ade_update<T>(p, a, s, 1, incy, p.ey[cell]);
+  }
+}
+
+// Block layout of a launch: the ADE blocks first (their dependent loads start
+// early), then the grid-stride blocks over (row, vector) units.
 template <typename T, int L, int V>
 __global__ void __launch_bounds__(256) e2d_kernel(const __grid_constant__ StepParams<T> p) {
   const int n = step_n(p);
-  const int b = blockIdx.x;
+  int b = blockIdx.x;
+  if (b < p.nade_blocks) {
+    if (p.roles & ROLE_ADE) {
+      const int s = b * 256 + threadIdx.x;
+      if (s < p.nade) ade_e2<T, L>(p, s, n);
+    }
+    return;
+  }
+  if (!(p.roles & (ROLE_MAIN | ROLE_PML))) return;
+  b -= p.nade_blocks;
   const long long units = (long long)(p.nx / V) * p.ny;
   for (long long t = (long long)b * 256 + threadIdx.x; t < units; t += (long long)p.ntile_blocks * 256)
     K2<T, L, V>::unit_e(p, t, n);

@@ -295,8 +295,7 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
   const int nx = p.nx, ny = p.ny;
   const int i = cell % nx, j = (cell / nx) % ny, k = cell / (nx * ny);
   F3<T> f(p);
-  const MatCoef<T> mc = p.mc[p.ade_mat[s]];
-  const AdeCoef<T> &a = p.ac[mc.ade];
+  const AdeCoef<T> a = ade_coef(p, p.ade_mat[s]);
   const T hxc = p.hx[cell], hyc = p.hy[cell], hzc = p.hz[cell];
   const T curlhzy = hzc - f.ly(p.hz, i, j - 1, k), curlhyz = -hyc + f.lz(p.hy, i, j, k - 1);
   const T curlhxz = hxc - f.lz(p.hx, i, j, k - 1), curlhzx = -hzc + f.lx(p.hz, i - 1, j, k);

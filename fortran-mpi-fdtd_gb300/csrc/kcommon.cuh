@@ -193,6 +193,13 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
   return e;
 }
 
+// coefficients of a dispersive material id (>= kAdeId)
+template <typename T>
+__device__ __forceinline__ AdeCoef<T> ade_coef(const StepParams<T> &p, int id) {
+  const int ai = id - kAdeId;
+  return ai < kAdeParam ? p.acp[ai] : p.ac[ai];
+}
+
 template <typename T>
 __device__ __forceinline__ T ade_update(const StepParams<T> &p, const AdeCoef<T> &a, int slot, int comp, T inc,
                                          T eold) {
