@@ -1542,3 +1542,13 @@ int fdtd_transfer_bytes(const fdtd_job *J, uint64_t *h2d, uint64_t *d2h) {
 }
 
 }  // extern "C"
+
+int fdtd::report_error(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}

@@ -223,4 +223,7 @@ struct LineParams {
 };
 template <typename T> void launch_line1d_stage(const LineParams<T> &p, T *stage, long long stage_row, void *stream);
 
+// Records a message for fdtd_last_error and returns `code`.
+int report_error(int code, const char *fmt, ...);
+
 }  // namespace fdtd

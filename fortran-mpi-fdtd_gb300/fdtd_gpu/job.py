@@ -24,6 +24,7 @@ EXPORTS = [
     "fdtd_pml_update_H", "fdtd_sample", "fdtd_sync", "fdtd_get_field", "fdtd_set_field",
     "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_profile",
     "fdtd_kernel_time", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
+    "fdtd_dft_sample_noalloc",
 ]
 
 
@@ -59,6 +60,8 @@ def lib(path=None):
             "fdtd_launch_count": [vp, C.POINTER(C.c_int64)],
             "fdtd_set_stream": [vp, vp],
             "fdtd_transfer_bytes": [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
+            "fdtd_dft_sample_noalloc": [vp, i32, i32, i32, i32, C.POINTER(i32), C.POINTER(i32), i32, i32, i32,
+                                        dbl, vp, i32, vp, vp, i32, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -66,6 +69,18 @@ def lib(path=None):
             fn.restype = C.c_int
         _lib = L
     return _lib
+
+
+def dft_sample_noalloc(field_ptr, precision, shape_xyz, lo, hi, n, n_first, n_last, dt, omega_ptr, nfreq,
+                       acc_re_ptr, acc_im_ptr, flush=False, stream=None):
+    """fdtd_dft_sample_noalloc on caller-owned device memory (all *_ptr are
+    device addresses); the library allocates nothing on this call."""
+    lo3 = (C.c_int32 * 3)(*lo)
+    hi3 = (C.c_int32 * 3)(*hi)
+    nx, ny, nz = shape_xyz
+    check(lib().fdtd_dft_sample_noalloc(field_ptr, int(precision), int(nx), int(ny), int(nz), lo3, hi3, int(n),
+                                        int(n_first), int(n_last), float(dt), omega_ptr, int(nfreq), acc_re_ptr,
+                                        acc_im_ptr, 1 if flush else 0, stream))
 
 
 def last_error():

@@ -264,6 +264,42 @@ int fdtd_set_stream(fdtd_job *job, void *cuda_stream);
  * since the job was created. */
 int fdtd_transfer_bytes(const fdtd_job *job, uint64_t *h2d, uint64_t *d2h);
 
+/* ---- allocation-free DFT of a caller-owned field ------------------------ *
+ * No counterpart in the reference: its DFT sums live inside program.f90's
+ * time loop (2D/.../program.f90:383-391, 3D/.../program.f90:441-540).  This
+ * entry point serves host codes that keep their own device fields and cannot
+ * let a library allocate device memory while they run (a time loop recorded
+ * into a CUDA graph by stream capture, or a code that takes every device
+ * byte from its own pool).
+ *
+ * Call it once per step n, after the H update, with the device field array
+ * `field` (nx*ny*nz values of `precision`, x fastest) and the box lo..hi
+ * (0-based, inclusive).  Steps n_first..n_last are sampled; the sums
+ *   acc_re[f*ncell + c] += sum_n cos(omega[f] (n-1) dt) F_n(c) dt,
+ *   acc_im[f*ncell + c] += sum_n sin(omega[f] (n-1) dt) F_n(c) dt
+ * are folded into the caller's device accumulators (FP64, zeroed by the
+ * caller) every FDTD_NOALLOC_RING steps, at n == n_last, and when `flush` is
+ * non-zero.  Calls for n outside the window return at once.  `omega`,
+ * `acc_re` and `acc_im` are device pointers; work is queued on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream).
+ *
+ * It allocates nothing: the samples of the current ring are staged in a
+ * static device array of FDTD_NOALLOC_STAGE_BYTES that the library holds on
+ * every device for the life of the process, so a box may hold at most
+ * FDTD_NOALLOC_MAX_CELLS cells (a 512 x 512 plane); a larger box fails with
+ * FDTD_ERANGE.  The first call on each device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current; make that first
+ * call before any stream capture.  The array is shared by all calls on a
+ * device, so one sequence of steps may run at a time per device: calls that
+ * overlap (two boxes at once, or two host threads or streams) race on it. */
+#define FDTD_NOALLOC_RING 32
+#define FDTD_NOALLOC_MAX_CELLS 262144
+#define FDTD_NOALLOC_STAGE_BYTES (FDTD_NOALLOC_MAX_CELLS * FDTD_NOALLOC_RING * 8)
+int fdtd_dft_sample_noalloc(const void *field, int32_t precision, int32_t nx, int32_t ny, int32_t nz,
+                            const int32_t lo[3], const int32_t hi[3], int32_t n, int32_t n_first,
+                            int32_t n_last, double dt, const double *omega, int32_t nfreq,
+                            double *acc_re, double *acc_im, int32_t flush, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
