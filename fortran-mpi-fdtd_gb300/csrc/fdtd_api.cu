@@ -169,6 +169,12 @@ struct fdtd_job {
   long long launches = 0;
   cudaStream_t own_stream = nullptr;
   uint64_t h2d = 0, d2h = 0;
+  // 2D work split (core box + edge unit list) and the streams that run the
+  // parts of a half step as parallel branches of the job's stream
+  int vec = 1, cv0 = 0, cw = 0, cy0 = 0, ncore = 0, nedge = 0;
+  int *d_edge = nullptr;
+  cudaStream_t side[2] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {};
 };
 
 namespace {
@@ -320,6 +326,46 @@ int upload_prof(fdtd_job *J, const Prof &P, void **f1, void **f2, void **g1, voi
 }
 
 // ---- commit ------------------------------------------------------------
+// 2D work split.  Core units: whole V-cell vectors of the main range outside
+// the split-PML shell, in rows without flags; they take only the interior
+// Yee update.  Every other unit goes to a list for the edge kernel.
+int split_2d(fdtd_job *J, const std::vector<uint8_t> &rf) {
+  const int nx = J->nx, ny = J->ny;
+  const int vw = J->esz == 4 ? 4 : 2;  // float4 / double2 rows when aligned
+  const int V = J->vec = (nx % vw == 0) ? vw : 1;
+  const int nvec = nx / V;
+  if ((long long)nvec * ny > (long long)INT32_MAX)
+    return set_err(FDTD_ERANGE, "2D grid of %d x %d cells is too large for 32-bit unit indices", nx, ny);
+  const int xlo = std::max(J->g.main_lo[0], J->slo[0]), xhi = std::min(J->g.main_hi[0], J->shi[0]);
+  const int ylo = std::max(J->g.main_lo[1], J->slo[1]), yhi = std::min(J->g.main_hi[1], J->shi[1]);
+  const int cv0 = (xlo + V - 1) / V, cv1 = std::max(cv0, (xhi + 1) / V);  // whole vectors in [xlo, xhi]
+  const int cy1 = std::max(ylo, yhi + 1);
+  J->cv0 = cv0;
+  J->cw = cv1 - cv0;
+  J->cy0 = ylo;
+  J->ncore = J->cw * (cy1 - ylo);
+  std::vector<int> edge;
+  edge.reserve((size_t)nvec * ny - (size_t)J->ncore + (size_t)nvec * 8);
+  for (int j = 0; j < ny; ++j) {
+    const bool core_row = j >= ylo && j < cy1 && rf[j] == 0;
+    for (int v = 0; v < nvec; ++v)
+      if (!(core_row && v >= cv0 && v < cv1)) edge.push_back(j * nvec + v);
+  }
+  J->nedge = (int)edge.size();
+  int rc;
+  if (!edge.empty()) {
+    if ((rc = alloc_dev(J, (void **)&J->d_edge, edge.size() * sizeof(int)))) return rc;
+    CK(cudaMemcpy(J->d_edge, edge.data(), edge.size() * sizeof(int), cudaMemcpyHostToDevice));
+    J->h2d += edge.size() * sizeof(int);
+  }
+  for (int q = 0; q < 2; ++q) {
+    CK(cudaStreamCreateWithFlags(&J->side[q], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&J->ev_join[q], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&J->ev_fork, cudaEventDisableTiming));
+  return FDTD_OK;
+}
+
 template <typename T>
 int commit_impl(fdtd_job *J) {
   int rc;
@@ -627,6 +673,7 @@ int commit_impl(fdtd_job *J) {
     if ((rc = alloc_dev(J, (void **)&J->d_rowflag, (size_t)ny))) return rc;
     CK(cudaMemcpy(J->d_rowflag, rf.data(), (size_t)ny, cudaMemcpyHostToDevice));
     J->h2d += (uint64_t)ny;
+    if ((rc = split_2d(J, rf))) return rc;
   }
   J->stage_row = base;
   J->acc_total = acc;
@@ -702,12 +749,13 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.sf1z[s] = (const T *)sc[8]; p.sf2z[s] = (const T *)sc[9]; p.sg1z[s] = (const T *)sc[10]; p.sg2z[s] = (const T *)sc[11];
   }
   if (J->dim == 2) {
-    const int vw = sizeof(T) == 4 ? 4 : 2;  // float4 / double2 rows when aligned
-    p.vec = (J->nx % vw == 0) ? vw : 1;
-    // grid-stride over (row, vector) units: up to 8 blocks of 256 per SM
-    const long long units = (long long)(J->nx / p.vec) * J->ny;
-    p.tiles_x = p.tiles_y = p.tiles_z = 0;
-    p.ntile_blocks = (int)std::min<long long>((units + 255) / 256, (long long)J->num_sms * 8);
+    p.vec = J->vec;
+    p.cv0 = J->cv0;
+    p.cw = J->cw;
+    p.cy0 = J->cy0;
+    p.ncore = J->ncore;
+    p.nedge = J->nedge;
+    p.edge_units = J->d_edge;
   } else {
     p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 7) / 8; p.tiles_z = (J->nz + 15) / 16;
     p.ntile_blocks = p.tiles_x * p.tiles_y * p.tiles_z;
@@ -855,6 +903,44 @@ int dft_fold(fdtd_job *J) {
 
 enum { ST_E = 1, ST_H = 2, ST_SAMPLE = 4 };
 
+// 2D: the parts of one half step (core, edge, ADE) write disjoint cells and
+// read only the other half's fields, so they run as parallel branches of the
+// job's stream (forked and joined with events; a stream capture records them
+// as parallel graph nodes).  Profiled runs launch them one after another so
+// that each part's events time that part alone.
+template <typename T>
+int run_parts_2d(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], bool e_half, bool graph) {
+  static const int kind[3] = {-1, FDTD_KERNEL_EDGE, FDTD_KERNEL_ADE};
+  const int units[3] = {p.ncore, p.nedge, e_half ? p.nade : 0};
+  int use[3], nuse = 0;
+  for (int q = 0; q < 3; ++q)
+    if (want[q] && units[q] > 0) use[nuse++] = q;
+  const bool par = !J->prof && nuse > 1;
+  cudaStream_t st[3] = {J->stream, J->stream, J->stream};
+  if (par) {
+    CK(cudaEventRecord(J->ev_fork, J->stream));
+    for (int b = 1; b < nuse; ++b) {
+      st[b] = J->side[b - 1];
+      CK(cudaStreamWaitEvent(st[b], J->ev_fork, 0));
+    }
+  }
+  for (int b = 0; b < nuse; ++b) {
+    const int q = use[b];
+    const int k = q == K2D_CORE ? (e_half ? FDTD_KERNEL_E : FDTD_KERNEL_H) : kind[q];
+    if (!graph) ev_record(J, k, true);
+    J->launches += e_half ? launch_e2d<T>(p, q, st[b]) : launch_h2d<T>(p, q, st[b]);
+    if (!graph) ev_record(J, k, false);
+  }
+  CK(cudaGetLastError());
+  if (par) {
+    for (int b = 1; b < nuse; ++b) {
+      CK(cudaEventRecord(J->ev_join[b - 1], st[b]));
+      CK(cudaStreamWaitEvent(J->stream, J->ev_join[b - 1], 0));
+    }
+  }
+  return FDTD_OK;
+}
+
 // 2D / 3D: one half step (or a role subset of it).  In graph mode the step
 // number comes from the device-side ring base (d_base) plus the ring slot.
 template <typename T>
@@ -866,10 +952,13 @@ int half_e(fdtd_job *J, int n, int roles, int slot = 0, bool graph = false) {
   p.n = n;
   p.slot = slot;
   p.d_base = graph ? J->d_base : nullptr;
+  if (J->dim == 2) {
+    const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML)) != 0, (roles & ROLE_ADE) != 0};
+    return run_parts_2d<T>(J, p, parts, true, graph);
+  }
   int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
   if (!graph) ev_record(J, FDTD_KERNEL_E, true);
-  if (J->dim == 2) launch_e2d<T>(p, blocks, J->stream);
-  else launch_e3d<T>(p, blocks, J->stream);
+  launch_e3d<T>(p, blocks, J->stream);
   if (!graph) ev_record(J, FDTD_KERNEL_E, false);
   J->launches++;
   CK(cudaGetLastError());
@@ -885,10 +974,13 @@ int half_h(fdtd_job *J, int n, int roles, bool gather, int slot = -1, bool graph
   p.gather = gather ? 1 : 0;
   p.slot = slot >= 0 ? slot : J->stage_fill;
   p.d_base = graph ? J->d_base : nullptr;
+  if (J->dim == 2) {
+    const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML)) != 0, false};
+    return run_parts_2d<T>(J, p, parts, false, graph);
+  }
   int blocks = p.ntile_blocks + p.nslab_blocks;
   if (!graph) ev_record(J, FDTD_KERNEL_H, true);
-  if (J->dim == 2) launch_h2d<T>(p, blocks, J->stream);
-  else launch_h3d<T>(p, blocks, J->stream);
+  launch_h3d<T>(p, blocks, J->stream);
   if (!graph) ev_record(J, FDTD_KERNEL_H, false);
   J->launches++;
   CK(cudaGetLastError());
@@ -1253,6 +1345,11 @@ int fdtd_destroy(fdtd_job *J) {
   destroy_graph(J);
   for (auto &e : J->pending) { cudaEventDestroy(e.a); if (e.b) cudaEventDestroy(e.b); }
   for (auto e : J->ev_pool) cudaEventDestroy(e);
+  for (int q = 0; q < 2; ++q) {
+    if (J->side[q]) cudaStreamDestroy(J->side[q]);
+    if (J->ev_join[q]) cudaEventDestroy(J->ev_join[q]);
+  }
+  if (J->ev_fork) cudaEventDestroy(J->ev_fork);
   if (J->own_stream) cudaStreamDestroy(J->own_stream);
   delete J;
   return FDTD_OK;
@@ -1517,6 +1614,22 @@ int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
   J->pending.clear();
   if (launches) *launches = J->kcount[kind];
   if (ms) *ms = J->kms[kind];
+  return FDTD_OK;
+}
+
+int fdtd_kernel_cells(const fdtd_job *J, int32_t kind, int64_t *cells) {
+  if (!J || !cells) return set_err(FDTD_EINVAL, "null argument");
+  if (kind < 0 || kind >= FDTD_KERNEL_COUNT) return set_err(FDTD_EINVAL, "bad kernel kind");
+  if (!J->committed) return set_err(FDTD_ESTATE, "job not committed");
+  int64_t c = 0;
+  if (kind == FDTD_KERNEL_E || kind == FDTD_KERNEL_H) c = J->dim == 2 ? (int64_t)J->ncore * J->vec : J->ncell;
+  else if (kind == FDTD_KERNEL_EDGE) c = J->dim == 2 ? (int64_t)J->nedge * J->vec : 0;
+  else if (kind == FDTD_KERNEL_ADE) c = J->dim == 2 ? J->nade : 0;
+  else if (kind == FDTD_KERNEL_LINE1D) c = J->dim == 1 ? J->ncell : 0;
+  else if (kind == FDTD_KERNEL_DFT) {
+    for (auto &m : J->mon_dev) c += (int64_t)m.ncomp * m.ncell;
+  }
+  *cells = c;
   return FDTD_OK;
 }
 

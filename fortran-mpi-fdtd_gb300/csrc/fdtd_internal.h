@@ -129,6 +129,11 @@ struct StepParams {
   int roles;               // ROLE_* bits
   int tiles_x, tiles_y, tiles_z, ntile_blocks;
   int nslab_blocks, nade_blocks;
+  // 2D work split: core units are vectors [cv0, cv0+cw) of rows cy0.. (ncore
+  // units in all); every other unit (j*nx/V + vector) is listed in edge_units
+  int cv0, cw, cy0, ncore;
+  int nedge;
+  const int *edge_units;
   // sampling fused into the H kernel
   int gather;              // 1: tile threads write the stage row / probes
   int nmon;
@@ -161,8 +166,10 @@ enum Role : int {
 constexpr int kAdeFields = 6;
 
 // launchers (defined in k2d.cu / k3d.cu / k1d.cu / kdft.cu)
-template <typename T> void launch_e2d(const StepParams<T> &p, int blocks, void *stream);
-template <typename T> void launch_h2d(const StepParams<T> &p, int blocks, void *stream);
+// 2D half steps: the parts of one half step are independent launches
+enum K2dPart { K2D_CORE = 0, K2D_EDGE = 1, K2D_ADE = 2 };
+template <typename T> int launch_e2d(const StepParams<T> &p, int part, void *stream);
+template <typename T> int launch_h2d(const StepParams<T> &p, int part, void *stream);
 template <typename T> void launch_e3d(const StepParams<T> &p, int blocks, void *stream);
 template <typename T> void launch_h3d(const StepParams<T> &p, int blocks, void *stream);
 

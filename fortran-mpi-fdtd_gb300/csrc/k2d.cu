@@ -1,20 +1,20 @@
 // k2d.cu -- 2D half-step kernels (TE: Ex, Ey, Hz; TM: Ez, Hx, Hy).
 //
-// One launch per half step; blockIdx selects the work:
-//   grid-stride blocks : each thread takes (row, V-cell vector) units in
-//                 turn (float4 / double2 when the row length allows); inputs
-//                 come through the read-only path, the neighbour row and the
-//                 neighbour cell at the vector edge from L1.  Main cells do the
-//                 Yee update with the constant-dielectric material folded in
-//                 (E += Ku/eps * curl: the reference's D update and E = D*gax,
-//                 2D/.../myfdtd_2Dfunc.f90:16-44, 2D/simpledielectric_mod.f90:
-//                 141-146); split-PML shell cells do the split update; rows of
-//                 the reference y-slabs (2D/BERpmly_HzExEy_mod.f90) run the
-//                 reference PML; monitored rows stage their samples.
-//                 Sources, shells, slabs and samples are tested per row (warp
-//                 uniform) before any per-cell test.
-//   ADE blocks  : one thread per dispersive cell (gold Drude+2CP,
-//                 2D/gold_mod.f90:47-75); tile threads never store E there.
+// The work unit is one row segment of V cells (float4 / double2 when the row
+// length allows).  A half step is split over independent kernels that write
+// disjoint cells, so the host runs them as parallel branches of its stream:
+//   core : the units of the interior box -- main cells outside the PML shell
+//          in rows without flags -- doing only the Yee update with the
+//          constant-dielectric material folded in (E += Ku/eps * curl: the
+//          reference's D update and E = D*gax, 2D/.../myfdtd_2Dfunc.f90:16-44,
+//          2D/simpledielectric_mod.f90:141-146).  This is nearly all of the
+//          grid, and leaving the rest out keeps its register count low.
+//   edge : every other unit, from a list built at commit: split-PML shell
+//          cells, the edges of the main range, source rows, monitored rows
+//          (which stage their samples) and the rows of the reference y-slabs
+//          (2D/BERpmly_HzExEy_mod.f90).
+//   ADE  : one thread per dispersive cell (gold Drude+2CP,
+//          2D/gold_mod.f90:47-75); core and edge threads never store E there.
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.h"
@@ -145,7 +145,20 @@ struct K2 {
         }
         return;
       }
+      // general unit (PML shell, source row, edge of the main range): every
+      // split part and profile value of the unit is loaded before any store,
+      // so the unit costs one round of loads like an interior unit
       const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
+      const bool pml = do_pml && shell;
+      T ezx[V], ezy[V], f1x[V], f2x[V], f1y = T(0), f2y = T(0);
+      if (pml) {
+        vld<T, V>(p.sp[0] + c, ezx);
+        if (kTwoParts<T>) vld<T, V>(p.sp[6] + c, ezy);
+        vld_ro<T, V>(p.cf1[0] + i0, f1x);
+        vld_ro<T, V>(p.cf2[0] + i0, f2x);
+        f1y = __ldg(p.cf1[1] + j);
+        f2y = __ldg(p.cf2[1] + j);
+      }
       bool wrote = false;
 #pragma unroll
       for (int q = 0; q < V; ++q) {
@@ -153,13 +166,11 @@ struct K2 {
         if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
           if (do_pml) {
             // Ez = Ezx + Ezy (3D/BERpmly_mod.f90:151,153 with d/dz = 0)
-            const long long cc = c + q;
-            const T ezx = p.sp[0][cc];
-            const T ezy = kTwoParts<T> ? p.sp[6][cc] : e0[q] - ezx;
-            const T nezx = p.cf1[0][i] * ezx + p.cf2[0][i] * dxp[q];
-            const T nezy = p.cf1[1][j] * ezy + p.cf2[1][j] * dyp[q];
-            p.sp[0][cc] = nezx;
-            if (kTwoParts<T>) p.sp[6][cc] = nezy;
+            const T py = kTwoParts<T> ? ezy[q] : e0[q] - ezx[q];
+            const T nezx = f1x[q] * ezx[q] + f2x[q] * dxp[q];
+            const T nezy = f1y * py + f2y * dyp[q];
+            ezx[q] = nezx;
+            ezy[q] = nezy;
             e0[q] = nezx + nezy;
             wrote = true;
           }
@@ -173,6 +184,10 @@ struct K2 {
         }
       }
       if (wrote) st_guard<T, V>(p.ez + c, e0, id);
+      if (pml) {  // cells of the unit outside the shell store back what they read
+        vst<T, V>(p.sp[0] + c, ezx);
+        if (kTwoParts<T>) vst<T, V>(p.sp[6] + c, ezy);
+      }
     } else {
       vld<T, V>(p.ex + c, e0);
       vld<T, V>(p.ey + c, e1);
@@ -199,13 +214,20 @@ struct K2 {
       }
       const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
       if (shell || (do_main && main_y)) {
+        T f1x[V], f2x[V], f1y = T(0), f2y = T(0);
+        if (do_pml && shell) {  // profile values loaded before any store
+          vld_ro<T, V>(p.cf1[0] + i0, f1x);
+          vld_ro<T, V>(p.cf2[0] + i0, f2x);
+          f1y = __ldg(p.cf1[1] + j);
+          f2y = __ldg(p.cf2[1] + j);
+        }
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const int i = i0 + q;
           if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
             if (do_pml) {
-              e0[q] = p.cf1[1][j] * e0[q] + p.cf2[1][j] * chy[q];
-              e1[q] = p.cf1[0][i] * e1[q] + p.cf2[0][i] * (-a0[q] + lft[q]);
+              e0[q] = f1y * e0[q] + f2y * chy[q];
+              e1[q] = f1x[q] * e1[q] + f2x[q] * (-a0[q] + lft[q]);
             }
           } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
             const T ca = coef_ca(p, id[q]);
@@ -273,6 +295,13 @@ struct K2 {
         return;
       }
       const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
+      T g1x[V], g2x[V], g1y = T(0), g2y = T(0);
+      if (do_pml && shell) {  // profile values loaded before any store
+        vld_ro<T, V>(p.cg1[0] + i0, g1x);
+        vld_ro<T, V>(p.cg2[0] + i0, g2x);
+        g1y = __ldg(p.cg1[1] + j);
+        g2y = __ldg(p.cg2[1] + j);
+      }
       bool wrote = false;
 #pragma unroll
       for (int q = 0; q < V; ++q) {
@@ -280,8 +309,8 @@ struct K2 {
         const T rgt = q < V - 1 ? cur[q + 1] : right;
         if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
           if (do_pml) {
-            h0[q] = p.cg1[1][j] * h0[q] + p.cg2[1][j] * (-up[q] + cur[q]);
-            h1[q] = p.cg1[0][i] * h1[q] + p.cg2[0][i] * (rgt - cur[q]);
+            h0[q] = g1y * h0[q] + g2y * (-up[q] + cur[q]);
+            h1[q] = g1x[q] * h1[q] + g2x[q] * (rgt - cur[q]);
             wrote = true;
           }
         } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
@@ -314,6 +343,16 @@ struct K2 {
         return;
       }
       const bool shell_y = split && (j < p.slo[1] || j > p.shi[1]);
+      const bool pml = do_pml && shell;
+      T hzx[V], hzy[V], g1x[V], g2x[V], g1y = T(0), g2y = T(0);
+      if (pml) {  // split parts and profile values loaded before any store
+        vld<T, V>(p.sp[0] + c, hzx);
+        if (kTwoParts<T>) vld<T, V>(p.sp[6] + c, hzy);
+        vld_ro<T, V>(p.cg1[0] + i0, g1x);
+        vld_ro<T, V>(p.cg2[0] + i0, g2x);
+        g1y = __ldg(p.cg1[1] + j);
+        g2y = __ldg(p.cg2[1] + j);
+      }
       bool wrote = false;
 #pragma unroll
       for (int q = 0; q < V; ++q) {
@@ -321,14 +360,12 @@ struct K2 {
         const T rgt = q < V - 1 ? xe[q + 1] : right;
         if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
           if (do_pml) {
-            const long long cc = c + q;
-            T hzx = p.sp[0][cc];
-            T hzy = kTwoParts<T> ? p.sp[6][cc] : h0[q] - hzx;
-            hzy = p.cg1[1][j] * hzy + p.cg2[1][j] * (up[q] - cur[q]);
-            hzx = p.cg1[0][i] * hzx + p.cg2[0][i] * (-rgt + xe[q]);
-            p.sp[0][cc] = hzx;
-            if (kTwoParts<T>) p.sp[6][cc] = hzy;
-            h0[q] = hzy + hzx;
+            const T py = kTwoParts<T> ? hzy[q] : h0[q] - hzx[q];
+            const T nhzy = g1y * py + g2y * (up[q] - cur[q]);
+            const T nhzx = g1x[q] * hzx[q] + g2x[q] * (-rgt + xe[q]);
+            hzx[q] = nhzx;
+            hzy[q] = nhzy;
+            h0[q] = nhzy + nhzx;
             wrote = true;
           }
         } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
@@ -338,6 +375,10 @@ struct K2 {
         }
       }
       if (wrote) vst<T, V>(p.hz + c, h0);
+      if (pml) {  // cells of the unit outside the shell store back what they read
+        vst<T, V>(p.sp[0] + c, hzx);
+        if (kTwoParts<T>) vst<T, V>(p.sp[6] + c, hzy);
+      }
       if (slab) {
 #pragma unroll
         for (int q = 0; q < V; ++q) {
@@ -379,66 +420,183 @@ __device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
   }
 }
 
-// Block layout of a launch: the ADE blocks first (their dependent loads start
-// early), then the grid-stride blocks over (row, vector) units.
+// ---- core units: the Yee update of interior cells, nothing else ----------
 template <typename T, int L, int V>
-__global__ void __launch_bounds__(256) e2d_kernel(const __grid_constant__ StepParams<T> p) {
-  const int n = step_n(p);
-  int b = blockIdx.x;
-  if (b < p.nade_blocks) {
-    if (p.roles & ROLE_ADE) {
-      const int s = b * 256 + threadIdx.x;
-      if (s < p.nade) ade_e2<T, L>(p, s, n);
+__device__ __forceinline__ void core_e(const StepParams<T> &p, int j, int i0) {
+  const int nx = p.nx, ny = p.ny;
+  const long long c = (long long)j * nx + i0;
+  const T *ydc = L == 3 ? p.hx : p.hz;  // component with the y derivative
+  const T *xdc = L == 3 ? p.hy : p.hz;  // component with the x derivative
+  T below[V], a0[V], e0[V];
+  uint8_t id[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) below[q] = T(0);
+  if (j > 0) vld_ro<T, V>(ydc + c - nx, below);
+  else if (p.per[1]) vld_ro<T, V>(ydc + (long long)(ny - 1) * nx + i0, below);
+  vld_ro<T, V>(xdc + c, a0);
+  const T left = i0 > 0 ? __ldg(xdc + c - 1) : (p.per[0] ? __ldg(xdc + c + nx - 1) : T(0));
+  vld_ids<V>(p.mat + c, id);
+  if (L == 3) {
+    T a1[V];
+    vld_ro<T, V>(p.hx + c, a1);
+    vld<T, V>(p.ez + c, e0);
+    if (__ldg(p.rowflag + j)) return;  // flagged rows belong to the edge kernel
+    // TM: Ez += Ku/eps ((Hy(i)-Hy(i-1)) + (-Hx(j)+Hx(j-1)))
+    T dxp[V], dyp[V];
+    bool uni = true;
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      dxp[q] = a0[q] - (q ? a0[q - 1] : left);  // curlhyx
+      dyp[q] = -a1[q] + below[q];              // curlhxy
+      uni &= id[q] == p.id0;
     }
-    return;
+    if (uni) {
+#pragma unroll
+      for (int q = 0; q < V; ++q) e0[q] = e0[q] + p.ca0 * (dxp[q] + dyp[q]);
+      vst<T, V>(p.ez + c, e0);
+    } else {
+#pragma unroll
+      for (int q = 0; q < V; ++q) e0[q] = e0[q] + coef_ca(p, id[q]) * (dxp[q] + dyp[q]);
+      st_guard<T, V>(p.ez + c, e0, id);
+    }
+  } else {
+    T e1[V];
+    vld<T, V>(p.ex + c, e0);
+    vld<T, V>(p.ey + c, e1);
+    if (__ldg(p.rowflag + j)) return;
+    // TE: Ex += Ku/eps (Hz(j)-Hz(j-1)), Ey -= Ku/eps (Hz(i)-Hz(i-1))
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const T ca = coef_ca(p, id[q]);
+      const T chx = a0[q] - (q ? a0[q - 1] : left);  // curlhx
+      const T chy = a0[q] - below[q];                // curlhy
+      e0[q] = e0[q] + ca * chy;
+      e1[q] = e1[q] - ca * chx;
+    }
+    st_guard<T, V>(p.ex + c, e0, id);
+    st_guard<T, V>(p.ey + c, e1, id);
   }
-  if (!(p.roles & (ROLE_MAIN | ROLE_PML))) return;
-  b -= p.nade_blocks;
-  const long long units = (long long)(p.nx / V) * p.ny;
-  for (long long t = (long long)b * 256 + threadIdx.x; t < units; t += (long long)p.ntile_blocks * 256)
-    K2<T, L, V>::unit_e(p, t, n);
 }
 
 template <typename T, int L, int V>
-__global__ void __launch_bounds__(256) h2d_kernel(const __grid_constant__ StepParams<T> p) {
-  const int n = step_n(p);
-  const long long units = (long long)(p.nx / V) * p.ny;
-  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < units; t += (long long)p.ntile_blocks * 256)
-    K2<T, L, V>::unit_h(p, t, n);
+__device__ __forceinline__ void core_h(const StepParams<T> &p, int j, int i0) {
+  const int nx = p.nx, ny = p.ny;
+  const long long c = (long long)j * nx + i0;
+  const T *ydc = L == 3 ? p.ez : p.ex;  // E component with a y derivative
+  const T *xdc = L == 3 ? p.ez : p.ey;  // E component with an x derivative
+  T cur[V], up[V], h0[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) up[q] = T(0);
+  vld_ro<T, V>(ydc + c, cur);
+  if (j + 1 < ny) vld_ro<T, V>(ydc + c + nx, up);
+  else if (p.per[1]) vld_ro<T, V>(ydc + i0, up);
+  const T right = i0 + V < nx ? __ldg(xdc + c + V) : (p.per[0] ? __ldg(xdc + c + V - nx) : T(0));
+  if (L == 3) {
+    T h1[V];
+    vld<T, V>(p.hx + c, h0);
+    vld<T, V>(p.hy + c, h1);
+    if (__ldg(p.rowflag + j)) return;
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const T rgt = q < V - 1 ? cur[q + 1] : right;
+      h0[q] = h0[q] + p.ku * (-up[q] + cur[q]);
+      h1[q] = h1[q] + p.ku * (rgt - cur[q]);
+    }
+    vst<T, V>(p.hx + c, h0);
+    vst<T, V>(p.hy + c, h1);
+  } else {
+    T xe[V];
+    vld_ro<T, V>(p.ey + c, xe);
+    vld<T, V>(p.hz + c, h0);
+    if (__ldg(p.rowflag + j)) return;
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const T rgt = q < V - 1 ? xe[q + 1] : right;
+      const T curlE = ((rgt - xe[q]) - up[q]) + cur[q];
+      h0[q] = h0[q] - p.ku * curlE;
+    }
+    vst<T, V>(p.hz + c, h0);
+  }
 }
 
-// V: cells per thread along x; 4 (float) / 2 (double) when the row length
-// allows aligned vector access, else 1
-template <typename T, int L>
-void launch_e2d_l(const StepParams<T> &p, int blocks, cudaStream_t s) {
-  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
-  if (p.vec == VW) e2d_kernel<T, L, VW><<<blocks, 256, 0, s>>>(p);
-  else e2d_kernel<T, L, 1><<<blocks, 256, 0, s>>>(p);
+// ---- kernels: one unit (or one dispersive cell) per thread -----------------
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) e2d_core(const __grid_constant__ StepParams<T> p) {
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  if (t >= p.ncore) return;
+  core_e<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
 }
+
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) h2d_core(const __grid_constant__ StepParams<T> p) {
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  if (t >= p.ncore) return;
+  core_h<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
+}
+
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) e2d_edge(const __grid_constant__ StepParams<T> p) {
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  if (t >= p.nedge) return;
+  K2<T, L, V>::unit_e(p, __ldg(p.edge_units + t), step_n(p));
+}
+
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) h2d_edge(const __grid_constant__ StepParams<T> p) {
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  if (t >= p.nedge) return;
+  K2<T, L, V>::unit_h(p, __ldg(p.edge_units + t), step_n(p));
+}
+
 template <typename T, int L>
-void launch_h2d_l(const StepParams<T> &p, int blocks, cudaStream_t s) {
-  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
-  if (p.vec == VW) h2d_kernel<T, L, VW><<<blocks, 256, 0, s>>>(p);
-  else h2d_kernel<T, L, 1><<<blocks, 256, 0, s>>>(p);
+__global__ void __launch_bounds__(256) e2d_ade(const __grid_constant__ StepParams<T> p) {
+  const int s = blockIdx.x * 256 + threadIdx.x;
+  if (s < p.nade) ade_e2<T, L>(p, s, step_n(p));
+}
+
+// V: cells per unit along x; 4 (float) / 2 (double) when the row length
+// allows aligned vector access, else 1.  Returns the kernels launched (0/1).
+template <typename T, int L, int V>
+int launch_e2d_v(const StepParams<T> &p, int part, cudaStream_t s) {
+  const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge : p.nade;
+  if (units <= 0) return 0;
+  const int blocks = (units + 255) / 256;
+  if (part == K2D_CORE) e2d_core<T, L, V><<<blocks, 256, 0, s>>>(p);
+  else if (part == K2D_EDGE) e2d_edge<T, L, V><<<blocks, 256, 0, s>>>(p);
+  else e2d_ade<T, L><<<blocks, 256, 0, s>>>(p);
+  return 1;
+}
+template <typename T, int L, int V>
+int launch_h2d_v(const StepParams<T> &p, int part, cudaStream_t s) {
+  const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge : 0;
+  if (units <= 0) return 0;
+  const int blocks = (units + 255) / 256;
+  if (part == K2D_CORE) h2d_core<T, L, V><<<blocks, 256, 0, s>>>(p);
+  else h2d_edge<T, L, V><<<blocks, 256, 0, s>>>(p);
+  return 1;
 }
 
 template <typename T>
-void launch_e2d(const StepParams<T> &p, int blocks, void *stream) {
+int launch_e2d(const StepParams<T> &p, int part, void *stream) {
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   cudaStream_t s = (cudaStream_t)stream;
-  if (p.layout == 3) launch_e2d_l<T, 3>(p, blocks, s);
-  else launch_e2d_l<T, 2>(p, blocks, s);
+  if (p.layout == 3)
+    return p.vec == VW ? launch_e2d_v<T, 3, VW>(p, part, s) : launch_e2d_v<T, 3, 1>(p, part, s);
+  return p.vec == VW ? launch_e2d_v<T, 2, VW>(p, part, s) : launch_e2d_v<T, 2, 1>(p, part, s);
 }
 
 template <typename T>
-void launch_h2d(const StepParams<T> &p, int blocks, void *stream) {
+int launch_h2d(const StepParams<T> &p, int part, void *stream) {
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   cudaStream_t s = (cudaStream_t)stream;
-  if (p.layout == 3) launch_h2d_l<T, 3>(p, blocks, s);
-  else launch_h2d_l<T, 2>(p, blocks, s);
+  if (p.layout == 3)
+    return p.vec == VW ? launch_h2d_v<T, 3, VW>(p, part, s) : launch_h2d_v<T, 3, 1>(p, part, s);
+  return p.vec == VW ? launch_h2d_v<T, 2, VW>(p, part, s) : launch_h2d_v<T, 2, 1>(p, part, s);
 }
 
-template void launch_e2d<float>(const StepParams<float> &, int, void *);
-template void launch_e2d<double>(const StepParams<double> &, int, void *);
-template void launch_h2d<float>(const StepParams<float> &, int, void *);
-template void launch_h2d<double>(const StepParams<double> &, int, void *);
+template int launch_e2d<float>(const StepParams<float> &, int, void *);
+template int launch_e2d<double>(const StepParams<double> &, int, void *);
+template int launch_h2d<float>(const StepParams<float> &, int, void *);
+template int launch_h2d<double>(const StepParams<double> &, int, void *);
 
 }  // namespace fdtd

@@ -23,7 +23,7 @@ EXPORTS = [
     "fdtd_step", "fdtd_update_DE", "fdtd_pml_update_E", "fdtd_interchange", "fdtd_update_H",
     "fdtd_pml_update_H", "fdtd_sample", "fdtd_sync", "fdtd_get_field", "fdtd_set_field",
     "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_profile",
-    "fdtd_kernel_time", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
+    "fdtd_kernel_time", "fdtd_kernel_cells", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
     "fdtd_dft_sample_noalloc",
 ]
 
@@ -57,6 +57,7 @@ def lib(path=None):
             "fdtd_get_monitor": [vp, i32, vp, vp], "fdtd_get_probe": [vp, i32, vp, C.POINTER(i32)],
             "fdtd_device_bytes": [vp, C.POINTER(C.c_uint64)], "fdtd_profile": [vp, i32],
             "fdtd_kernel_time": [vp, i32, C.POINTER(C.c_int64), C.POINTER(dbl)],
+            "fdtd_kernel_cells": [vp, i32, C.POINTER(C.c_int64)],
             "fdtd_launch_count": [vp, C.POINTER(C.c_int64)],
             "fdtd_set_stream": [vp, vp],
             "fdtd_transfer_bytes": [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
@@ -207,6 +208,11 @@ class Job:
         n, ms = C.c_int64(), C.c_double()
         check(lib().fdtd_kernel_time(self.h, int(kind), C.byref(n), C.byref(ms)))
         return n.value, ms.value
+
+    def kernel_cells(self, kind):
+        c = C.c_int64()
+        check(lib().fdtd_kernel_cells(self.h, int(kind), C.byref(c)))
+        return c.value
 
     def launch_count(self):
         n = C.c_int64()

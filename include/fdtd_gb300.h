@@ -251,10 +251,17 @@ int fdtd_device_bytes(const fdtd_job *job, uint64_t *bytes);
 /* When enabled, every launch of the job's kernels is bracketed by CUDA events
  * on the job's stream; fdtd_kernel_time returns the number of launches and
  * the summed device time of kernel class `kind` since the last reset. */
+/* FDTD_KERNEL_E / _H: the 3D half-step kernels, and in 2D the interior
+ * (core) kernels; FDTD_KERNEL_EDGE: the 2D kernels for PML cells, the edges
+ * of the main range and rows with sources, monitors or reference slabs;
+ * FDTD_KERNEL_ADE: the 2D dispersive-cell kernel. */
 enum { FDTD_KERNEL_E = 0, FDTD_KERNEL_H = 1, FDTD_KERNEL_DFT = 2, FDTD_KERNEL_LINE1D = 3,
-       FDTD_KERNEL_PML = 4, FDTD_KERNEL_COUNT = 5 };
+       FDTD_KERNEL_EDGE = 4, FDTD_KERNEL_ADE = 5, FDTD_KERNEL_COUNT = 6 };
 int fdtd_profile(fdtd_job *job, int32_t enable);
 int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms);
+/* Cells one launch of kernel class `kind` updates (FDTD_KERNEL_DFT: monitored
+ * samples per fold), for the algorithmic bytes of a roofline. */
+int fdtd_kernel_cells(const fdtd_job *job, int32_t kind, int64_t *cells);
 /* Launches of this library's kernels since the job was created. */
 int fdtd_launch_count(const fdtd_job *job, int64_t *launches);
 /* Run the job's work on a caller-owned cudaStream_t (NULL: the job's own
