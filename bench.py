@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=24, help="jobs in the serving run (0: none)")
+    ap.add_argument("--serve-rate", type=float, default=16.0, help="Poisson arrival rate, jobs/s")
     return ap.parse_args()
 
 
@@ -147,6 +149,46 @@ class Clocks:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def serving_run(njobs, rate):
+    """The serving workload: seeded Poisson arrivals of 2D TMz and 3D sphere
+    jobs, continuously batched by the library's server in FP32, against the
+    same arrivals run one at a time in FP64 plain."""
+    from fdtd_gpu import abi, serve
+    from fdtd_gpu.job import Job
+    mix = serve.poisson_mix(njobs, rate, seed=1)
+    S = serve.Server(max_active=16, chunk_steps=256)
+    lat, wall = serve.run_mix(S, mix)
+    st = S.stats()
+    S.close()
+    cells = sum(sp.cells() * nst for _, sp, nst in mix)
+    mix64 = serve.poisson_mix(njobs, rate, seed=1, precision=abi.F64)
+    t0 = time.perf_counter()
+    lat64 = []
+    for ta, spec, nst in mix64:
+        idle = ta - (time.perf_counter() - t0)
+        if idle > 0:
+            time.sleep(idle)
+        J = Job(spec)
+        J.step(1, nst)
+        for q in range(len(spec.monitors)):
+            J.get_monitor(q)
+        J.close()
+        lat64.append(time.perf_counter() - t0 - ta)
+    wall64 = time.perf_counter() - t0
+    return {
+        "workload": f"{njobs} jobs, Poisson {rate:g}/s, seed 1: 80% 2D TMz N in {{256,512,1024}} with 1-20 "
+                    "cylinders, 20% 3D spheres N in {128,192,256}; 2000-8000 steps, 32-128 frequencies",
+        "served_fp32": {"jobs_per_s": njobs / wall, "p50_s": serve.percentile(lat, 50),
+                        "p99_s": serve.percentile(lat, 99), "wall_s": wall,
+                        "mcell_updates_per_s": cells / wall / 1e6, "max_active": 16, "chunk_steps": 256,
+                        "hbm_held_max_bytes": st["held_bytes_max"]},
+        "sequential_fp64_plain": {"jobs_per_s": njobs / wall64, "p50_s": serve.percentile(lat64, 50),
+                                  "p99_s": serve.percentile(lat64, 99), "wall_s": wall64,
+                                  "mcell_updates_per_s": cells / wall64 / 1e6},
+        "latency": "host time from submission (at the Poisson arrival time) to the job's completion",
+    }
 
 
 def cpu_baseline(n, seconds, nthreads=None):
@@ -353,6 +395,8 @@ def main():
         "kernel_ms_fp64": {k: {"launches": v[0], "ms": v[1], "cells": v[2]} for k, v in kt64.items()},
         "clocks": clocks,
     }
+    if rank == 0 and args.serve_jobs > 0:
+        out["serving"] = serving_run(args.serve_jobs, args.serve_rate)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)
     if rank == 0:

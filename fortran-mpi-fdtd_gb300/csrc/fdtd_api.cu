@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -179,10 +180,35 @@ struct fdtd_job {
 
 namespace {
 
+// Job buffers come from the device's stream-ordered memory pool: freeing
+// them (fdtd_destroy, buffer growth) queues behind the job's own work and
+// does not synchronise the device, so jobs that come and go on a shared GPU
+// do not stall the others.  The pool keeps freed memory for reuse.
+void keep_pool_memory(int dev) {
+  static std::once_flag once[64];
+  if (dev < 0 || dev >= 64) return;
+  std::call_once(once[dev], [dev] {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  });
+}
+
+cudaError_t pool_alloc(fdtd_job *J, void **p, size_t bytes) {
+  keep_pool_memory(J->device);
+  return cudaMallocAsync(p, bytes, J->stream);
+}
+
+void pool_free(fdtd_job *J, void *p) {
+  if (p) cudaFreeAsync(p, J->stream);
+}
+
 int alloc_dev(fdtd_job *J, void **p, size_t bytes) {
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(p, bytes);
-  if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  cudaError_t e = pool_alloc(J, p, bytes);
+  if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
   J->allocs.push_back(*p);
   J->dev_bytes += bytes;
   e = cudaMemsetAsync(*p, 0, bytes, J->stream);
@@ -820,10 +846,10 @@ int ensure_srctab(fdtd_job *J, int n_max) {
   if (n_max > J->srctab_cap_steps) {
     long long cap = std::max<long long>(2 * J->srctab_cap_steps, std::max(n_max, 4096));
     double *nb = nullptr;
-    cudaError_t e = cudaMalloc(&nb, (size_t)cap * nsrc * sizeof(double));
+    cudaError_t e = pool_alloc(J, (void **)&nb, (size_t)cap * nsrc * sizeof(double));
     if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "source table: %s", cudaGetErrorString(e));
     CK(cudaStreamSynchronize(J->stream));
-    if (J->d_srctab) { cudaFree(J->d_srctab); J->dev_bytes -= (uint64_t)J->srctab_cap_steps * nsrc * sizeof(double); }
+    if (J->d_srctab) { pool_free(J, J->d_srctab); J->dev_bytes -= (uint64_t)J->srctab_cap_steps * nsrc * sizeof(double); }
     J->d_srctab = nb;
     J->srctab_cap_steps = cap;
     J->dev_bytes += (uint64_t)cap * nsrc * sizeof(double);
@@ -855,13 +881,13 @@ int ensure_probe_cap(fdtd_job *J, int n_max) {
     long long cap = std::max<long long>(need, 2LL * P.cap);
     cap = std::max<long long>(cap, 1024);
     double *nb = nullptr;
-    cudaError_t e = cudaMalloc(&nb, (size_t)cap * P.ncomp * sizeof(double));
+    cudaError_t e = pool_alloc(J, (void **)&nb, (size_t)cap * P.ncomp * sizeof(double));
     if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "probe buffer: %s", cudaGetErrorString(e));
     CK(cudaMemsetAsync(nb, 0, (size_t)cap * P.ncomp * sizeof(double), J->stream));
     if (P.buf) {
       CK(cudaMemcpyAsync(nb, P.buf, (size_t)P.cap * P.ncomp * sizeof(double), cudaMemcpyDeviceToDevice, J->stream));
       CK(cudaStreamSynchronize(J->stream));
-      cudaFree(P.buf);
+      pool_free(J, P.buf);
       J->dev_bytes -= (uint64_t)P.cap * P.ncomp * sizeof(double);
     }
     P.buf = nb;
@@ -1136,9 +1162,9 @@ int line_run(fdtd_job *J, int n_first, int n_steps, int stages) {
       }
     }
     if ((long long)v.size() > J->srcval_cap) {
-      if (J->d_srcval) { cudaFree(J->d_srcval); J->dev_bytes -= J->srcval_cap * sizeof(double); }
+      if (J->d_srcval) { pool_free(J, J->d_srcval); J->dev_bytes -= J->srcval_cap * sizeof(double); }
       J->srcval_cap = std::max<long long>((long long)v.size(), 4096);
-      CK(cudaMalloc(&J->d_srcval, J->srcval_cap * sizeof(double)));
+      CK(pool_alloc(J, (void **)&J->d_srcval, J->srcval_cap * sizeof(double)));
       J->dev_bytes += J->srcval_cap * sizeof(double);
     }
     CK(cudaMemcpyAsync(J->d_srcval, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, J->stream));
@@ -1338,10 +1364,11 @@ int fdtd_create(const fdtd_grid_desc *g, fdtd_job **out) {
 int fdtd_destroy(fdtd_job *J) {
   if (!J) return FDTD_OK;
   if (J->stream) cudaStreamSynchronize(J->stream);
-  for (void *p : J->allocs) cudaFree(p);
-  for (auto &P : J->probes) if (P.buf) cudaFree(P.buf);
-  if (J->d_srcval) cudaFree(J->d_srcval);
-  if (J->d_srctab) cudaFree(J->d_srctab);
+  J->stream = J->own_stream;  // the frees queue on the job's own stream
+  for (void *p : J->allocs) pool_free(J, p);
+  for (auto &P : J->probes) pool_free(J, P.buf);
+  pool_free(J, J->d_srcval);
+  pool_free(J, J->d_srctab);
   destroy_graph(J);
   for (auto &e : J->pending) { cudaEventDestroy(e.a); if (e.b) cudaEventDestroy(e.b); }
   for (auto e : J->ev_pool) cudaEventDestroy(e);
@@ -1589,6 +1616,60 @@ int fdtd_get_probe(fdtd_job *J, int32_t id, double *host, int32_t *count) {
 int fdtd_device_bytes(const fdtd_job *J, uint64_t *bytes) {
   if (!J || !bytes) return set_err(FDTD_EINVAL, "null argument");
   *bytes = J->dev_bytes;
+  return FDTD_OK;
+}
+
+int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
+  if (!J || !bytes) return set_err(FDTD_EINVAL, "null argument");
+  if (J->committed) {
+    *bytes = J->dev_bytes;
+    return FDTD_OK;
+  }
+  const uint64_t N = (uint64_t)J->ncell, w = J->esz;
+  const int nx = J->nx, ny = J->ny, nz = J->nz;
+  uint64_t b = N * w * (J->dim == 3 ? 6 : J->dim == 2 ? 3 : 2) + N;  // fields, material ids
+  if (J->has_tfsf) b += 2 * N * w;
+  // dispersive cells: each region's cells, bounded per sphere / box
+  uint64_t nade = 0;
+  for (auto &m : J->mats) {
+    if (m.kind != MK_GOLD && m.kind != MK_GRAPHENE) continue;
+    if (m.region.kind == FDTD_REGION_MASK) {
+      for (uint8_t v : m.mask) nade += v != 0;
+    } else if (m.region.kind == FDTD_REGION_SPHERES) {
+      for (int q = 0; q < m.region.count; ++q) {
+        const double d = 2.0 * m.centers[4 * q + 3] + 3.0;
+        uint64_t c = 1;
+        for (int a = 0; a < J->dim; ++a) c *= (uint64_t)d;
+        nade += c;
+      }
+    } else {
+      int lo[3], hi[3];
+      region_bounds(J, m, lo, hi);
+      uint64_t c = 1;
+      for (int a = 0; a < 3; ++a) c *= (uint64_t)std::max(0, hi[a] - lo[a] + 1);
+      nade += c;
+    }
+  }
+  nade = std::min(nade, N);
+  b += nade * ((uint64_t)kAdeFields * 3 * w + 5) + 32ull * kAdeFields * 3 * w;
+  if (J->has_pml && J->pml.mode == FDTD_PML_SPLIT) {
+    b += (uint64_t)(J->dim == 3 ? 6 : 1) * (w == 8 ? 2 : 1) * N * w;
+    b += 4ull * (nx + ny + nz) * w;
+  } else if (J->has_pml && J->pml.mode == FDTD_PML_REFERENCE) {
+    b += 2ull * 12 * (uint64_t)nx * (J->pml.npml[1][0] + 2) * nz * w + 24ull * (nx + ny + nz) * w;
+  }
+  if (J->dim == 2) {  // row flags and the edge unit list
+    const uint64_t units = (uint64_t)nx * ny;
+    const uint64_t frame = 2ull * ny * (J->pml.npml[0][0] + J->pml.npml[0][1] + 8) +
+                           (uint64_t)nx * (J->pml.npml[1][0] + J->pml.npml[1][1] + 16);
+    b += ny + 4 * std::min(units, frame);
+  }
+  for (auto &M : J->mons) {
+    const uint64_t smp = (uint64_t)M.ncomp * M.ncell;
+    b += smp * (J->dim == 1 ? 4096 : kStageSteps) * w + 2 * smp * M.d.nfreq * 8 + (uint64_t)M.d.nfreq * 8;
+  }
+  for (auto &P : J->probes) b += 1024ull * P.ncomp * 8;
+  *bytes = b + (1ull << 20);  // coefficient tables, source table, step counter
   return FDTD_OK;
 }
 

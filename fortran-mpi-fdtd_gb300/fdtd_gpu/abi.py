@@ -62,3 +62,15 @@ class ProbeDesc(C.Structure):
 
 class Tfsf1dDesc(C.Structure):
     _fields_ = [("boundary", C.c_int32), ("eps_lo", C.c_double), ("eps_hi", C.c_double)]
+
+
+class ServerDesc(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_active", C.c_int32), ("chunk_steps", C.c_int32)]
+
+
+class ServerStatus(C.Structure):
+    _fields_ = [("queued", C.c_int32), ("active", C.c_int32), ("finished", C.c_int64),
+                ("held_bytes", C.c_uint64), ("held_bytes_max", C.c_uint64), ("budget_bytes", C.c_uint64)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)

@@ -22,9 +22,11 @@ EXPORTS = [
     "fdtd_add_tfsf_1d", "fdtd_add_source", "fdtd_add_monitor", "fdtd_add_probe", "fdtd_commit",
     "fdtd_step", "fdtd_update_DE", "fdtd_pml_update_E", "fdtd_interchange", "fdtd_update_H",
     "fdtd_pml_update_H", "fdtd_sample", "fdtd_sync", "fdtd_get_field", "fdtd_set_field",
-    "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_profile",
+    "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_estimate_bytes", "fdtd_profile",
     "fdtd_kernel_time", "fdtd_kernel_cells", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
     "fdtd_dft_sample_noalloc",
+    "fdtd_server_create", "fdtd_server_submit", "fdtd_server_wait", "fdtd_server_job", "fdtd_server_times",
+    "fdtd_server_release", "fdtd_server_stats", "fdtd_server_destroy",
 ]
 
 
@@ -56,6 +58,7 @@ def lib(path=None):
             "fdtd_get_field": [vp, i32, vp], "fdtd_set_field": [vp, i32, vp],
             "fdtd_get_monitor": [vp, i32, vp, vp], "fdtd_get_probe": [vp, i32, vp, C.POINTER(i32)],
             "fdtd_device_bytes": [vp, C.POINTER(C.c_uint64)], "fdtd_profile": [vp, i32],
+            "fdtd_estimate_bytes": [vp, C.POINTER(C.c_uint64)],
             "fdtd_kernel_time": [vp, i32, C.POINTER(C.c_int64), C.POINTER(dbl)],
             "fdtd_kernel_cells": [vp, i32, C.POINTER(C.c_int64)],
             "fdtd_launch_count": [vp, C.POINTER(C.c_int64)],
@@ -63,6 +66,12 @@ def lib(path=None):
             "fdtd_transfer_bytes": [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
             "fdtd_dft_sample_noalloc": [vp, i32, i32, i32, i32, C.POINTER(i32), C.POINTER(i32), i32, i32, i32,
                                         dbl, vp, i32, vp, vp, i32, vp],
+            "fdtd_server_create": [vp, C.POINTER(vp)], "fdtd_server_submit": [vp, vp, i32, C.POINTER(C.c_int64)],
+            "fdtd_server_wait": [vp, C.c_int64, i32, C.POINTER(i32)],
+            "fdtd_server_job": [vp, C.c_int64, C.POINTER(vp)],
+            "fdtd_server_times": [vp, C.c_int64, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(dbl)],
+            "fdtd_server_release": [vp, C.c_int64], "fdtd_server_stats": [vp, vp],
+            "fdtd_server_destroy": [vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -105,7 +114,10 @@ def device_count():
 class Job:
     """One simulation on the GPU, built from a ``JobSpec``."""
 
-    def __init__(self, spec):
+    def __init__(self, spec, commit=True):
+        """Builds the job on the device.  With commit=False the set-up calls
+        are made but nothing is allocated: the handle can then be handed to
+        a Server (``detach``), which commits it when it admits the job."""
         self.spec = spec
         L = lib()
         g = spec.grid_desc()
@@ -140,11 +152,25 @@ class Job:
             for p in spec.probes:
                 d = S.probe_struct(p)
                 check(L.fdtd_add_probe(self.h, C.byref(d), C.byref(mid)))
-            check(L.fdtd_commit(self.h))
+            if commit:
+                check(L.fdtd_commit(self.h))
         except Exception:
             self.close()
             raise
         self.n_done = 0
+        self.owned = True
+
+    @classmethod
+    def view(cls, handle, spec):
+        """A non-owning wrapper of a job handle held elsewhere (a Server)."""
+        j = cls.__new__(cls)
+        j.spec, j.h, j.n_done, j.owned = spec, C.c_void_p(handle), 0, False
+        return j
+
+    def detach(self):
+        """Gives up ownership of the handle (to a Server) and returns it."""
+        h, self.h = self.h, None
+        return h
 
     # -- the time loop ---------------------------------------------------
     def step(self, n_first, n_steps):
@@ -201,6 +227,11 @@ class Job:
         check(lib().fdtd_device_bytes(self.h, C.byref(b)))
         return b.value
 
+    def estimate_bytes(self):
+        b = C.c_uint64()
+        check(lib().fdtd_estimate_bytes(self.h, C.byref(b)))
+        return b.value
+
     def profile(self, enable=True):
         check(lib().fdtd_profile(self.h, 1 if enable else 0))
 
@@ -229,9 +260,9 @@ class Job:
         return h.value, d.value
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "owned", True):
             lib().fdtd_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

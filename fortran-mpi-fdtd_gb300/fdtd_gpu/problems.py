@@ -341,7 +341,7 @@ def cylinders_2d(n=2048, count=40, seed=0, rmin=10, rmax=40, ylo=200, yhi=1948, 
     return [(x, y, 0.0, float(r)) for x, y, r in out]
 
 
-def config_2d_tmz(precision=abi.F32, n=2048, steps=10000, ncyl=40, nfreq=100, npml=32):
+def config_2d_tmz(precision=abi.F32, n=2048, steps=10000, ncyl=40, nfreq=100, npml=32, seed=0):
     """2D TMz 2048^2, dx=1 nm, Ku=0.5, 32-cell split-field PML on all faces,
     40 seeded gold cylinders, Ez line source at y=100 (600 nm pulse), line DFT
     of Ez and Hx at y=200 (incident/reflected) and y=1948 (transmitted)."""
@@ -354,7 +354,7 @@ def config_2d_tmz(precision=abi.F32, n=2048, steps=10000, ncyl=40, nfreq=100, np
                    name="config_2d_tmz")
     spec.add_dielectric(box((0, 0, 0), (n - 1, n - 1, 0)), 1.0)
     scale = n / 2048.0
-    cyl = cylinders_2d(n=n, count=ncyl, ylo=max(int(200 * scale), npml + 12), yhi=min(int(1948 * scale), n - npml - 4), pml=npml,
+    cyl = cylinders_2d(n=n, count=ncyl, seed=seed, ylo=max(int(200 * scale), npml + 12), yhi=min(int(1948 * scale), n - npml - 4), pml=npml,
                        rmin=max(2, int(10 * scale)), rmax=max(3, int(40 * scale))) if ncyl else []
     if cyl:
         spec.add_gold(spheres(cyl), GOLD_CONFIG)

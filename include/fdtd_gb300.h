@@ -246,6 +246,9 @@ int fdtd_get_monitor(fdtd_job *job, int32_t id, double *re, double *im);
 int fdtd_get_probe(fdtd_job *job, int32_t id, double *host, int32_t *count);
 /* Bytes of device memory the job holds (HBM admission). */
 int fdtd_device_bytes(const fdtd_job *job, uint64_t *bytes);
+/* Before fdtd_commit: an upper bound of the bytes the job will hold once
+ * committed (after commit: the bytes it holds), for admission by footprint. */
+int fdtd_estimate_bytes(const fdtd_job *job, uint64_t *bytes);
 
 /* ---- measurement --------------------------------------------------------- */
 /* When enabled, every launch of the job's kernels is bracketed by CUDA events
@@ -270,6 +273,47 @@ int fdtd_set_stream(fdtd_job *job, void *cuda_stream);
 /* Host->device and device->host bytes moved by set-up, getters and setters
  * since the job was created. */
 int fdtd_transfer_bytes(const fdtd_job *job, uint64_t *h2d, uint64_t *d2h);
+
+/* ---- serving: continuous batching of jobs on one GPU ---------------------
+ * No counterpart in the reference, which runs one simulation per MPI job.
+ * A server owns the jobs submitted to it (built with the fdtd_add_* calls,
+ * not committed) and advances every admitted job on its own stream in chunks
+ * of chunk_steps steps, so the kernels of different jobs overlap on the GPU.
+ * Jobs are admitted in submission order when fewer than max_active are
+ * running and their fdtd_estimate_bytes fits in what hbm_budget has left
+ * (0: 90% of the device's free memory at creation); a job that can never fit
+ * fails with FDTD_ENOMEM.  A finished job keeps its memory until
+ * fdtd_server_release.  Each job runs steps 1..n_steps, with the same
+ * kernels in the same order as fdtd_step(job, 1, n_steps) on its own, so its
+ * results do not depend on the other jobs. */
+typedef struct fdtd_server fdtd_server;
+typedef struct {
+  uint64_t hbm_budget;  /* device bytes the admitted jobs may hold (0: 90% of free) */
+  int32_t max_active;   /* jobs advanced at once */
+  int32_t chunk_steps;  /* steps per scheduling turn (rounded up to whole 32-step rings) */
+} fdtd_server_desc;
+typedef struct {
+  int32_t queued, active;
+  int64_t finished;
+  uint64_t held_bytes, held_bytes_max, budget_bytes;
+} fdtd_server_status;
+enum { FDTD_REQ_QUEUED = 0, FDTD_REQ_RUNNING = 1, FDTD_REQ_DONE = 2, FDTD_REQ_FAILED = 3 };
+int fdtd_server_create(const fdtd_server_desc *desc, fdtd_server **server);
+/* Takes ownership of `job` (uncommitted) on success. */
+int fdtd_server_submit(fdtd_server *server, fdtd_job *job, int32_t n_steps, int64_t *ticket);
+/* Waits until the job is done or failed, or timeout_ms passes (< 0: no
+ * limit); *state is its FDTD_REQ_* state. */
+int fdtd_server_wait(fdtd_server *server, int64_t ticket, int32_t timeout_ms, int32_t *state);
+/* The finished job, for fdtd_get_monitor / fdtd_get_probe / fdtd_get_field;
+ * valid until fdtd_server_release. */
+int fdtd_server_job(fdtd_server *server, int64_t ticket, fdtd_job **job);
+/* Host times in seconds since the server was created (-1: not yet). */
+int fdtd_server_times(fdtd_server *server, int64_t ticket, double *t_submit, double *t_admit, double *t_done);
+/* Destroys a finished job and returns its memory to the budget. */
+int fdtd_server_release(fdtd_server *server, int64_t ticket);
+int fdtd_server_stats(fdtd_server *server, fdtd_server_status *stats);
+/* Stops admitting, lets the chunks in flight end and destroys every job. */
+int fdtd_server_destroy(fdtd_server *server);
 
 /* ---- allocation-free DFT of a caller-owned field ------------------------ *
  * No counterpart in the reference: its DFT sums live inside program.f90's
