@@ -173,7 +173,8 @@ struct fdtd_job {
   // 2D work split (core box + edge unit list) and the streams that run the
   // parts of a half step as parallel branches of the job's stream
   int vec = 1, cv0 = 0, cw = 0, cy0 = 0, ncore = 0, nedge = 0;
-  int *d_edge = nullptr;
+  int ch = 0, cz0 = 0, cd = 0, ntiles = 0;  // 3D: core box and general-tile count
+  int *d_edge = nullptr, *d_tiles = nullptr;
   cudaStream_t side[2] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {};
 };
@@ -352,6 +353,16 @@ int upload_prof(fdtd_job *J, const Prof &P, void **f1, void **f2, void **g1, voi
 }
 
 // ---- commit ------------------------------------------------------------
+// side streams and events that fork a half step's parts off the job's stream
+int make_branches(fdtd_job *J) {
+  for (int q = 0; q < 2; ++q) {
+    CK(cudaStreamCreateWithFlags(&J->side[q], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&J->ev_join[q], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&J->ev_fork, cudaEventDisableTiming));
+  return FDTD_OK;
+}
+
 // 2D work split.  Core units: whole V-cell vectors of the main range outside
 // the split-PML shell, in rows without flags; they take only the interior
 // Yee update.  Every other unit goes to a list for the edge kernel.
@@ -384,12 +395,52 @@ int split_2d(fdtd_job *J, const std::vector<uint8_t> &rf) {
     CK(cudaMemcpy(J->d_edge, edge.data(), edge.size() * sizeof(int), cudaMemcpyHostToDevice));
     J->h2d += edge.size() * sizeof(int);
   }
-  for (int q = 0; q < 2; ++q) {
-    CK(cudaStreamCreateWithFlags(&J->side[q], cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&J->ev_join[q], cudaEventDisableTiming));
+  return make_branches(J);
+}
+
+// 3D work split.  Core units: whole V-cell x-vectors of the main range
+// outside the split-PML shell, in (y, z) rows without a source.  The general
+// launch takes every 32 x 8 x kKZ tile that holds any other cell.
+int split_3d(fdtd_job *J, const std::vector<uint8_t> &rf) {
+  const int nx = J->nx, ny = J->ny, nz = J->nz;
+  const int vw = J->esz == 4 ? 4 : 2;
+  const int V = J->vec = (nx % vw == 0) ? vw : 1;
+  int lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = std::max(J->g.main_lo[a], J->slo[a]);
+    hi[a] = std::min(J->g.main_hi[a], J->shi[a]);
   }
-  CK(cudaEventCreateWithFlags(&J->ev_fork, cudaEventDisableTiming));
-  return FDTD_OK;
+  const int cv0 = (lo[0] + V - 1) / V, cv1 = std::max(cv0, (hi[0] + 1) / V);
+  J->cv0 = cv0;
+  J->cw = cv1 - cv0;
+  J->cy0 = lo[1];
+  J->ch = std::max(0, hi[1] - lo[1] + 1);
+  J->cz0 = lo[2];
+  J->cd = std::max(0, hi[2] - lo[2] + 1);
+  const long long ncore = (long long)J->cw * J->ch * J->cd;
+  if (ncore > (long long)INT32_MAX) return set_err(FDTD_ERANGE, "3D core box too large for 32-bit unit indices");
+  J->ncore = (int)ncore;
+  const int x0 = cv0 * V, x1 = cv1 * V, y0 = lo[1], y1 = lo[1] + J->ch, z0 = lo[2], z1 = lo[2] + J->cd;
+  const int tx = (nx + 31) / 32, ty = (ny + 7) / 8, tz = (nz + kKZ3 - 1) / kKZ3;
+  std::vector<int> tiles;
+  for (int c = 0; c < tz; ++c)
+    for (int b = 0; b < ty; ++b)
+      for (int a = 0; a < tx; ++a) {
+        const int i0 = a * 32, i1 = std::min(nx, i0 + 32), j0 = b * 8, j1 = std::min(ny, j0 + 8);
+        const int k0 = c * kKZ3, k1 = std::min(nz, k0 + kKZ3);
+        bool need = J->ncore == 0 || i0 < x0 || i1 > x1 || j0 < y0 || j1 > y1 || k0 < z0 || k1 > z1;
+        for (int k = k0; k < k1 && !need; ++k)
+          for (int j = j0; j < j1 && !need; ++j) need = rf[(size_t)k * ny + j] != 0;
+        if (need) tiles.push_back((c * ty + b) * tx + a);
+      }
+  J->ntiles = (int)tiles.size();
+  int rc;
+  if (!tiles.empty()) {
+    if ((rc = alloc_dev(J, (void **)&J->d_tiles, tiles.size() * sizeof(int)))) return rc;
+    CK(cudaMemcpy(J->d_tiles, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
+    J->h2d += tiles.size() * sizeof(int);
+  }
+  return make_branches(J);
 }
 
 template <typename T>
@@ -683,7 +734,7 @@ int commit_impl(fdtd_job *J) {
   for (auto &P : J->probes)
     if (ref && J->dim == 3 && J->slab_rows > 0 && (P.d.cell[1] <= J->slab_rows - 1 || P.d.cell[1] >= ny - J->slab_rows))
       touches_slab = true;
-  J->gather_fused = !touches_slab;
+  J->gather_fused = J->dim == 2 || (J->dim == 1 && !touches_slab);  // 3D: stand-alone gather kernel
   if (J->dim == 2) {
     std::vector<uint8_t> rf((size_t)ny, 0);
     for (auto &sr : J->srcs) {
@@ -700,6 +751,18 @@ int commit_impl(fdtd_job *J) {
     CK(cudaMemcpy(J->d_rowflag, rf.data(), (size_t)ny, cudaMemcpyHostToDevice));
     J->h2d += (uint64_t)ny;
     if ((rc = split_2d(J, rf))) return rc;
+  } else if (J->dim == 3) {
+    std::vector<uint8_t> rf((size_t)ny * nz, 0);
+    for (auto &sr : J->srcs) {
+      if (sr.component == FDTD_EX_INC) continue;
+      for (int k = std::max(sr.lo[2], J->g.main_lo[2]); k <= std::min(sr.hi[2], J->g.main_hi[2]); ++k)
+        for (int j = std::max(sr.lo[1], J->g.main_lo[1]); j <= std::min(sr.hi[1], J->g.main_hi[1]); ++j)
+          rf[(size_t)k * ny + j] |= ROW_SRC;
+    }
+    if ((rc = alloc_dev(J, (void **)&J->d_rowflag, rf.size()))) return rc;
+    CK(cudaMemcpy(J->d_rowflag, rf.data(), rf.size(), cudaMemcpyHostToDevice));
+    J->h2d += rf.size();
+    if ((rc = split_3d(J, rf))) return rc;
   }
   J->stage_row = base;
   J->acc_total = acc;
@@ -783,8 +846,12 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.nedge = J->nedge;
     p.edge_units = J->d_edge;
   } else {
-    p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 7) / 8; p.tiles_z = (J->nz + 15) / 16;
-    p.ntile_blocks = p.tiles_x * p.tiles_y * p.tiles_z;
+    p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 7) / 8; p.tiles_z = (J->nz + kKZ3 - 1) / kKZ3;
+    p.ntile_blocks = J->ntiles;
+    p.tile_list = J->d_tiles;
+    p.vec = J->vec;
+    p.cv0 = J->cv0; p.cw = J->cw; p.cy0 = J->cy0; p.ch = J->ch; p.cz0 = J->cz0; p.cd = J->cd;
+    p.ncore = J->ncore;
   }
   p.nslab_blocks = (J->dim == 3 && J->slab_rows > 0) ? (2 * J->nx * J->slab_rows * J->nz + 255) / 256 : 0;
   p.nade_blocks = (J->nade + 255) / 256;
@@ -929,15 +996,24 @@ int dft_fold(fdtd_job *J) {
 
 enum { ST_E = 1, ST_H = 2, ST_SAMPLE = 4 };
 
-// 2D: the parts of one half step (core, edge, ADE) write disjoint cells and
-// read only the other half's fields, so they run as parallel branches of the
-// job's stream (forked and joined with events; a stream capture records them
-// as parallel graph nodes).  Profiled runs launch them one after another so
-// that each part's events time that part alone.
+// The parts of one half step write disjoint cells and read only the other
+// half's fields, so they run as parallel branches of the job's stream
+// (forked and joined with events; a stream capture records them as parallel
+// graph nodes).  2D: core, edge and ADE launches; 3D: core and the general
+// launch (tiles with non-core cells, reference slabs, ADE cells).  Profiled
+// runs launch them one after another so that each part's events time that
+// part alone.
 template <typename T>
-int run_parts_2d(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], bool e_half, bool graph) {
+int launch_part(const fdtd_job *J, const StepParams<T> &p, int part, bool e_half, cudaStream_t s) {
+  if (J->dim == 2) return e_half ? launch_e2d<T>(p, part, s) : launch_h2d<T>(p, part, s);
+  return e_half ? launch_e3d<T>(p, part, s) : launch_h3d<T>(p, part, s);
+}
+
+template <typename T>
+int run_parts(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], bool e_half, bool graph) {
   static const int kind[3] = {-1, FDTD_KERNEL_EDGE, FDTD_KERNEL_ADE};
-  const int units[3] = {p.ncore, p.nedge, e_half ? p.nade : 0};
+  const int general = J->dim == 2 ? p.nedge : p.ntile_blocks + p.nslab_blocks + (e_half ? p.nade_blocks : 0);
+  const int units[3] = {p.ncore, general, J->dim == 2 && e_half ? p.nade : 0};
   int use[3], nuse = 0;
   for (int q = 0; q < 3; ++q)
     if (want[q] && units[q] > 0) use[nuse++] = q;
@@ -954,7 +1030,7 @@ int run_parts_2d(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], boo
     const int q = use[b];
     const int k = q == K2D_CORE ? (e_half ? FDTD_KERNEL_E : FDTD_KERNEL_H) : kind[q];
     if (!graph) ev_record(J, k, true);
-    J->launches += e_half ? launch_e2d<T>(p, q, st[b]) : launch_h2d<T>(p, q, st[b]);
+    J->launches += launch_part<T>(J, p, q, e_half, st[b]);
     if (!graph) ev_record(J, k, false);
   }
   CK(cudaGetLastError());
@@ -978,17 +1054,9 @@ int half_e(fdtd_job *J, int n, int roles, int slot = 0, bool graph = false) {
   p.n = n;
   p.slot = slot;
   p.d_base = graph ? J->d_base : nullptr;
-  if (J->dim == 2) {
-    const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML)) != 0, (roles & ROLE_ADE) != 0};
-    return run_parts_2d<T>(J, p, parts, true, graph);
-  }
-  int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
-  if (!graph) ev_record(J, FDTD_KERNEL_E, true);
-  launch_e3d<T>(p, blocks, J->stream);
-  if (!graph) ev_record(J, FDTD_KERNEL_E, false);
-  J->launches++;
-  CK(cudaGetLastError());
-  return FDTD_OK;
+  const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML | (J->dim == 3 ? ROLE_ADE : 0))) != 0,
+                         J->dim == 2 && (roles & ROLE_ADE) != 0};
+  return run_parts<T>(J, p, parts, true, graph);
 }
 
 template <typename T>
@@ -1000,17 +1068,8 @@ int half_h(fdtd_job *J, int n, int roles, bool gather, int slot = -1, bool graph
   p.gather = gather ? 1 : 0;
   p.slot = slot >= 0 ? slot : J->stage_fill;
   p.d_base = graph ? J->d_base : nullptr;
-  if (J->dim == 2) {
-    const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML)) != 0, false};
-    return run_parts_2d<T>(J, p, parts, false, graph);
-  }
-  int blocks = p.ntile_blocks + p.nslab_blocks;
-  if (!graph) ev_record(J, FDTD_KERNEL_H, true);
-  launch_h3d<T>(p, blocks, J->stream);
-  if (!graph) ev_record(J, FDTD_KERNEL_H, false);
-  J->launches++;
-  CK(cudaGetLastError());
-  return FDTD_OK;
+  const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML)) != 0, false};
+  return run_parts<T>(J, p, parts, false, graph);
 }
 
 template <typename T>
@@ -1703,8 +1762,9 @@ int fdtd_kernel_cells(const fdtd_job *J, int32_t kind, int64_t *cells) {
   if (kind < 0 || kind >= FDTD_KERNEL_COUNT) return set_err(FDTD_EINVAL, "bad kernel kind");
   if (!J->committed) return set_err(FDTD_ESTATE, "job not committed");
   int64_t c = 0;
-  if (kind == FDTD_KERNEL_E || kind == FDTD_KERNEL_H) c = J->dim == 2 ? (int64_t)J->ncore * J->vec : J->ncell;
-  else if (kind == FDTD_KERNEL_EDGE) c = J->dim == 2 ? (int64_t)J->nedge * J->vec : 0;
+  if (kind == FDTD_KERNEL_E || kind == FDTD_KERNEL_H) c = J->dim >= 2 ? (int64_t)J->ncore * J->vec : 0;
+  else if (kind == FDTD_KERNEL_EDGE)
+    c = J->dim == 2 ? (int64_t)J->nedge * J->vec : J->dim == 3 ? (int64_t)J->ntiles * 32 * 8 * kKZ3 : 0;
   else if (kind == FDTD_KERNEL_ADE) c = J->dim == 2 ? J->nade : 0;
   else if (kind == FDTD_KERNEL_LINE1D) c = J->dim == 1 ? J->ncell : 0;
   else if (kind == FDTD_KERNEL_DFT) {

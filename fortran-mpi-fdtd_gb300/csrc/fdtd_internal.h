@@ -24,6 +24,7 @@ constexpr int kMaxMat = 256;
 constexpr int kMaxSrc = 8;
 constexpr int kMaxMon = 16;
 constexpr int kMaxProbe = 16;
+constexpr int kKZ3 = 16;         // 3D tiles: cells each thread marches along z
 constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
 
 enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3 };
@@ -95,7 +96,7 @@ struct StepParams {
   const T *mca, *mcs;      // per id: Ku/eps and 1/eps (0 for none and ADE ids)
   int id0;                 // most common material id of the main cells and
   T ca0;                   //   its Ku/eps (no table lookup for it)
-  const uint8_t *rowflag;  // 2D: per row, ROW_* bits
+  const uint8_t *rowflag;  // per x-row, ROW_* bits: 2D [j], 3D [k*ny + j]
   // ADE slots
   int nade;
   const int *ade_cell;     // linear cell index
@@ -134,6 +135,10 @@ struct StepParams {
   int cv0, cw, cy0, ncore;
   int nedge;
   const int *edge_units;
+  // 3D: the core box is vectors [cv0, cv0+cw) x rows [cy0, cy0+ch) x planes
+  // [cz0, cz0+cd); the general launch takes its tiles from tile_list
+  int ch, cz0, cd;
+  const int *tile_list;
   // sampling fused into the H kernel
   int gather;              // 1: tile threads write the stage row / probes
   int nmon;
@@ -170,8 +175,8 @@ constexpr int kAdeFields = 6;
 enum K2dPart { K2D_CORE = 0, K2D_EDGE = 1, K2D_ADE = 2 };
 template <typename T> int launch_e2d(const StepParams<T> &p, int part, void *stream);
 template <typename T> int launch_h2d(const StepParams<T> &p, int part, void *stream);
-template <typename T> void launch_e3d(const StepParams<T> &p, int blocks, void *stream);
-template <typename T> void launch_h3d(const StepParams<T> &p, int blocks, void *stream);
+template <typename T> int launch_e3d(const StepParams<T> &p, int part, void *stream);
+template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *stream);
 
 // separate gather (per-procedure API, or monitors inside reference slabs)
 template <typename T> void launch_gather(const StepParams<T> &p, void *stream);

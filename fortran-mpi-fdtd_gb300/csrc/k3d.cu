@@ -1,15 +1,22 @@
 // k3d.cu -- 3D half-step kernels (3D/.../include/myfdtd_func.f90:19-64).
 //
-// One launch per half step; blockIdx selects the work:
-//   tile blocks : 32 (x) x 8 (y) threads, each marching kKZ cells along z
-//                 with the previous (E) or next (H) plane kept in registers;
-//                 x neighbours by warp shuffle.  Main cells do the Yee
-//                 update with the constant-dielectric material folded in;
-//                 shell cells of the split-field PML do the split update.
-//   slab blocks : the reference's y-slab PML (3D/BERpmly_mod.f90:72-306),
+// A half step is two independent launches that write disjoint cells, run by
+// the host as parallel branches of its stream:
+//   core    : the interior box -- main cells outside the PML shell, in
+//             (y, z) rows without a source -- one x-vector of V cells per
+//             thread, only the Yee update with the constant-dielectric
+//             material folded in.  Nearly all of a large grid.
+//   general : blockIdx selects the work:
+//     tile blocks : the 32 (x) x 8 (y) x kKZ (z) tiles, from a list, that
+//                 hold any non-core cell; each thread marches kKZ cells along
+//                 z with the previous (E) or next (H) plane in registers and
+//                 x neighbours by warp shuffle.  Main cells do the Yee update
+//                 and the sources; shell cells of the split-field PML do the
+//                 split update; core cells are left to the core launch.
+//     slab blocks : the reference's y-slab PML (3D/BERpmly_mod.f90:72-306),
 //                 one thread per slab cell and side, 12 split arrays, the
 //                 coupling rows read straight from the main arrays.
-//   ADE blocks  : one thread per dispersive cell (3D/gold_mod.f90:50-88).
+//     ADE blocks  : one thread per dispersive cell (3D/gold_mod.f90:50-88).
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.h"
@@ -17,7 +24,21 @@
 
 namespace fdtd {
 
-constexpr int kKZ = 16;
+constexpr int kKZ = kKZ3;
+
+// Ku/eps of a cell: the dominant material's coefficient is a parameter
+template <typename T>
+__device__ __forceinline__ T coef_ca3(const StepParams<T> &p, uint8_t id) {
+  return id == p.id0 ? p.ca0 : __ldg(p.mca + id);
+}
+
+// store V values, skipping cells whose E belongs to an ADE thread
+template <typename T, int V>
+__device__ __forceinline__ void st_guard3(T *a, const T (&v)[V], const uint8_t (&id)[V]) {
+#pragma unroll
+  for (int q = 0; q < V; ++q)
+    if (id[q] < kAdeId) a[q] = v[q];
+}
 
 template <typename T>
 struct F3 {
@@ -44,6 +65,13 @@ struct F3 {
   }
 };
 
+// a cell of the core box in a row without flags: updated by the core launch
+template <typename T>
+__device__ __forceinline__ bool in_core3(const StepParams<T> &p, int i, int j, int k) {
+  return p.ncore > 0 && i >= p.cv0 * p.vec && i < (p.cv0 + p.cw) * p.vec && j >= p.cy0 && j < p.cy0 + p.ch &&
+         k >= p.cz0 && k < p.cz0 + p.cd && !__ldg(p.rowflag + (long long)k * p.ny + j);
+}
+
 template <typename T>
 __device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b, int n) {
   const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
@@ -66,7 +94,7 @@ __device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b, int n) {
     const T hxkm = hx_km, hykm = hy_km;
     hx_km = hxc;
     hy_km = hyc;
-    if (!inx) continue;
+    if (!inx || in_core3(p, i, j, k)) continue;
     const T hzd = f.ly(p.hz, i, j - 1, k), hxd = f.ly(p.hx, i, j - 1, k);
     const T curlhzy = hzc - hzd, curlhyz = -hyc + hykm;
     const T curlhxz = hxc - hxkm, curlhzx = -hzc + hzl;
@@ -131,7 +159,7 @@ __device__ __forceinline__ void tile_h3(const StepParams<T> &p, int b, int n) {
     const T ex0 = exc, ey0 = eyc;
     exc = exkp;
     eyc = eykp;
-    if (!inx) continue;
+    if (!inx || in_core3(p, i, j, k)) continue;  // 3D samples in the gather kernel
     const T ezu = f.ly(p.ez, i, j + 1, k), exu = f.ly(p.ex, i, j + 1, k);
     const T curleyz = eykp - ey0, curlezy = -ezu + ezc;
     const T curlezx = ezr - ezc, curlexz = -exkp + ex0;
@@ -313,7 +341,7 @@ __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepPa
   const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
-    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_e3<T>(p, b, n);
+    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_e3<T>(p, p.tile_list ? __ldg(p.tile_list + b) : b, n);
     return;
   }
   b -= p.ntile_blocks;
@@ -333,25 +361,182 @@ __global__ void __launch_bounds__(256) h3d_kernel(const __grid_constant__ StepPa
   const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
-    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_h3<T>(p, b, n);
+    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_h3<T>(p, p.tile_list ? __ldg(p.tile_list + b) : b, n);
     return;
   }
   b -= p.ntile_blocks;
   if (b < p.nslab_blocks && (p.roles & ROLE_PML)) slab_h3<T>(p, b * 256 + threadIdx.x);
 }
 
-template <typename T>
-void launch_e3d(const StepParams<T> &p, int blocks, void *stream) {
-  e3d_kernel<T><<<blocks, 256, 0, (cudaStream_t)stream>>>(p);
-}
-template <typename T>
-void launch_h3d(const StepParams<T> &p, int blocks, void *stream) {
-  h3d_kernel<T><<<blocks, 256, 0, (cudaStream_t)stream>>>(p);
+// ---- core units: one x-vector of V interior cells per thread --------------
+// Block: 32 vectors along x by 8 rows along y, one z plane; blocks run x, y,
+// then z, so the plane below (E) or above (H) was read moments earlier and
+// its loads hit L2.
+template <typename T, int V>
+struct Core3 {
+  int j, k, i0;
+  long long c;
+  bool live;
+  __device__ __forceinline__ Core3(const StepParams<T> &p) {
+    const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
+    const int bx = (p.cw + 31) >> 5, by = (p.ch + 7) >> 3;
+    const int b = blockIdx.x, tx = b % bx, t2 = b / bx, ty = t2 % by, tz = t2 / by;
+    const int v = tx * 32 + lane, r = ty * 8 + wy;
+    live = v < p.cw && r < p.ch && tz < p.cd;
+    j = p.cy0 + r;
+    k = p.cz0 + tz;
+    i0 = (p.cv0 + v) * V;
+    c = ((long long)k * p.ny + j) * p.nx + i0;
+  }
+};
+
+// neighbour vector one row (dy = +-1) or one plane (dz = +-1) away, wrapped
+// on periodic axes and zero beyond open ones
+template <typename T, int V>
+__device__ __forceinline__ void nb_vec(const StepParams<T> &p, const T *a, long long c, int j, int k, int dy, int dz,
+                                       T (&v)[V]) {
+  const long long plane = (long long)p.nx * p.ny;
+  long long d = 0;
+  bool ok = true;
+  if (dy) {
+    const int jj = j + dy;
+    if (jj >= 0 && jj < p.ny) d = (long long)dy * p.nx;
+    else if (p.per[1]) d = (long long)(dy > 0 ? -(p.ny - 1) : (p.ny - 1)) * p.nx;
+    else ok = false;
+  } else {
+    const int kk = k + dz;
+    if (kk >= 0 && kk < p.nz) d = (long long)dz * plane;
+    else if (p.per[2]) d = (long long)(dz > 0 ? -(p.nz - 1) : (p.nz - 1)) * plane;
+    else ok = false;
+  }
+  if (ok) vld_ro<T, V>(a + c + d, v);
+  else {
+#pragma unroll
+    for (int q = 0; q < V; ++q) v[q] = T(0);
+  }
 }
 
-template void launch_e3d<float>(const StepParams<float> &, int, void *);
-template void launch_e3d<double>(const StepParams<double> &, int, void *);
-template void launch_h3d<float>(const StepParams<float> &, int, void *);
-template void launch_h3d<double>(const StepParams<double> &, int, void *);
+// cell next to the vector along x (dx = -1: left of its first cell, +1:
+// right of its last), wrapped on a periodic axis, zero beyond an open one
+template <typename T, int V>
+__device__ __forceinline__ T nb_x(const StepParams<T> &p, const T *a, long long c, int i0, int dx) {
+  if (dx < 0) return i0 > 0 ? __ldg(a + c - 1) : (p.per[0] ? __ldg(a + c + p.nx - 1) : T(0));
+  return i0 + V < p.nx ? __ldg(a + c + V) : (p.per[0] ? __ldg(a + c + V - p.nx) : T(0));
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256) e3d_core(const __grid_constant__ StepParams<T> p) {
+  const Core3<T, V> u(p);
+  if (!u.live) return;
+  const long long c = u.c;
+  T hx[V], hy[V], hz[V], hzd[V], hxd[V], hyb[V], hxb[V], ex[V], ey[V], ez[V];
+  uint8_t id[V];
+  vld_ro<T, V>(p.hx + c, hx);
+  vld_ro<T, V>(p.hy + c, hy);
+  vld_ro<T, V>(p.hz + c, hz);
+  nb_vec<T, V>(p, p.hz, c, u.j, u.k, -1, 0, hzd);
+  nb_vec<T, V>(p, p.hx, c, u.j, u.k, -1, 0, hxd);
+  nb_vec<T, V>(p, p.hy, c, u.j, u.k, 0, -1, hyb);
+  nb_vec<T, V>(p, p.hx, c, u.j, u.k, 0, -1, hxb);
+  const T hzl = nb_x<T, V>(p, p.hz, c, u.i0, -1), hyl = nb_x<T, V>(p, p.hy, c, u.i0, -1);
+  vld<T, V>(p.ex + c, ex);
+  vld<T, V>(p.ey + c, ey);
+  vld<T, V>(p.ez + c, ez);
+  vld_ids<V>(p.mat + c, id);
+  if (__ldg(p.rowflag + (long long)u.k * p.ny + u.j)) return;  // source rows: general launch
+  bool uni = true;
+#pragma unroll
+  for (int q = 0; q < V; ++q) uni &= id[q] == p.id0;
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    const T ca = uni ? p.ca0 : coef_ca3(p, id[q]);
+    const T curlhzy = hz[q] - hzd[q], curlhyz = -hy[q] + hyb[q];
+    const T curlhxz = hx[q] - hxb[q], curlhzx = -hz[q] + (q ? hz[q - 1] : hzl);
+    const T curlhyx = hy[q] - (q ? hy[q - 1] : hyl), curlhxy = -hx[q] + hxd[q];
+    ex[q] = ex[q] + ca * (curlhzy + curlhyz);
+    ey[q] = ey[q] + ca * (curlhxz + curlhzx);
+    ez[q] = ez[q] + ca * (curlhyx + curlhxy);
+  }
+  if (uni) {
+    vst<T, V>(p.ex + c, ex);
+    vst<T, V>(p.ey + c, ey);
+    vst<T, V>(p.ez + c, ez);
+  } else {  // dispersive cells belong to the ADE blocks
+    st_guard3<T, V>(p.ex + c, ex, id);
+    st_guard3<T, V>(p.ey + c, ey, id);
+    st_guard3<T, V>(p.ez + c, ez, id);
+  }
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256) h3d_core(const __grid_constant__ StepParams<T> p) {
+  const Core3<T, V> u(p);
+  if (!u.live) return;
+  const long long c = u.c;
+  T ex[V], ey[V], ez[V], ezu[V], exu[V], exa[V], eya[V], hx[V], hy[V], hz[V];
+  vld_ro<T, V>(p.ex + c, ex);
+  vld_ro<T, V>(p.ey + c, ey);
+  vld_ro<T, V>(p.ez + c, ez);
+  nb_vec<T, V>(p, p.ez, c, u.j, u.k, 1, 0, ezu);
+  nb_vec<T, V>(p, p.ex, c, u.j, u.k, 1, 0, exu);
+  nb_vec<T, V>(p, p.ex, c, u.j, u.k, 0, 1, exa);
+  nb_vec<T, V>(p, p.ey, c, u.j, u.k, 0, 1, eya);
+  const T ezr = nb_x<T, V>(p, p.ez, c, u.i0, 1), eyr = nb_x<T, V>(p, p.ey, c, u.i0, 1);
+  vld<T, V>(p.hx + c, hx);
+  vld<T, V>(p.hy + c, hy);
+  vld<T, V>(p.hz + c, hz);
+  if (__ldg(p.rowflag + (long long)u.k * p.ny + u.j)) return;
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    const T rz = q < V - 1 ? ez[q + 1] : ezr, ry = q < V - 1 ? ey[q + 1] : eyr;
+    const T curleyz = eya[q] - ey[q], curlezy = -ezu[q] + ez[q];
+    const T curlezx = rz - ez[q], curlexz = -exa[q] + ex[q];
+    const T curlexy = exu[q] - ex[q], curleyx = -ry + ey[q];
+    hx[q] = hx[q] + p.ku * (curleyz + curlezy);
+    hy[q] = hy[q] + p.ku * (curlezx + curlexz);
+    hz[q] = hz[q] + p.ku * (curlexy + curleyx);
+  }
+  vst<T, V>(p.hx + c, hx);
+  vst<T, V>(p.hy + c, hy);
+  vst<T, V>(p.hz + c, hz);
+}
+
+template <typename T>
+int launch_e3d(const StepParams<T> &p, int part, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+  if (part == K2D_CORE) {
+    if (p.ncore <= 0) return 0;
+    const int blocks = ((p.cw + 31) / 32) * ((p.ch + 7) / 8) * p.cd;
+    if (p.vec == VW) e3d_core<T, VW><<<blocks, 256, 0, s>>>(p);
+    else e3d_core<T, 1><<<blocks, 256, 0, s>>>(p);
+    return 1;
+  }
+  const int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
+  if (blocks <= 0) return 0;
+  e3d_kernel<T><<<blocks, 256, 0, s>>>(p);
+  return 1;
+}
+template <typename T>
+int launch_h3d(const StepParams<T> &p, int part, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+  if (part == K2D_CORE) {
+    if (p.ncore <= 0) return 0;
+    const int blocks = ((p.cw + 31) / 32) * ((p.ch + 7) / 8) * p.cd;
+    if (p.vec == VW) h3d_core<T, VW><<<blocks, 256, 0, s>>>(p);
+    else h3d_core<T, 1><<<blocks, 256, 0, s>>>(p);
+    return 1;
+  }
+  const int blocks = p.ntile_blocks + p.nslab_blocks;
+  if (blocks <= 0) return 0;
+  h3d_kernel<T><<<blocks, 256, 0, s>>>(p);
+  return 1;
+}
+
+template int launch_e3d<float>(const StepParams<float> &, int, void *);
+template int launch_e3d<double>(const StepParams<double> &, int, void *);
+template int launch_h3d<float>(const StepParams<float> &, int, void *);
+template int launch_h3d<double>(const StepParams<double> &, int, void *);
 
 }  // namespace fdtd
