@@ -173,8 +173,8 @@ struct fdtd_job {
   // 2D work split (core box + edge unit list) and the streams that run the
   // parts of a half step as parallel branches of the job's stream
   int vec = 1, cv0 = 0, cw = 0, cy0 = 0, ncore = 0, nedge = 0;
-  int ch = 0, cz0 = 0, cd = 0, ntiles = 0;  // 3D: core box and general-tile count
-  int *d_edge = nullptr, *d_tiles = nullptr;
+  int ch = 0, cz0 = 0, cd = 0;  // 3D: core box rows and planes
+  int *d_edge = nullptr;
   cudaStream_t side[2] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {};
 };
@@ -214,6 +214,10 @@ int alloc_dev(fdtd_job *J, void **p, size_t bytes) {
   J->dev_bytes += bytes;
   e = cudaMemsetAsync(*p, 0, bytes, J->stream);
   if (e != cudaSuccess) return set_err(FDTD_ECUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+  // the buffer is ready only in the job stream's order: wait for it (and its
+  // zeroing) before uploads on other streams or the host may touch it
+  e = cudaStreamSynchronize(J->stream);
+  if (e != cudaSuccess) return set_err(FDTD_ECUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
   return FDTD_OK;
 }
 
@@ -399,12 +403,15 @@ int split_2d(fdtd_job *J, const std::vector<uint8_t> &rf) {
 }
 
 // 3D work split.  Core units: whole V-cell x-vectors of the main range
-// outside the split-PML shell, in (y, z) rows without a source.  The general
-// launch takes every 32 x 8 x kKZ tile that holds any other cell.
+// outside the split-PML shell, in (y, z) rows without a source.  Every other
+// x-vector is listed for the edge blocks of the general launch.
 int split_3d(fdtd_job *J, const std::vector<uint8_t> &rf) {
   const int nx = J->nx, ny = J->ny, nz = J->nz;
   const int vw = J->esz == 4 ? 4 : 2;
   const int V = J->vec = (nx % vw == 0) ? vw : 1;
+  const int nvec = nx / V;
+  if ((long long)nvec * ny * nz > (long long)INT32_MAX)
+    return set_err(FDTD_ERANGE, "3D grid of %d x %d x %d cells is too large for 32-bit unit indices", nx, ny, nz);
   int lo[3], hi[3];
   for (int a = 0; a < 3; ++a) {
     lo[a] = std::max(J->g.main_lo[a], J->slo[a]);
@@ -417,28 +424,21 @@ int split_3d(fdtd_job *J, const std::vector<uint8_t> &rf) {
   J->ch = std::max(0, hi[1] - lo[1] + 1);
   J->cz0 = lo[2];
   J->cd = std::max(0, hi[2] - lo[2] + 1);
-  const long long ncore = (long long)J->cw * J->ch * J->cd;
-  if (ncore > (long long)INT32_MAX) return set_err(FDTD_ERANGE, "3D core box too large for 32-bit unit indices");
-  J->ncore = (int)ncore;
-  const int x0 = cv0 * V, x1 = cv1 * V, y0 = lo[1], y1 = lo[1] + J->ch, z0 = lo[2], z1 = lo[2] + J->cd;
-  const int tx = (nx + 31) / 32, ty = (ny + 7) / 8, tz = (nz + kKZ3 - 1) / kKZ3;
-  std::vector<int> tiles;
-  for (int c = 0; c < tz; ++c)
-    for (int b = 0; b < ty; ++b)
-      for (int a = 0; a < tx; ++a) {
-        const int i0 = a * 32, i1 = std::min(nx, i0 + 32), j0 = b * 8, j1 = std::min(ny, j0 + 8);
-        const int k0 = c * kKZ3, k1 = std::min(nz, k0 + kKZ3);
-        bool need = J->ncore == 0 || i0 < x0 || i1 > x1 || j0 < y0 || j1 > y1 || k0 < z0 || k1 > z1;
-        for (int k = k0; k < k1 && !need; ++k)
-          for (int j = j0; j < j1 && !need; ++j) need = rf[(size_t)k * ny + j] != 0;
-        if (need) tiles.push_back((c * ty + b) * tx + a);
-      }
-  J->ntiles = (int)tiles.size();
+  J->ncore = J->cw * J->ch * J->cd;
+  std::vector<int> edge;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j) {
+      const int row = k * ny + j;
+      const bool core_row = j >= J->cy0 && j < J->cy0 + J->ch && k >= J->cz0 && k < J->cz0 + J->cd && rf[row] == 0;
+      for (int v = 0; v < nvec; ++v)
+        if (!(core_row && v >= cv0 && v < cv1)) edge.push_back(row * nvec + v);
+    }
+  J->nedge = (int)edge.size();
   int rc;
-  if (!tiles.empty()) {
-    if ((rc = alloc_dev(J, (void **)&J->d_tiles, tiles.size() * sizeof(int)))) return rc;
-    CK(cudaMemcpy(J->d_tiles, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
-    J->h2d += tiles.size() * sizeof(int);
+  if (!edge.empty()) {
+    if ((rc = alloc_dev(J, (void **)&J->d_edge, edge.size() * sizeof(int)))) return rc;
+    CK(cudaMemcpy(J->d_edge, edge.data(), edge.size() * sizeof(int), cudaMemcpyHostToDevice));
+    J->h2d += edge.size() * sizeof(int);
   }
   return make_branches(J);
 }
@@ -846,9 +846,9 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.nedge = J->nedge;
     p.edge_units = J->d_edge;
   } else {
-    p.tiles_x = (J->nx + 31) / 32; p.tiles_y = (J->ny + 7) / 8; p.tiles_z = (J->nz + kKZ3 - 1) / kKZ3;
-    p.ntile_blocks = J->ntiles;
-    p.tile_list = J->d_tiles;
+    p.ntile_blocks = (J->nedge + 255) / 256;
+    p.nedge = J->nedge;
+    p.edge_units = J->d_edge;
     p.vec = J->vec;
     p.cv0 = J->cv0; p.cw = J->cw; p.cy0 = J->cy0; p.ch = J->ch; p.cz0 = J->cz0; p.cd = J->cd;
     p.ncore = J->ncore;
@@ -1764,7 +1764,7 @@ int fdtd_kernel_cells(const fdtd_job *J, int32_t kind, int64_t *cells) {
   int64_t c = 0;
   if (kind == FDTD_KERNEL_E || kind == FDTD_KERNEL_H) c = J->dim >= 2 ? (int64_t)J->ncore * J->vec : 0;
   else if (kind == FDTD_KERNEL_EDGE)
-    c = J->dim == 2 ? (int64_t)J->nedge * J->vec : J->dim == 3 ? (int64_t)J->ntiles * 32 * 8 * kKZ3 : 0;
+    c = J->dim >= 2 ? (int64_t)J->nedge * J->vec : 0;
   else if (kind == FDTD_KERNEL_ADE) c = J->dim == 2 ? J->nade : 0;
   else if (kind == FDTD_KERNEL_LINE1D) c = J->dim == 1 ? J->ncell : 0;
   else if (kind == FDTD_KERNEL_DFT) {

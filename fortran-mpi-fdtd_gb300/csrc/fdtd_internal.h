@@ -24,7 +24,6 @@ constexpr int kMaxMat = 256;
 constexpr int kMaxSrc = 8;
 constexpr int kMaxMon = 16;
 constexpr int kMaxProbe = 16;
-constexpr int kKZ3 = 16;         // 3D tiles: cells each thread marches along z
 constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
 
 enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3 };
@@ -128,7 +127,7 @@ struct StepParams {
   const T *sf1z[2], *sf2z[2], *sg1z[2], *sg2z[2];  // per side, len nz
   // work split of one launch
   int roles;               // ROLE_* bits
-  int tiles_x, tiles_y, tiles_z, ntile_blocks;
+  int ntile_blocks;        // edge blocks of the general launch (3D)
   int nslab_blocks, nade_blocks;
   // 2D work split: core units are vectors [cv0, cv0+cw) of rows cy0.. (ncore
   // units in all); every other unit (j*nx/V + vector) is listed in edge_units
@@ -136,9 +135,8 @@ struct StepParams {
   int nedge;
   const int *edge_units;
   // 3D: the core box is vectors [cv0, cv0+cw) x rows [cy0, cy0+ch) x planes
-  // [cz0, cz0+cd); the general launch takes its tiles from tile_list
+  // [cz0, cz0+cd); edge_units are then x-vectors (k*ny + j)*nx/V + vector
   int ch, cz0, cd;
-  const int *tile_list;
   // sampling fused into the H kernel
   int gather;              // 1: tile threads write the stage row / probes
   int nmon;

@@ -7,12 +7,10 @@
 //             thread, only the Yee update with the constant-dielectric
 //             material folded in.  Nearly all of a large grid.
 //   general : blockIdx selects the work:
-//     tile blocks : the 32 (x) x 8 (y) x kKZ (z) tiles, from a list, that
-//                 hold any non-core cell; each thread marches kKZ cells along
-//                 z with the previous (E) or next (H) plane in registers and
-//                 x neighbours by warp shuffle.  Main cells do the Yee update
-//                 and the sources; shell cells of the split-field PML do the
-//                 split update; core cells are left to the core launch.
+//     edge blocks : one x-vector per thread from a list of the units outside
+//                 the core box or in a source row: shell cells of the
+//                 split-field PML do the split update, main cells the Yee
+//                 update with their material and the sources.
 //     slab blocks : the reference's y-slab PML (3D/BERpmly_mod.f90:72-306),
 //                 one thread per slab cell and side, 12 split arrays, the
 //                 coupling rows read straight from the main arrays.
@@ -24,7 +22,6 @@
 
 namespace fdtd {
 
-constexpr int kKZ = kKZ3;
 
 // Ku/eps of a cell: the dominant material's coefficient is a parameter
 template <typename T>
@@ -66,137 +63,261 @@ struct F3 {
 };
 
 // a cell of the core box in a row without flags: updated by the core launch
-template <typename T>
-__device__ __forceinline__ bool in_core3(const StepParams<T> &p, int i, int j, int k) {
-  return p.ncore > 0 && i >= p.cv0 * p.vec && i < (p.cv0 + p.cw) * p.vec && j >= p.cy0 && j < p.cy0 + p.ch &&
-         k >= p.cz0 && k < p.cz0 + p.cd && !__ldg(p.rowflag + (long long)k * p.ny + j);
+// ---- core units: one x-vector of V interior cells per thread --------------
+// Block: 32 vectors along x by 8 rows along y, one z plane; blocks run x, y,
+// then z, so the plane below (E) or above (H) was read moments earlier and
+// its loads hit L2.
+template <typename T, int V>
+struct Core3 {
+  int j, k, i0;
+  long long c;
+  bool live;
+  __device__ __forceinline__ Core3(const StepParams<T> &p) {
+    const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
+    const int bx = (p.cw + 31) >> 5, by = (p.ch + 7) >> 3;
+    const int b = blockIdx.x, tx = b % bx, t2 = b / bx, ty = t2 % by, tz = t2 / by;
+    const int v = tx * 32 + lane, r = ty * 8 + wy;
+    live = v < p.cw && r < p.ch && tz < p.cd;
+    j = p.cy0 + r;
+    k = p.cz0 + tz;
+    i0 = (p.cv0 + v) * V;
+    c = ((long long)k * p.ny + j) * p.nx + i0;
+  }
+};
+
+// neighbour vector one row (dy = +-1) or one plane (dz = +-1) away, wrapped
+// on periodic axes and zero beyond open ones
+template <typename T, int V>
+__device__ __forceinline__ void nb_vec(const StepParams<T> &p, const T *a, long long c, int j, int k, int dy, int dz,
+                                       T (&v)[V]) {
+  const long long plane = (long long)p.nx * p.ny;
+  long long d = 0;
+  bool ok = true;
+  if (dy) {
+    const int jj = j + dy;
+    if (jj >= 0 && jj < p.ny) d = (long long)dy * p.nx;
+    else if (p.per[1]) d = (long long)(dy > 0 ? -(p.ny - 1) : (p.ny - 1)) * p.nx;
+    else ok = false;
+  } else {
+    const int kk = k + dz;
+    if (kk >= 0 && kk < p.nz) d = (long long)dz * plane;
+    else if (p.per[2]) d = (long long)(dz > 0 ? -(p.nz - 1) : (p.nz - 1)) * plane;
+    else ok = false;
+  }
+  if (ok) vld_ro<T, V>(a + c + d, v);
+  else {
+#pragma unroll
+    for (int q = 0; q < V; ++q) v[q] = T(0);
+  }
 }
 
-template <typename T>
-__device__ __forceinline__ void tile_e3(const StepParams<T> &p, int b, int n) {
-  const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
-  const int tx = b % p.tiles_x, t2 = b / p.tiles_x;
-  const int ty = t2 % p.tiles_y, tz = t2 / p.tiles_y;
-  const int i = tx * 32 + lane, j = ty * 8 + wy, k0 = tz * kKZ;
-  if (j >= p.ny || k0 >= p.nz) return;
-  const bool inx = i < p.nx;
-  F3<T> f(p);
-  T hx_km = inx ? f.lz(p.hx, i, j, k0 - 1) : T(0);
-  T hy_km = inx ? f.lz(p.hy, i, j, k0 - 1) : T(0);
-  const int k1 = min(k0 + kKZ, p.nz);
-  for (int k = k0; k < k1; ++k) {
-    const long long c = f.ix(i, j, k);
-    const T hxc = inx ? p.hx[c] : T(0);
-    const T hyc = inx ? p.hy[c] : T(0);
-    const T hzc = inx ? p.hz[c] : T(0);
-    T hzl = shfl_left(hzc, lane), hyl = shfl_left(hyc, lane);
-    if (lane == 0 && inx) { hzl = f.lx(p.hz, i - 1, j, k); hyl = f.lx(p.hy, i - 1, j, k); }
-    const T hxkm = hx_km, hykm = hy_km;
-    hx_km = hxc;
-    hy_km = hyc;
-    if (!inx || in_core3(p, i, j, k)) continue;
-    const T hzd = f.ly(p.hz, i, j - 1, k), hxd = f.ly(p.hx, i, j - 1, k);
-    const T curlhzy = hzc - hzd, curlhyz = -hyc + hykm;
-    const T curlhxz = hxc - hxkm, curlhzx = -hzc + hzl;
-    const T curlhyx = hyc - hyl, curlhxy = -hxc + hxd;
-    if (p.pml_mode == 2 && in_shell3(p, i, j, k)) {
-      if (p.roles & ROLE_PML) {
-        const T f1x = p.cf1[0][i], f2x = p.cf2[0][i], f1y = p.cf1[1][j], f2y = p.cf2[1][j];
-        const T f1z = p.cf1[2][k], f2z = p.cf2[2][k];
-        T exy = p.sp[0][c], eyz = p.sp[1][c], ezx = p.sp[2][c];
-        T exz, eyx, ezy;
-        if (kTwoParts<T>) { exz = p.sp[6][c]; eyx = p.sp[7][c]; ezy = p.sp[8][c]; }
-        else { exz = p.ex[c] - exy; eyx = p.ey[c] - eyz; ezy = p.ez[c] - ezx; }
-        exy = f1y * exy + f2y * curlhzy;
-        exz = f1z * exz + f2z * curlhyz;
-        eyz = f1z * eyz + f2z * curlhxz;
-        eyx = f1x * eyx + f2x * curlhzx;
-        ezx = f1x * ezx + f2x * curlhyx;
-        ezy = f1y * ezy + f2y * curlhxy;
-        p.sp[0][c] = exy; p.sp[1][c] = eyz; p.sp[2][c] = ezx;
-        if (kTwoParts<T>) { p.sp[6][c] = exz; p.sp[7][c] = eyx; p.sp[8][c] = ezy; }
-        p.ex[c] = exy + exz; p.ey[c] = eyz + eyx; p.ez[c] = ezx + ezy;
-      }
-      continue;
+// cell next to the vector along x (dx = -1: left of its first cell, +1:
+// right of its last), wrapped on a periodic axis, zero beyond an open one
+template <typename T, int V>
+__device__ __forceinline__ T nb_x(const StepParams<T> &p, const T *a, long long c, int i0, int dx) {
+  if (dx < 0) return i0 > 0 ? __ldg(a + c - 1) : (p.per[0] ? __ldg(a + c + p.nx - 1) : T(0));
+  return i0 + V < p.nx ? __ldg(a + c + V) : (p.per[0] ? __ldg(a + c + V - p.nx) : T(0));
+}
+
+// ---- edge units: x-vectors of V cells outside the core launch's box --------
+// (split-PML shell, the edges of the main range, rows with a source).  Every
+// value a unit needs is loaded before any store, then each cell takes the
+// split update (shell), the Yee update with material and source (main), or
+// is left alone.
+template <typename T, int V>
+struct Edge3 {
+  int i0, j, k;
+  long long c;
+  __device__ __forceinline__ Edge3(const StepParams<T> &p, int unit) {
+    const int nvec = p.nx / V;
+    const int row = unit / nvec;
+    i0 = (unit - row * nvec) * V;
+    j = row % p.ny;
+    k = row / p.ny;
+    c = (long long)row * p.nx + i0;
+  }
+};
+
+template <typename T, int V>
+__device__ __forceinline__ void edge_e3(const StepParams<T> &p, int unit, int n) {
+  const Edge3<T, V> u(p, unit);
+  const long long c = u.c;
+  const int i0 = u.i0, j = u.j, k = u.k;
+  const bool do_main = p.roles & ROLE_MAIN, do_pml = p.roles & ROLE_PML;
+  const bool split = p.pml_mode == 2;
+  const bool shell_yz = split && (j < p.slo[1] || j > p.shi[1] || k < p.slo[2] || k > p.shi[2]);
+  const bool pml = do_pml && split && (shell_yz || i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
+  const bool main_yz = j >= p.mlo[1] && j <= p.mhi[1] && k >= p.mlo[2] && k <= p.mhi[2];
+  T hx[V], hy[V], hz[V], hzd[V], hxd[V], hyb[V], hxb[V], ex[V], ey[V], ez[V];
+  uint8_t id[V];
+  vld_ro<T, V>(p.hx + c, hx);
+  vld_ro<T, V>(p.hy + c, hy);
+  vld_ro<T, V>(p.hz + c, hz);
+  nb_vec<T, V>(p, p.hz, c, j, k, -1, 0, hzd);
+  nb_vec<T, V>(p, p.hx, c, j, k, -1, 0, hxd);
+  nb_vec<T, V>(p, p.hy, c, j, k, 0, -1, hyb);
+  nb_vec<T, V>(p, p.hx, c, j, k, 0, -1, hxb);
+  const T hzl = nb_x<T, V>(p, p.hz, c, i0, -1), hyl = nb_x<T, V>(p, p.hy, c, i0, -1);
+  vld<T, V>(p.ex + c, ex);
+  vld<T, V>(p.ey + c, ey);
+  vld<T, V>(p.ez + c, ez);
+  vld_ids<V>(p.mat + c, id);
+  const int rf = __ldg(p.rowflag + (long long)k * p.ny + j);
+  // split parts Exy Eyz Ezx (and, in FP64, Exz Eyx Ezy) and the profiles
+  T s0[V], s1[V], s2[V], s6[V], s7[V], s8[V], f1x[V], f2x[V];
+  T f1y = T(0), f2y = T(0), f1z = T(0), f2z = T(0);
+  if (pml) {
+    vld<T, V>(p.sp[0] + c, s0);
+    vld<T, V>(p.sp[1] + c, s1);
+    vld<T, V>(p.sp[2] + c, s2);
+    if (kTwoParts<T>) {
+      vld<T, V>(p.sp[6] + c, s6);
+      vld<T, V>(p.sp[7] + c, s7);
+      vld<T, V>(p.sp[8] + c, s8);
     }
-    if ((p.roles & ROLE_MAIN) && in_main3(p, i, j, k)) {
-      const MatCoef<T> mc = p.mc[p.mat[c]];
-      if (mc.kind == MK_DIEL) {
-        T ex = p.ex[c] + mc.ca * (curlhzy + curlhyz);
-        T ey = p.ey[c] + mc.ca * (curlhxz + curlhzx);
-        T ez = p.ez[c] + mc.ca * (curlhyx + curlhxy);
-        if (p.nsrc) {
-          const T sx = src_sum<T>(p, n, 0, i, j, k), sy = src_sum<T>(p, n, 1, i, j, k), sz = src_sum<T>(p, n, 2, i, j, k);
-          if (sx != T(0)) ex += mc.cs * sx;
-          if (sy != T(0)) ey += mc.cs * sy;
-          if (sz != T(0)) ez += mc.cs * sz;
-        }
-        p.ex[c] = ex; p.ey[c] = ey; p.ez[c] = ez;
+    vld_ro<T, V>(p.cf1[0] + i0, f1x);
+    vld_ro<T, V>(p.cf2[0] + i0, f2x);
+    f1y = __ldg(p.cf1[1] + j); f2y = __ldg(p.cf2[1] + j);
+    f1z = __ldg(p.cf1[2] + k); f2z = __ldg(p.cf2[2] + k);
+  }
+  bool wrote = false;
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    const int i = i0 + q;
+    const T curlhzy = hz[q] - hzd[q], curlhyz = -hy[q] + hyb[q];
+    const T curlhxz = hx[q] - hxb[q], curlhzx = -hz[q] + (q ? hz[q - 1] : hzl);
+    const T curlhyx = hy[q] - (q ? hy[q - 1] : hyl), curlhxy = -hx[q] + hxd[q];
+    if (split && (shell_yz || i < p.slo[0] || i > p.shi[0])) {
+      if (do_pml) {  // 3D/BERpmly_mod.f90:117-159 on every face
+        const T exz = kTwoParts<T> ? s6[q] : ex[q] - s0[q];
+        const T eyx = kTwoParts<T> ? s7[q] : ey[q] - s1[q];
+        const T ezy = kTwoParts<T> ? s8[q] : ez[q] - s2[q];
+        const T nexy = f1y * s0[q] + f2y * curlhzy;
+        const T nexz = f1z * exz + f2z * curlhyz;
+        const T neyz = f1z * s1[q] + f2z * curlhxz;
+        const T neyx = f1x[q] * eyx + f2x[q] * curlhzx;
+        const T nezx = f1x[q] * s2[q] + f2x[q] * curlhyx;
+        const T nezy = f1y * ezy + f2y * curlhxy;
+        s0[q] = nexy; s1[q] = neyz; s2[q] = nezx;
+        s6[q] = nexz; s7[q] = neyx; s8[q] = nezy;
+        ex[q] = nexy + nexz; ey[q] = neyz + neyx; ez[q] = nezx + nezy;
+        wrote = true;
       }
+    } else if (do_main && main_yz && i >= p.mlo[0] && i <= p.mhi[0]) {
+      const T ca = coef_ca3(p, id[q]);
+      ex[q] = ex[q] + ca * (curlhzy + curlhyz);
+      ey[q] = ey[q] + ca * (curlhxz + curlhzx);
+      ez[q] = ez[q] + ca * (curlhyx + curlhxy);
+      if (rf & ROW_SRC) {
+        const T cs = __ldg(p.mcs + id[q]);
+        const T sx = src_sum<T>(p, n, 0, i, j, k), sy = src_sum<T>(p, n, 1, i, j, k), sz = src_sum<T>(p, n, 2, i, j, k);
+        if (sx != T(0)) ex[q] += cs * sx;
+        if (sy != T(0)) ey[q] += cs * sy;
+        if (sz != T(0)) ez[q] += cs * sz;
+      }
+      wrote = true;
+    }
+  }
+  if (wrote) {  // cells not updated store back what they read; ADE cells are skipped
+    st_guard3<T, V>(p.ex + c, ex, id);
+    st_guard3<T, V>(p.ey + c, ey, id);
+    st_guard3<T, V>(p.ez + c, ez, id);
+  }
+  if (pml) {
+    vst<T, V>(p.sp[0] + c, s0);
+    vst<T, V>(p.sp[1] + c, s1);
+    vst<T, V>(p.sp[2] + c, s2);
+    if (kTwoParts<T>) {
+      vst<T, V>(p.sp[6] + c, s6);
+      vst<T, V>(p.sp[7] + c, s7);
+      vst<T, V>(p.sp[8] + c, s8);
     }
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void tile_h3(const StepParams<T> &p, int b, int n) {
-  const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
-  const int tx = b % p.tiles_x, t2 = b / p.tiles_x;
-  const int ty = t2 % p.tiles_y, tz = t2 / p.tiles_y;
-  const int i = tx * 32 + lane, j = ty * 8 + wy, k0 = tz * kKZ;
-  if (j >= p.ny || k0 >= p.nz) return;
-  const bool inx = i < p.nx;
-  F3<T> f(p);
-  T exc = inx ? p.ex[f.ix(i, j, k0)] : T(0);
-  T eyc = inx ? p.ey[f.ix(i, j, k0)] : T(0);
-  const int k1 = min(k0 + kKZ, p.nz);
-  for (int k = k0; k < k1; ++k) {
-    const long long c = f.ix(i, j, k);
-    const T ezc = inx ? p.ez[c] : T(0);
-    T ezr = shfl_right(ezc, lane), eyr = shfl_right(eyc, lane);
-    if ((lane == 31 || i + 1 >= p.nx) && inx) { ezr = f.lx(p.ez, i + 1, j, k); eyr = f.lx(p.ey, i + 1, j, k); }
-    const T exkp = inx ? f.lz(p.ex, i, j, k + 1) : T(0);
-    const T eykp = inx ? f.lz(p.ey, i, j, k + 1) : T(0);
-    const T ex0 = exc, ey0 = eyc;
-    exc = exkp;
-    eyc = eykp;
-    if (!inx || in_core3(p, i, j, k)) continue;  // 3D samples in the gather kernel
-    const T ezu = f.ly(p.ez, i, j + 1, k), exu = f.ly(p.ex, i, j + 1, k);
-    const T curleyz = eykp - ey0, curlezy = -ezu + ezc;
-    const T curlezx = ezr - ezc, curlexz = -exkp + ex0;
-    const T curlexy = exu - ex0, curleyx = -eyr + ey0;
-    T hx, hy, hz;
-    bool wrote = false;
-    if (p.pml_mode == 2 && in_shell3(p, i, j, k)) {
-      if (p.roles & ROLE_PML) {
-        const T g1x = p.cg1[0][i], g2x = p.cg2[0][i], g1y = p.cg1[1][j], g2y = p.cg2[1][j];
-        const T g1z = p.cg1[2][k], g2z = p.cg2[2][k];
-        T hxy = p.sp[3][c], hyz = p.sp[4][c], hzx = p.sp[5][c];
-        T hxz, hyx, hzy;
-        if (kTwoParts<T>) { hxz = p.sp[9][c]; hyx = p.sp[10][c]; hzy = p.sp[11][c]; }
-        else { hxz = p.hx[c] - hxy; hyx = p.hy[c] - hyz; hzy = p.hz[c] - hzx; }
-        hxy = g1y * hxy + g2y * curlezy;
-        hxz = g1z * hxz + g2z * curleyz;
-        hyz = g1z * hyz + g2z * curlexz;
-        hyx = g1x * hyx + g2x * curlezx;
-        hzx = g1x * hzx + g2x * curleyx;
-        hzy = g1y * hzy + g2y * curlexy;
-        p.sp[3][c] = hxy; p.sp[4][c] = hyz; p.sp[5][c] = hzx;
-        if (kTwoParts<T>) { p.sp[9][c] = hxz; p.sp[10][c] = hyx; p.sp[11][c] = hzy; }
-        hx = hxy + hxz; hy = hyz + hyx; hz = hzx + hzy;
-        p.hx[c] = hx; p.hy[c] = hy; p.hz[c] = hz;
+template <typename T, int V>
+__device__ __forceinline__ void edge_h3(const StepParams<T> &p, int unit) {
+  const Edge3<T, V> u(p, unit);
+  const long long c = u.c;
+  const int i0 = u.i0, j = u.j, k = u.k;
+  const bool do_main = p.roles & ROLE_MAIN, do_pml = p.roles & ROLE_PML;
+  const bool split = p.pml_mode == 2;
+  const bool shell_yz = split && (j < p.slo[1] || j > p.shi[1] || k < p.slo[2] || k > p.shi[2]);
+  const bool pml = do_pml && split && (shell_yz || i0 < p.slo[0] || i0 + V - 1 > p.shi[0]);
+  const bool main_yz = j >= p.mlo[1] && j <= p.mhi[1] && k >= p.mlo[2] && k <= p.mhi[2];
+  T ex[V], ey[V], ez[V], ezu[V], exu[V], exa[V], eya[V], hx[V], hy[V], hz[V];
+  vld_ro<T, V>(p.ex + c, ex);
+  vld_ro<T, V>(p.ey + c, ey);
+  vld_ro<T, V>(p.ez + c, ez);
+  nb_vec<T, V>(p, p.ez, c, j, k, 1, 0, ezu);
+  nb_vec<T, V>(p, p.ex, c, j, k, 1, 0, exu);
+  nb_vec<T, V>(p, p.ex, c, j, k, 0, 1, exa);
+  nb_vec<T, V>(p, p.ey, c, j, k, 0, 1, eya);
+  const T ezr = nb_x<T, V>(p, p.ez, c, i0, 1), eyr = nb_x<T, V>(p, p.ey, c, i0, 1);
+  vld<T, V>(p.hx + c, hx);
+  vld<T, V>(p.hy + c, hy);
+  vld<T, V>(p.hz + c, hz);
+  // split parts Hxy Hyz Hzx (and, in FP64, Hxz Hyx Hzy) and the profiles
+  T s3[V], s4[V], s5[V], s9[V], s10[V], s11[V], g1x[V], g2x[V];
+  T g1y = T(0), g2y = T(0), g1z = T(0), g2z = T(0);
+  if (pml) {
+    vld<T, V>(p.sp[3] + c, s3);
+    vld<T, V>(p.sp[4] + c, s4);
+    vld<T, V>(p.sp[5] + c, s5);
+    if (kTwoParts<T>) {
+      vld<T, V>(p.sp[9] + c, s9);
+      vld<T, V>(p.sp[10] + c, s10);
+      vld<T, V>(p.sp[11] + c, s11);
+    }
+    vld_ro<T, V>(p.cg1[0] + i0, g1x);
+    vld_ro<T, V>(p.cg2[0] + i0, g2x);
+    g1y = __ldg(p.cg1[1] + j); g2y = __ldg(p.cg2[1] + j);
+    g1z = __ldg(p.cg1[2] + k); g2z = __ldg(p.cg2[2] + k);
+  }
+  bool wrote = false;
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    const int i = i0 + q;
+    const T rz = q < V - 1 ? ez[q + 1] : ezr, ry = q < V - 1 ? ey[q + 1] : eyr;
+    const T curleyz = eya[q] - ey[q], curlezy = -ezu[q] + ez[q];
+    const T curlezx = rz - ez[q], curlexz = -exa[q] + ex[q];
+    const T curlexy = exu[q] - ex[q], curleyx = -ry + ey[q];
+    if (split && (shell_yz || i < p.slo[0] || i > p.shi[0])) {
+      if (do_pml) {  // 3D/BERpmly_mod.f90:161-195 on every face
+        const T hxz = kTwoParts<T> ? s9[q] : hx[q] - s3[q];
+        const T hyx = kTwoParts<T> ? s10[q] : hy[q] - s4[q];
+        const T hzy = kTwoParts<T> ? s11[q] : hz[q] - s5[q];
+        const T nhxy = g1y * s3[q] + g2y * curlezy;
+        const T nhxz = g1z * hxz + g2z * curleyz;
+        const T nhyz = g1z * s4[q] + g2z * curlexz;
+        const T nhyx = g1x[q] * hyx + g2x[q] * curlezx;
+        const T nhzx = g1x[q] * s5[q] + g2x[q] * curleyx;
+        const T nhzy = g1y * hzy + g2y * curlexy;
+        s3[q] = nhxy; s4[q] = nhyz; s5[q] = nhzx;
+        s9[q] = nhxz; s10[q] = nhyx; s11[q] = nhzy;
+        hx[q] = nhxy + nhxz; hy[q] = nhyz + nhyx; hz[q] = nhzx + nhzy;
         wrote = true;
       }
-    } else if ((p.roles & ROLE_MAIN) && in_main3(p, i, j, k)) {
-      hx = p.hx[c] + p.ku * (curleyz + curlezy);
-      hy = p.hy[c] + p.ku * (curlezx + curlexz);
-      hz = p.hz[c] + p.ku * (curlexy + curleyx);
-      p.hx[c] = hx; p.hy[c] = hy; p.hz[c] = hz;
+    } else if (do_main && main_yz && i >= p.mlo[0] && i <= p.mhi[0]) {
+      hx[q] = hx[q] + p.ku * (curleyz + curlezy);
+      hy[q] = hy[q] + p.ku * (curlezx + curlexz);
+      hz[q] = hz[q] + p.ku * (curlexy + curleyx);
       wrote = true;
     }
-    if (p.gather) {
-      if (!wrote) { hx = p.hx[c]; hy = p.hy[c]; hz = p.hz[c]; }
-      const T vals[6] = {ex0, ey0, ezc, hx, hy, hz};
-      gather_cell<T>(p, n, i, j, k, vals);
+  }
+  if (wrote) {
+    vst<T, V>(p.hx + c, hx);
+    vst<T, V>(p.hy + c, hy);
+    vst<T, V>(p.hz + c, hz);
+  }
+  if (pml) {
+    vst<T, V>(p.sp[3] + c, s3);
+    vst<T, V>(p.sp[4] + c, s4);
+    vst<T, V>(p.sp[5] + c, s5);
+    if (kTwoParts<T>) {
+      vst<T, V>(p.sp[9] + c, s9);
+      vst<T, V>(p.sp[10] + c, s10);
+      vst<T, V>(p.sp[11] + c, s11);
     }
   }
 }
@@ -336,12 +457,15 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
   p.ez[cell] = ade_update<T>(p, a, s, 2, iz_, p.ez[cell]);
 }
 
-template <typename T>
+// general launch: blockIdx selects edge units, reference slab cells, then
+// dispersive cells
+template <typename T, int V>
 __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepParams<T> p) {
   const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
-    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_e3<T>(p, p.tile_list ? __ldg(p.tile_list + b) : b, n);
+    const int t = b * 256 + threadIdx.x;
+    if (t < p.nedge && (p.roles & (ROLE_MAIN | ROLE_PML))) edge_e3<T, V>(p, __ldg(p.edge_units + t), n);
     return;
   }
   b -= p.ntile_blocks;
@@ -356,72 +480,16 @@ __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepPa
   }
 }
 
-template <typename T>
+template <typename T, int V>
 __global__ void __launch_bounds__(256) h3d_kernel(const __grid_constant__ StepParams<T> p) {
-  const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
-    if (p.roles & (ROLE_MAIN | ROLE_PML)) tile_h3<T>(p, p.tile_list ? __ldg(p.tile_list + b) : b, n);
+    const int t = b * 256 + threadIdx.x;
+    if (t < p.nedge && (p.roles & (ROLE_MAIN | ROLE_PML))) edge_h3<T, V>(p, __ldg(p.edge_units + t));
     return;
   }
   b -= p.ntile_blocks;
   if (b < p.nslab_blocks && (p.roles & ROLE_PML)) slab_h3<T>(p, b * 256 + threadIdx.x);
-}
-
-// ---- core units: one x-vector of V interior cells per thread --------------
-// Block: 32 vectors along x by 8 rows along y, one z plane; blocks run x, y,
-// then z, so the plane below (E) or above (H) was read moments earlier and
-// its loads hit L2.
-template <typename T, int V>
-struct Core3 {
-  int j, k, i0;
-  long long c;
-  bool live;
-  __device__ __forceinline__ Core3(const StepParams<T> &p) {
-    const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
-    const int bx = (p.cw + 31) >> 5, by = (p.ch + 7) >> 3;
-    const int b = blockIdx.x, tx = b % bx, t2 = b / bx, ty = t2 % by, tz = t2 / by;
-    const int v = tx * 32 + lane, r = ty * 8 + wy;
-    live = v < p.cw && r < p.ch && tz < p.cd;
-    j = p.cy0 + r;
-    k = p.cz0 + tz;
-    i0 = (p.cv0 + v) * V;
-    c = ((long long)k * p.ny + j) * p.nx + i0;
-  }
-};
-
-// neighbour vector one row (dy = +-1) or one plane (dz = +-1) away, wrapped
-// on periodic axes and zero beyond open ones
-template <typename T, int V>
-__device__ __forceinline__ void nb_vec(const StepParams<T> &p, const T *a, long long c, int j, int k, int dy, int dz,
-                                       T (&v)[V]) {
-  const long long plane = (long long)p.nx * p.ny;
-  long long d = 0;
-  bool ok = true;
-  if (dy) {
-    const int jj = j + dy;
-    if (jj >= 0 && jj < p.ny) d = (long long)dy * p.nx;
-    else if (p.per[1]) d = (long long)(dy > 0 ? -(p.ny - 1) : (p.ny - 1)) * p.nx;
-    else ok = false;
-  } else {
-    const int kk = k + dz;
-    if (kk >= 0 && kk < p.nz) d = (long long)dz * plane;
-    else if (p.per[2]) d = (long long)(dz > 0 ? -(p.nz - 1) : (p.nz - 1)) * plane;
-    else ok = false;
-  }
-  if (ok) vld_ro<T, V>(a + c + d, v);
-  else {
-#pragma unroll
-    for (int q = 0; q < V; ++q) v[q] = T(0);
-  }
-}
-
-// cell next to the vector along x (dx = -1: left of its first cell, +1:
-// right of its last), wrapped on a periodic axis, zero beyond an open one
-template <typename T, int V>
-__device__ __forceinline__ T nb_x(const StepParams<T> &p, const T *a, long long c, int i0, int dx) {
-  if (dx < 0) return i0 > 0 ? __ldg(a + c - 1) : (p.per[0] ? __ldg(a + c + p.nx - 1) : T(0));
-  return i0 + V < p.nx ? __ldg(a + c + V) : (p.per[0] ? __ldg(a + c + V - p.nx) : T(0));
 }
 
 template <typename T, int V>
@@ -514,7 +582,8 @@ int launch_e3d(const StepParams<T> &p, int part, void *stream) {
   }
   const int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
   if (blocks <= 0) return 0;
-  e3d_kernel<T><<<blocks, 256, 0, s>>>(p);
+  if (p.vec == VW) e3d_kernel<T, VW><<<blocks, 256, 0, s>>>(p);
+  else e3d_kernel<T, 1><<<blocks, 256, 0, s>>>(p);
   return 1;
 }
 template <typename T>
@@ -530,7 +599,8 @@ int launch_h3d(const StepParams<T> &p, int part, void *stream) {
   }
   const int blocks = p.ntile_blocks + p.nslab_blocks;
   if (blocks <= 0) return 0;
-  h3d_kernel<T><<<blocks, 256, 0, s>>>(p);
+  if (p.vec == VW) h3d_kernel<T, VW><<<blocks, 256, 0, s>>>(p);
+  else h3d_kernel<T, 1><<<blocks, 256, 0, s>>>(p);
   return 1;
 }
 
