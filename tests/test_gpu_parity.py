@@ -209,3 +209,23 @@ def test_1d_gold_slab_vs_oracle(gpu, oracle_lib, prec):
     O.step(1, steps)
     err = _dft_err(J, O, 3)
     assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+def test_3d_graphene_sheet_vs_oracle(gpu, oracle_lib, prec):
+    """The graphene configuration (Drude sheet from E_F, Kerr and Raman) on a
+    laterally periodic 8 x 8 column of the 384-cell stack: the same physics
+    per cell as the full 256 x 256 plane, which the problem's lateral
+    periodicity makes uniform."""
+    spec, meta = problems.config_3d_graphene(precision=prec, nxy=8, nz=384, nfreq=32)
+    steps = 3000
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64))
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, 1)
+    if prec == abi.F64:
+        assert err <= TOL64
+        check_state(J, O, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ))
+    else:
+        assert err <= TOL32_DFT
