@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the 3D, graphene and 1D runs")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs in the serving run (0: none)")
     ap.add_argument("--serve-rate", type=float, default=16.0, help="Poisson arrival rate, jobs/s")
     return ap.parse_args()
@@ -149,6 +150,52 @@ class Clocks:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def config_runs(stream):
+    """The other named configurations, each timed over a short run after a
+    warm-up (CUDA events on the bench stream): Mcell-updates/s and the step's
+    ideal bytes (each field read and written once, plus the material id:
+    12w+1 per cell in 3D, 4w+1 in 1D) over the measured HBM peak."""
+    import torch
+    from fdtd_gpu import abi, problems
+    from fdtd_gpu.job import Job
+    peak, _ = measured_peaks()
+
+    def timed(spec, warm, k, per_cell):
+        J = Job(spec)
+        J.set_stream(stream.cuda_stream)
+        J.step(1, warm)
+        J.sync()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        J.step(warm + 1, k)
+        J.sync()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        J.close()
+        mc = spec.cells() * k / (ms / 1e3) / 1e6
+        w = 4 if spec.precision == abi.F32 else 8
+        return {"mcell_updates_per_s": mc, "ms_per_step": ms / k, "timed_steps": k,
+                "step_bytes_frac_of_hbm": mc * 1e6 * per_cell(w) / (peak * 1e9)}
+
+    out = {}
+    s32, _ = problems.config_3d_sphere(precision=abi.F32)
+    s64, _ = problems.config_3d_sphere(precision=abi.F64)
+    r32, r64 = timed(s32, 64, 256, lambda w: 12 * w + 1), timed(s64, 32, 96, lambda w: 12 * w + 1)
+    out["3d_sphere_512^3_splitpml16_64freq"] = {"fp32": r32, "fp64_plain": r64,
+                                               "fp32_over_fp64": r32["mcell_updates_per_s"] / r64["mcell_updates_per_s"]}
+    g32, _ = problems.config_3d_graphene(precision=abi.F32)
+    out["3d_graphene_256x256x384_pmlz10_128freq"] = {"fp32": timed(g32, 64, 512, lambda w: 12 * w + 1)}
+    o32, _ = problems.config_1d_gold(precision=abi.F32)
+    o64, _ = problems.config_1d_gold(precision=abi.F64)
+    l32, l64 = timed(o32, 2000, 18000, lambda w: 4 * w + 1), timed(o64, 2000, 18000, lambda w: 4 * w + 1)
+    for r in (l32, l64):
+        r["steps_per_s"] = 1e3 / r["ms_per_step"]
+        r["note"] = "4000 cells: one persistent block, latency-bound; the roofline does not apply"
+    out["1d_gold_slab_4000"] = {"fp32": l32, "fp64_plain": l64}
+    return out
 
 
 def serving_run(njobs, rate):
@@ -395,6 +442,8 @@ def main():
         "kernel_ms_fp64": {k: {"launches": v[0], "ms": v[1], "cells": v[2]} for k, v in kt64.items()},
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_configs:
+        out["configs"] = config_runs(stream)
     if rank == 0 and args.serve_jobs > 0:
         out["serving"] = serving_run(args.serve_jobs, args.serve_rate)
     if rank == 0 and not args.no_cpu:
