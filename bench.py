@@ -60,6 +60,24 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(x, device, world):
+    """The largest x over all ranks: a replicated job's time is its slowest
+    replica's."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_mcells(world, cells, steps, seconds):
+    """Whole-job Mcell-updates/s: every replica updates `cells` cells for
+    `steps` time steps in `seconds` (the slowest replica's time)."""
+    return world * cells * steps / seconds / 1e6
+
+
 def workload(n, nt, precision):
     from fdtd_gpu import problems
     spec, meta = problems.config_2d_tmz(precision=precision, n=n, steps=nt)
@@ -286,8 +304,10 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": workload_name(args.n, per_step),
-                                            "note": f"each bench step = {per_step} time steps of the workload"},
+            "data": "synthetic", "config": {"workload": workload_name(args.n, args.nt),
+                                            "note": f"each bench step = a sample of {per_step} time steps of "
+                                                    f"the workload, from a state already {args.warmup * per_step} "
+                                                    f"steps in"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
                              "sample": f"FP64 oracle (the reference's algorithm restated in C; the Fortran/MPI "
                                        f"reference needs gfortran+MPI, absent on this box), {per_step} time steps "
@@ -365,17 +385,14 @@ def main():
     # ---- FP32 (headline) ----
     spec32, meta, jobs32, ms32, launches, kt32, clocks = timed_jobs(abi.F32, args.steps, args.warmup)
     t_step = max(ms32) if False else sum(ms32) / len(ms32)
-    if world > 1:
-        t = torch.tensor([t_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item())
+    t_step = max_over_ranks(t_step, dev, world)
     cells = spec32.cells()
-    value = world * cells * args.nt / (t_step / 1e3) / 1e6
+    value = aggregate_mcells(world, cells, args.nt, t_step / 1e3)
 
     # ---- FP64 plain ----
     spec64, _, jobs64, ms64, _, kt64, _ = timed_jobs(abi.F64, args.fp64_steps, 1)
-    t64 = sum(ms64) / len(ms64)
-    value64 = world * cells * args.nt / (t64 / 1e3) / 1e6
+    t64 = max_over_ranks(sum(ms64) / len(ms64), dev, world)
+    value64 = aggregate_mcells(world, cells, args.nt, t64 / 1e3)
 
     # ---- DFT error FP32 vs FP64 (same job, same steps) ----
     num = den = 0.0
@@ -419,7 +436,7 @@ def main():
         t_e2e.append(time.perf_counter() - t0)
         h2d, d2h = J.transfer_bytes()
         J.close()
-    e2e_value = world * cells * args.nt / (sum(t_e2e) / len(t_e2e)) / 1e6
+    e2e_value = aggregate_mcells(world, cells, args.nt, max_over_ranks(sum(t_e2e) / len(t_e2e), dev, world))
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
