@@ -60,12 +60,12 @@ def test_reference_arm_other_ranks_exit_without_work():
 
 def test_reference_arm_line_on_rank0():
     import json
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "128",
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "512",
                         "--steps", "2", "--warmup", "1"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT and line["higher_is_better"] is True
-    assert line["config"]["workload"] == bench.workload_name(128, 10000)
+    assert line["config"]["workload"] == bench.workload_name(512, 10000)
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0
