@@ -492,12 +492,39 @@ int commit_impl(fdtd_job *J) {
   }
   std::vector<uint8_t> mat((size_t)N, 0);
   for (size_t m = 0; m < J->mats.size(); ++m) {
+    const MatRec &R = J->mats[m];
+    if (R.region.kind == FDTD_REGION_SPHERES) {
+      // a union of spheres: each sphere over its own bounding box, with the
+      // distance test of inside()
+      const int n3[3] = {nx, ny, nz};
+      for (int q = 0; q < R.region.count; ++q) {
+        const double *c = R.centers.data() + 4 * q;
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+          if (a == 2 && J->dim < 3) { lo[2] = 0; hi[2] = n3[2] - 1; continue; }
+          lo[a] = std::max(0, (int)std::floor(c[a] - c[3] - 1.0));
+          hi[a] = std::min(n3[a] - 1, (int)std::ceil(c[a] + c[3] + 1.0));
+        }
+        for (int k = lo[2]; k <= hi[2]; ++k)
+          for (int j = lo[1]; j <= hi[1]; ++j)
+            for (int i = lo[0]; i <= hi[0]; ++i) {
+              const double dx = i + 0.5 - c[0], dy = j + 0.5 - c[1];
+              double d2 = dx * dx + dy * dy;
+              if (J->dim == 3) {
+                const double dz = k + 0.5 - c[2];
+                d2 += dz * dz;
+              }
+              if (d2 <= c[3] * c[3]) mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = (uint8_t)mid[m];
+            }
+      }
+      continue;
+    }
     int lo[3], hi[3];
-    region_bounds(J, J->mats[m], lo, hi);
+    region_bounds(J, R, lo, hi);
     for (int k = lo[2]; k <= hi[2]; ++k)
       for (int j = lo[1]; j <= hi[1]; ++j)
         for (int i = lo[0]; i <= hi[0]; ++i)
-          if (inside(J, J->mats[m], i, j, k)) mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = (uint8_t)mid[m];
+          if (inside(J, R, i, j, k)) mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = (uint8_t)mid[m];
   }
   std::vector<MatCoef<T>> mc(kMaxMat);
   std::vector<AdeCoef<T>> ac;
@@ -1352,6 +1379,215 @@ static int set_field_impl(fdtd_job *J, int comp, const double *host) {
   CK(cudaMemcpyAsync(J->F[comp], tmp.data(), (size_t)J->ncell * sizeof(T), cudaMemcpyHostToDevice, J->stream));
   CK(cudaStreamSynchronize(J->stream));
   J->h2d += (uint64_t)J->ncell * sizeof(T);
+  return FDTD_OK;
+}
+
+// ---- packs of small 2D jobs ----------------------------------------------
+// A pack advances several committed 2D jobs of one precision, layout and
+// vector width together: each part of each half step is one launch over all
+// the jobs' units (k2d.cu, *_pk kernels), each job's parameters coming from a
+// device table with one copy per ring slot.  One ring of kStageSteps steps,
+// with every job's DFT fold and the advance of every job's step base, is
+// captured as a CUDA graph.  The kernels and their order per job are those of
+// the job's own ring, so a job's results do not depend on its pack.
+__global__ void pack_advance_kernel(int *n0, int njobs, int k) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < njobs) n0[q] += k;
+}
+
+struct fdtd::Pack {
+  std::vector<fdtd_job *> jobs;
+  int layout = 0, vec = 1;
+  bool f64 = false;
+  cudaStream_t stream = nullptr, side[2] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {};
+  void *d_tab = nullptr;  // [2 halves][kStageSteps slots][jobs] StepParams
+  int *d_n0 = nullptr;    // first step of each job's current ring
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int kernels_per_ring = 0;
+};
+
+namespace {
+
+template <typename T>
+int pack_capture(fdtd::Pack *P) {
+  const int nj = (int)P->jobs.size();
+  std::vector<StepParams<T>> tab((size_t)2 * kStageSteps * nj);
+  for (int s = 0; s < kStageSteps; ++s)
+    for (int q = 0; q < nj; ++q) {
+      fdtd_job *J = P->jobs[q];
+      StepParams<T> &e = tab[(size_t)s * nj + q];
+      fill_common<T>(J, e);
+      set_sources<T>(J, e);
+      e.roles = ROLE_MAIN | ROLE_PML | ROLE_ADE;
+      e.slot = s;
+      e.d_base = P->d_n0 + q;
+      StepParams<T> &h = tab[((size_t)kStageSteps + s) * nj + q];
+      fill_common<T>(J, h);
+      h.roles = ROLE_MAIN | ROLE_PML;
+      h.gather = 1;
+      h.slot = s;
+      h.d_base = P->d_n0 + q;
+    }
+  CK(cudaMallocAsync(&P->d_tab, tab.size() * sizeof(StepParams<T>), P->stream));
+  CK(cudaMemcpyAsync(P->d_tab, tab.data(), tab.size() * sizeof(StepParams<T>), cudaMemcpyHostToDevice, P->stream));
+  CK(cudaStreamSynchronize(P->stream));
+  // block ranges of each job in the five launches of a step
+  PackLaunch<T> L[2][3];
+  for (int h = 0; h < 2; ++h)
+    for (int part = 0; part < 3; ++part) {
+      PackLaunch<T> &a = L[h][part];
+      memset(&a, 0, sizeof a);
+      a.njobs = nj;
+      int b = 0;
+      for (int q = 0; q < nj; ++q) {
+        const fdtd_job *J = P->jobs[q];
+        const long long units = part == K2D_CORE ? J->ncore : part == K2D_EDGE ? J->nedge : (h == 0 ? J->nade : 0);
+        a.bstart[q] = b;
+        b += (int)((units + 255) / 256);
+      }
+      a.bstart[nj] = b;
+    }
+  const StepParams<T> *base = (const StepParams<T> *)P->d_tab;
+  int kernels = 0;
+  CK(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t bad = cudaSuccess;
+  for (int s = 0; s < kStageSteps && bad == cudaSuccess; ++s)
+    for (int h = 0; h < 2 && bad == cudaSuccess; ++h) {
+      int use[3], nuse = 0;
+      for (int part = 0; part < (h == 0 ? 3 : 2); ++part)
+        if (L[h][part].bstart[nj] > 0) use[nuse++] = part;
+      cudaStream_t st[3] = {P->stream, P->stream, P->stream};
+      if (nuse > 1) {
+        bad = cudaEventRecord(P->ev_fork, P->stream);
+        for (int b = 1; b < nuse && bad == cudaSuccess; ++b) {
+          st[b] = P->side[b - 1];
+          bad = cudaStreamWaitEvent(st[b], P->ev_fork, 0);
+        }
+      }
+      for (int b = 0; b < nuse && bad == cudaSuccess; ++b) {
+        PackLaunch<T> a = L[h][use[b]];
+        a.tab = base + ((size_t)h * kStageSteps + s) * nj;
+        kernels += launch_pack2d<T>(a, P->layout, P->vec, h == 0, use[b], st[b]);
+      }
+      for (int b = 1; b < nuse && bad == cudaSuccess; ++b) {
+        bad = cudaEventRecord(P->ev_join[b - 1], st[b]);
+        if (bad == cudaSuccess) bad = cudaStreamWaitEvent(P->stream, P->ev_join[b - 1], 0);
+      }
+      if (bad == cudaSuccess) bad = cudaGetLastError();
+    }
+  for (int q = 0; q < nj && bad == cudaSuccess; ++q) {  // each job's DFT fold of the ring
+    fdtd_job *J = P->jobs[q];
+    if (J->mon_dev.empty() || J->dft_blocks <= 0) continue;
+    DftParams d{};
+    d.nmon = (int)J->mon_dev.size();
+    for (int m = 0; m < d.nmon; ++m) d.mon[m] = J->mon_dev[m];
+    d.omega = J->d_omega;
+    d.acc_re = J->d_acc_re;
+    d.acc_im = J->d_acc_im;
+    d.dt = J->g.dt;
+    d.stage_row = J->stage_row;
+    d.total_work_blocks = J->dft_blocks;
+    d.nslots = kStageSteps;
+    d.d_base = P->d_n0 + q;
+    launch_dft<T>(d, (const T *)J->d_stage, P->stream);
+    ++kernels;
+    bad = cudaGetLastError();
+  }
+  if (bad == cudaSuccess) {
+    pack_advance_kernel<<<(nj + 31) / 32, 32, 0, P->stream>>>(P->d_n0, nj, kStageSteps);
+    ++kernels;
+    bad = cudaGetLastError();
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(P->stream, &g);
+  if (bad != cudaSuccess || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return set_err(FDTD_ECUDA, "pack graph capture: %s", cudaGetErrorString(bad != cudaSuccess ? bad : e));
+  }
+  P->graph = g;
+  CK(cudaGraphInstantiate(&P->exec, P->graph, 0));
+  P->kernels_per_ring = kernels;
+  return FDTD_OK;
+}
+
+}  // namespace
+
+long long fdtd::pack_key(const fdtd_job *J) {
+  if (!J || !J->committed || J->dim != 2 || !J->gather_fused || J->prof || J->stage_fill != 0) return -1;
+  return ((long long)J->g.precision * 16 + J->g.layout) * 16 + J->vec;
+}
+
+int fdtd::job_reserve(fdtd_job *J, int n_last) {
+  if (!J || !J->committed) return set_err(FDTD_ESTATE, "job not committed");
+  int rc = ensure_probe_cap(J, n_last);
+  if (!rc && J->dim >= 2) rc = ensure_srctab(J, n_last);
+  return rc;
+}
+
+void fdtd::pack_destroy(fdtd::Pack *P) {
+  if (!P) return;
+  if (P->stream) cudaStreamSynchronize(P->stream);
+  if (P->exec) cudaGraphExecDestroy(P->exec);
+  if (P->graph) cudaGraphDestroy(P->graph);
+  if (P->d_tab) cudaFreeAsync(P->d_tab, P->stream);
+  if (P->d_n0) cudaFreeAsync(P->d_n0, P->stream);
+  for (int q = 0; q < 2; ++q) {
+    if (P->side[q]) cudaStreamDestroy(P->side[q]);
+    if (P->ev_join[q]) cudaEventDestroy(P->ev_join[q]);
+  }
+  if (P->ev_fork) cudaEventDestroy(P->ev_fork);
+  if (P->stream) cudaStreamDestroy(P->stream);
+  delete P;
+}
+
+int fdtd::pack_create(fdtd_job *const *jobs, int njobs, fdtd::Pack **out) {
+  *out = nullptr;
+  if (njobs < 1 || njobs > kMaxPack) return set_err(FDTD_EINVAL, "a pack holds 1..%d jobs", kMaxPack);
+  const long long key = pack_key(jobs[0]);
+  for (int q = 0; q < njobs; ++q)
+    if (key < 0 || pack_key(jobs[q]) != key) return set_err(FDTD_EINVAL, "jobs of a pack must be 2D jobs of one kind");
+  fdtd::Pack *P = new fdtd::Pack;
+  P->jobs.assign(jobs, jobs + njobs);
+  P->layout = jobs[0]->g.layout;
+  P->vec = jobs[0]->vec;
+  P->f64 = jobs[0]->g.precision == FDTD_F64;
+  bool ok = cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int q = 0; q < 2 && ok; ++q)
+    ok = cudaStreamCreateWithFlags(&P->side[q], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&P->ev_join[q], cudaEventDisableTiming) == cudaSuccess;
+  std::vector<int> n0(njobs);
+  for (int q = 0; q < njobs && ok; ++q) {
+    ok = cudaStreamSynchronize(jobs[q]->stream) == cudaSuccess;  // the job's own work is done
+    n0[q] = jobs[q]->last_n + 1;
+  }
+  if (ok) ok = cudaMallocAsync((void **)&P->d_n0, njobs * sizeof(int), P->stream) == cudaSuccess &&
+               cudaMemcpyAsync(P->d_n0, n0.data(), njobs * sizeof(int), cudaMemcpyHostToDevice, P->stream) == cudaSuccess &&
+               cudaStreamSynchronize(P->stream) == cudaSuccess;
+  if (!ok) {
+    pack_destroy(P);
+    return set_err(FDTD_ECUDA, "pack set-up failed");
+  }
+  const int rc = P->f64 ? pack_capture<double>(P) : pack_capture<float>(P);
+  if (rc) {
+    pack_destroy(P);
+    return rc;
+  }
+  *out = P;
+  return FDTD_OK;
+}
+
+int fdtd::pack_run(fdtd::Pack *P, int rings, cudaEvent_t done) {
+  for (int r = 0; r < rings; ++r) CK(cudaGraphLaunch(P->exec, P->stream));
+  if (done) CK(cudaEventRecord(done, P->stream));
+  const int nj = (int)P->jobs.size();
+  for (fdtd_job *J : P->jobs) {  // the jobs' own step bookkeeping, as after their own rings
+    J->last_n += rings * kStageSteps;
+    J->stage_n0 = J->last_n + 1;
+    J->launches += (long long)rings * ((P->kernels_per_ring + nj - 1) / nj);
+  }
   return FDTD_OK;
 }
 

@@ -16,7 +16,11 @@
 //   * DFT: samples of the monitored cells are staged per step in a ring of
 //     kStageSteps slots and folded into FP64 accumulators once per ring.
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
+
+#include "fdtd_gb300.h"
 
 namespace fdtd {
 
@@ -172,6 +176,17 @@ constexpr int kAdeFields = 6;
 // 2D half steps: the parts of one half step are independent launches
 enum K2dPart { K2D_CORE = 0, K2D_EDGE = 1, K2D_ADE = 2 };
 template <typename T> int launch_e2d(const StepParams<T> &p, int part, void *stream);
+
+// packs of 2D jobs: one launch runs one part of every job's half step
+constexpr int kMaxPack = 32;
+template <typename T>
+struct PackLaunch {
+  const StepParams<T> *tab;  // one StepParams per job (this ring slot)
+  int njobs;
+  int bstart[kMaxPack + 1];  // first block of each job; bstart[njobs] = blocks
+};
+template <typename T>
+int launch_pack2d(const PackLaunch<T> &a, int layout, int vec, bool e_half, int part, void *stream);
 template <typename T> int launch_h2d(const StepParams<T> &p, int part, void *stream);
 template <typename T> int launch_e3d(const StepParams<T> &p, int part, void *stream);
 template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *stream);
@@ -235,5 +250,18 @@ template <typename T> void launch_line1d_stage(const LineParams<T> &p, T *stage,
 
 // Records a message for fdtd_last_error and returns `code`.
 int report_error(int code, const char *fmt, ...);
+
+// Packs of 2D jobs advanced by shared launches (fdtd_api.cu).  pack_key is
+// -1 for a job that cannot join a pack (not a committed 2D job at a ring
+// boundary) and otherwise equal for jobs that can share one.  job_reserve
+// sizes a job's source table and probe buffers for steps up to n_last, as a
+// pack bakes their addresses into its tables.  pack_run queues `rings`
+// rings of every member on the pack's stream and records `done` after them.
+struct Pack;
+long long pack_key(const fdtd_job *J);
+int job_reserve(fdtd_job *J, int n_last);
+int pack_create(fdtd_job *const *jobs, int njobs, Pack **out);
+int pack_run(Pack *P, int rings, cudaEvent_t done);
+void pack_destroy(Pack *P);
 
 }  // namespace fdtd

@@ -10,10 +10,17 @@
 //     chunk_steps time steps (CUDA-graph replays of 32-step rings), so the
 //     kernels of different jobs overlap on the device, and jobs join and
 //     leave between chunks without stopping the others;
+//   * small 2D jobs (at most pack_cells cells) of one precision and layout
+//     are packed: one launch per part of a half step covers all of them
+//     (fdtd::Pack), as each alone would leave most of the GPU idle; a packed
+//     job leaves its pack when less than a ring of steps is left and
+//     finishes on its own stream;
 //   * a finished job keeps its memory until the caller has read its results
 //     and released it.
 // One host thread runs the loop.  It never waits on the device except
-// through event queries, so a slow job does not hold up the others.
+// through event queries, so a slow job does not hold up the others; commits
+// (host set-up and uploads) run on worker threads, so they overlap the
+// running jobs' GPU work.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -47,6 +54,8 @@ struct Req {
   char err[256] = {};
   int next_n = 1;
   bool inflight = false;
+  long long key = -1;  // pack group, -1: runs alone
+  bool in_pack = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev = nullptr;
   double t_submit = 0, t_admit = 0, t_done = 0;
@@ -54,8 +63,16 @@ struct Req {
 
 }  // namespace
 
+struct PackGroup {
+  fdtd::Pack *pack = nullptr;
+  std::vector<Req *> members;
+  cudaEvent_t ev = nullptr;
+  bool inflight = false;
+};
+
 struct fdtd_server {
   fdtd_server_desc d{};
+  std::map<long long, PackGroup> groups;
   int device = 0;
   uint64_t budget = 0;
   double t0 = 0;
@@ -67,8 +84,15 @@ struct fdtd_server {
   uint64_t held = 0, held_max = 0;
   int64_t next_ticket = 1;
   int64_t done_count = 0;
+  int64_t packed_rings = 0, pack_builds = 0;
+  double pack_build_s = 0;
   bool stop = false;
   std::thread th;
+  // admitted jobs waiting for a commit worker
+  std::deque<Req *> to_commit;
+  int committing = 0;
+  std::condition_variable cv_commit;
+  std::vector<std::thread> workers;
 };
 
 namespace {
@@ -82,9 +106,10 @@ void finish(fdtd_server *S, Req *r, int rc, const char *why) {
   S->cv_done.notify_all();
 }
 
-// admit queued jobs in order while slots and memory allow (lock held)
-void admit(fdtd_server *S, std::unique_lock<std::mutex> &lk) {
-  while (!S->queue.empty() && (int)S->active.size() < S->d.max_active && !S->stop) {
+// admit queued jobs in order while slots and memory allow (lock held); a
+// commit worker then sets them up
+void admit(fdtd_server *S) {
+  while (!S->queue.empty() && (int)S->active.size() + S->committing < S->d.max_active && !S->stop) {
     Req *r = S->queue.front();
     if (r->est > S->budget) {
       S->queue.pop_front();
@@ -94,37 +119,156 @@ void admit(fdtd_server *S, std::unique_lock<std::mutex> &lk) {
     if (S->held + r->est > S->budget) return;  // wait for memory to be released
     S->queue.pop_front();
     S->held += r->est;
+    S->held_max = std::max(S->held_max, S->held);
     r->state = FDTD_REQ_RUNNING;
+    ++S->committing;
+    S->to_commit.push_back(r);
+    S->cv_commit.notify_one();
+  }
+}
+
+// commit worker: allocate and upload an admitted job, then hand it to the loop
+void commit_worker(fdtd_server *S) {
+  cudaSetDevice(S->device);
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    S->cv_commit.wait(lk, [S] { return S->stop || !S->to_commit.empty(); });
+    if (S->stop) return;
+    Req *r = S->to_commit.front();
+    S->to_commit.pop_front();
     lk.unlock();
     char msg[256] = {};
     int rc = fdtd_set_stream(r->job, r->stream);
     if (!rc) rc = fdtd_commit(r->job);
     uint64_t real = r->est;
     if (!rc) rc = fdtd_device_bytes(r->job, &real);
+    long long key = -1;
+    if (!rc && S->d.pack_cells >= 0 && r->n_steps >= fdtd::kStageSteps && fdtd::pack_key(r->job) >= 0) {
+      int64_t cells = 0;
+      fdtd_kernel_cells(r->job, FDTD_KERNEL_E, &cells);
+      if (cells <= (S->d.pack_cells ? S->d.pack_cells : (1 << 20)) && !fdtd::job_reserve(r->job, r->n_steps))
+        key = fdtd::pack_key(r->job);
+    }
     if (rc) fdtd_last_error(msg, sizeof msg);
     lk.lock();
+    --S->committing;
     S->held -= r->est;
     if (rc) {
       finish(S, r, rc, msg);
+    } else {
+      r->bytes = std::max(real, r->est);
+      S->held += r->bytes;
+      S->held_max = std::max(S->held_max, S->held);
+      r->t_admit = now_s();
+      r->key = key;
+      S->active.push_back(r);
+    }
+    S->cv_work.notify_one();
+  }
+}
+
+// Advance the pack groups (lock held).  A group whose pack is idle takes in
+// the packable active jobs with at least a ring of steps left, lets go of
+// the others, rebuilds its pack when its members changed, and queues whole
+// rings up to chunk_steps.
+bool advance_packs(fdtd_server *S, std::unique_lock<std::mutex> &lk) {
+  bool progressed = false;
+  for (Req *r : S->active)
+    if (r->key >= 0 && !r->in_pack && !r->inflight && r->n_steps - r->next_n + 1 >= fdtd::kStageSteps &&
+        S->groups[r->key].members.size() < (size_t)fdtd::kMaxPack && !S->groups[r->key].inflight) {
+      S->groups[r->key].members.push_back(r);
+      r->in_pack = true;
+      if (S->groups[r->key].pack) {  // membership changed: rebuild below
+        lk.unlock();
+        fdtd::pack_destroy(S->groups[r->key].pack);
+        lk.lock();
+        S->groups[r->key].pack = nullptr;
+      }
+    }
+  for (auto &kv : S->groups) {
+    PackGroup &G = kv.second;
+    if (G.inflight) {
+      const cudaError_t q = cudaEventQuery(G.ev);
+      if (q == cudaErrorNotReady) continue;
+      G.inflight = false;
+      if (q != cudaSuccess) {
+        for (Req *r : G.members) {
+          r->in_pack = false;
+          r->key = -1;
+          r->next_n = r->n_steps + 1;
+          finish(S, r, FDTD_ECUDA, cudaGetErrorString(q));
+          S->active.erase(std::find(S->active.begin(), S->active.end(), r));
+        }
+        G.members.clear();
+      }
+    }
+    // members with less than a ring left finish alone
+    bool changed = false;
+    for (size_t i = 0; i < G.members.size();) {
+      Req *r = G.members[i];
+      if (r->n_steps - r->next_n + 1 < fdtd::kStageSteps) {
+        r->in_pack = false;
+        r->key = -1;
+        G.members.erase(G.members.begin() + i);
+        changed = true;
+      } else {
+        ++i;
+      }
+    }
+    if (changed && G.pack) {
+      lk.unlock();
+      fdtd::pack_destroy(G.pack);
+      lk.lock();
+      G.pack = nullptr;
+    }
+    if (G.members.empty()) continue;
+    if (!G.ev && cudaEventCreateWithFlags(&G.ev, cudaEventDisableTiming) != cudaSuccess) continue;
+    int rings = S->d.chunk_steps / fdtd::kStageSteps;
+    for (Req *r : G.members) rings = std::min(rings, (r->n_steps - r->next_n + 1) / fdtd::kStageSteps);
+    std::vector<fdtd_job *> jobs;
+    for (Req *r : G.members) jobs.push_back(r->job);
+    lk.unlock();
+    int rc = FDTD_OK;
+    char msg[256] = {};
+    double tb = 0;
+    if (!G.pack) {
+      tb = now_s();
+      rc = fdtd::pack_create(jobs.data(), (int)jobs.size(), &G.pack);
+      tb = now_s() - tb;
+    }
+    if (!rc) rc = fdtd::pack_run(G.pack, rings, G.ev);
+    if (rc) fdtd_last_error(msg, sizeof msg);
+    lk.lock();
+    if (tb > 0) {
+      ++S->pack_builds;
+      S->pack_build_s += tb;
+    }
+    if (rc) {  // the members go on alone
+      for (Req *r : G.members) {
+        r->in_pack = false;
+        r->key = -1;
+      }
+      G.members.clear();
       continue;
     }
-    r->bytes = std::max(real, r->est);
-    S->held += r->bytes;
-    S->held_max = std::max(S->held_max, S->held);
-    r->t_admit = now_s();
-    S->active.push_back(r);
+    for (Req *r : G.members) r->next_n += rings * fdtd::kStageSteps;
+    S->packed_rings += rings;
+    G.inflight = true;
+    progressed = true;
   }
+  return progressed;
 }
 
 void serve(fdtd_server *S) {
   cudaSetDevice(S->device);
   std::unique_lock<std::mutex> lk(S->mu);
   for (;;) {
-    admit(S, lk);
+    admit(S);
     if (S->stop) break;
-    bool progressed = false;
+    bool progressed = advance_packs(S, lk);
     for (size_t i = 0; i < S->active.size();) {
       Req *r = S->active[i];
+      if (r->key >= 0) { ++i; continue; }  // in a pack, or waiting for its group to be idle
       if (r->inflight) {
         const cudaError_t q = cudaEventQuery(r->ev);
         if (q == cudaErrorNotReady) { ++i; continue; }
@@ -166,6 +310,13 @@ void serve(fdtd_server *S) {
     if (!progressed) S->cv_work.wait_for(lk, std::chrono::microseconds(50));
   }
   // stopping: let the chunks in flight end, then leave the jobs to the destructor
+  for (auto &kv : S->groups) {
+    lk.unlock();
+    if (kv.second.pack) fdtd::pack_destroy(kv.second.pack);  // waits for its rings
+    if (kv.second.ev) cudaEventDestroy(kv.second.ev);
+    lk.lock();
+    kv.second.pack = nullptr;
+  }
   for (Req *r : S->active)
     if (r->inflight) {
       lk.unlock();
@@ -209,6 +360,7 @@ int fdtd_server_create(const fdtd_server_desc *desc, fdtd_server **out) {
   S->budget = desc->hbm_budget ? desc->hbm_budget : (uint64_t)(0.9 * (double)free_b);
   S->t0 = now_s();
   S->th = std::thread(serve, S);
+  for (int w = 0; w < 2; ++w) S->workers.emplace_back(commit_worker, S);
   *out = S;
   return FDTD_OK;
 }
@@ -302,6 +454,9 @@ int fdtd_server_stats(fdtd_server *S, fdtd_server_status *st) {
   st->held_bytes = S->held;
   st->held_bytes_max = S->held_max;
   st->budget_bytes = S->budget;
+  st->packed_rings = S->packed_rings;
+  st->pack_builds = S->pack_builds;
+  st->pack_build_s = S->pack_build_s;
   return FDTD_OK;
 }
 
@@ -312,6 +467,9 @@ int fdtd_server_destroy(fdtd_server *S) {
     S->stop = true;
   }
   S->cv_work.notify_all();
+  S->cv_commit.notify_all();
+  for (auto &w : S->workers)
+    if (w.joinable()) w.join();
   if (S->th.joinable()) S->th.join();
   for (auto &kv : S->reqs) drop(kv.second);
   delete S;

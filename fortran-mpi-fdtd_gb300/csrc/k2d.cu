@@ -594,6 +594,104 @@ int launch_h2d(const StepParams<T> &p, int part, void *stream) {
   return p.vec == VW ? launch_h2d_v<T, 2, VW>(p, part, s) : launch_h2d_v<T, 2, 1>(p, part, s);
 }
 
+// ---- packs: one launch runs the same part of many jobs' half steps ---------
+// Block b belongs to the job q with bstart[q] <= b < bstart[q+1]; the job's
+// parameters come from the slot's table in device memory.
+template <typename T>
+__device__ __forceinline__ int pack_job(const PackLaunch<T> &a) {
+  int q = 0;
+  while (q + 1 < a.njobs && (int)blockIdx.x >= a.bstart[q + 1]) ++q;
+  return q;
+}
+
+// The block's job parameters, copied once into shared memory: the kernels
+// read many of them before their first field load, and from the table each
+// would be a dependent global load.
+template <typename T>
+__device__ __forceinline__ const StepParams<T> &pack_params(const PackLaunch<T> &a, int q) {
+  static_assert(sizeof(StepParams<T>) % 8 == 0, "StepParams is copied in 8-byte words");
+  __shared__ unsigned long long sm[sizeof(StepParams<T>) / 8];
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(a.tab + q);
+  for (int w = threadIdx.x; w < (int)(sizeof(StepParams<T>) / 8); w += blockDim.x) sm[w] = __ldg(src + w);
+  __syncthreads();
+  return *reinterpret_cast<const StepParams<T> *>(sm);
+}
+
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) e2d_core_pk(const __grid_constant__ PackLaunch<T> a) {
+  const int q = pack_job(a);
+  const StepParams<T> &p = pack_params(a, q);
+  const int t = ((int)blockIdx.x - a.bstart[q]) * 256 + threadIdx.x;
+  if (t >= p.ncore) return;
+  core_e<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
+}
+
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) h2d_core_pk(const __grid_constant__ PackLaunch<T> a) {
+  const int q = pack_job(a);
+  const StepParams<T> &p = pack_params(a, q);
+  const int t = ((int)blockIdx.x - a.bstart[q]) * 256 + threadIdx.x;
+  if (t >= p.ncore) return;
+  core_h<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
+}
+
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) e2d_edge_pk(const __grid_constant__ PackLaunch<T> a) {
+  const int q = pack_job(a);
+  const StepParams<T> &p = pack_params(a, q);
+  const int t = ((int)blockIdx.x - a.bstart[q]) * 256 + threadIdx.x;
+  if (t >= p.nedge) return;
+  K2<T, L, V>::unit_e(p, __ldg(p.edge_units + t), step_n(p));
+}
+
+template <typename T, int L, int V>
+__global__ void __launch_bounds__(256) h2d_edge_pk(const __grid_constant__ PackLaunch<T> a) {
+  const int q = pack_job(a);
+  const StepParams<T> &p = pack_params(a, q);
+  const int t = ((int)blockIdx.x - a.bstart[q]) * 256 + threadIdx.x;
+  if (t >= p.nedge) return;
+  K2<T, L, V>::unit_h(p, __ldg(p.edge_units + t), step_n(p));
+}
+
+template <typename T, int L>
+__global__ void __launch_bounds__(256) e2d_ade_pk(const __grid_constant__ PackLaunch<T> a) {
+  const int q = pack_job(a);
+  const StepParams<T> &p = pack_params(a, q);
+  const int s = ((int)blockIdx.x - a.bstart[q]) * 256 + threadIdx.x;
+  if (s < p.nade) ade_e2<T, L>(p, s, step_n(p));
+}
+
+template <typename T, int L, int V>
+void launch_pack_v(const PackLaunch<T> &a, bool e_half, int part, cudaStream_t s) {
+  const int blocks = a.bstart[a.njobs];
+  if (e_half) {
+    if (part == K2D_CORE) e2d_core_pk<T, L, V><<<blocks, 256, 0, s>>>(a);
+    else if (part == K2D_EDGE) e2d_edge_pk<T, L, V><<<blocks, 256, 0, s>>>(a);
+    else e2d_ade_pk<T, L><<<blocks, 256, 0, s>>>(a);
+  } else {
+    if (part == K2D_CORE) h2d_core_pk<T, L, V><<<blocks, 256, 0, s>>>(a);
+    else h2d_edge_pk<T, L, V><<<blocks, 256, 0, s>>>(a);
+  }
+}
+
+template <typename T>
+int launch_pack2d(const PackLaunch<T> &a, int layout, int vec, bool e_half, int part, void *stream) {
+  if (a.njobs <= 0 || a.bstart[a.njobs] <= 0) return 0;
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (layout == 3) {
+    if (vec == VW) launch_pack_v<T, 3, VW>(a, e_half, part, s);
+    else launch_pack_v<T, 3, 1>(a, e_half, part, s);
+  } else {
+    if (vec == VW) launch_pack_v<T, 2, VW>(a, e_half, part, s);
+    else launch_pack_v<T, 2, 1>(a, e_half, part, s);
+  }
+  return 1;
+}
+
+template int launch_pack2d<float>(const PackLaunch<float> &, int, int, bool, int, void *);
+template int launch_pack2d<double>(const PackLaunch<double> &, int, int, bool, int, void *);
+
 template int launch_e2d<float>(const StepParams<float> &, int, void *);
 template int launch_e2d<double>(const StepParams<double> &, int, void *);
 template int launch_h2d<float>(const StepParams<float> &, int, void *);

@@ -65,12 +65,14 @@ class Tfsf1dDesc(C.Structure):
 
 
 class ServerDesc(C.Structure):
-    _fields_ = [("hbm_budget", C.c_uint64), ("max_active", C.c_int32), ("chunk_steps", C.c_int32)]
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_active", C.c_int32), ("chunk_steps", C.c_int32),
+                ("pack_cells", C.c_int32)]
 
 
 class ServerStatus(C.Structure):
     _fields_ = [("queued", C.c_int32), ("active", C.c_int32), ("finished", C.c_int64),
-                ("held_bytes", C.c_uint64), ("held_bytes_max", C.c_uint64), ("budget_bytes", C.c_uint64)]
+                ("held_bytes", C.c_uint64), ("held_bytes_max", C.c_uint64), ("budget_bytes", C.c_uint64),
+                ("packed_rings", C.c_int64), ("pack_builds", C.c_int64), ("pack_build_s", C.c_double)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)

@@ -18,8 +18,11 @@ from .job import Job, check, lib
 
 
 class Server:
-    def __init__(self, hbm_budget=0, max_active=16, chunk_steps=256):
-        d = abi.ServerDesc(hbm_budget=int(hbm_budget), max_active=int(max_active), chunk_steps=int(chunk_steps))
+    def __init__(self, hbm_budget=0, max_active=16, chunk_steps=256, pack_cells=0):
+        """pack_cells: 2D jobs of at most this many cells share launches
+        (0: the library's default, 2^20 cells; < 0: every job runs alone)."""
+        d = abi.ServerDesc(hbm_budget=int(hbm_budget), max_active=int(max_active), chunk_steps=int(chunk_steps),
+                           pack_cells=int(pack_cells))
         h = C.c_void_p()
         check(lib().fdtd_server_create(C.byref(d), C.byref(h)))
         self.h = h

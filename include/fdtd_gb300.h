@@ -282,7 +282,8 @@ int fdtd_transfer_bytes(const fdtd_job *job, uint64_t *h2d, uint64_t *d2h);
  * Jobs are admitted in submission order when fewer than max_active are
  * running and their fdtd_estimate_bytes fits in what hbm_budget has left
  * (0: 90% of the device's free memory at creation); a job that can never fit
- * fails with FDTD_ENOMEM.  A finished job keeps its memory until
+ * fails with FDTD_ENOMEM.  Small 2D jobs of one precision and layout are
+ * packed: each part of a half step is one launch over all of them.  A finished job keeps its memory until
  * fdtd_server_release.  Each job runs steps 1..n_steps, with the same
  * kernels in the same order as fdtd_step(job, 1, n_steps) on its own, so its
  * results do not depend on the other jobs. */
@@ -291,11 +292,15 @@ typedef struct {
   uint64_t hbm_budget;  /* device bytes the admitted jobs may hold (0: 90% of free) */
   int32_t max_active;   /* jobs advanced at once */
   int32_t chunk_steps;  /* steps per scheduling turn (rounded up to whole 32-step rings) */
+  int32_t pack_cells;   /* 2D jobs of at most this many cells share launches (0: 2^20; < 0: never) */
 } fdtd_server_desc;
 typedef struct {
   int32_t queued, active;
   int64_t finished;
   uint64_t held_bytes, held_bytes_max, budget_bytes;
+  int64_t packed_rings;  /* 32-step rings run by packs (one per pack and ring) */
+  int64_t pack_builds;   /* packs set up (each change of a pack's members) */
+  double pack_build_s;   /* host seconds spent setting packs up */
 } fdtd_server_status;
 enum { FDTD_REQ_QUEUED = 0, FDTD_REQ_RUNNING = 1, FDTD_REQ_DONE = 2, FDTD_REQ_FAILED = 3 };
 int fdtd_server_create(const fdtd_server_desc *desc, fdtd_server **server);

@@ -41,7 +41,10 @@ def gpu_lib():
 
 
 @gpu
-def test_mixed_results_equal_alone(gpu_lib):
+@pytest.mark.parametrize("pack_cells", [0, -1])
+def test_mixed_results_equal_alone(gpu_lib, pack_cells):
+    """pack_cells 0: the small 2D jobs share launches (packs); -1: every job
+    runs on its own stream."""
     jobs = small_mix()
     alone = []
     for spec, nst in jobs:
@@ -49,7 +52,7 @@ def test_mixed_results_equal_alone(gpu_lib):
         J.step(1, nst)
         alone.append(spectra(J, spec))
         J.close()
-    S = serve.Server(max_active=8, chunk_steps=64)
+    S = serve.Server(max_active=8, chunk_steps=64, pack_cells=pack_cells)
     tickets = [S.submit(spec, nst) for spec, nst in jobs]
     for q, tk in enumerate(tickets):
         assert S.wait(tk) == abi.REQ_DONE
@@ -63,6 +66,7 @@ def test_mixed_results_equal_alone(gpu_lib):
     st = S.stats()
     assert st["finished"] == len(jobs) and st["active"] == 0 and st["queued"] == 0
     assert st["held_bytes"] == 0
+    assert (st["packed_rings"] > 0) == (pack_cells == 0)
     S.close()
 
 
