@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -174,6 +175,7 @@ struct fdtd_job {
   // parts of a half step as parallel branches of the job's stream
   int vec = 1, cv0 = 0, cw = 0, cy0 = 0, ncore = 0, nedge = 0;
   int ch = 0, cz0 = 0, cd = 0;  // 3D: core box rows and planes
+  int tile_req = 0, tile = 1;    // core block shape: requested (0: tune) and used
   int *d_edge = nullptr;
   cudaStream_t side[2] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {};
@@ -442,6 +444,9 @@ int split_3d(fdtd_job *J, const std::vector<uint8_t> &rf) {
   }
   return make_branches(J);
 }
+
+template <typename T>
+int tune_tiles(fdtd_job *J);
 
 template <typename T>
 int commit_impl(fdtd_job *J) {
@@ -807,6 +812,7 @@ int commit_impl(fdtd_job *J) {
     blocks += ((m.ncomp * m.ncell + 255) / 256) * ((m.nfreq + 7) / 8);
   J->dft_blocks = blocks;
   CK(cudaStreamSynchronize(J->stream));
+  if ((rc = tune_tiles<T>(J))) return rc;
   J->committed = true;
   return FDTD_OK;
 }
@@ -870,6 +876,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.cw = J->cw;
     p.cy0 = J->cy0;
     p.ncore = J->ncore;
+    p.tile = J->tile;
     p.nedge = J->nedge;
     p.edge_units = J->d_edge;
   } else {
@@ -879,6 +886,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.vec = J->vec;
     p.cv0 = J->cv0; p.cw = J->cw; p.cy0 = J->cy0; p.ch = J->ch; p.cz0 = J->cz0; p.cd = J->cd;
     p.ncore = J->ncore;
+    p.tile = J->tile;
   }
   p.nslab_blocks = (J->dim == 3 && J->slab_rows > 0) ? (2 * J->nx * J->slab_rows * J->nz + 255) / 256 : 0;
   p.nade_blocks = (J->nade + 255) / 256;
@@ -1067,6 +1075,72 @@ int run_parts(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], bool e
       CK(cudaStreamWaitEvent(J->stream, J->ev_join[b - 1], 0));
     }
   }
+  return FDTD_OK;
+}
+
+// Commit-time tuner of the core kernels' block shape.  Each candidate runs a
+// few E and H core launches on the job's own grid, whose fields are still
+// zero -- a core update of zero fields writes back the zeros it read -- and
+// the fastest is kept.  The choice is cached per kind of grid (dimension,
+// layout, precision, vector width, log2 of the core cells).
+std::mutex g_tune_mu;
+std::map<long long, int> g_tune;
+
+template <typename T>
+int tune_tiles(fdtd_job *J) {
+  if (J->dim < 2 || J->ncore <= 0) return FDTD_OK;
+  if (J->tile_req > 0) {
+    J->tile = J->tile_req - 1;
+    return FDTD_OK;
+  }
+  const char *off = getenv("FDTD_TUNE");
+  if (off && off[0] == '0') {
+    J->tile = 1;
+    return FDTD_OK;
+  }
+  int lg = 0;
+  for (long long c = J->ncore; c > 1; c >>= 1) ++lg;
+  const long long key = ((((long long)J->dim * 8 + J->g.layout) * 4 + J->g.precision) * 8 + J->vec) * 64 + lg;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      J->tile = it->second;
+      return FDTD_OK;
+    }
+  }
+  StepParams<T> p;
+  fill_common<T>(J, p);
+  p.roles = ROLE_MAIN;
+  cudaEvent_t a = nullptr, b = nullptr;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  float best = 3.0e38f;
+  int choice = 1;
+  for (int c = 0; c < 3; ++c) {
+    p.tile = c;
+    for (int w = 0; w < 2; ++w) {
+      launch_part<T>(J, p, K2D_CORE, true, J->stream);
+      launch_part<T>(J, p, K2D_CORE, false, J->stream);
+    }
+    cudaEventRecord(a, J->stream);
+    for (int r = 0; r < 5; ++r) {
+      launch_part<T>(J, p, K2D_CORE, true, J->stream);
+      launch_part<T>(J, p, K2D_CORE, false, J->stream);
+    }
+    cudaEventRecord(b, J->stream);
+    float ms = 0.f;
+    if (cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms < best) {
+      best = ms;
+      choice = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CK(cudaGetLastError());
+  J->tile = choice;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = choice;
   return FDTD_OK;
 }
 
@@ -1990,6 +2064,21 @@ int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
   J->pending.clear();
   if (launches) *launches = J->kcount[kind];
   if (ms) *ms = J->kms[kind];
+  return FDTD_OK;
+}
+
+int fdtd_set_tile(fdtd_job *J, int32_t tile) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (tile < 0 || tile > 3) return set_err(FDTD_EINVAL, "tile must be 0 (tune) or 1..3");
+  J->tile_req = tile;
+  return FDTD_OK;
+}
+
+int fdtd_get_tile(const fdtd_job *J, int32_t *tile) {
+  if (!J || !tile) return set_err(FDTD_EINVAL, "null argument");
+  if (!J->committed) return set_err(FDTD_ESTATE, "job not committed");
+  *tile = J->dim >= 2 && J->ncore > 0 ? J->tile + 1 : 0;
   return FDTD_OK;
 }
 

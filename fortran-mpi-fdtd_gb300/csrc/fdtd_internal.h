@@ -141,6 +141,7 @@ struct StepParams {
   // 3D: the core box is vectors [cv0, cv0+cw) x rows [cy0, cy0+ch) x planes
   // [cz0, cz0+cd); edge_units are then x-vectors (k*ny + j)*nx/V + vector
   int ch, cz0, cd;
+  int tile;                // block shape of the core kernels (0..2, tuned)
   // sampling fused into the H kernel
   int gather;              // 1: tile threads write the stage row / probes
   int nmon;

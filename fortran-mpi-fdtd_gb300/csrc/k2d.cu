@@ -520,18 +520,35 @@ __device__ __forceinline__ void core_h(const StepParams<T> &p, int j, int i0) {
 }
 
 // ---- kernels: one unit (or one dispersive cell) per thread -----------------
-template <typename T, int L, int V>
-__global__ void __launch_bounds__(256) e2d_core(const __grid_constant__ StepParams<T> p) {
-  const int t = blockIdx.x * 256 + threadIdx.x;
+// core kernels: NT threads per block, one of the candidate shapes that the
+// commit-time tuner times on the job's grid
+template <typename T, int L, int V, int NT>
+__global__ void __launch_bounds__(NT) e2d_core(const __grid_constant__ StepParams<T> p) {
+  const int t = blockIdx.x * NT + threadIdx.x;
   if (t >= p.ncore) return;
   core_e<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
 }
 
-template <typename T, int L, int V>
-__global__ void __launch_bounds__(256) h2d_core(const __grid_constant__ StepParams<T> p) {
-  const int t = blockIdx.x * 256 + threadIdx.x;
+template <typename T, int L, int V, int NT>
+__global__ void __launch_bounds__(NT) h2d_core(const __grid_constant__ StepParams<T> p) {
+  const int t = blockIdx.x * NT + threadIdx.x;
   if (t >= p.ncore) return;
   core_h<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
+}
+
+template <typename T, int L, int V, int NT>
+void launch_core2(const StepParams<T> &p, bool e_half, cudaStream_t s) {
+  const int blocks = (p.ncore + NT - 1) / NT;
+  if (e_half) e2d_core<T, L, V, NT><<<blocks, NT, 0, s>>>(p);
+  else h2d_core<T, L, V, NT><<<blocks, NT, 0, s>>>(p);
+}
+
+// tile 0: 128 threads, 1: 256, 2: 512
+template <typename T, int L, int V>
+void launch_core2_tiled(const StepParams<T> &p, bool e_half, cudaStream_t s) {
+  if (p.tile == 0) launch_core2<T, L, V, 128>(p, e_half, s);
+  else if (p.tile == 2) launch_core2<T, L, V, 512>(p, e_half, s);
+  else launch_core2<T, L, V, 256>(p, e_half, s);
 }
 
 template <typename T, int L, int V>
@@ -561,7 +578,7 @@ int launch_e2d_v(const StepParams<T> &p, int part, cudaStream_t s) {
   const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge : p.nade;
   if (units <= 0) return 0;
   const int blocks = (units + 255) / 256;
-  if (part == K2D_CORE) e2d_core<T, L, V><<<blocks, 256, 0, s>>>(p);
+  if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, true, s);
   else if (part == K2D_EDGE) e2d_edge<T, L, V><<<blocks, 256, 0, s>>>(p);
   else e2d_ade<T, L><<<blocks, 256, 0, s>>>(p);
   return 1;
@@ -571,7 +588,7 @@ int launch_h2d_v(const StepParams<T> &p, int part, cudaStream_t s) {
   const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge : 0;
   if (units <= 0) return 0;
   const int blocks = (units + 255) / 256;
-  if (part == K2D_CORE) h2d_core<T, L, V><<<blocks, 256, 0, s>>>(p);
+  if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, false, s);
   else h2d_edge<T, L, V><<<blocks, 256, 0, s>>>(p);
   return 1;
 }

@@ -64,19 +64,19 @@ struct F3 {
 
 // a cell of the core box in a row without flags: updated by the core launch
 // ---- core units: one x-vector of V interior cells per thread --------------
-// Block: 32 vectors along x by 8 rows along y, one z plane; blocks run x, y,
-// then z, so the plane below (E) or above (H) was read moments earlier and
-// its loads hit L2.
-template <typename T, int V>
+// Block: 32 vectors along x by RY rows along y (RY from the commit-time
+// tuner), one z plane; blocks run x, y, then z, so the plane below (E) or
+// above (H) was read moments earlier and its loads hit L2.
+template <typename T, int V, int RY = 8>
 struct Core3 {
   int j, k, i0;
   long long c;
   bool live;
   __device__ __forceinline__ Core3(const StepParams<T> &p) {
     const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
-    const int bx = (p.cw + 31) >> 5, by = (p.ch + 7) >> 3;
+    const int bx = (p.cw + 31) >> 5, by = (p.ch + RY - 1) / RY;
     const int b = blockIdx.x, tx = b % bx, t2 = b / bx, ty = t2 % by, tz = t2 / by;
-    const int v = tx * 32 + lane, r = ty * 8 + wy;
+    const int v = tx * 32 + lane, r = ty * RY + wy;
     live = v < p.cw && r < p.ch && tz < p.cd;
     j = p.cy0 + r;
     k = p.cz0 + tz;
@@ -492,9 +492,9 @@ __global__ void __launch_bounds__(256) h3d_kernel(const __grid_constant__ StepPa
   if (b < p.nslab_blocks && (p.roles & ROLE_PML)) slab_h3<T>(p, b * 256 + threadIdx.x);
 }
 
-template <typename T, int V>
-__global__ void __launch_bounds__(256) e3d_core(const __grid_constant__ StepParams<T> p) {
-  const Core3<T, V> u(p);
+template <typename T, int V, int RY>
+__global__ void __launch_bounds__(32 * RY) e3d_core(const __grid_constant__ StepParams<T> p) {
+  const Core3<T, V, RY> u(p);
   if (!u.live) return;
   const long long c = u.c;
   T hx[V], hy[V], hz[V], hzd[V], hxd[V], hyb[V], hxb[V], ex[V], ey[V], ez[V];
@@ -536,9 +536,9 @@ __global__ void __launch_bounds__(256) e3d_core(const __grid_constant__ StepPara
   }
 }
 
-template <typename T, int V>
-__global__ void __launch_bounds__(256) h3d_core(const __grid_constant__ StepParams<T> p) {
-  const Core3<T, V> u(p);
+template <typename T, int V, int RY>
+__global__ void __launch_bounds__(32 * RY) h3d_core(const __grid_constant__ StepParams<T> p) {
+  const Core3<T, V, RY> u(p);
   if (!u.live) return;
   const long long c = u.c;
   T ex[V], ey[V], ez[V], ezu[V], exu[V], exa[V], eya[V], hx[V], hy[V], hz[V];
@@ -569,15 +569,35 @@ __global__ void __launch_bounds__(256) h3d_core(const __grid_constant__ StepPara
   vst<T, V>(p.hz + c, hz);
 }
 
+template <typename T, int V, int RY>
+void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s) {
+  const int blocks = ((p.cw + 31) / 32) * ((p.ch + RY - 1) / RY) * p.cd;
+  if (e_half) e3d_core<T, V, RY><<<blocks, 32 * RY, 0, s>>>(p);
+  else h3d_core<T, V, RY><<<blocks, 32 * RY, 0, s>>>(p);
+}
+
+// tile 0: 4 rows of 32 x-vectors, 1: 8 rows, 2: 16 rows
+template <typename T>
+void launch_core3_tiled(const StepParams<T> &p, bool e_half, cudaStream_t s) {
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+  if (p.vec == VW) {
+    if (p.tile == 0) launch_core3<T, VW, 4>(p, e_half, s);
+    else if (p.tile == 2) launch_core3<T, VW, 16>(p, e_half, s);
+    else launch_core3<T, VW, 8>(p, e_half, s);
+  } else {
+    if (p.tile == 0) launch_core3<T, 1, 4>(p, e_half, s);
+    else if (p.tile == 2) launch_core3<T, 1, 16>(p, e_half, s);
+    else launch_core3<T, 1, 8>(p, e_half, s);
+  }
+}
+
 template <typename T>
 int launch_e3d(const StepParams<T> &p, int part, void *stream) {
   cudaStream_t s = (cudaStream_t)stream;
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   if (part == K2D_CORE) {
     if (p.ncore <= 0) return 0;
-    const int blocks = ((p.cw + 31) / 32) * ((p.ch + 7) / 8) * p.cd;
-    if (p.vec == VW) e3d_core<T, VW><<<blocks, 256, 0, s>>>(p);
-    else e3d_core<T, 1><<<blocks, 256, 0, s>>>(p);
+    launch_core3_tiled<T>(p, true, s);
     return 1;
   }
   const int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
@@ -592,9 +612,7 @@ int launch_h3d(const StepParams<T> &p, int part, void *stream) {
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   if (part == K2D_CORE) {
     if (p.ncore <= 0) return 0;
-    const int blocks = ((p.cw + 31) / 32) * ((p.ch + 7) / 8) * p.cd;
-    if (p.vec == VW) h3d_core<T, VW><<<blocks, 256, 0, s>>>(p);
-    else h3d_core<T, 1><<<blocks, 256, 0, s>>>(p);
+    launch_core3_tiled<T>(p, false, s);
     return 1;
   }
   const int blocks = p.ntile_blocks + p.nslab_blocks;

@@ -23,7 +23,7 @@ EXPORTS = [
     "fdtd_step", "fdtd_update_DE", "fdtd_pml_update_E", "fdtd_interchange", "fdtd_update_H",
     "fdtd_pml_update_H", "fdtd_sample", "fdtd_sync", "fdtd_get_field", "fdtd_set_field",
     "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_estimate_bytes", "fdtd_profile",
-    "fdtd_kernel_time", "fdtd_kernel_cells", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
+    "fdtd_kernel_time", "fdtd_kernel_cells", "fdtd_set_tile", "fdtd_get_tile", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
     "fdtd_dft_sample_noalloc",
     "fdtd_server_create", "fdtd_server_submit", "fdtd_server_wait", "fdtd_server_job", "fdtd_server_times",
     "fdtd_server_release", "fdtd_server_stats", "fdtd_server_destroy",
@@ -61,6 +61,7 @@ def lib(path=None):
             "fdtd_estimate_bytes": [vp, C.POINTER(C.c_uint64)],
             "fdtd_kernel_time": [vp, i32, C.POINTER(C.c_int64), C.POINTER(dbl)],
             "fdtd_kernel_cells": [vp, i32, C.POINTER(C.c_int64)],
+            "fdtd_set_tile": [vp, i32], "fdtd_get_tile": [vp, C.POINTER(i32)],
             "fdtd_launch_count": [vp, C.POINTER(C.c_int64)],
             "fdtd_set_stream": [vp, vp],
             "fdtd_transfer_bytes": [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
@@ -114,7 +115,7 @@ def device_count():
 class Job:
     """One simulation on the GPU, built from a ``JobSpec``."""
 
-    def __init__(self, spec, commit=True):
+    def __init__(self, spec, commit=True, tile=0):
         """Builds the job on the device.  With commit=False the set-up calls
         are made but nothing is allocated: the handle can then be handed to
         a Server (``detach``), which commits it when it admits the job."""
@@ -152,6 +153,8 @@ class Job:
             for p in spec.probes:
                 d = S.probe_struct(p)
                 check(L.fdtd_add_probe(self.h, C.byref(d), C.byref(mid)))
+            if tile:
+                check(L.fdtd_set_tile(self.h, int(tile)))
             if commit:
                 check(L.fdtd_commit(self.h))
         except Exception:
@@ -239,6 +242,11 @@ class Job:
         n, ms = C.c_int64(), C.c_double()
         check(lib().fdtd_kernel_time(self.h, int(kind), C.byref(n), C.byref(ms)))
         return n.value, ms.value
+
+    def tile(self):
+        t = C.c_int32()
+        check(lib().fdtd_get_tile(self.h, C.byref(t)))
+        return t.value
 
     def kernel_cells(self, kind):
         c = C.c_int64()

@@ -262,6 +262,14 @@ enum { FDTD_KERNEL_E = 0, FDTD_KERNEL_H = 1, FDTD_KERNEL_DFT = 2, FDTD_KERNEL_LI
        FDTD_KERNEL_EDGE = 4, FDTD_KERNEL_ADE = 5, FDTD_KERNEL_COUNT = 6 };
 int fdtd_profile(fdtd_job *job, int32_t enable);
 int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms);
+/* Block shape of the interior (core) kernels.  Before fdtd_commit, tile 0
+ * (the default) lets commit time the candidates on the job's own grid and
+ * keep the fastest (cached per kind of grid; environment FDTD_TUNE=0 skips
+ * the timing); 1..3 pins a candidate: 2D 128 / 256 / 512 threads per block,
+ * 3D 4 / 8 / 16 rows of 32 x-vectors.  Results do not depend on the shape.
+ * fdtd_get_tile returns the shape in use (0: the job has no core kernels). */
+int fdtd_set_tile(fdtd_job *job, int32_t tile);
+int fdtd_get_tile(const fdtd_job *job, int32_t *tile);
 /* Cells one launch of kernel class `kind` updates (FDTD_KERNEL_DFT: monitored
  * samples per fold), for the algorithmic bytes of a roofline. */
 int fdtd_kernel_cells(const fdtd_job *job, int32_t kind, int64_t *cells);

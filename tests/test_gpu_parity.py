@@ -229,3 +229,32 @@ def test_3d_graphene_sheet_vs_oracle(gpu, oracle_lib, prec):
         check_state(J, O, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ))
     else:
         assert err <= TOL32_DFT
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_core_block_shapes_give_identical_results(gpu, dim):
+    """Every candidate block shape of the interior kernels (pinned with
+    fdtd_set_tile) gives the same fields bit for bit; the commit-time tuner
+    picks one of them."""
+    if dim == 2:
+        spec, _ = problems.config_2d_tmz(precision=abi.F32, n=384, ncyl=8, nfreq=8)
+        comps, steps = (abi.EZ, abi.HX, abi.HY), 400
+    else:
+        spec, _ = problems.config_3d_sphere(precision=abi.F32, n=96, nfreq=4, npml=8, radius=40.0, half=20)
+        comps, steps = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ), 200
+    ref = None
+    for tile in (1, 2, 3):
+        J = gpu.Job(spec, tile=tile)
+        assert J.tile() == tile
+        J.step(1, steps)
+        got = [J.get_field(c) for c in comps]
+        if ref is None:
+            ref = got
+            assert any(np.abs(g).max() > 0 for g in got)
+        else:
+            for a, b in zip(ref, got):
+                np.testing.assert_array_equal(a, b)
+        J.close()
+    J = gpu.Job(spec)
+    assert J.tile() in (1, 2, 3)
+    J.close()
