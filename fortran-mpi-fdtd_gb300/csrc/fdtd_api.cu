@@ -1279,6 +1279,7 @@ int line_run(fdtd_job *J, int n_first, int n_steps, int stages) {
   p.mat = J->d_mat;
   p.mc = (const MatCoef<T> *)J->d_mc;
   p.ac = (const AdeCoef<T> *)J->d_ac;
+  p.nac = (int)(J->ac_host.size() / sizeof(AdeCoef<T>));
   p.nade = J->nade;
   p.ade_cell = J->d_ade_cell;
   p.ade_mat = J->d_ade_mat;

@@ -222,6 +222,7 @@ struct LineParams {
   const uint8_t *mat;
   const MatCoef<T> *mc;
   const AdeCoef<T> *ac;
+  int nac;                 // entries of ac
   int nade;
   const int *ade_cell;
   const uint8_t *ade_mat;
