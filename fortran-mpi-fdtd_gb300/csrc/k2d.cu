@@ -524,6 +524,8 @@ __device__ __forceinline__ void core_h(const StepParams<T> &p, int j, int i0) {
 // commit-time tuner times on the job's grid
 template <typename T, int L, int V, int NT>
 __global__ void __launch_bounds__(NT) e2d_core(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
+  pdl_release();
   const int t = blockIdx.x * NT + threadIdx.x;
   if (t >= p.ncore) return;
   core_e<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
@@ -531,16 +533,22 @@ __global__ void __launch_bounds__(NT) e2d_core(const __grid_constant__ StepParam
 
 template <typename T, int L, int V, int NT>
 __global__ void __launch_bounds__(NT) h2d_core(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
+  pdl_release();
   const int t = blockIdx.x * NT + threadIdx.x;
   if (t >= p.ncore) return;
   core_h<T, L, V>(p, p.cy0 + t / p.cw, (p.cv0 + t % p.cw) * V);
 }
 
+// The core kernels follow the previous core kernel on the job's stream with
+// a programmatic dependency, so their launch overlaps its drain (the edge and
+// dispersive-cell kernels, which run beside them, launch plainly: releasing
+// their successors early measured slower).
 template <typename T, int L, int V, int NT>
 void launch_core2(const StepParams<T> &p, bool e_half, cudaStream_t s) {
   const int blocks = (p.ncore + NT - 1) / NT;
-  if (e_half) e2d_core<T, L, V, NT><<<blocks, NT, 0, s>>>(p);
-  else h2d_core<T, L, V, NT><<<blocks, NT, 0, s>>>(p);
+  if (e_half) launch_pdl(e2d_core<T, L, V, NT>, blocks, NT, s, p);
+  else launch_pdl(h2d_core<T, L, V, NT>, blocks, NT, s, p);
 }
 
 // tile 0: 128 threads, 1: 256, 2: 512

@@ -494,6 +494,8 @@ __global__ void __launch_bounds__(256) h3d_kernel(const __grid_constant__ StepPa
 
 template <typename T, int V, int RY>
 __global__ void __launch_bounds__(32 * RY) e3d_core(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
+  pdl_release();
   const Core3<T, V, RY> u(p);
   if (!u.live) return;
   const long long c = u.c;
@@ -538,6 +540,8 @@ __global__ void __launch_bounds__(32 * RY) e3d_core(const __grid_constant__ Step
 
 template <typename T, int V, int RY>
 __global__ void __launch_bounds__(32 * RY) h3d_core(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
+  pdl_release();
   const Core3<T, V, RY> u(p);
   if (!u.live) return;
   const long long c = u.c;
@@ -572,8 +576,8 @@ __global__ void __launch_bounds__(32 * RY) h3d_core(const __grid_constant__ Step
 template <typename T, int V, int RY>
 void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s) {
   const int blocks = ((p.cw + 31) / 32) * ((p.ch + RY - 1) / RY) * p.cd;
-  if (e_half) e3d_core<T, V, RY><<<blocks, 32 * RY, 0, s>>>(p);
-  else h3d_core<T, V, RY><<<blocks, 32 * RY, 0, s>>>(p);
+  if (e_half) launch_pdl(e3d_core<T, V, RY>, blocks, 32 * RY, s, p);
+  else launch_pdl(h3d_core<T, V, RY>, blocks, 32 * RY, s, p);
 }
 
 // tile 0: 4 rows of 32 x-vectors, 1: 8 rows, 2: 16 rows

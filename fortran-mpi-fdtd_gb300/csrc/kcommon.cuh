@@ -11,6 +11,31 @@ namespace fdtd {
 template <typename T>
 constexpr bool kTwoParts = sizeof(T) == 8;
 
+// ---- programmatic dependent launch ----------------------------------------
+// A kernel launched with programmatic stream serialisation may be scheduled
+// while the kernel before it on its stream drains.  pdl_wait blocks until
+// that kernel has completed and its writes are visible (with no such
+// dependency it returns at once); pdl_release lets the next kernel on the
+// stream be scheduled, which then waits in its own pdl_wait.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// launch a step kernel with a programmatic dependency on the kernel before it
+// on the stream (the kernel starts with pdl_wait)
+template <typename K, typename P>
+inline void launch_pdl(K kernel, int blocks, int threads, cudaStream_t s, const P &p) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(threads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, p);
+}
+
 // ---- vector access of V consecutive cells along x ------------------------
 template <typename T, int V> struct VecOf;
 template <> struct VecOf<float, 1> { typedef float t; };
