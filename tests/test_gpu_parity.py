@@ -258,3 +258,48 @@ def test_core_block_shapes_give_identical_results(gpu, dim):
     J = gpu.Job(spec)
     assert J.tile() in (1, 2, 3)
     J.close()
+
+
+@pytest.mark.parametrize("dim", [1, 3])
+def test_per_procedure_path_equals_fused(gpu, dim):
+    """The reference's loop body through the per-procedure entry points
+    (update_DE, pml_update_E, interchange, update_H, pml_update_H, sample)
+    gives the fused fdtd_step's fields and spectra bit for bit: in 3D the
+    core and general launches split by role, in 1D the line kernel runs one
+    stage per call."""
+    if dim == 3:
+        spec, _ = problems.config_3d_sphere(precision=abi.F64, n=64, nfreq=4, npml=8, radius=40.0, half=12)
+        comps, steps = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ), 120
+    else:
+        spec, _ = problems.config_1d_gold(precision=abi.F64)
+        comps, steps = (abi.EX, abi.HZ), 400
+    a, b = gpu.Job(spec), gpu.Job(spec)
+    a.step(1, steps)
+    for n in range(1, steps + 1):
+        b.step_procedures(n)
+    for c in comps:
+        np.testing.assert_array_equal(a.get_field(c), b.get_field(c))
+    for q in range(len(spec.monitors)):
+        for x, y in zip(a.get_monitor(q), b.get_monitor(q)):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_footprint_estimate_bounds_the_commit(gpu):
+    """fdtd_estimate_bytes, which the server admits jobs by, is an upper
+    bound of what commit allocates."""
+    cases = [problems.config_2d_tmz(precision=abi.F32, n=384, ncyl=8, nfreq=24)[0],
+             problems.config_2d_tmz(precision=abi.F64, n=256, ncyl=4, nfreq=8, npml=16)[0],
+             problems.config_3d_sphere(precision=abi.F32, n=96, nfreq=8, npml=8, radius=40.0, half=20)[0],
+             problems.config_3d_sphere(precision=abi.F64, n=64, nfreq=4, npml=8, radius=40.0, half=12)[0],
+             problems.config_3d_graphene(precision=abi.F32, nxy=8, nz=384, nfreq=32)[0],
+             problems.config_1d_gold(precision=abi.F64)[0],
+             problems.reference_2d()[0]]
+    for spec in cases:
+        j = gpu.Job(spec, commit=False)
+        est = j.estimate_bytes()
+        j.close()
+        J = gpu.Job(spec)
+        held = J.device_bytes()
+        J.close()
+        assert held <= est, (spec.name, held, est)
+        assert est <= 4 * held + (4 << 20), (spec.name, held, est)
