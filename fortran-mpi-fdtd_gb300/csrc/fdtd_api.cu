@@ -73,7 +73,8 @@ struct MonRec {
   std::vector<double> omega;
   int ncomp;
   int comps[6];
-  long long ncell;
+  long long ncell;     // transformed samples per component (1 for a mean monitor)
+  long long boxcells;  // cells of the box
 };
 
 struct ProbeRec {
@@ -741,7 +742,7 @@ int commit_impl(fdtd_job *J) {
   long long base = 0, acc = 0;
   int foff = 0;
   std::vector<double> omega;
-  bool touches_slab = false;
+  bool touches_slab = false, has_mean = false;
   for (auto &M : J->mons) {
     Monitor m{};
     for (int a = 0; a < 3; ++a) { m.lo[a] = M.d.lo[a]; m.hi[a] = M.d.hi[a]; }
@@ -754,6 +755,9 @@ int commit_impl(fdtd_job *J) {
     m.nfreq = M.d.nfreq;
     m.acc = acc;
     m.freq_off = foff;
+    m.mean = M.d.reduce == FDTD_MONITOR_MEAN;
+    m.boxcells = (int)M.boxcells;
+    if (m.mean) has_mean = true;
     base += (long long)M.ncomp * M.ncell;
     acc += (long long)M.ncomp * M.d.nfreq * M.ncell;
     foff += M.d.nfreq;
@@ -766,7 +770,9 @@ int commit_impl(fdtd_job *J) {
   for (auto &P : J->probes)
     if (ref && J->dim == 3 && J->slab_rows > 0 && (P.d.cell[1] <= J->slab_rows - 1 || P.d.cell[1] >= ny - J->slab_rows))
       touches_slab = true;
-  J->gather_fused = J->dim == 2 || (J->dim == 1 && !touches_slab);  // 3D: stand-alone gather kernel
+  // 2D samples fused into the H edge rows unless a monitor reduces its box
+  // (the reduction runs in the stand-alone gather); 3D: stand-alone gather
+  J->gather_fused = (J->dim == 2 && !has_mean) || (J->dim == 1 && !touches_slab);
   if (J->dim == 2) {
     std::vector<uint8_t> rf((size_t)ny, 0);
     for (auto &sr : J->srcs) {
@@ -774,7 +780,8 @@ int commit_impl(fdtd_job *J) {
       for (int j = std::max(sr.lo[1], J->g.main_lo[1]); j <= std::min(sr.hi[1], J->g.main_hi[1]); ++j) rf[j] |= ROW_SRC;
     }
     for (auto &M : J->mons)
-      for (int j = M.d.lo[1]; j <= M.d.hi[1]; ++j) rf[j] |= ROW_SAMPLE;
+      if (M.d.reduce == FDTD_MONITOR_CELLS)
+        for (int j = M.d.lo[1]; j <= M.d.hi[1]; ++j) rf[j] |= ROW_SAMPLE;
     for (auto &P : J->probes) rf[P.d.cell[1]] |= ROW_SAMPLE;
     if (ref && J->slab_rows > 0)
       for (int j = 0; j < ny; ++j)
@@ -1180,8 +1187,7 @@ int sample_sep(fdtd_job *J, int n, int slot = -1, bool graph = false) {
   p.n = n;
   p.slot = slot >= 0 ? slot : J->stage_fill;
   p.d_base = graph ? J->d_base : nullptr;
-  launch_gather<T>(p, J->stream);
-  J->launches++;
+  J->launches += launch_gather<T>(p, J->stream);
   CK(cudaGetLastError());
   return FDTD_OK;
 }
@@ -1866,7 +1872,11 @@ int fdtd_add_monitor(fdtd_job *J, const fdtd_monitor_desc *m, int32_t *id) {
     if ((R.comps[u] >= FDTD_EX_INC) != (J->dim == 1 && R.comps[u] >= FDTD_EX_INC) ||
         (R.comps[u] >= FDTD_EX_INC && !J->has_tfsf))
       return set_err(FDTD_EINVAL, "component %d not available", R.comps[u]);
-  R.ncell = (long long)(m->hi[0] - m->lo[0] + 1) * (m->hi[1] - m->lo[1] + 1) * (m->hi[2] - m->lo[2] + 1);
+  if (m->reduce != FDTD_MONITOR_CELLS && m->reduce != FDTD_MONITOR_MEAN)
+    return set_err(FDTD_EINVAL, "monitor reduce must be FDTD_MONITOR_CELLS or FDTD_MONITOR_MEAN");
+  if (m->reduce == FDTD_MONITOR_MEAN && J->dim == 1) return set_err(FDTD_EINVAL, "mean monitors need a 2D or 3D job");
+  R.boxcells = (long long)(m->hi[0] - m->lo[0] + 1) * (m->hi[1] - m->lo[1] + 1) * (m->hi[2] - m->lo[2] + 1);
+  R.ncell = m->reduce == FDTD_MONITOR_MEAN ? 1 : R.boxcells;
   J->mons.push_back(R);
   if (id) *id = (int32_t)J->mons.size() - 1;
   return FDTD_OK;

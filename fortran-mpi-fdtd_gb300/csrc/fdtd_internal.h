@@ -72,6 +72,8 @@ struct Monitor {
   int nfreq;
   long long acc;           // offset of this monitor's accumulators
   int freq_off;            // offset into the omega table
+  int mean;                // 1: one sample per component, the box mean
+  int boxcells;            // cells of the box
 };
 
 struct Probe {
@@ -193,7 +195,8 @@ template <typename T> int launch_e3d(const StepParams<T> &p, int part, void *str
 template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *stream);
 
 // separate gather (per-procedure API, or monitors inside reference slabs)
-template <typename T> void launch_gather(const StepParams<T> &p, void *stream);
+// returns the kernels launched
+template <typename T> int launch_gather(const StepParams<T> &p, void *stream);
 
 // DFT fold: acc += sum over valid ring slots of e^{i w t} * sample * dt
 struct DftParams {

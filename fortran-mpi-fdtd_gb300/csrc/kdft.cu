@@ -95,6 +95,7 @@ __global__ void gather_kernel(const __grid_constant__ StepParams<T> p) {
     const Monitor &m = p.mon[q];
     const long long ns = (long long)m.ncomp * m.ncell;
     if (t < ns) {
+      if (m.mean) return;  // the mean kernel writes these samples
       const int u = (int)(t / m.ncell);
       const long long c = t % m.ncell;
       const int wx = m.hi[0] - m.lo[0] + 1, wy = m.hi[1] - m.lo[1] + 1;
@@ -121,17 +122,66 @@ __global__ void gather_kernel(const __grid_constant__ StepParams<T> p) {
   }
 }
 
+// Mean monitors: one block per (monitor, component) sums the box in FP64 --
+// each thread a strided subset in order, then a warp-shuffle tree and the
+// warps' partial sums in order, so the result does not depend on timing --
+// and stages the mean as the component's one sample.
+constexpr int kMeanThreads = 256;
+
 template <typename T>
-void launch_gather(const StepParams<T> &p, void *stream) {
-  long long total = p.nprobe;
-  for (int q = 0; q < p.nmon; ++q) total += (long long)p.mon[q].ncomp * p.mon[q].ncell;
-  if (total <= 0) return;
-  const int threads = 256;
-  const long long blocks = (total + threads - 1) / threads;
-  gather_kernel<T><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(p);
+__global__ void __launch_bounds__(kMeanThreads) gather_mean_kernel(const __grid_constant__ StepParams<T> p) {
+  __shared__ double part[kMeanThreads / 32];
+  int b = blockIdx.x, q = 0;
+  for (; q < p.nmon; ++q) {
+    if (!p.mon[q].mean) continue;
+    if (b < p.mon[q].ncomp) break;
+    b -= p.mon[q].ncomp;
+  }
+  if (q >= p.nmon) return;  // uniform over the block
+  const Monitor &m = p.mon[q];
+  const T *F[6] = {p.ex, p.ey, p.ez, p.hx, p.hy, p.hz};
+  const T *f = F[m.comps[b]];
+  const int wx = m.hi[0] - m.lo[0] + 1, wy = m.hi[1] - m.lo[1] + 1;
+  double sum = 0.0;
+  if (f)
+    for (int c = threadIdx.x; c < m.boxcells; c += kMeanThreads) {
+      const int i = m.lo[0] + c % wx, j = m.lo[1] + (c / wx) % wy, k = m.lo[2] + c / (wx * wy);
+      sum += (double)f[(long long)i + (long long)p.nx * (j + (long long)p.ny * k)];
+    }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < kMeanThreads / 32; ++w) tot += part[w];
+    p.stage[(long long)p.slot * p.stage_row + m.base + b] = T(tot / (double)m.boxcells);
+  }
 }
 
-template void launch_gather<float>(const StepParams<float> &, void *);
-template void launch_gather<double>(const StepParams<double> &, void *);
+template <typename T>
+int launch_gather(const StepParams<T> &p, void *stream) {
+  long long total = p.nprobe;
+  int nmean = 0;
+  for (int q = 0; q < p.nmon; ++q) {
+    total += (long long)p.mon[q].ncomp * p.mon[q].ncell;
+    if (p.mon[q].mean) nmean += p.mon[q].ncomp;
+  }
+  int launched = 0;
+  if (total > 0) {
+    const int threads = 256;
+    const long long blocks = (total + threads - 1) / threads;
+    gather_kernel<T><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(p);
+    ++launched;
+  }
+  if (nmean > 0) {
+    gather_mean_kernel<T><<<nmean, kMeanThreads, 0, (cudaStream_t)stream>>>(p);
+    ++launched;
+  }
+  return launched;
+}
+
+template int launch_gather<float>(const StepParams<float> &, void *);
+template int launch_gather<double>(const StepParams<double> &, void *);
 
 }  // namespace fdtd

@@ -52,7 +52,7 @@ class SourceDesc(C.Structure):
 class MonitorDesc(C.Structure):
     _fields_ = [("lo", I3), ("hi", I3), ("comp_mask", C.c_int32),
                 ("n_first", C.c_int32), ("n_last", C.c_int32), ("nfreq", C.c_int32),
-                ("omega", C.POINTER(C.c_double))]
+                ("omega", C.POINTER(C.c_double)), ("reduce", C.c_int32)]
 
 
 class ProbeDesc(C.Structure):
@@ -76,3 +76,5 @@ class ServerStatus(C.Structure):
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
+
+MONITOR_CELLS, MONITOR_MEAN = 0, 1

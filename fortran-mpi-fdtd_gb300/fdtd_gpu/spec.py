@@ -32,6 +32,7 @@ class Monitor:
     omega: np.ndarray
     n_first: int = 1
     n_last: int = 2 ** 31 - 1
+    mean: bool = False  # transform the box mean of each component
 
 
 @dataclass
@@ -74,10 +75,10 @@ class JobSpec:
         self.materials.append(Material("graphene", region, params=dict(params)))
         return len(self.materials)
 
-    def add_monitor(self, lo, hi, comps, omega, n_first=1, n_last=2 ** 31 - 1):
+    def add_monitor(self, lo, hi, comps, omega, n_first=1, n_last=2 ** 31 - 1, mean=False):
         self.monitors.append(Monitor(tuple(lo), tuple(hi), tuple(comps),
                                      np.ascontiguousarray(omega, dtype=np.float64),
-                                     int(n_first), int(n_last)))
+                                     int(n_first), int(n_last), bool(mean)))
         return len(self.monitors) - 1
 
     def add_probe(self, cell, comps, n_first=1, n_last=2 ** 31 - 1):
@@ -184,7 +185,8 @@ def comp_mask(comps):
 def monitor_struct(m, keep):
     keep.append(m.omega)
     return abi.MonitorDesc(abi.I3(*m.lo), abi.I3(*m.hi), comp_mask(m.comps), m.n_first, m.n_last,
-                           len(m.omega), m.omega.ctypes.data_as(C.POINTER(C.c_double)))
+                           len(m.omega), m.omega.ctypes.data_as(C.POINTER(C.c_double)),
+                           abi.MONITOR_MEAN if m.mean else abi.MONITOR_CELLS)
 
 
 def probe_struct(p):
@@ -198,5 +200,5 @@ def tfsf_struct(t):
 def monitor_shape(m):
     ncell = 1
     for a in range(3):
-        ncell *= m.hi[a] - m.lo[a] + 1
+        ncell *= 1 if m.mean else m.hi[a] - m.lo[a] + 1
     return len(sorted(set(m.comps))), len(m.omega), ncell

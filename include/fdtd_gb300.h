@@ -159,7 +159,12 @@ typedef struct fdtd_monitor_desc {
   int32_t n_first, n_last;
   int32_t nfreq;
   const double *omega;   /* nfreq angular frequencies (arg(m))             */
+  int32_t reduce;        /* FDTD_MONITOR_CELLS: every cell of the box;
+                            FDTD_MONITOR_MEAN (2D/3D): the box mean of each
+                            component, one value per component and
+                            frequency (the DFT of a plane-averaged field)  */
 } fdtd_monitor_desc;
+enum { FDTD_MONITOR_CELLS = 0, FDTD_MONITOR_MEAN = 1 };
 
 /* Per-step samples at one cell (the r*infld/rfld/tfld time series,
  * 2D/.../program.f90:376-419). */
@@ -239,7 +244,8 @@ int fdtd_sync(fdtd_job *job);
 int fdtd_get_field(fdtd_job *job, int32_t comp, double *host);
 int fdtd_set_field(fdtd_job *job, int32_t comp, const double *host);
 /* DFT sums: for each transformed component (ascending component code), for
- * each frequency, for each cell of the box (x fastest): re[], im[]. */
+ * each frequency, for each cell of the box (x fastest; one value for a
+ * FDTD_MONITOR_MEAN monitor): re[], im[]. */
 int fdtd_get_monitor(fdtd_job *job, int32_t id, double *re, double *im);
 /* Samples of steps n_first..min(n_last, last stepped n): for each step the
  * selected components in ascending code order.  *count = steps returned. */

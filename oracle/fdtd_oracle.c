@@ -356,7 +356,10 @@ int ora_add_monitor(ora_job *J, const fdtd_monitor_desc *m) {
   M->omega = (double *)malloc(sizeof(double) * (size_t)m->nfreq);
   memcpy(M->omega, m->omega, sizeof(double) * (size_t)m->nfreq);
   M->d.omega = M->omega;
-  M->ncell = (int64_t)(m->hi[0] - m->lo[0] + 1) * (m->hi[1] - m->lo[1] + 1) * (m->hi[2] - m->lo[2] + 1);
+  if (m->reduce != FDTD_MONITOR_CELLS && m->reduce != FDTD_MONITOR_MEAN) FAIL("bad monitor reduce mode");
+  M->ncell = m->reduce == FDTD_MONITOR_MEAN
+                 ? 1
+                 : (int64_t)(m->hi[0] - m->lo[0] + 1) * (m->hi[1] - m->lo[1] + 1) * (m->hi[2] - m->lo[2] + 1);
   size_t n = (size_t)M->ncomp * M->nfreq * M->ncell;
   M->re = (double *)calloc(n, sizeof(double));
   M->im = (double *)calloc(n, sizeof(double));
@@ -1205,6 +1208,26 @@ static void sample(ora_job *J, int n, int nth) {
     if (n < M->d.n_first || n > M->d.n_last) continue;
     const int *lo = M->d.lo, *hi = M->d.hi;
     int wx = hi[0] - lo[0] + 1, wy = hi[1] - lo[1] + 1;
+    if (M->d.reduce == FDTD_MONITOR_MEAN) {
+      /* the DFT of the box mean of each component (the plane-averaged
+         transmitted field of a laterally uniform problem) */
+      const int64_t cnt = (int64_t)wx * wy * (hi[2] - lo[2] + 1);
+      for (int u = 0; u < M->ncomp; u++) {
+        const double *F = comp_ptr(J, M->comps[u]);
+        double sum = 0.0;
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) sum += F[cell_ix(J, i, j, k)];
+        const double f = sum / (double)cnt;
+        for (int m = 0; m < M->nfreq; m++) {
+          const double cs = cos(M->omega[m] * t), sn = sin(M->omega[m] * t);
+          double *re = M->re + (size_t)u * M->nfreq + m, *im = M->im + (size_t)u * M->nfreq + m;
+          *re = *re + cs * f * dt;
+          *im = *im + sn * f * dt;
+        }
+      }
+      continue;
+    }
 #pragma omp parallel for num_threads(nth) schedule(static) if (nth > 1)
     for (int m = 0; m < M->nfreq; m++) {
       /* dcos(arg(m)*t) is the same for every cell of the plane */

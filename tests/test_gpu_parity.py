@@ -303,3 +303,27 @@ def test_footprint_estimate_bounds_the_commit(gpu):
         J.close()
         assert held <= est, (spec.name, held, est)
         assert est <= 4 * held + (4 << 20), (spec.name, held, est)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mean_monitor_is_the_mean_of_the_cell_spectra(gpu, dim):
+    """A FDTD_MONITOR_MEAN monitor transforms the box mean of each
+    component; by linearity its spectrum equals the mean over the box of a
+    per-cell monitor's spectra on the same box (FP64)."""
+    if dim == 2:
+        spec, meta = problems.config_2d_tmz(precision=abi.F64, n=256, ncyl=4, nfreq=8, npml=16)
+        mon = spec.monitors[2]
+        steps = 600
+    else:
+        spec, meta = problems.config_3d_sphere(precision=abi.F64, n=64, nfreq=4, npml=8, radius=40.0, half=12)
+        mon = spec.monitors[5]
+        steps = 200
+    spec.add_monitor(mon.lo, mon.hi, mon.comps, mon.omega, mon.n_first, mon.n_last, mean=True)
+    J = gpu.Job(spec)
+    J.step(1, steps)
+    cre, cim = J.get_monitor(spec.monitors.index(mon))
+    mre, mim = J.get_monitor(len(spec.monitors) - 1)
+    assert mre.shape == (cre.shape[0], cre.shape[1], 1)
+    assert np.linalg.norm(cre) > 0
+    for a, b in ((mre[..., 0], cre.mean(axis=2)), (mim[..., 0], cim.mean(axis=2))):
+        assert rel_l2(a, b) <= 1e-12
