@@ -1,0 +1,131 @@
+"""The reference 2D program's output files, written from a run of the engine.
+
+The reference's post-processing -- transforms/calR_Sy.f90, which reads the
+Sy spectra and writes RTA_2Dfdtd.data, and the gnuplot scripts that read the
+frame files -- reads per-rank text files named after the MPI rank that held
+each line or point (2D/.../program.f90:296-320, 370-470, 477-530).  The
+engine runs the whole domain at once; ``write_reference_2d`` splits its
+results by the reference's row decomposition and writes the same files, in
+the same record layout, so those tools run unchanged:
+
+  transforms/r<k>infld.dat, r<k>rfld.dat, r<k>tfld.dat   per-step probes
+  transforms/r<k>Syin.dat, r<k>Syr.dat, r<k>Syt.dat       Sy per wavelength
+  transforms/r<k>tf_r.dat                                 per-x products
+  timesLiney/r<k>E_time<f>.dat                            Ex, Hz along x=ic
+  timesGnuplotmap/r<k>E_time<f>.dat                       Hz maps
+
+Free-format records use a full-precision exponent form that Fortran
+list-directed input reads; the fixed-format records follow the reference's
+edit descriptors (E30.19, F30.19, F15.5, E20.10).
+"""
+import math
+import os
+
+import numpy as np
+
+from . import problems
+
+NANO = 1e-9
+
+
+def fortran_e(x, w, d):
+    """Fortran Ew.d: 0.<d digits>E+xx (three-digit exponents drop the E)."""
+    if x == 0.0 or not math.isfinite(x):
+        body, exp = "0." + "0" * d, 0
+    else:
+        s = f"{abs(x):.{d - 1}e}"           # d significant digits, rounded once
+        mant, e = s.split("e")
+        body = "0." + mant.replace(".", "")
+        exp = int(e) + 1
+    ex = f"E{exp:+03d}" if abs(exp) < 100 else f"{exp:+04d}"
+    s = ("-" if x < 0 else "") + body + ex
+    return s.rjust(w)
+
+
+def fortran_f(x, w, d):
+    """Fortran Fw.d."""
+    return f"{x:{w}.{d}f}"
+
+
+def free(*vals):
+    """One list-directed record: every value with 17 significant digits."""
+    return " ".join(f"{v: .17E}" for v in vals)
+
+
+def rank_rows(ny, nranks):
+    """Global 0-based row ranges [a, b) of each rank (rows split evenly, the
+    remainder to the first ranks, as the reference's set_index does)."""
+    base, extra = divmod(ny, nranks)
+    out, a = [], 0
+    for r in range(nranks):
+        b = a + base + (1 if r < extra else 0)
+        out.append((a, b))
+        a = b
+    return out
+
+
+def owner(rows, j):
+    return next(r for r, (a, b) in enumerate(rows) if a <= j < b)
+
+
+def write_reference_2d(outdir, meta, monitors, probes, frames, nranks=3):
+    """Writes the reference 2D program's files under ``outdir``.
+
+    meta      the meta dict of ``problems.reference_2d()``
+    monitors  [(re, im)] of its three monitors (incident, reflected,
+              transmitted), each of shape (2, nfreq, nx) for (Ex, Hz)
+    probes    [samples] of its three probes, each (steps, 2) for (Ex, Hz),
+              starting at the probe's first step
+    frames    {frame: (ex, hz)} full 2D fields (ny, nx) at step frame*dn
+    """
+    ds, dt = meta["ds"], meta["dt"]
+    ny, nx = meta["ny"], meta["nx"]
+    rows = rank_rows(ny, nranks)
+    tr = os.path.join(outdir, "transforms")
+    os.makedirs(tr, exist_ok=True)
+    os.makedirs(os.path.join(outdir, "timesLiney"), exist_ok=True)
+    os.makedirs(os.path.join(outdir, "timesGnuplotmap"), exist_ok=True)
+    pts = meta["probe_cells"]  # [(i, j)] 0-based: incident, reflected, transmitted
+    firsts = meta["probe_first"]
+
+    # ---- per-step probes (program.f90:376-378, 397-399, 417-419) ----
+    for q, name in enumerate(("infld", "rfld", "tfld")):
+        i, j = pts[q]
+        k = owner(rows, j)
+        with open(os.path.join(tr, f"r{k}{name}.dat"), "w") as fh:
+            for s, (e, h) in enumerate(probes[q]):
+                n = firsts[q] + s
+                if name == "infld":
+                    fh.write(free(n * dt, e, h) + "\n")
+                else:  # '(E30.19,4F30.19)'
+                    fh.write(fortran_e(n * dt, 30, 19) + fortran_f(e, 30, 19) + fortran_f(h, 30, 19) + "\n")
+
+    # ---- spectra (program.f90:477-530) ----
+    lam = 2.0 * math.pi * problems.C0 / np.asarray(meta["arg"]) / NANO
+    sy = [problems.poynting_2d_te(re, im, ds) for re, im in monitors]
+    for q, name in enumerate(("Syin", "Syr", "Syt")):
+        k = owner(rows, pts[q][1])
+        with open(os.path.join(tr, f"r{k}{name}.dat"), "w") as fh:
+            for m in range(len(lam)):
+                fh.write(free(lam[m], sy[q][m]) + "\n")
+    k = owner(rows, pts[1][1])
+    re, im = monitors[1]
+    with open(os.path.join(tr, f"r{k}tf_r.dat"), "w") as fh:  # '(2F15.5,2E20.10)' per x, blank per m
+        for m in range(len(lam)):
+            for i in range(nx):
+                fh.write(fortran_f(lam[m], 15, 5) + fortran_f((i + 1) * ds / NANO, 15, 5) +
+                         fortran_e(re[0, m, i] * re[1, m, i], 20, 10) + fortran_e(im[1, m, i] * im[0, m, i], 20, 10) + "\n")
+            fh.write("\n")
+
+    # ---- frames (program.f90:436-469) ----
+    ic = meta["ic"] - 1
+    for f, (ex, hz) in frames.items():
+        for k, (a, b) in enumerate(rows):
+            with open(os.path.join(outdir, "timesLiney", f"r{k}E_time{f}.dat"), "w") as fh:
+                for j in range(a, b):
+                    fh.write(free((j + 1) * ds / NANO, ex[j, ic], hz[j, ic]) + "\n")
+            with open(os.path.join(outdir, "timesGnuplotmap", f"r{k}E_time{f}.dat"), "w") as fh:
+                for j in range(a, b):
+                    for i in range(nx):
+                        fh.write(free(float(i + 1), float(j + 1), hz[j, i]) + "\n")
+                    fh.write("\n")

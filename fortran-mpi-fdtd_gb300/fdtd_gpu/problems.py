@@ -155,7 +155,9 @@ def reference_2d(precision=abi.F64):
     spec.add_probe((ptinx - 1, ptiny - 1, 0), (abi.EX, abi.HZ), tfinStop + 1, 2 ** 31 - 1)
     spec.add_probe((ptinx - 1, ptty - 1, 0), (abi.EX, abi.HZ), 1, 2 ** 31 - 1)
     meta = dict(sigmam=sigmam, dt=dt, ds=ds, Nt=Nt, dn=dn, tfinStop=tfinStop, ic=ic, n_y=n_y,
-                ptty=ptty, arg=arg, au=au, air=air, sio2=sio2, si=si, nx=nx, ny=ny)
+                ptty=ptty, arg=arg, au=au, air=air, sio2=sio2, si=si, nx=nx, ny=ny,
+                probe_cells=[(ptinx - 1, ptiny - 1), (ptinx - 1, ptiny - 1), (ptinx - 1, ptty - 1)],
+                probe_first=[1, tfinStop + 1, 1])
     return spec, meta
 
 

@@ -61,7 +61,7 @@ def run2d_gpu(gpu):
     J = gpu.Job(spec)
     ic = meta["ic"] - 1
     liney = np.zeros((20, meta["ny"], 2))
-    maps = {}
+    maps, frames = {}, {}
     n = 0
     for f in range(1, 21):
         target = f * meta["dn"]
@@ -71,10 +71,11 @@ def run2d_gpu(gpu):
         hz = J.get_field(abi.HZ)[0]
         liney[f - 1, :, 0] = ex[:, ic]
         liney[f - 1, :, 1] = hz[:, ic]
+        frames[f] = (ex.copy(), hz.copy())
         if f in (1, 20):
             maps[f] = hz.copy()
     J.step(n + 1, meta["Nt"] - n)
-    out = dict(meta=meta, liney=liney, maps=maps, job=J)
+    out = dict(meta=meta, liney=liney, maps=maps, frames=frames, job=J)
     out["mon"] = [J.get_monitor(q) for q in range(3)]
     out["probe"] = [J.get_probe(q) for q in range(3)]
     return out
@@ -100,6 +101,38 @@ def test_2d_reference_fields_match_shipped_outputs(run2d_gpu):
     assert rel_l2(run2d_gpu["probe"][0], g["infld"][:, 1:]) <= TOL64
     assert rel_l2(run2d_gpu["probe"][2], g["tfld"][:, 1:]) <= TOL64
     assert rel_l2(run2d_gpu["probe"][1], g["rfld"][:, 1:]) <= 1e-9  # F30.19 print precision
+
+
+def test_2d_reference_output_files_match_shipped_files(run2d_gpu, tmp_path):
+    """The reference program's per-rank output files, written from the GPU
+    run by fdtd_gpu.outputs and read back with the same parser that read the
+    reference's shipped files, hold the shipped values."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden_2d import load_table
+    from fdtd_gpu import outputs
+    r = run2d_gpu
+    probes = [p[:, :2] for p in r["probe"]]
+    outputs.write_reference_2d(str(tmp_path), r["meta"], r["mon"], probes, r["frames"])
+    g = golden()
+    tr = tmp_path / "transforms"
+    for key, fn in (("syin", "r0Syin.dat"), ("syr", "r0Syr.dat"), ("syt", "r2Syt.dat")):
+        t = load_table(str(tr / fn))
+        assert rel_l2(t[:, 1], g[key][:, 1]) <= TOL64, key
+        np.testing.assert_allclose(t[:, 0], g[key][:, 0], rtol=1e-12)
+    assert rel_l2(load_table(str(tr / "r0infld.dat")), g["infld"]) <= TOL64
+    assert rel_l2(load_table(str(tr / "r2tfld.dat")), g["tfld"]) <= TOL64
+    assert rel_l2(load_table(str(tr / "r0rfld.dat")), g["rfld"]) <= 1e-9
+    np.testing.assert_allclose(load_table(str(tr / "r0tf_r.dat")), g["tf_r"], rtol=5.01e-10, atol=1e-30)
+    for f in (1, 7, 20):
+        parts = [load_table(str(tmp_path / "timesLiney" / f"r{k}E_time{f}.dat")) for k in range(3)]
+        assert rel_l2(np.concatenate(parts)[:, 1:], g["liney"][f - 1]) <= TOL64
+    for q, f in enumerate(g["map_frames"]):
+        m = np.zeros_like(g["maps"][q])
+        for k in range(3):
+            t = load_table(str(tmp_path / "timesGnuplotmap" / f"r{k}E_time{int(f)}.dat"))
+            m[t[:, 1].astype(int) - 1, t[:, 0].astype(int) - 1] = t[:, 2]
+        assert rel_l2(m, g["maps"][q]) <= TOL64
 
 
 def test_2d_per_procedure_path_equals_fused(gpu):
