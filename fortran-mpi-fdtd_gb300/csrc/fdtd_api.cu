@@ -63,6 +63,7 @@ struct MatRec {
   double eps;
   fdtd_drude2cp gold;
   fdtd_graphene_desc gr;
+  fdtd_lorentz_desc lz;
   fdtd_region region;
   std::vector<double> centers;
   std::vector<uint8_t> mask;
@@ -492,7 +493,7 @@ int commit_impl(fdtd_job *J) {
   std::vector<int> mid(J->mats.size());
   int ndiel = 0, nadem = 0;
   for (size_t m = 0; m < J->mats.size(); ++m) {
-    const bool ade = J->mats[m].kind == MK_GOLD || J->mats[m].kind == MK_GRAPHENE;
+    const bool ade = is_ade_kind(J->mats[m].kind);
     mid[m] = ade ? kAdeId + nadem++ : 1 + ndiel++;
     if (ndiel >= kAdeId || nadem > 255 - kAdeId) return set_err(FDTD_ERANGE, "too many materials of one kind");
   }
@@ -607,6 +608,32 @@ int commit_impl(fdtd_job *J) {
       c.ca = T(Ku);
       c.cs = T(1);
       ac.push_back(a);
+    } else if (R.kind == MK_LORENTZ) {
+      // Both reference codings reduce to one recursion in p = c0 P (JP) = S
+      // (si_mod) and v = p(n) - p(n-1):
+      //   JP (3D/goldLorentzJp_mod.f90:140-161): gamma1L = 1 - lv,
+      //     gamma2L dt = ls, xi1 gamma2L dt = le;  c0 dt Jp = v
+      //   S (3D/si_mod.f90:180-206): ga_l + gb_l = 1 - ls, -gb_l = 1 - lv,
+      //     gc_l = le;  S(n) - S(n-1) = v
+      // and E(n+1) = E(n) + (1/eps_inf) (Ku curl + source - sum_l v_l), the
+      // E-form of update_EJp, since ds Ku sum_l Jp_l = sum_l v_l.
+      const fdtd_lorentz_desc &p = R.lz;
+      AdeCoef<T> a{};
+      a.kind = MK_LORENTZ;
+      a.normal = -1;
+      a.ga = T(1.0 / p.eps_inf);
+      a.npoles = p.npoles;
+      for (int l = 0; l < kMaxPoles; ++l) {
+        if (l >= p.npoles) { a.lv[l] = a.ls[l] = a.le[l] = T(0); continue; }
+        const double w = p.omega[l], nu = p.gamma[l], den = 1.0 + nu * dt;
+        a.lv[l] = T(2.0 * nu * dt / den);
+        a.ls[l] = T((w * dt) * (w * dt) / den);
+        a.le[l] = T(p.delta_eps[l] * ((w * dt) * (w * dt) / den));
+      }
+      c.ade = (int)ac.size();
+      c.ca = T(Ku);
+      c.cs = T(1);
+      ac.push_back(a);
     }
   }
   if ((rc = alloc_dev(J, (void **)&J->d_mat, (size_t)N))) return rc;
@@ -631,7 +658,7 @@ int commit_impl(fdtd_job *J) {
   std::vector<uint8_t> ade_mat;
   for (long long c = 0; c < N; ++c) {
     const uint8_t id = mat[(size_t)c];
-    if (!id || (mc[id].kind != MK_GOLD && mc[id].kind != MK_GRAPHENE)) continue;
+    if (!id || !is_ade_kind(mc[id].kind)) continue;
     const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((long long)nx * ny));
     if (in_shell(i, j, k)) continue;
     if (!(i >= J->g.main_lo[0] && i <= J->g.main_hi[0] && j >= J->g.main_lo[1] && j <= J->g.main_hi[1] &&
@@ -1809,6 +1836,18 @@ int fdtd_add_graphene(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_des
   return add_mat(J, r, m, id);
 }
 
+int fdtd_add_lorentz(fdtd_job *J, const fdtd_region *r, const fdtd_lorentz_desc *p, int32_t *id) {
+  if (!p) return set_err(FDTD_EINVAL, "null Lorentz parameters");
+  if (p->form != FDTD_LORENTZ_JP && p->form != FDTD_LORENTZ_S) return set_err(FDTD_EINVAL, "bad Lorentz form %d", p->form);
+  if (p->npoles < 1 || p->npoles > FDTD_LORENTZ_MAX_POLES)
+    return set_err(FDTD_EINVAL, "npoles %d outside 1..%d", p->npoles, FDTD_LORENTZ_MAX_POLES);
+  if (!(p->eps_inf != 0.0) || !std::isfinite(p->eps_inf)) return set_err(FDTD_EINVAL, "eps_inf must be finite and nonzero");
+  MatRec m{};
+  m.kind = MK_LORENTZ;
+  m.lz = *p;
+  return add_mat(J, r, m, id);
+}
+
 int fdtd_add_pml(fdtd_job *J, const fdtd_pml_desc *p) {
   int rc = check_job(J, false);
   if (rc) return rc;
@@ -2012,7 +2051,7 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
   // dispersive cells: each region's cells, bounded per sphere / box
   uint64_t nade = 0;
   for (auto &m : J->mats) {
-    if (m.kind != MK_GOLD && m.kind != MK_GRAPHENE) continue;
+    if (!is_ade_kind(m.kind)) continue;
     if (m.region.kind == FDTD_REGION_MASK) {
       for (uint8_t v : m.mask) nade += v != 0;
     } else if (m.region.kind == FDTD_REGION_SPHERES) {

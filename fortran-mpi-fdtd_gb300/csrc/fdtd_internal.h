@@ -30,7 +30,9 @@ constexpr int kMaxMon = 16;
 constexpr int kMaxProbe = 16;
 constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
 
-enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3 };
+enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3, MK_LORENTZ = 4 };
+constexpr int kMaxPoles = FDTD_LORENTZ_MAX_POLES;
+__host__ __device__ constexpr bool is_ade_kind(int k) { return k == MK_GOLD || k == MK_GRAPHENE || k == MK_LORENTZ; }
 
 // per material id, in the job's precision
 template <typename T>
@@ -55,6 +57,11 @@ struct AdeCoef {
   T wr, wi;                // 1/ga (E = Re(num * (wr + i wi)))
   T r0, rv, rs, kerr, ga;  // graphene Raman in velocity form: V = rv*V + rs*SR + r0*E^2,
                            // SR += V (rv = 1-(1+r2), rs = (r1-2)+(1+r2)); Kerr; eps
+                           // (Lorentz: ga = 1/eps_inf)
+  int npoles;              // Lorentz: per pole l, with p = c0 P and v = p(n)-p(n-1):
+  T lv[kMaxPoles];         //   v += -lv v + (le E - ls p);  p += v
+  T ls[kMaxPoles];         //   lv = 2 nu dt/(1+nu dt), ls = (w dt)^2/(1+nu dt),
+  T le[kMaxPoles];         //   le = deps ls
 };
 
 struct Source {
@@ -172,8 +179,9 @@ enum Role : int {
 };
 
 // ADE state layout: state[(f*3 + comp)*stride + slot] with fields
-// 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:S_R 3:V = S_R(n)-S_R(n-1))
-constexpr int kAdeFields = 6;
+// 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:S_R 3:V = S_R(n)-S_R(n-1);
+// Lorentz: 2l: p_l, 2l+1: v_l for pole l < kMaxPoles)
+constexpr int kAdeFields = 2 * kMaxPoles;
 
 // launchers (defined in k2d.cu / k3d.cu / k1d.cu / kdft.cu)
 // 2D half steps: the parts of one half step are independent launches

@@ -174,6 +174,8 @@ __device__ __forceinline__ bool sample_row(const StepParams<T> &p, int j, int k)
 // Graphene sheet (1D/graphene633_mod.f90:33-41, 3D/graphene_mod.f90:70-76):
 //   E = (Q + ha S + 2 kerr E^3) / (ga + S_R + 3 kerr E^2) with the Raman
 //   recursion S_R(n) = r1 S_R(n-1) + r2 S_R(n-2) + r0 E^2 in velocity form.
+// Lorentz poles (3D/goldLorentzJp_mod.f90:60-86, 3D/si_mod.f90:55-60):
+//   E += ga (inc - sum_l v_l);  v_l += -lv v_l + (le E - ls p_l);  p_l += v_l
 template <typename T>
 __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int comp, const AdeCoef<T> &a,
                                                T inc, T eold) {
@@ -181,6 +183,28 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
   T *s_ = st + (1 * 3 + comp) * (long long)stride + slot;
   T *f2 = st + (2 * 3 + comp) * (long long)stride + slot;
   T *f3 = st + (3 * 3 + comp) * (long long)stride + slot;
+  if (a.kind == MK_LORENTZ) {
+    T pl[kMaxPoles], vl[kMaxPoles];
+    T sv = T(0);
+#pragma unroll
+    for (int l = 0; l < kMaxPoles; ++l) {
+      if (l < a.npoles) {
+        pl[l] = st[(2 * l * 3 + comp) * (long long)stride + slot];
+        vl[l] = st[((2 * l + 1) * 3 + comp) * (long long)stride + slot];
+        sv += vl[l];
+      }
+    }
+    const T e = eold + a.ga * (inc - sv);
+#pragma unroll
+    for (int l = 0; l < kMaxPoles; ++l) {
+      if (l < a.npoles) {
+        const T nv = vl[l] + ((a.le[l] * e - a.ls[l] * pl[l]) - a.lv[l] * vl[l]);
+        st[((2 * l + 1) * 3 + comp) * (long long)stride + slot] = nv;
+        st[(2 * l * 3 + comp) * (long long)stride + slot] = pl[l] + nv;
+      }
+    }
+    return e;
+  }
   T Q = *q_ + inc;
   T S = *s_;
   if (a.kind == MK_GOLD) {

@@ -38,6 +38,16 @@ class GrapheneDesc(C.Structure):
                 ("raman_tau", C.c_double), ("thickness", C.c_double), ("e_scale", C.c_double)]
 
 
+LORENTZ_JP, LORENTZ_S = 0, 1
+LORENTZ_MAX_POLES = 4
+
+
+class LorentzDesc(C.Structure):
+    _fields_ = [("form", C.c_int32), ("npoles", C.c_int32), ("eps_inf", C.c_double),
+                ("delta_eps", C.c_double * LORENTZ_MAX_POLES), ("omega", C.c_double * LORENTZ_MAX_POLES),
+                ("gamma", C.c_double * LORENTZ_MAX_POLES)]
+
+
 class PmlDesc(C.Structure):
     _fields_ = [("mode", C.c_int32), ("npml", (C.c_int32 * 2) * 3),
                 ("eps_lo", C.c_double), ("eps_hi", C.c_double),

@@ -36,6 +36,57 @@ GOLD_REFERENCE = dict(eps_inf=1.1431, omega_d=1.3202e16, gamma_d=1.0805e14,
 GOLD_CONFIG = dict(GOLD_REFERENCE, gamma=(4.4642e14, 2.3555e15))
 
 
+# Lorentz-pole fits of the reference's material modules; omega and gamma in
+# rad/s, from the (2 pi c0/micro) * (...) tables.
+_W = 2.0 * PI * C0 / 1e-6
+
+
+def _lorentz(form, eps_inf, xi, w, nu):
+    return dict(form=form, eps_inf=eps_inf, delta_eps=tuple(xi),
+                omega=tuple(_W * x for x in w), gamma=tuple(_W * x for x in nu))
+
+
+# Si, second-order form (M3/si_mod.f90:32-35, M1/si_mod.f90:25-28; no eps_inf term)
+SI_S = _lorentz(abi.LORENTZ_S, 1.0, (8.0, 2.85, -0.107), (3.64, 2.76, 1.73), (0.0, 0.063, 2.5))
+# Si, polarisation-current form (M3/siLorentzJp_mod.f90:22-26)
+SI_JP = _lorentz(abi.LORENTZ_JP, 1.0, (8.0, 2.85, -0.107), (3.64, 2.76, 1.73), (0.0, 0.063, 2.5))
+# Gold 500-800 nm (M3/goldLorentzJp_mod.f90:22-26)
+GOLD_JP = _lorentz(abi.LORENTZ_JP, 1.053787, (2.862890, -0.0722398, 367.7668),
+                   (-2.445679, 1.480982, 0.3371279), (0.2170955, 0.1429645, 0.02285188))
+# Gold film (M3/filmGoldLorentzJp_mod.f90:21-25)
+FILMGOLD_JP = _lorentz(abi.LORENTZ_JP, 3.497071, (2.301113, 400.0), (-2.393546, 0.3441309),
+                       (0.2460773, 0.02533959))
+# Titanium 600-1000 nm (M3/titaniumJp_mod.f90:22-26)
+TI_JP = _lorentz(abi.LORENTZ_JP, 1.1, (-12.74873, 0.9605442, 67.66233, 55.0525),
+                 (4.36014, -1.261863, 0.4063879, -2.176176), (-5.825585, 0.2087635, 1.246245, 8.059584))
+
+
+def lorentz_eps(p, omega):
+    """Continuous-time permittivity of the Lorentz recursion (both codings):
+    P'' + 2 nu P' + w^2 P = w^2 deps E, so eps = eps_inf + sum deps w^2 /
+    (w^2 - omega^2 - 2i nu omega) in the exp(-i omega t) convention."""
+    omega = np.asarray(omega, dtype=np.float64)
+    eps = np.full(omega.shape, p["eps_inf"], dtype=np.complex128)
+    for de, w, nu in zip(p["delta_eps"], p["omega"], p["gamma"]):
+        eps += de * w * w / (w * w - omega * omega - 2j * nu * omega)
+    return eps
+
+
+def slab_rt(eps, d, omega):
+    """|r|^2 and |t|^2 of a slab of permittivity eps and thickness d in
+    vacuum at normal incidence (Airy formulas)."""
+    k0 = np.asarray(omega) / C0
+    n = np.sqrt(np.asarray(eps, dtype=np.complex128))
+    n = np.where(n.imag < 0, -n, n)
+    r12 = (1.0 - n) / (1.0 + n)
+    t12, t21 = 2.0 / (1.0 + n), 2.0 * n / (1.0 + n)
+    ph = np.exp(1j * n * k0 * d)
+    den = 1.0 - r12 * r12 * ph * ph
+    r = r12 * (1.0 - ph * ph) / den
+    t = t12 * t21 * ph / den
+    return np.abs(r) ** 2, np.abs(t) ** 2
+
+
 def fint(x):
     """Fortran real -> integer assignment (truncation toward zero)."""
     return int(x)
@@ -316,12 +367,54 @@ def config_1d_gold(precision=abi.F64, steps=20000):
     p["t0"] = 4.0 * p["st"]
     spec.sources.append(dict(component=abi.EX, lo=(0, 100, 0), hi=(0, 100, 0), amp=1.0, **p))
     arg = dft_omegas(400e-9, 900e-9, 200)
-    dist = ds * float(2000 - 100) + 4.5 * 600e-9
-    tfin = math.floor(dist / C0 / dt)
+    # gate between the incident pulse's tail passing cell 300 (t0 + 4 st after
+    # its peak) and the slab's reflection reaching it (3600 cells of travel)
+    t_inc_end = ds * float(300 - 100) / C0 + 2.0 * p["t0"]
+    t_ref = ds * float(2 * 2000 - 100 - 300) / C0
+    tfin = math.floor(0.5 * (t_inc_end + t_ref) / dt)
     spec.add_monitor((0, 300, 0), (0, 300, 0), (abi.EX, abi.HZ), arg, 1, tfin - 1)
     spec.add_monitor((0, 300, 0), (0, 300, 0), (abi.EX, abi.HZ), arg, tfin + 1, 2 ** 31 - 1)
     spec.add_monitor((0, 3000, 0), (0, 3000, 0), (abi.EX, abi.HZ), arg)
     return spec, dict(Nt=steps, tfinStop=tfin, arg=arg, ds=ds, dt=dt)
+
+
+def config_1d_slab(material, lo=2000, thickness=50, precision=abi.F64, steps=20000):
+    """config_1d_gold's line with the gold slab replaced by ``material``
+    (a Lorentz parameter dict) over cells lo .. lo+thickness-1."""
+    spec, meta = config_1d_gold(precision=precision, steps=steps)
+    spec.materials = spec.materials[:1]
+    spec.add_lorentz(box((0, lo, 0), (0, lo + thickness - 1, 0)), material)
+    spec.name = "config_1d_slab"
+    return spec, meta
+
+
+def swap_gold(spec, material):
+    """A copy of ``spec`` whose gold (Drude+2CP) materials are replaced by the
+    Lorentz material ``material`` on the same regions."""
+    import copy
+    from .spec import Material
+    s = copy.deepcopy(spec)
+    s.materials = [Material("lorentz", m.region, params=dict(material)) if m.kind == "gold" else m
+                   for m in s.materials]
+    return s
+
+
+def as_te(spec):
+    """The TE (Hz, Ex, Ey) counterpart of a 2D TMz spec: Ez sources drive Ex
+    and the monitors record (Ex, Hz) in place of (Ez, Hx)."""
+    import copy
+    s = copy.deepcopy(spec)
+    s.layout = abi.LAYOUT_2D_TE
+    for src in s.sources:
+        if src["component"] == abi.EZ:
+            src["component"] = abi.EX
+    swap = {abi.EZ: abi.EX, abi.HX: abi.HZ}
+    for m in s.monitors:
+        m.comps = tuple(swap.get(c, c) for c in m.comps)
+    for pr in s.probes:
+        pr.comps = tuple(swap.get(c, c) for c in pr.comps)
+    s.name = spec.name + "_te"
+    return s
 
 
 def cylinders_2d(n=2048, count=40, seed=0, rmin=10, rmax=40, ylo=200, yhi=1948, pml=32):

@@ -18,7 +18,7 @@ Box = Tuple[Tuple[int, int, int], Tuple[int, int, int]]
 
 @dataclass
 class Material:
-    kind: str                      # "dielectric" | "gold" | "graphene"
+    kind: str                      # "dielectric" | "gold" | "graphene" | "lorentz"
     region: dict                   # {"kind": "box", "lo":..., "hi":...} | spheres | mask
     eps: float = 1.0
     params: Optional[dict] = None
@@ -73,6 +73,12 @@ class JobSpec:
 
     def add_graphene(self, region, params):
         self.materials.append(Material("graphene", region, params=dict(params)))
+        return len(self.materials)
+
+    def add_lorentz(self, region, params):
+        """params: {"form": abi.LORENTZ_JP | abi.LORENTZ_S, "eps_inf",
+        "delta_eps": [...], "omega": [...], "gamma": [...]} (rad/s)."""
+        self.materials.append(Material("lorentz", region, params=dict(params)))
         return len(self.materials)
 
     def add_monitor(self, lo, hi, comps, omega, n_first=1, n_last=2 ** 31 - 1, mean=False):
@@ -155,6 +161,18 @@ def drude2cp_struct(p):
 def graphene_struct(p):
     return abi.GrapheneDesc(p["fermi_ev"], p["tau"], p["temperature"], p["chi3"], p["raman_frac"],
                             p["raman_freq"], p["raman_tau"], p["thickness"], p.get("e_scale", 1.0))
+
+
+def lorentz_struct(p):
+    d = abi.LorentzDesc()
+    d.form = int(p.get("form", abi.LORENTZ_JP))
+    d.npoles = len(p["delta_eps"])
+    d.eps_inf = p["eps_inf"]
+    for q in range(d.npoles):
+        d.delta_eps[q] = p["delta_eps"][q]
+        d.omega[q] = p["omega"][q]
+        d.gamma[q] = p["gamma"][q]
+    return d
 
 
 def pml_struct(p):

@@ -119,6 +119,35 @@ typedef struct fdtd_graphene_desc {
   double e_scale;       /* V/m per normalised field unit (for chi3 E^2)    */
 } fdtd_graphene_desc;
 
+/* Lorentz poles (up to FDTD_LORENTZ_MAX_POLES), in either of the reference's
+ * two codings of the same discrete recursion:
+ *   FDTD_LORENTZ_JP  the polarisation-current form of gold_LJp, si_LJp,
+ *                    Ti_LJp and filmgold_LJp (3D/goldLorentzJp_mod.f90:37-91,
+ *                    3D/siLorentzJp_mod.f90:41-96, 3D/titaniumJp_mod.f90:37-91,
+ *                    2D/siLorentzJp_mod.f90:40-80):
+ *                      E += Ku/eps_inf (curl H - ds sum_l Jp_l)
+ *                      Jp_l = g1 Jp_l + g2 (xi_l E/c0 - P_l);  P_l += dt Jp_l
+ *                    g1 = (1 - nu dt)/(1 + nu dt), g2 = w0^2 dt/(1 + nu dt)
+ *   FDTD_LORENTZ_S   the second-order form of Si (3D/si_mod.f90:46-82,
+ *                    1D/si_mod.f90:38-53), D-form with E = (D - sum_l S_l)/eps_inf
+ *                    (eps_inf = 1 in the reference):
+ *                      S_l(n) = ga S_l(n-1) + gb S_l(n-2) + gc E(n)
+ *                    ga = (2 - (w dt)^2)/(1 + nu dt), gb = (nu dt - 1)/(1 + nu dt),
+ *                    gc = deps (w dt)^2/(1 + nu dt)
+ * delta_eps is xi1 / dep, omega is w0l / wp and gamma is dnu0l / dnup, all
+ * angular [rad/s].  Signs are taken as given (the reference's fits have
+ * negative w0 and nu for some poles). */
+enum { FDTD_LORENTZ_JP = 0, FDTD_LORENTZ_S = 1 };
+#define FDTD_LORENTZ_MAX_POLES 4
+typedef struct fdtd_lorentz_desc {
+  int32_t form;          /* FDTD_LORENTZ_JP or FDTD_LORENTZ_S            */
+  int32_t npoles;        /* 1..FDTD_LORENTZ_MAX_POLES                    */
+  double eps_inf;
+  double delta_eps[FDTD_LORENTZ_MAX_POLES];
+  double omega[FDTD_LORENTZ_MAX_POLES];
+  double gamma[FDTD_LORENTZ_MAX_POLES];
+} fdtd_lorentz_desc;
+
 /* ---- PML ---------------------------------------------------------------- */
 enum {
   FDTD_PML_REFERENCE = 1, /* the reference's y-slab split-field PML with its
@@ -204,6 +233,11 @@ int fdtd_add_gold(fdtd_job *job, const fdtd_region *region,
 /* Graphene sheet (3D/graphene_mod.f90:59-269, 1D/graphene633_mod.f90:26-105). */
 int fdtd_add_graphene(fdtd_job *job, const fdtd_region *region,
                       const fdtd_graphene_desc *params, int32_t *material_id);
+/* gold_LJp / si_LJp / Ti_LJp / filmgold_LJp%initialize_material and
+ * Si%initialize_material (3D/goldLorentzJp_mod.f90:93-161,
+ * 3D/si_mod.f90:84-206).  Every E component of the layout gets the update. */
+int fdtd_add_lorentz(fdtd_job *job, const fdtd_region *region,
+                     const fdtd_lorentz_desc *params, int32_t *material_id);
 /* pmly%initialize (3D/BERpmly_mod.f90:485-508, 2D/BERpmly_HzExEy_mod.f90:229-247,
  * 1D/BERpmly_ExHz_mod.f90:163-175). */
 int fdtd_add_pml(fdtd_job *job, const fdtd_pml_desc *pml);

@@ -59,7 +59,8 @@ static double cdiv_re(cplx a, cplx b) {
 }
 
 /* ---- job ------------------------------------------------------------------ */
-enum { MAT_DIEL = 1, MAT_GOLD = 2, MAT_GRAPHENE = 3 };
+enum { MAT_DIEL = 1, MAT_GOLD = 2, MAT_GRAPHENE = 3, MAT_LORENTZ_JP = 4, MAT_LORENTZ_S = 5 };
+#define NPOLE FDTD_LORENTZ_MAX_POLES
 #define MAXMAT 250
 
 typedef struct {
@@ -72,6 +73,13 @@ typedef struct {
   double *I[3], *S[3];                 /* Drude running sums per comp    */
   cplx *g1[3], *g2[3];                 /* critical-point terms           */
   double *SR[3], *SRm1[3], *SRm2[3];   /* graphene Raman recursion       */
+  /* Lorentz poles: JP form (M3/goldLorentzJp_mod.f90:14-18) and S form
+     (M3/si_mod.f90:14-26) */
+  int npoles; double l_ga;             /* 1/epinf                        */
+  double g1L[NPOLE], g2L[NPOLE], xi[NPOLE];       /* gamma1L, gamma2L, xi1 */
+  double sa[NPOLE], sb[NPOLE], sc[NPOLE];         /* ga_l, gb_l, gc_l      */
+  double *P[3][NPOLE], *Jp[3][NPOLE], *JpT[3];    /* JP state              */
+  double *Sm1[3][NPOLE], *Sm2[3][NPOLE];          /* S state: S(n-1), S(n-2) */
   fdtd_region region;                  /* painted at commit              */
   double *centers;                     /* owned copy for SPHERES         */
   uint8_t *mask;                       /* owned copy for MASK            */
@@ -184,7 +192,8 @@ void ora_destroy(ora_job *J) {
     omat *M = &J->mat[m];
     free(M->cells); free(M->centers); free(M->mask);
     for (int c = 0; c < 3; c++) { free(M->I[c]); free(M->S[c]); free(M->g1[c]); free(M->g2[c]);
-      free(M->SR[c]); free(M->SRm1[c]); free(M->SRm2[c]); }
+      free(M->SR[c]); free(M->SRm1[c]); free(M->SRm2[c]); free(M->JpT[c]);
+      for (int l = 0; l < NPOLE; l++) { free(M->P[c][l]); free(M->Jp[c][l]); free(M->Sm1[c][l]); free(M->Sm2[c][l]); } }
   }
   for (int q = 0; q < J->nmon; q++) { free(J->mon[q].omega); free(J->mon[q].re); free(J->mon[q].im); }
   for (int q = 0; q < J->nprobe; q++) free(J->probe[q].buf);
@@ -287,6 +296,30 @@ int ora_add_graphene(ora_job *J, const fdtd_region *r, const fdtd_graphene_desc 
   M->r1 = 2.0 * exp(-alfaR * dt) * cos(betaR * dt);
   M->r2 = -exp(-2.0 * alfaR * dt);
   M->kerr = (1.0 - p->raman_frac) * chi3n;
+  return id;
+}
+
+/* Lorentz poles.  JP: gamma1L = (1-dnu dt)/(1+dnu dt), gamma2L = w0^2 dt/(1+dnu dt),
+ * ga = 1/epinf (M3/goldLorentzJp_mod.f90:140-161).  S: ga_l = (2-(dt wp)^2)/(1+dt dnup),
+ * gb_l = (dt dnup-1)/(1+dt dnup), gc_l = dep (wp dt)^2/(1+dt dnup) (M3/si_mod.f90:180-206). */
+int ora_add_lorentz(ora_job *J, const fdtd_region *r, const fdtd_lorentz_desc *p) {
+  if (p->npoles < 1 || p->npoles > NPOLE) FAIL("npoles must be 1..%d", NPOLE);
+  if (p->form != FDTD_LORENTZ_JP && p->form != FDTD_LORENTZ_S) FAIL("bad Lorentz form");
+  if (!(p->eps_inf != 0.0)) FAIL("eps_inf must be nonzero");
+  omat *M; int id = add_material(J, r, &M); if (id < 0) return id;
+  M->kind = p->form == FDTD_LORENTZ_JP ? MAT_LORENTZ_JP : MAT_LORENTZ_S;
+  M->npoles = p->npoles;
+  M->l_ga = 1.0 / p->eps_inf;
+  double dt = J->g.dt;
+  for (int l = 0; l < p->npoles; l++) {
+    double w = p->omega[l], nu = p->gamma[l];
+    M->xi[l] = p->delta_eps[l];
+    M->g1L[l] = (1.0 - nu * dt) / (1.0 + nu * dt);
+    M->g2L[l] = (w * w) * dt / (1.0 + nu * dt);
+    M->sa[l] = (2.0 - (dt * w) * (dt * w)) / (1.0 + dt * nu);
+    M->sb[l] = (dt * nu - 1.0) / (1.0 + dt * nu);
+    M->sc[l] = (p->delta_eps[l] * ((w * dt) * (w * dt))) / (1.0 + dt * nu);
+  }
   return id;
 }
 
@@ -628,6 +661,14 @@ int ora_commit(ora_job *J) {
         M->g2[c] = (cplx *)calloc((size_t)(cnt > 0 ? cnt : 1), sizeof(cplx));
         M->SR[c] = zalloc(cnt); M->SRm1[c] = zalloc(cnt); M->SRm2[c] = zalloc(cnt);
       }
+    } else if (M->kind == MAT_LORENTZ_JP || M->kind == MAT_LORENTZ_S) {
+      for (int c = 0; c < 3; c++) {
+        M->JpT[c] = zalloc(cnt);
+        for (int l = 0; l < M->npoles; l++) {
+          M->P[c][l] = zalloc(cnt); M->Jp[c][l] = zalloc(cnt);
+          M->Sm1[c][l] = zalloc(cnt); M->Sm2[c][l] = zalloc(cnt);
+        }
+      }
     }
   }
   if (J->pml_mode == FDTD_PML_REFERENCE) {
@@ -666,7 +707,40 @@ static int in_main(const ora_job *J, int i0, int j0, int k0) {
 }
 
 /* ---- materials: update_E -------------------------------------------------- */
-static void materials_update_E(ora_job *J) {
+/* curl H of E component a at padded cell c, as the E-form update_EJp writes
+   it (M3/goldLorentzJp_mod.f90:53-58, M2/siLorentzJp_mod.f90:54-55); the 1D
+   line is the 2D TE Ex row along y */
+static double curl_at(const ora_job *J, int a, int64_t c) {
+  const double *hx = J->F[HX], *hy = J->F[HY], *hz = J->F[HZ];
+  const int64_t sy = J->px, sz = (int64_t)J->px * J->py;
+  if (J->g.layout == FDTD_LAYOUT_3D) {
+    if (a == 0) return (hz[c] - hz[c - sy]) + (-hy[c] + hy[c - sz]);
+    if (a == 1) return (hx[c] - hx[c - sz]) + (-hz[c] + hz[c - 1]);
+    return (hy[c] - hy[c - 1]) + (-hx[c] + hx[c - sy]);
+  }
+  if (J->g.layout == FDTD_LAYOUT_2D_TM) return (hy[c] - hy[c - 1]) + (-hx[c] + hx[c - sy]);
+  if (a == 0) return hz[c] - hz[c - sy];
+  return -hz[c] + hz[c - 1];
+}
+
+/* what updateD adds to D at cell c beside Ku*curl: the soft sources and the
+   1D TFSF correction (P1/program.f90:229-235) */
+static double d_extra_at(const ora_job *J, int n, int a, int64_t c) {
+  const int64_t ii = c % J->px, jj = (c / J->px) % J->py, kk = c / ((int64_t)J->px * J->py);
+  const int i = J->dim >= 2 ? (int)ii - 1 : 0, j = (int)jj - 1, k = J->dim == 3 ? (int)kk - 1 : 0;
+  const double t = (double)(n - 1) * J->g.dt;
+  double s = 0.0;
+  for (int q = 0; q < J->nsrc; q++) {
+    const fdtd_source_desc *d = &J->src[q].d;
+    if (d->component != a) continue;
+    if (i < d->lo[0] || i > d->hi[0] || j < d->lo[1] || j > d->hi[1] || k < d->lo[2] || k > d->hi[2]) continue;
+    s += gauss_t(d, t) * d->amp;
+  }
+  if (J->tfsf && J->dim == 1 && c == J->tf.boundary + 1) s -= J->g.ku * J->hzi[c - 1];
+  return s;
+}
+
+static void materials_update_E(ora_job *J, int n) {
   double *E[3] = {J->F[EX], J->F[EY], J->F[EZ]};
   double *D[3] = {J->F[DX], J->F[DY], J->F[DZ]};
   int ncomp_list[3], nc = 0;
@@ -719,6 +793,48 @@ static void materials_update_E(ora_job *J) {
           M->SR[a][q] = sr; M->SRm2[a][q] = M->SRm1[a][q]; M->SRm1[a][q] = sr;
           M->I[a][q] = M->I[a][q] + M->g_hb * e;
           M->S[a][q] = M->g_ha * M->S[a][q] + M->g_hb * e;
+        }
+      }
+    } else if (M->kind == MAT_LORENTZ_JP) {
+      /* E += Ku ga (curl - ds JpT); JpT = sum_l Jp_l with
+         Jp_l = gamma1L Jp_l + gamma2L (xi_l E/c0 - P_l), P_l += dt Jp_l
+         (M3/goldLorentzJp_mod.f90:60-86, M2/siLorentzJp_mod.f90:57-77) */
+      const double Ku = J->g.ku, ds = J->g.ds, dt = J->g.dt;
+      for (int64_t q = 0; q < M->ncell; q++) {
+        int64_t c = M->cells[q];
+        for (int u = 0; u < nc; u++) {
+          int a = ncomp_list[u];
+          double e = E[a][c] + Ku * M->l_ga * (curl_at(J, a, c) - ds * M->JpT[a][q]);
+          e = e + M->l_ga * d_extra_at(J, n, a, c);
+          E[a][c] = e;
+          double jt = 0.0;
+          for (int l = 0; l < M->npoles; l++) {
+            double p0 = M->xi[l] * e / K_C0;
+            double jp = M->g1L[l] * M->Jp[a][l][q] + M->g2L[l] * (p0 - M->P[a][l][q]);
+            M->Jp[a][l][q] = jp;
+            M->P[a][l][q] = M->P[a][l][q] + dt * jp;
+            jt = jt + jp;
+          }
+          M->JpT[a][q] = jt;
+        }
+      }
+    } else if (M->kind == MAT_LORENTZ_S) {
+      /* E = D - S_1 - S_2 - S_3; S_l(n) = ga_l S_l(n-1) + gb_l S_l(n-2) + gc_l E
+         (M3/si_mod.f90:55-60, M1/si_mod.f90:43-48); E is scaled by 1/eps_inf,
+         which is 1 in the reference */
+      for (int64_t q = 0; q < M->ncell; q++) {
+        int64_t c = M->cells[q];
+        for (int u = 0; u < nc; u++) {
+          int a = ncomp_list[u];
+          double e = D[a][c];
+          for (int l = 0; l < M->npoles; l++) e = e - M->Sm1[a][l][q];
+          e = e * M->l_ga;
+          E[a][c] = e;
+          for (int l = 0; l < M->npoles; l++) {
+            double sn = M->sa[l] * M->Sm1[a][l][q] + M->sb[l] * M->Sm2[a][l][q] + M->sc[l] * e;
+            M->Sm2[a][l][q] = M->Sm1[a][l][q];
+            M->Sm1[a][l][q] = sn;
+          }
         }
       }
     }
@@ -1166,7 +1282,7 @@ static void d1_step(ora_job *J, int n) {
     int bd = J->tf.boundary + 1;
     dx[bd] = dx[bd] - Ku * J->hzi[bd - 1];
   }
-  materials_update_E(J);
+  materials_update_E(J, n);
   d1_pml_E(J, J->slab, ex);
   for (int j = j0; j <= j1; j++) {
     hz[j] = hz[j] + Ku * (ex[j + 1] - ex[j]);
@@ -1260,7 +1376,7 @@ int ora_step(ora_job *J, int n_first, int n_steps, int nth) {
     } else if (L == FDTD_LAYOUT_2D_TE) {
       te2d_updateD(J);
       apply_sources(J, n, 0);
-      materials_update_E(J);
+      materials_update_E(J, n);
       if (J->pml_mode == FDTD_PML_REFERENCE) te2d_pml_E(J);
       if (J->pml_mode == FDTD_PML_SPLIT) split_E(J);
       /* interchange_E: Ey x-wrap (Ex y-exchange is the identity) */
@@ -1275,7 +1391,7 @@ int ora_step(ora_job *J, int n_first, int n_steps, int nth) {
     } else if (L == FDTD_LAYOUT_2D_TM) {
       tm2d_updateD(J);
       apply_sources(J, n, 0);
-      materials_update_E(J);
+      materials_update_E(J, n);
       if (J->pml_mode == FDTD_PML_SPLIT) split_E(J);
       if (J->g.periodic[0]) wrap_x_high(J, J->F[EZ]);
       if (J->g.periodic[1]) wrap_y_both(J, J->F[EZ]);
@@ -1286,7 +1402,7 @@ int ora_step(ora_job *J, int n_first, int n_steps, int nth) {
     } else {
       d3_updateD(J, nth);
       apply_sources(J, n, 0);
-      materials_update_E(J);
+      materials_update_E(J, n);
       if (J->pml_mode == FDTD_PML_REFERENCE) d3_pml_E(J);
       if (J->pml_mode == FDTD_PML_SPLIT) split_E(J);
       /* interchange_E (P3/include/mympi_func.f90:241-518) */

@@ -30,6 +30,7 @@ const char *ora_error(void);
 int ora_add_dielectric(ora_job *job, const fdtd_region *region, double eps_r);
 int ora_add_gold(ora_job *job, const fdtd_region *region, const fdtd_drude2cp *p);
 int ora_add_graphene(ora_job *job, const fdtd_region *region, const fdtd_graphene_desc *p);
+int ora_add_lorentz(ora_job *job, const fdtd_region *region, const fdtd_lorentz_desc *p);
 int ora_add_pml(ora_job *job, const fdtd_pml_desc *pml);
 int ora_add_tfsf_1d(ora_job *job, const fdtd_tfsf1d_desc *tfsf);
 int ora_add_source(ora_job *job, const fdtd_source_desc *src);

@@ -35,16 +35,17 @@ def test_struct_sizes_match_header(built, tmp_path):
     # compile a tiny C program that prints sizeof/offsetof of the descriptors
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "fdtd_gb300.h"\n'
-                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",'
                    'sizeof(fdtd_grid_desc),sizeof(fdtd_region),sizeof(fdtd_drude2cp),'
                    'sizeof(fdtd_graphene_desc),sizeof(fdtd_pml_desc),sizeof(fdtd_source_desc),'
-                   'sizeof(fdtd_monitor_desc),sizeof(fdtd_probe_desc),sizeof(fdtd_tfsf1d_desc));return 0;}\n')
+                   'sizeof(fdtd_monitor_desc),sizeof(fdtd_probe_desc),sizeof(fdtd_tfsf1d_desc),'
+                   'sizeof(fdtd_lorentz_desc));return 0;}\n')
     exe = tmp_path / "sz"
     import subprocess
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     got = [C.sizeof(t) for t in (abi.GridDesc, abi.Region, abi.Drude2CP, abi.GrapheneDesc, abi.PmlDesc,
-                                 abi.SourceDesc, abi.MonitorDesc, abi.ProbeDesc, abi.Tfsf1dDesc)]
+                                 abi.SourceDesc, abi.MonitorDesc, abi.ProbeDesc, abi.Tfsf1dDesc, abi.LorentzDesc)]
     assert [int(x) for x in out] == got
 
 
@@ -67,3 +68,10 @@ def test_bad_arguments_are_rejected(built):
     assert "layout" in job.last_error()
     assert L.fdtd_create(None, C.byref(h)) == abi.FDTD_EINVAL
     assert L.fdtd_step(None, 1, 1) == abi.FDTD_EINVAL
+    d = abi.LorentzDesc()
+    d.form, d.npoles, d.eps_inf = abi.LORENTZ_JP, abi.LORENTZ_MAX_POLES + 1, 1.0
+    assert L.fdtd_add_lorentz(None, None, C.byref(d), None) == abi.FDTD_EINVAL
+    assert "npoles" in job.last_error()
+    d.npoles, d.form = 1, 7
+    assert L.fdtd_add_lorentz(None, None, C.byref(d), None) == abi.FDTD_EINVAL
+    assert "form" in job.last_error()

@@ -360,3 +360,64 @@ def test_mean_monitor_is_the_mean_of_the_cell_spectra(gpu, dim):
     assert np.linalg.norm(cre) > 0
     for a, b in ((mre[..., 0], cre.mean(axis=2)), (mim[..., 0], cim.mean(axis=2))):
         assert rel_l2(a, b) <= 1e-12
+
+
+# ---------------------------------------------------------------------------
+# Lorentz-pole materials (the *LorentzJp modules and si_mod) against the
+# oracle's literal restatement of each reference coding
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("name", ["SI_S", "GOLD_JP"])
+def test_lorentz_1d_slab_vs_oracle(gpu, oracle_lib, prec, name):
+    spec, meta = problems.config_1d_slab(getattr(problems, name), precision=prec)
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64))
+    J.step(1, meta["Nt"])
+    O.step(1, meta["Nt"])
+    err = _dft_err(J, O, 3)
+    if prec == abi.F64:
+        assert err <= TOL64
+        check_state(J, O, (abi.EX, abi.HZ))
+    else:
+        assert err <= TOL32_DFT
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("case", ["tm_gold_jp", "te_gold_jp", "te_gold", "te_si_s"])
+def test_2d_cylinders_other_materials_vs_oracle(gpu, oracle_lib, prec, case):
+    """The cylinder workload with Lorentz gold or Si in place of Drude+2CP
+    gold, in TMz and in the reference's own TE layout (Hz, Ex, Ey)."""
+    spec, meta = problems.config_2d_tmz(precision=prec, n=384, ncyl=8, nfreq=24)
+    mat = {"gold_jp": problems.GOLD_JP, "si_s": problems.SI_S}.get(case.split("_", 1)[1])
+    if mat is not None:
+        spec = problems.swap_gold(spec, mat)
+    if case.startswith("te"):
+        spec = problems.as_te(spec)
+    steps = 2500
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64))
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, 3)
+    if prec == abi.F64:
+        assert err <= TOL64
+        check_state(J, O, (abi.EX, abi.EY, abi.HZ) if case.startswith("te") else (abi.EZ, abi.HX, abi.HY))
+    else:
+        assert err <= TOL32_DFT
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+def test_lorentz_3d_sphere_vs_oracle(gpu, oracle_lib, prec):
+    spec, meta = problems.config_3d_sphere(precision=prec, n=96, nfreq=8, npml=8, radius=40.0, half=20)
+    spec = problems.swap_gold(spec, problems.GOLD_JP)
+    steps = 600
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, 6)
+    if prec == abi.F64:
+        assert err <= TOL64
+        check_state(J, O, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ))
+    else:
+        assert err <= TOL32_DFT
