@@ -14,6 +14,10 @@ the same record layout, so those tools run unchanged:
   timesLiney/r<k>E_time<f>.dat                            Ex, Hz along x=ic
   timesGnuplotmap/r<k>E_time<f>.dat                       Hz maps
 
+``cal_r_sy`` then does what transforms/calR_Sy.f90 does with those files:
+R = -Syr/Syin, T = Syt/Syin, A = 1 - R - T per wavelength, written to
+RTA_2Dfdtd.data (3D/.../transforms/calR_Sy.f90:16-35).
+
 Free-format records use a full-precision exponent form that Fortran
 list-directed input reads; the fixed-format records follow the reference's
 edit descriptors (E30.19, F30.19, F15.5, E20.10).
@@ -129,3 +133,39 @@ def write_reference_2d(outdir, meta, monitors, probes, frames, nranks=3):
                     for i in range(nx):
                         fh.write(free(float(i + 1), float(j + 1), hz[j, i]) + "\n")
                     fh.write("\n")
+
+
+def read_free(path):
+    """Rows of a list-directed text file (blank lines skipped)."""
+    rows = []
+    with open(path) as fh:
+        for line in fh:
+            f = line.replace("D", "E").replace("d", "e").split()
+            if f:
+                rows.append([float(x) for x in f])
+    return np.asarray(rows, dtype=np.float64)
+
+
+def rta(syin, syr, syt):
+    """r = -y1/y0, t = y2/y0, a = 1 - r - t (calR_Sy.f90:27-35)."""
+    syin, syr, syt = (np.asarray(x, dtype=np.float64) for x in (syin, syr, syt))
+    r = -syr / syin
+    t = syt / syin
+    return r, t, 1.0 - r - t
+
+
+def cal_r_sy(transforms_dir, inc=0, ref=0, tras=2, out_name="RTA_2Dfdtd.data"):
+    """calR_Sy on the per-rank spectra under ``transforms_dir``: the ranks
+    that hold the incident, reflected and transmitted planes are the
+    reference's config.xml entries <inc>, <ref>, <tras>.  Writes
+    ``out_name`` (x0, r, t, a per line) beside them and returns its rows."""
+    y0 = read_free(os.path.join(transforms_dir, f"r{inc}Syin.dat"))
+    y1 = read_free(os.path.join(transforms_dir, f"r{ref}Syr.dat"))
+    y2 = read_free(os.path.join(transforms_dir, f"r{tras}Syt.dat"))
+    n = min(len(y0), len(y1), len(y2))
+    r, t, a = rta(y0[:n, 1], y1[:n, 1], y2[:n, 1])
+    rows = np.stack([y0[:n, 0], r, t, a], 1)
+    with open(os.path.join(transforms_dir, out_name), "w") as fh:
+        for row in rows:
+            fh.write(free(*row) + "\n")
+    return rows

@@ -124,6 +124,8 @@ def test_2d_reference_output_files_match_shipped_files(run2d_gpu, tmp_path):
     assert rel_l2(load_table(str(tr / "r2tfld.dat")), g["tfld"]) <= TOL64
     assert rel_l2(load_table(str(tr / "r0rfld.dat")), g["rfld"]) <= 1e-9
     np.testing.assert_allclose(load_table(str(tr / "r0tf_r.dat")), g["tf_r"], rtol=5.01e-10, atol=1e-30)
+    rows = outputs.cal_r_sy(str(tr))          # transforms/calR_Sy.f90 on the written files
+    assert rel_l2(rows[:, 1:], g["rta"][:, 1:]) <= TOL64
     for f in (1, 7, 20):
         parts = [load_table(str(tmp_path / "timesLiney" / f"r{k}E_time{f}.dat")) for k in range(3)]
         assert rel_l2(np.concatenate(parts)[:, 1:], g["liney"][f - 1]) <= TOL64

@@ -49,3 +49,21 @@ def test_write_read_round_trip(tmp_path):
     m = load_table(str(tmp_path / "timesGnuplotmap" / "r1E_time3.dat"))
     assert m.shape == (422 * nx, 3) and m[0, 0] == 1.0 and m[0, 1] == 423.0
     np.testing.assert_array_equal(m[:, 2], frames[3][1][422:844].ravel())
+
+
+def test_cal_r_sy_on_written_spectra(tmp_path):
+    """calR_Sy restated: the RTA rows computed from the written per-rank Sy
+    files equal R, T, A of the in-memory spectra bit for bit (the files keep
+    17 significant digits), and the file it writes reads back the same."""
+    spec, meta = problems.reference_2d()
+    rng = np.random.default_rng(1)
+    nf, nx, ny = len(meta["arg"]), meta["nx"], meta["ny"]
+    mons = [(rng.standard_normal((2, nf, nx)), rng.standard_normal((2, nf, nx))) for _ in range(3)]
+    probes = [rng.standard_normal((2, 2)) for _ in range(3)]
+    outputs.write_reference_2d(str(tmp_path), meta, mons, probes, {})
+    rows = outputs.cal_r_sy(str(tmp_path / "transforms"))
+    sy = [problems.poynting_2d_te(*m, meta["ds"]) for m in mons]
+    r, t, a = outputs.rta(*sy)
+    np.testing.assert_array_equal(rows[:, 1:], np.stack([r, t, a], 1))
+    back = load_table(str(tmp_path / "transforms" / "RTA_2Dfdtd.data"))
+    np.testing.assert_array_equal(back, rows)
