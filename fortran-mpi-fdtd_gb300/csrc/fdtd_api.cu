@@ -109,6 +109,10 @@ struct fdtd_job {
   fdtd_pml_desc pml{};
   bool has_tfsf = false;
   fdtd_tfsf1d_desc tfsf{};
+  bool has_tfbox = false;        // 2D/3D total-field/scattered-field box
+  fdtd_tfsf_desc tfbox{};
+  int tb_face[3] = {0, 0, 0};
+  void *d_tf_abc = nullptr;
   std::vector<fdtd_source_desc> srcs;
   std::vector<MonRec> mons;
   std::vector<ProbeRec> probes;
@@ -450,6 +454,49 @@ int split_3d(fdtd_job *J, const std::vector<uint8_t> &rf) {
 template <typename T>
 int tune_tiles(fdtd_job *J);
 
+// The TFSF box: faces, and the cells its face terms touch (the box widened by
+// one cell across each face) inside the grid, the main range and the PML's
+// interior, with no dispersive cell where an E term lands.
+int check_tfbox(fdtd_job *J, const std::vector<uint8_t> &mat) {
+  const int nx = J->nx, ny = J->ny, nz = J->nz;
+  const int n3[3] = {nx, ny, nz};
+  const int *lo = J->tfbox.lo, *hi = J->tfbox.hi;
+  for (int a = 0; a < 3; ++a)
+    J->tb_face[a] = a == 1 || (a < J->dim && !(J->g.periodic[a] && lo[a] == 0 && hi[a] == n3[a] - 1));
+  if (J->dim == 2) J->tb_face[2] = 0;
+  if (lo[1] < 1 || hi[1] > ny - 2 || hi[1] <= lo[1])
+    return set_err(FDTD_ERANGE, "TFSF box rows %d..%d: need 1 <= lo < hi <= ny-2", lo[1], hi[1]);
+  int wlo[3], whi[3];
+  for (int a = 0; a < 3; ++a) {
+    if (lo[a] < 0 || hi[a] >= n3[a] || lo[a] > hi[a]) return set_err(FDTD_ERANGE, "TFSF box out of grid on axis %d", a);
+    if (J->tb_face[a] && hi[a] <= lo[a]) return set_err(FDTD_ERANGE, "TFSF box needs two cells across axis %d", a);
+    wlo[a] = J->tb_face[a] ? lo[a] - 1 : lo[a];
+    whi[a] = J->tb_face[a] ? hi[a] + 1 : hi[a];
+    if (a >= J->dim) continue;
+    if (wlo[a] < std::max(J->g.main_lo[a], J->slo[a]) || whi[a] > std::min(J->g.main_hi[a], J->shi[a]))
+      return set_err(FDTD_ERANGE, "TFSF box faces on axis %d leave the main range or enter the PML", a);
+  }
+  if (J->slab_rows > 0 && (wlo[1] < J->slab_rows || whi[1] > ny - 1 - J->slab_rows))
+    return set_err(FDTD_ERANGE, "TFSF box faces enter the PML slabs");
+  auto disp = [&](int i, int j, int k) { return mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] >= kAdeId; };
+  const int k0 = J->dim == 3 ? lo[2] : 0, k1 = J->dim == 3 ? hi[2] : 0;
+  for (int k = k0; k <= k1; ++k)
+    for (int i = lo[0]; i <= hi[0]; ++i)
+      if (disp(i, lo[1], k) || disp(i, hi[1], k)) return set_err(FDTD_EINVAL, "a dispersive cell lies on a TFSF face");
+  if (J->tb_face[0])
+    for (int k = k0; k <= k1; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        if (disp(lo[0], j, k) || disp(hi[0] + 1, j, k)) return set_err(FDTD_EINVAL, "a dispersive cell lies on a TFSF face");
+  if (J->dim == 3 && J->tb_face[2])
+    for (int j = lo[1]; j <= hi[1]; ++j)
+      for (int i = lo[0]; i <= hi[0]; ++i)
+        if (disp(i, j, lo[2]) || disp(i, j, hi[2] + 1)) return set_err(FDTD_EINVAL, "a dispersive cell lies on a TFSF face");
+  for (auto &sr : J->srcs)
+    if (sr.component == FDTD_E_INC && (sr.lo[1] < 0 || sr.hi[1] >= ny || sr.lo[1] > sr.hi[1]))
+      return set_err(FDTD_ERANGE, "incident-line source rows out of the line");
+  return FDTD_OK;
+}
+
 template <typename T>
 int commit_impl(fdtd_job *J) {
   int rc;
@@ -487,6 +534,11 @@ int commit_impl(fdtd_job *J) {
   if (J->has_tfsf) {
     if ((rc = alloc_dev(J, &J->F[6], (size_t)N * sizeof(T)))) return rc;
     if ((rc = alloc_dev(J, &J->F[7], (size_t)N * sizeof(T)))) return rc;
+  }
+  if (J->has_tfbox) {
+    if ((rc = alloc_dev(J, &J->F[6], (size_t)ny * sizeof(T)))) return rc;
+    if ((rc = alloc_dev(J, &J->F[7], (size_t)ny * sizeof(T)))) return rc;
+    if ((rc = alloc_dev(J, &J->d_tf_abc, 4 * sizeof(T)))) return rc;
   }
   // ---- materials: device ids (constant dielectrics 1..127, dispersive
   // materials kAdeId..255), painted in call order ----
@@ -797,9 +849,11 @@ int commit_impl(fdtd_job *J) {
   for (auto &P : J->probes)
     if (ref && J->dim == 3 && J->slab_rows > 0 && (P.d.cell[1] <= J->slab_rows - 1 || P.d.cell[1] >= ny - J->slab_rows))
       touches_slab = true;
+  if (J->has_tfbox && (rc = check_tfbox(J, mat))) return rc;
   // 2D samples fused into the H edge rows unless a monitor reduces its box
-  // (the reduction runs in the stand-alone gather); 3D: stand-alone gather
-  J->gather_fused = (J->dim == 2 && !has_mean) || (J->dim == 1 && !touches_slab);
+  // (the reduction runs in the stand-alone gather) or a TFSF box adds face
+  // terms after the H kernels; 3D: stand-alone gather
+  J->gather_fused = (J->dim == 2 && !has_mean && !J->has_tfbox) || (J->dim == 1 && !touches_slab);
   if (J->dim == 2) {
     std::vector<uint8_t> rf((size_t)ny, 0);
     for (auto &sr : J->srcs) {
@@ -922,6 +976,19 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.ncore = J->ncore;
     p.tile = J->tile;
   }
+  if (J->has_tfbox) {
+    p.tf_on = 1;
+    for (int a = 0; a < 3; ++a) {
+      p.tf_lo[a] = J->tfbox.lo[a];
+      p.tf_hi[a] = J->tfbox.hi[a];
+      p.tf_face[a] = J->tb_face[a];
+    }
+    p.tf_cb = T(J->g.ku / J->tfbox.eps_line);
+    p.tf_sign = T(J->g.layout == FDTD_LAYOUT_2D_TE ? 1.0 : -1.0);
+    p.tf_e = (T *)J->F[6];
+    p.tf_h = (T *)J->F[7];
+    p.tf_abc = (T *)J->d_tf_abc;
+  }
   p.nslab_blocks = (J->dim == 3 && J->slab_rows > 0) ? (2 * J->nx * J->slab_rows * J->nz + 255) / 256 : 0;
   p.nade_blocks = (J->nade + 255) / 256;
   p.nmon = (int)J->mon_dev.size();
@@ -942,16 +1009,22 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   }
 }
 
+// sources the 2D/3D kernels see: grid sources, and the incident line's when
+// a TFSF box is present (their rows index the line)
+bool src_on_device(const fdtd_job *J, const fdtd_source_desc &s) {
+  return s.component != FDTD_EX_INC || J->has_tfbox;
+}
+
 template <typename T>
 void set_sources(fdtd_job *J, StepParams<T> &p) {
   p.nsrc = 0;
   for (auto &s : J->srcs) {
-    if (s.component == FDTD_EX_INC) continue;
+    if (!src_on_device(J, s)) continue;
     Source &d = p.src[p.nsrc];
     d.comp = s.component;
     for (int a = 0; a < 3; ++a) {
-      d.lo[a] = std::max(s.lo[a], J->g.main_lo[a]);
-      d.hi[a] = std::min(s.hi[a], J->g.main_hi[a]);
+      d.lo[a] = s.component == FDTD_E_INC ? s.lo[a] : std::max(s.lo[a], J->g.main_lo[a]);
+      d.hi[a] = s.component == FDTD_E_INC ? s.hi[a] : std::min(s.hi[a], J->g.main_hi[a]);
     }
     d.amp = s.amp;
     ++p.nsrc;
@@ -969,14 +1042,14 @@ void destroy_graph(fdtd_job *J) {
 // amp*g(t) for steps 1..n_max of the 2D/3D sources, kept on the device
 int ensure_srctab(fdtd_job *J, int n_max) {
   int nsrc = 0;
-  for (auto &s : J->srcs) if (s.component != FDTD_EX_INC) ++nsrc;
+  for (auto &s : J->srcs) if (src_on_device(J, s)) ++nsrc;
   J->nsrc_dev = nsrc;
   if (nsrc == 0 || n_max <= J->srctab_steps) return FDTD_OK;
   const long long old_steps = J->srctab_steps;
   for (long long n = old_steps + 1; n <= n_max; ++n) {
     const double t = (double)(n - 1) * J->g.dt;           // t=real(n-1,8)*dt
     for (auto &s : J->srcs)
-      if (s.component != FDTD_EX_INC) J->srctab.push_back(gauss_t(s, t) * s.amp);
+      if (src_on_device(J, s)) J->srctab.push_back(gauss_t(s, t) * s.amp);
   }
   J->srctab_steps = n_max;
   if (n_max > J->srctab_cap_steps) {
@@ -1178,6 +1251,16 @@ int tune_tiles(fdtd_job *J) {
   return FDTD_OK;
 }
 
+// the TFSF box's launch of a half step, after the half step's other kernels
+template <typename T>
+int tfsf_part(fdtd_job *J, const StepParams<T> &p, bool e_half, bool graph) {
+  if (!graph) ev_record(J, FDTD_KERNEL_EDGE, true);
+  J->launches += launch_tfsf<T>(p, e_half, J->stream);
+  if (!graph) ev_record(J, FDTD_KERNEL_EDGE, false);
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
 // 2D / 3D: one half step (or a role subset of it).  In graph mode the step
 // number comes from the device-side ring base (d_base) plus the ring slot.
 template <typename T>
@@ -1191,7 +1274,9 @@ int half_e(fdtd_job *J, int n, int roles, int slot = 0, bool graph = false) {
   p.d_base = graph ? J->d_base : nullptr;
   const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML | (J->dim == 3 ? ROLE_ADE : 0))) != 0,
                          J->dim == 2 && (roles & ROLE_ADE) != 0};
-  return run_parts<T>(J, p, parts, true, graph);
+  int rc = run_parts<T>(J, p, parts, true, graph);
+  if (!rc && J->has_tfbox && (roles & ROLE_MAIN)) rc = tfsf_part<T>(J, p, true, graph);
+  return rc;
 }
 
 template <typename T>
@@ -1204,7 +1289,9 @@ int half_h(fdtd_job *J, int n, int roles, bool gather, int slot = -1, bool graph
   p.slot = slot >= 0 ? slot : J->stage_fill;
   p.d_base = graph ? J->d_base : nullptr;
   const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML)) != 0, false};
-  return run_parts<T>(J, p, parts, false, graph);
+  int rc = run_parts<T>(J, p, parts, false, graph);
+  if (!rc && J->has_tfbox && (roles & ROLE_MAIN)) rc = tfsf_part<T>(J, p, false, graph);
+  return rc;
 }
 
 template <typename T>
@@ -1469,24 +1556,31 @@ static int proc_call(fdtd_job *J, int n, int what) {
   return FDTD_OK;
 }
 
+// values of a component: the grid, or the ny cells of a TFSF box's line
+static long long field_elems(const fdtd_job *J, int comp) {
+  return (J->has_tfbox && comp >= FDTD_E_INC) ? (long long)J->ny : J->ncell;
+}
+
 template <typename T>
 static int get_field_impl(fdtd_job *J, int comp, double *host) {
   if (comp < 0 || comp > 7 || !J->F[comp]) return set_err(FDTD_EINVAL, "component %d not in this layout", comp);
-  std::vector<T> tmp((size_t)J->ncell);
-  CK(cudaMemcpyAsync(tmp.data(), J->F[comp], (size_t)J->ncell * sizeof(T), cudaMemcpyDeviceToHost, J->stream));
+  const long long cnt = field_elems(J, comp);
+  std::vector<T> tmp((size_t)cnt);
+  CK(cudaMemcpyAsync(tmp.data(), J->F[comp], (size_t)cnt * sizeof(T), cudaMemcpyDeviceToHost, J->stream));
   CK(cudaStreamSynchronize(J->stream));
-  for (long long c = 0; c < J->ncell; ++c) host[c] = (double)tmp[(size_t)c];
-  J->d2h += (uint64_t)J->ncell * sizeof(T);
+  for (long long c = 0; c < cnt; ++c) host[c] = (double)tmp[(size_t)c];
+  J->d2h += (uint64_t)cnt * sizeof(T);
   return FDTD_OK;
 }
 
 template <typename T>
 static int set_field_impl(fdtd_job *J, int comp, const double *host) {
   if (comp < 0 || comp > 7 || !J->F[comp]) return set_err(FDTD_EINVAL, "component %d not in this layout", comp);
-  std::vector<T> tmp(host, host + J->ncell);
-  CK(cudaMemcpyAsync(J->F[comp], tmp.data(), (size_t)J->ncell * sizeof(T), cudaMemcpyHostToDevice, J->stream));
+  const long long cnt = field_elems(J, comp);
+  std::vector<T> tmp(host, host + cnt);
+  CK(cudaMemcpyAsync(J->F[comp], tmp.data(), (size_t)cnt * sizeof(T), cudaMemcpyHostToDevice, J->stream));
   CK(cudaStreamSynchronize(J->stream));
-  J->h2d += (uint64_t)J->ncell * sizeof(T);
+  J->h2d += (uint64_t)cnt * sizeof(T);
   return FDTD_OK;
 }
 
@@ -1879,6 +1973,19 @@ int fdtd_add_tfsf_1d(fdtd_job *J, const fdtd_tfsf1d_desc *t) {
   return FDTD_OK;
 }
 
+int fdtd_add_tfsf(fdtd_job *J, const fdtd_tfsf_desc *t) {
+  int rc = check_job(J, false);
+  if (rc) return rc;
+  if (!t) return set_err(FDTD_EINVAL, "null tfsf");
+  if (J->dim < 2) return set_err(FDTD_EINVAL, "the TFSF box is 2D/3D; a 1D line uses fdtd_add_tfsf_1d");
+  if (J->has_tfbox) return set_err(FDTD_ESTATE, "the job already has a TFSF box");
+  if (!(t->eps_line > 0.0) || !std::isfinite(t->eps_line)) return set_err(FDTD_EINVAL, "eps_line must be positive");
+  J->has_tfbox = true;
+  J->tfbox = *t;
+  if (J->dim == 2) J->tfbox.lo[2] = J->tfbox.hi[2] = 0;
+  return FDTD_OK;
+}
+
 int fdtd_add_source(fdtd_job *J, const fdtd_source_desc *s, int32_t *id) {
   int rc = check_job(J, false);
   if (rc) return rc;
@@ -2048,6 +2155,7 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
   const int nx = J->nx, ny = J->ny, nz = J->nz;
   uint64_t b = N * w * (J->dim == 3 ? 6 : J->dim == 2 ? 3 : 2) + N;  // fields, material ids
   if (J->has_tfsf) b += 2 * N * w;
+  if (J->has_tfbox) b += 2ull * ny * w + 4 * w;
   // dispersive cells: each region's cells, bounded per sphere / box
   uint64_t nade = 0;
   for (auto &m : J->mats) {

@@ -164,6 +164,13 @@ struct StepParams {
   const int *d_base;       // graph replays: step number of ring slot 0 on the
                            // device; then n = *d_base + slot
   int vec;                 // cells per thread along x in the 2D tile path
+  // 2D/3D total-field/scattered-field box (plane wave along +y)
+  int tf_on;
+  int tf_lo[3], tf_hi[3];  // total-field box, inclusive cells
+  int tf_face[3];          // 1: the box has the two faces normal to the axis
+  T tf_cb, tf_sign;        // line E coefficient Ku/eps_line; +1 Ex/Hz, -1 Ez/Hx
+  T *tf_e, *tf_h;          // incident line E and H (ny values)
+  T *tf_abc;               // two-step absorbing ends: low m1 m2, high m1 m2
 };
 
 // per-row flags of the 2D tile path (precomputed from the job's set-up)
@@ -205,6 +212,8 @@ template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *str
 // separate gather (per-procedure API, or monitors inside reference slabs)
 // returns the kernels launched
 template <typename T> int launch_gather(const StepParams<T> &p, void *stream);
+// total-field/scattered-field box: incident line and face terms of a half step
+template <typename T> int launch_tfsf(const StepParams<T> &p, bool e_half, void *stream);
 
 // DFT fold: acc += sum over valid ring slots of e^{i w t} * sample * dt
 struct DftParams {

@@ -38,6 +38,11 @@ class GrapheneDesc(C.Structure):
                 ("raman_tau", C.c_double), ("thickness", C.c_double), ("e_scale", C.c_double)]
 
 
+class TfsfDesc(C.Structure):
+    _fields_ = [("lo", I3), ("hi", I3), ("eps_line", C.c_double)]
+
+
+E_INC, H_INC = 6, 7
 LORENTZ_JP, LORENTZ_S = 0, 1
 LORENTZ_MAX_POLES = 4
 

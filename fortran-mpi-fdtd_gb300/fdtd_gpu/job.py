@@ -19,7 +19,7 @@ _lib = None
 EXPORTS = [
     "fdtd_create", "fdtd_destroy", "fdtd_last_error", "fdtd_device_count",
     "fdtd_add_dielectric", "fdtd_add_gold", "fdtd_add_graphene", "fdtd_add_lorentz", "fdtd_add_pml",
-    "fdtd_add_tfsf_1d", "fdtd_add_source", "fdtd_add_monitor", "fdtd_add_probe", "fdtd_commit",
+    "fdtd_add_tfsf_1d", "fdtd_add_tfsf", "fdtd_add_source", "fdtd_add_monitor", "fdtd_add_probe", "fdtd_commit",
     "fdtd_step", "fdtd_update_DE", "fdtd_pml_update_E", "fdtd_interchange", "fdtd_update_H",
     "fdtd_pml_update_H", "fdtd_sample", "fdtd_sync", "fdtd_get_field", "fdtd_set_field",
     "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_estimate_bytes", "fdtd_profile",
@@ -50,7 +50,7 @@ def lib(path=None):
             "fdtd_add_dielectric": [vp, vp, dbl, C.POINTER(i32)],
             "fdtd_add_gold": [vp, vp, vp, C.POINTER(i32)], "fdtd_add_graphene": [vp, vp, vp, C.POINTER(i32)],
             "fdtd_add_lorentz": [vp, vp, vp, C.POINTER(i32)],
-            "fdtd_add_pml": [vp, vp], "fdtd_add_tfsf_1d": [vp, vp],
+            "fdtd_add_pml": [vp, vp], "fdtd_add_tfsf_1d": [vp, vp], "fdtd_add_tfsf": [vp, vp],
             "fdtd_add_source": [vp, vp, C.POINTER(i32)], "fdtd_add_monitor": [vp, vp, C.POINTER(i32)],
             "fdtd_add_probe": [vp, vp, C.POINTER(i32)], "fdtd_commit": [vp],
             "fdtd_step": [vp, i32, i32], "fdtd_update_DE": [vp, i32], "fdtd_pml_update_E": [vp, i32],
@@ -148,6 +148,9 @@ class Job:
             if spec.tfsf:
                 t = S.tfsf_struct(spec.tfsf)
                 check(L.fdtd_add_tfsf_1d(self.h, C.byref(t)))
+            if spec.tfsf_box:
+                t = S.tfsf_box_struct(spec.tfsf_box)
+                check(L.fdtd_add_tfsf(self.h, C.byref(t)))
             for s in spec.sources:
                 d = S.source_struct(s)
                 check(L.fdtd_add_source(self.h, C.byref(d), C.byref(mid)))
@@ -206,9 +209,10 @@ class Job:
     # -- results ---------------------------------------------------------
     def get_field(self, comp):
         n = self.spec.n
-        out = np.empty(n[0] * n[1] * n[2])
+        cnt = S.field_count(self.spec, comp)
+        out = np.empty(cnt)
         check(lib().fdtd_get_field(self.h, int(comp), out.ctypes.data))
-        return out.reshape(n[2], n[1], n[0])
+        return out if cnt != self.spec.cells() else out.reshape(n[2], n[1], n[0])
 
     def set_field(self, comp, arr):
         a = np.ascontiguousarray(arr, dtype=np.float64).ravel()

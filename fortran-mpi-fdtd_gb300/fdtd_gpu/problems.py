@@ -419,6 +419,57 @@ def as_te(spec):
     return s
 
 
+def config_tfsf(layout=abi.LAYOUT_2D_TM, precision=abi.F64, n=96, npml=10, margin=10, periodic_x=False,
+                scatterer=None, radius=8.0, nfreq=8, eps_line=1.0):
+    """A plane wave along +y entering a vacuum grid through a total-field /
+    scattered-field box: n^2 (2D) or n^3 (3D) cells of 1 nm, Ku = 0.5,
+    split-field PML (none along x when ``periodic_x``, where the box spans x
+    end to end and has no x faces).  The incident line is driven at a row
+    below the box (600 nm carrier, 0.5 fs width).  ``scatterer``: None, a
+    material dict for a centred cylinder/sphere of ``radius`` cells, or
+    "gold" (Drude+2CP).  Monitors: a row below the box (scattered field), the
+    centre row (total) and a row above it (scattered)."""
+    ds, Ku = 1e-9, 0.5
+    dt = Ku * ds / C0
+    dim3 = layout == abi.LAYOUT_3D
+    nz = n if dim3 else 1
+    order, R0 = 3.0, math.exp(-16.0)
+    sigmam = pml_sigma_max(order, R0, npml, ds)
+    spec = JobSpec(layout=layout, n=(n, n, nz), ku=Ku, dt=dt, ds=ds, precision=precision,
+                   periodic=(1 if periodic_x else 0, 0, 0), name="config_tfsf")
+    spec.add_dielectric(box((0, 0, 0), (n - 1, n - 1, nz - 1)), 1.0)
+    px = 0 if periodic_x else npml
+    spec.pml = dict(mode=abi.PML_SPLIT, npml=((px, px), (npml, npml), (npml, npml) if dim3 else (0, 0)),
+                    eps_lo=1.0, sigma_max=sigmam, order=order)
+    c = n / 2.0
+    if scatterer is not None:
+        reg = spheres([(c, c, c if dim3 else 0.0, radius)])
+        if scatterer == "gold":
+            spec.add_gold(reg, GOLD_CONFIG)
+        else:
+            spec.add_lorentz(reg, scatterer)
+    m = npml + margin
+    lo = (0 if periodic_x else m, m, m if dim3 else 0)
+    hi = (n - 1 if periodic_x else n - 1 - m, n - 1 - m, n - 1 - m if dim3 else 0)
+    spec.tfsf_box = dict(lo=lo, hi=hi, eps_line=eps_line)
+    p = _pulse(600e-9)
+    p["st"] = 0.5e-15
+    p["t0"] = 4.0 * p["st"]
+    ys = npml + margin // 2
+    spec.sources.append(dict(component=abi.E_INC, lo=(0, ys, 0), hi=(0, ys, 0), amp=1.0, **p))
+    arg = dft_omegas(500e-9, 800e-9, nfreq)
+    if layout == abi.LAYOUT_2D_TE:
+        comps = (abi.EX, abi.HZ)
+    elif layout == abi.LAYOUT_2D_TM:
+        comps = (abi.EZ, abi.HX)
+    else:
+        comps = (abi.EX, abi.EZ, abi.HX, abi.HZ)
+    k0, k1 = (m, n - 1 - m) if dim3 else (0, 0)
+    for y in (lo[1] - 3, int(c), hi[1] + 3):
+        spec.add_monitor((lo[0], y, k0), (hi[0], y, k1), comps, arg)
+    return spec, dict(arg=arg, ds=ds, dt=dt, box=(lo, hi), ys=ys)
+
+
 def cylinders_2d(n=2048, count=40, seed=0, rmin=10, rmax=40, ylo=200, yhi=1948, pml=32):
     """40 non-overlapping gold cylinders: radii uniform in {10..40}, centres
     uniform in x in [pml+r+8, n-pml-r-8], y in [ylo+r+8, yhi-r-8], rejected

@@ -59,7 +59,8 @@ class JobSpec:
     sources: List[dict] = field(default_factory=list)
     monitors: List[Monitor] = field(default_factory=list)
     probes: List[Probe] = field(default_factory=list)
-    tfsf: Optional[dict] = None
+    tfsf: Optional[dict] = None        # 1D line: {"boundary", "eps_lo", "eps_hi"}
+    tfsf_box: Optional[dict] = None    # 2D/3D: {"lo", "hi", "eps_line"}
     name: str = ""
 
     # -- builders ---------------------------------------------------------
@@ -209,6 +210,18 @@ def monitor_struct(m, keep):
 
 def probe_struct(p):
     return abi.ProbeDesc(abi.I3(*p.cell), comp_mask(p.comps), p.n_first, p.n_last)
+
+
+def tfsf_box_struct(t):
+    return abi.TfsfDesc(abi.I3(*t["lo"]), abi.I3(*t["hi"]), float(t.get("eps_line", 1.0)))
+
+
+def field_count(spec, comp):
+    """Values fdtd_get_field returns for ``comp``: the grid, or the ny
+    cells of a 2D/3D box's incident line."""
+    if spec.tfsf_box is not None and comp >= abi.E_INC:
+        return int(spec.n[1])
+    return spec.cells()
 
 
 def tfsf_struct(t):

@@ -58,12 +58,15 @@ enum {
 
 enum { FDTD_F32 = 1, FDTD_F64 = 2 };
 
-/* Field components.  The *_INC codes address the 1D total-field/scattered-
- * field auxiliary incident line (1D/.../program.f90:45). */
+/* Field components.  The *_INC codes address the auxiliary incident line of
+ * a total-field/scattered-field set-up: the 1D line (1D/.../program.f90:45)
+ * or the line of a 2D/3D box (fdtd_add_tfsf), whose E and H are FDTD_E_INC
+ * and FDTD_H_INC. */
 enum {
   FDTD_EX = 0, FDTD_EY = 1, FDTD_EZ = 2,
   FDTD_HX = 3, FDTD_HY = 4, FDTD_HZ = 5,
-  FDTD_EX_INC = 6, FDTD_HZ_INC = 7
+  FDTD_EX_INC = 6, FDTD_HZ_INC = 7,
+  FDTD_E_INC = 6, FDTD_H_INC = 7
 };
 
 typedef struct fdtd_grid_desc {
@@ -242,6 +245,22 @@ int fdtd_add_lorentz(fdtd_job *job, const fdtd_region *region,
  * 1D/BERpmly_ExHz_mod.f90:163-175). */
 int fdtd_add_pml(fdtd_job *job, const fdtd_pml_desc *pml);
 int fdtd_add_tfsf_1d(fdtd_job *job, const fdtd_tfsf1d_desc *tfsf);
+/* Total-field/scattered-field box for a plane wave along +y (2D and 3D).
+ * The incident wave runs on an auxiliary line along y (cells 0..ny-1),
+ * driven by FDTD_E_INC sources at row lo[1] of their box, with the two-step
+ * absorbing ends of a Ku = 0.5 line (exact in vacuum at Ku = 0.5).  Each face
+ * of the box adds the incident term to the updates that cross it, as
+ * consistCond_dy/dz/hx/hy do for Ez/Hx incidence
+ * (3D/.../include/myTFSF_incEzHx_3Dfunc.f90:80-221): 3D and 2D TM carry Ez/Hx,
+ * 2D TE carries Ex/Hz.  The total field holds Ez (Ex in TE) at cells lo..hi;
+ * a periodic axis that the box spans end to end has no faces.  Face cells
+ * must be non-dispersive main cells outside the PML.  FDTD_E_INC/FDTD_H_INC
+ * address the line in fdtd_get_field (ny values). */
+typedef struct fdtd_tfsf_desc {
+  int32_t lo[3], hi[3];  /* total-field box, inclusive cells               */
+  double eps_line;       /* relative permittivity of the incident line     */
+} fdtd_tfsf_desc;
+int fdtd_add_tfsf(fdtd_job *job, const fdtd_tfsf_desc *tfsf);
 int fdtd_add_source(fdtd_job *job, const fdtd_source_desc *src, int32_t *id);
 int fdtd_add_monitor(fdtd_job *job, const fdtd_monitor_desc *mon, int32_t *id);
 int fdtd_add_probe(fdtd_job *job, const fdtd_probe_desc *probe, int32_t *id);

@@ -140,6 +140,11 @@ struct ora_job {
   int tfsf; fdtd_tfsf1d_desc tf;
   double *exi, *hzi;             /* padded 0..N+1                     */
   oslab islab[2];
+  /* 2D/3D total-field/scattered-field box: incident line along y */
+  int tfbox; fdtd_tfsf_desc tb;
+  int tb_face[3];                /* 1: the box has faces normal to axis */
+  double *le, *lh;               /* incident line E and H, 0..ny-1      */
+  double labc[4];                /* two-step absorbing ends: low m1 m2, high m1 m2 */
   int committed;
   int last_n;
   int nth;
@@ -202,6 +207,7 @@ void ora_destroy(ora_job *J) {
   for (int a = 0; a < 3; a++) { free(J->cf1[a]); free(J->cf2[a]); free(J->cg1[a]); free(J->cg2[a]); }
   for (int q = 0; q < 12; q++) free(J->sp[q]);
   free(J->exi); free(J->hzi);
+  free(J->le); free(J->lh);
   free(J);
 }
 
@@ -681,6 +687,17 @@ int ora_commit(ora_job *J) {
     int nsplit = J->dim == 3 ? 12 : 2;
     for (int q = 0; q < nsplit; q++) J->sp[q] = zalloc(J->ntot);
   }
+  if (J->tfbox) {
+    const int n3[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; a++)
+      J->tb_face[a] = (a == 1) || (a < J->dim && !(J->g.periodic[a] && J->tb.lo[a] == 0 && J->tb.hi[a] == n3[a] - 1));
+    const int *lo = J->tb.lo, *hi = J->tb.hi;
+    if (lo[1] < 1 || hi[1] > ny - 2 || hi[1] <= lo[1]) FAIL("TFSF box rows must satisfy 1 <= lo < hi <= ny-2");
+    for (int a = 0; a < 3; a += 2)
+      if (J->tb_face[a] && (lo[a] < 1 || hi[a] > n3[a] - 2 || hi[a] <= lo[a]))
+        FAIL("TFSF box faces on axis %d must lie inside the grid", a);
+    J->le = zalloc(ny); J->lh = zalloc(ny);
+  }
   if (J->tfsf) {
     J->exi = zalloc(J->ntot); J->hzi = zalloc(J->ntot);
     if (J->pml_mode == FDTD_PML_REFERENCE && J->pml.npml[1][0] > 0) {
@@ -691,6 +708,121 @@ int ora_commit(ora_job *J) {
   }
   J->committed = 1;
   return 0;
+}
+
+static double gauss_t(const fdtd_source_desc *s, double t);
+
+/* ---- 2D/3D total-field/scattered-field box --------------------------------- */
+/* The incident plane wave runs along +y on its own line, E at rows j and H
+ * between j and j+1, with the main grid's differences: Ez/Hx for 3D and 2D TM
+ * (update_ezincz / update_hxincy, P3/include/myTFSF_incEzHx_3Dfunc.f90:80-99),
+ * Ex/Hz for 2D TE (the TE grid's own updateD/updateH,
+ * P2/include/myfdtd_2Dfunc.f90:16-44).  Its ends are the two-step absorbing
+ * boundary of ezincy_boundaryCond (P3/include/myTFSF_incEzHx_3Dfunc.f90:101-113). */
+int ora_add_tfsf(ora_job *J, const fdtd_tfsf_desc *t) {
+  if (J->committed) FAIL("job already committed");
+  if (J->dim < 2) FAIL("the TFSF box is 2D/3D; 1D uses ora_add_tfsf_1d");
+  if (!(t->eps_line > 0.0)) FAIL("eps_line must be positive");
+  J->tfbox = 1; J->tb = *t;
+  return 0;
+}
+
+/* sign of the line's differences: +1 for Ex/Hz (TE), -1 for Ez/Hx */
+static double tb_sign(const ora_job *J) { return J->g.layout == FDTD_LAYOUT_2D_TE ? 1.0 : -1.0; }
+
+static void tfbox_line_E(ora_job *J, int n) {
+  const int ny = J->ny;
+  const double cb = J->g.ku / J->tb.eps_line, sg = tb_sign(J);
+  double *e = J->le, *h = J->lh;
+  for (int j = 1; j <= ny - 2; j++) e[j] = e[j] + cb * (sg * (h[j] - h[j - 1]));
+  const double t = (double)(n - 1) * J->g.dt;
+  for (int q = 0; q < J->nsrc; q++) {
+    const fdtd_source_desc *d = &J->src[q].d;
+    if (d->component != FDTD_E_INC) continue;
+    const double g = gauss_t(d, t) * d->amp;
+    for (int j = d->lo[1]; j <= d->hi[1]; j++) e[j] = e[j] + g;
+  }
+  e[0] = J->labc[1]; J->labc[1] = J->labc[0]; J->labc[0] = e[1];
+  e[ny - 1] = J->labc[3]; J->labc[3] = J->labc[2]; J->labc[2] = e[ny - 2];
+}
+
+static void tfbox_line_H(ora_job *J) {
+  const int ny = J->ny;
+  const double Ku = J->g.ku, sg = tb_sign(J);
+  double *e = J->le, *h = J->lh;
+  for (int j = 0; j <= ny - 2; j++) h[j] = h[j] + Ku * (sg * (e[j + 1] - e[j]));
+}
+
+/* the incident terms of the D updates that cross a face (consistCond_dz /
+   consistCond_dy, P3/include/myTFSF_incEzHx_3Dfunc.f90:117-170; TE: Ex at the
+   y faces and Ey at the x faces) */
+static void tfbox_faces_D(ora_job *J) {
+  const int *lo = J->tb.lo, *hi = J->tb.hi;
+  const double Ku = J->g.ku;
+  const double *h = J->lh;
+  const int k0 = J->dim == 3 ? lo[2] : 0, k1 = J->dim == 3 ? hi[2] : 0;
+  if (J->g.layout == FDTD_LAYOUT_2D_TE) {
+    double *dx = J->F[DX], *dy = J->F[DY];
+    for (int i = lo[0]; i <= hi[0]; i++) {
+      int64_t a = cell_ix(J, i, lo[1], 0), b = cell_ix(J, i, hi[1], 0);
+      dx[a] = dx[a] - Ku * h[lo[1] - 1];
+      dx[b] = dx[b] + Ku * h[hi[1]];
+    }
+    if (J->tb_face[0])
+      for (int j = lo[1]; j <= hi[1] - 1; j++) {
+        int64_t a = cell_ix(J, lo[0], j, 0), b = cell_ix(J, hi[0] + 1, j, 0);
+        dy[a] = dy[a] + Ku * h[j];
+        dy[b] = dy[b] - Ku * h[j];
+      }
+    return;
+  }
+  double *dy = J->F[DY], *dz = J->F[DZ];
+  for (int k = k0; k <= k1; k++)
+    for (int i = lo[0]; i <= hi[0]; i++) {
+      int64_t a = cell_ix(J, i, lo[1], k), b = cell_ix(J, i, hi[1], k);
+      dz[a] = dz[a] + Ku * h[lo[1] - 1];
+      dz[b] = dz[b] - Ku * h[hi[1]];
+    }
+  if (J->dim == 3 && J->tb_face[2])
+    for (int j = lo[1]; j <= hi[1] - 1; j++)
+      for (int i = lo[0]; i <= hi[0]; i++) {
+        int64_t a = cell_ix(J, i, j, lo[2]), b = cell_ix(J, i, j, hi[2] + 1);
+        dy[a] = dy[a] - Ku * h[j];
+        dy[b] = dy[b] + Ku * h[j];
+      }
+}
+
+/* the incident terms of the H updates that cross a face (consistCond_hx /
+   consistCond_hy, P3/include/myTFSF_incEzHx_3Dfunc.f90:172-221; TE: Hz at the
+   y faces) */
+static void tfbox_faces_H(ora_job *J) {
+  const int *lo = J->tb.lo, *hi = J->tb.hi;
+  const double Ku = J->g.ku;
+  const double *e = J->le;
+  const int k0 = J->dim == 3 ? lo[2] : 0, k1 = J->dim == 3 ? hi[2] : 0;
+  if (J->g.layout == FDTD_LAYOUT_2D_TE) {
+    double *hz = J->F[HZ];
+    for (int i = lo[0]; i <= hi[0]; i++) {
+      int64_t a = cell_ix(J, i, lo[1] - 1, 0), b = cell_ix(J, i, hi[1], 0);
+      hz[a] = hz[a] - Ku * e[lo[1]];
+      hz[b] = hz[b] + Ku * e[hi[1]];
+    }
+    return;
+  }
+  double *hx = J->F[HX], *hy = J->F[HY];
+  for (int k = k0; k <= k1; k++)
+    for (int i = lo[0]; i <= hi[0]; i++) {
+      int64_t a = cell_ix(J, i, lo[1] - 1, k), b = cell_ix(J, i, hi[1], k);
+      hx[a] = hx[a] + Ku * e[lo[1]];
+      hx[b] = hx[b] - Ku * e[hi[1]];
+    }
+  if (J->tb_face[0])
+    for (int k = k0; k <= k1; k++)
+      for (int j = lo[1]; j <= hi[1]; j++) {
+        int64_t a = cell_ix(J, lo[0] - 1, j, k), b = cell_ix(J, hi[0], j, k);
+        hy[a] = hy[a] - Ku * e[j];
+        hy[b] = hy[b] + Ku * e[j];
+      }
 }
 
 /* ---- helpers for the loop ------------------------------------------------- */
@@ -1376,6 +1508,7 @@ int ora_step(ora_job *J, int n_first, int n_steps, int nth) {
     } else if (L == FDTD_LAYOUT_2D_TE) {
       te2d_updateD(J);
       apply_sources(J, n, 0);
+      if (J->tfbox) { tfbox_line_E(J, n); tfbox_faces_D(J); }
       materials_update_E(J, n);
       if (J->pml_mode == FDTD_PML_REFERENCE) te2d_pml_E(J);
       if (J->pml_mode == FDTD_PML_SPLIT) split_E(J);
@@ -1385,23 +1518,27 @@ int ora_step(ora_job *J, int n_first, int n_steps, int nth) {
       te2d_updateH(J);
       if (J->pml_mode == FDTD_PML_REFERENCE) te2d_pml_H(J);
       if (J->pml_mode == FDTD_PML_SPLIT) split_H(J);
+      if (J->tfbox) { tfbox_line_H(J); tfbox_faces_H(J); }
       /* interchange_H: Hz x-wrap */
       if (J->g.periodic[0]) wrap_x_both(J, J->F[HZ], 1);
       if (J->g.periodic[1]) wrap_y_both(J, J->F[HZ]);
     } else if (L == FDTD_LAYOUT_2D_TM) {
       tm2d_updateD(J);
       apply_sources(J, n, 0);
+      if (J->tfbox) { tfbox_line_E(J, n); tfbox_faces_D(J); }
       materials_update_E(J, n);
       if (J->pml_mode == FDTD_PML_SPLIT) split_E(J);
       if (J->g.periodic[0]) wrap_x_high(J, J->F[EZ]);
       if (J->g.periodic[1]) wrap_y_both(J, J->F[EZ]);
       tm2d_updateH(J);
       if (J->pml_mode == FDTD_PML_SPLIT) split_H(J);
+      if (J->tfbox) { tfbox_line_H(J); tfbox_faces_H(J); }
       if (J->g.periodic[0]) wrap_x_low(J, J->F[HY]);
       if (J->g.periodic[1]) wrap_y_low(J, J->F[HX]);
     } else {
       d3_updateD(J, nth);
       apply_sources(J, n, 0);
+      if (J->tfbox) { tfbox_line_E(J, n); tfbox_faces_D(J); }
       materials_update_E(J, n);
       if (J->pml_mode == FDTD_PML_REFERENCE) d3_pml_E(J);
       if (J->pml_mode == FDTD_PML_SPLIT) split_E(J);
@@ -1412,6 +1549,7 @@ int ora_step(ora_job *J, int n_first, int n_steps, int nth) {
       d3_updateH(J, nth);
       if (J->pml_mode == FDTD_PML_REFERENCE) d3_pml_H(J);
       if (J->pml_mode == FDTD_PML_SPLIT) split_H(J);
+      if (J->tfbox) { tfbox_line_H(J); tfbox_faces_H(J); }
       /* interchange_H (P3/include/mympi_func.f90:522-690) */
       if (J->g.periodic[0]) { wrap_x_low(J, J->F[HY]); wrap_x_low(J, J->F[HZ]); }
       if (J->g.periodic[1]) { wrap_y_low(J, J->F[HX]); wrap_y_low(J, J->F[HZ]); }
@@ -1431,6 +1569,10 @@ static int field_index(ora_job *J, int comp) {
 
 int ora_get_field(ora_job *J, int comp, double *host) {
   if (field_index(J, comp) < 0) FAIL("bad component");
+  if (J->tfbox && comp >= FDTD_E_INC) {  /* the box's incident line: ny values */
+    memcpy(host, comp == FDTD_E_INC ? J->le : J->lh, sizeof(double) * (size_t)J->ny);
+    return 0;
+  }
   double *F = comp_ptr(J, comp);
   if (!F) FAIL("component not present");
   int64_t q = 0;

@@ -33,6 +33,7 @@ int ora_add_graphene(ora_job *job, const fdtd_region *region, const fdtd_graphen
 int ora_add_lorentz(ora_job *job, const fdtd_region *region, const fdtd_lorentz_desc *p);
 int ora_add_pml(ora_job *job, const fdtd_pml_desc *pml);
 int ora_add_tfsf_1d(ora_job *job, const fdtd_tfsf1d_desc *tfsf);
+int ora_add_tfsf(ora_job *job, const fdtd_tfsf_desc *tfsf);
 int ora_add_source(ora_job *job, const fdtd_source_desc *src);
 int ora_add_monitor(ora_job *job, const fdtd_monitor_desc *mon);
 int ora_add_probe(ora_job *job, const fdtd_probe_desc *probe);

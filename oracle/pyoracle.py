@@ -33,9 +33,9 @@ def lib():
         L.ora_error.restype = C.c_char_p
         for name in ("ora_add_dielectric",):
             getattr(L, name).argtypes = [vp, vp, C.c_double]
-        for name in ("ora_add_gold", "ora_add_graphene", "ora_add_lorentz", "ora_add_pml", "ora_add_tfsf_1d",
+        for name in ("ora_add_gold", "ora_add_graphene", "ora_add_lorentz", "ora_add_pml", "ora_add_tfsf_1d", "ora_add_tfsf",
                      "ora_add_source", "ora_add_monitor", "ora_add_probe"):
-            getattr(L, name).argtypes = [vp, vp] if name in ("ora_add_pml", "ora_add_tfsf_1d", "ora_add_source",
+            getattr(L, name).argtypes = [vp, vp] if name in ("ora_add_pml", "ora_add_tfsf_1d", "ora_add_tfsf", "ora_add_source",
                                                               "ora_add_monitor", "ora_add_probe") else [vp, vp, vp]
         L.ora_commit.argtypes = [vp]
         L.ora_step.argtypes = [vp, C.c_int, C.c_int, C.c_int]
@@ -81,6 +81,9 @@ class OracleJob:
         if spec.tfsf:
             t = S.tfsf_struct(spec.tfsf)
             self._check(L.ora_add_tfsf_1d(self.h, C.byref(t)))
+        if spec.tfsf_box:
+            t = S.tfsf_box_struct(spec.tfsf_box)
+            self._check(L.ora_add_tfsf(self.h, C.byref(t)))
         for s in spec.sources:
             d = S.source_struct(s)
             self._check(L.ora_add_source(self.h, C.byref(d)))
@@ -106,10 +109,12 @@ class OracleJob:
         self.step(self.n_done + 1, n_steps)
 
     def get_field(self, comp):
+        from fdtd_gpu import spec as S
         n = self.spec.n
-        out = np.empty(n[0] * n[1] * n[2])
+        cnt = S.field_count(self.spec, comp)
+        out = np.empty(cnt)
         self._check(lib().ora_get_field(self.h, int(comp), out.ctypes.data))
-        return out.reshape(n[2], n[1], n[0])
+        return out if cnt != self.spec.cells() else out.reshape(n[2], n[1], n[0])
 
     def set_field(self, comp, arr):
         a = np.ascontiguousarray(arr, dtype=np.float64).ravel()

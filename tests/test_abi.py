@@ -39,13 +39,14 @@ def test_struct_sizes_match_header(built, tmp_path):
                    'sizeof(fdtd_grid_desc),sizeof(fdtd_region),sizeof(fdtd_drude2cp),'
                    'sizeof(fdtd_graphene_desc),sizeof(fdtd_pml_desc),sizeof(fdtd_source_desc),'
                    'sizeof(fdtd_monitor_desc),sizeof(fdtd_probe_desc),sizeof(fdtd_tfsf1d_desc),'
-                   'sizeof(fdtd_lorentz_desc));return 0;}\n')
+                   'sizeof(fdtd_lorentz_desc));printf("%zu\\n",sizeof(fdtd_tfsf_desc));return 0;}\n')
     exe = tmp_path / "sz"
     import subprocess
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     got = [C.sizeof(t) for t in (abi.GridDesc, abi.Region, abi.Drude2CP, abi.GrapheneDesc, abi.PmlDesc,
-                                 abi.SourceDesc, abi.MonitorDesc, abi.ProbeDesc, abi.Tfsf1dDesc, abi.LorentzDesc)]
+                                 abi.SourceDesc, abi.MonitorDesc, abi.ProbeDesc, abi.Tfsf1dDesc, abi.LorentzDesc,
+                                 abi.TfsfDesc)]
     assert [int(x) for x in out] == got
 
 

@@ -423,3 +423,63 @@ def test_lorentz_3d_sphere_vs_oracle(gpu, oracle_lib, prec):
         check_state(J, O, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ))
     else:
         assert err <= TOL32_DFT
+
+
+# ---------------------------------------------------------------------------
+# 2D/3D total-field/scattered-field box
+# ---------------------------------------------------------------------------
+def _tfsf_masks(spec, meta, shape, npml=10):
+    lo, hi = meta["box"]
+    inside = np.zeros(shape, bool)
+    inside[lo[2]:hi[2] + 1, lo[1]:hi[1] + 1, lo[0]:hi[0] + 1] = True
+    core = np.zeros(shape, bool)
+    px = 0 if spec.periodic[0] else npml
+    zs = slice(npml, shape[0] - npml) if spec.layout == abi.LAYOUT_3D else slice(None)
+    core[zs, npml:shape[1] - npml, px:shape[2] - px] = True
+    return inside, core & ~inside
+
+
+TFSF_CASES = [(abi.LAYOUT_2D_TM, False, 128, 1200), (abi.LAYOUT_2D_TE, True, 128, 1200),
+              (abi.LAYOUT_2D_TE, False, 128, 1200), (abi.LAYOUT_3D, False, 64, 500)]
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("layout,periodic_x,n,steps", TFSF_CASES)
+def test_tfsf_plane_wave_fills_the_box_only(gpu, prec, layout, periodic_x, n, steps):
+    """In vacuum the box holds exactly the incident line's wave and the
+    scattered region stays empty: to rounding in FP64, to FP32 rounding of
+    the incident amplitude in FP32."""
+    spec, meta = problems.config_tfsf(layout=layout, periodic_x=periodic_x, n=n, precision=prec)
+    J = gpu.Job(spec)
+    J.step(1, steps // 2)
+    ce = abi.EX if layout == abi.LAYOUT_2D_TE else abi.EZ
+    e, le = J.get_field(ce), J.get_field(abi.E_INC)
+    inside, outside = _tfsf_masks(spec, meta, e.shape)
+    peak = np.abs(e[inside]).max()
+    tol = 1e-12 if prec == abi.F64 else 1e-5
+    assert peak > 0
+    assert np.abs(e[inside] - np.broadcast_to(le[None, :, None], e.shape)[inside]).max() <= tol * peak
+    assert np.abs(e[outside]).max() <= tol * peak
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("layout,periodic_x,n,steps", TFSF_CASES)
+def test_tfsf_scatterer_vs_oracle(gpu, oracle_lib, prec, layout, periodic_x, n, steps):
+    """A gold cylinder (2D) or sphere (3D) in the box: the scattered field
+    leaves the box through the faces."""
+    spec, meta = problems.config_tfsf(layout=layout, periodic_x=periodic_x, n=n, precision=prec,
+                                      scatterer="gold", radius=8.0)
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, 3)
+    if prec == abi.F64:
+        assert err <= TOL64
+        comps = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ) if layout == abi.LAYOUT_3D else \
+            (abi.EX, abi.EY, abi.HZ) if layout == abi.LAYOUT_2D_TE else (abi.EZ, abi.HX, abi.HY)
+        check_state(J, O, comps)
+        assert rel_l2(J.get_field(abi.E_INC), O.get_field(abi.E_INC)) <= TOL64
+        assert rel_l2(J.get_field(abi.H_INC), O.get_field(abi.H_INC)) <= TOL64
+    else:
+        assert err <= TOL32_DFT
