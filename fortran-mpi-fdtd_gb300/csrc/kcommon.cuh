@@ -255,6 +255,17 @@ __device__ __forceinline__ T ade_update(const StepParams<T> &p, const AdeCoef<T>
   return ade_update_state<T>(p.ade_state, p.ade_stride, slot, comp, a, inc, eold);
 }
 
+// vals[c] for a component number known only at run time, by constant-index
+// selects: an indexed read would put the caller's array in local memory
+template <typename T>
+__device__ __forceinline__ T pick6(const T *vals, int c) {
+  T r = vals[0];
+#pragma unroll
+  for (int q = 1; q < 6; ++q)
+    if (c == q) r = vals[q];
+  return r;
+}
+
 // Fused sampling: write the monitored components of cell (i,j,k) into this
 // step's stage row, and probe samples.  vals[c] = value of component c.
 template <typename T>
@@ -265,7 +276,7 @@ __device__ __forceinline__ void gather_cell(const StepParams<T> &p, int n, int i
     const int wx = m.hi[0] - m.lo[0] + 1, wy = m.hi[1] - m.lo[1] + 1;
     const long long idx = (long long)(i - m.lo[0]) + (long long)wx * ((j - m.lo[1]) + (long long)wy * (k - m.lo[2]));
     T *row = p.stage + (long long)p.slot * p.stage_row + m.base;
-    for (int u = 0; u < m.ncomp; ++u) row[(long long)u * m.ncell + idx] = vals[m.comps[u]];
+    for (int u = 0; u < m.ncomp; ++u) row[(long long)u * m.ncell + idx] = pick6(vals, m.comps[u]);
   }
   for (int q = 0; q < p.nprobe; ++q) {
     const Probe &pr = p.probe[q];
@@ -274,7 +285,7 @@ __device__ __forceinline__ void gather_cell(const StepParams<T> &p, int n, int i
     const long long st = n - pr.n_first;
     if (st >= pr.cap) continue;
     double *out = pr.buf + st * pr.ncomp;
-    for (int u = 0; u < pr.ncomp; ++u) out[u] = (double)vals[pr.comps[u]];
+    for (int u = 0; u < pr.ncomp; ++u) out[u] = (double)pick6(vals, pr.comps[u]);
   }
 }
 
