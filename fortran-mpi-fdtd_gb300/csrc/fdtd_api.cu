@@ -149,6 +149,7 @@ struct fdtd_job {
   long long stage_cap_rows = 0;
   int stage_fill = 0, stage_n0 = 1;
   double *d_omega = nullptr, *d_acc_re = nullptr, *d_acc_im = nullptr;
+  double *d_rot = nullptr;  // per frequency and ring slot: cos, sin of w s dt
   long long acc_total = 0;
   bool gather_fused = true;
   int dft_blocks = 0;
@@ -889,6 +890,17 @@ int commit_impl(fdtd_job *J) {
   if (!omega.empty()) {
     if ((rc = alloc_dev(J, (void **)&J->d_omega, omega.size() * sizeof(double)))) return rc;
     CK(cudaMemcpy(J->d_omega, omega.data(), omega.size() * sizeof(double), cudaMemcpyHostToDevice));
+    // e^{i w s dt} for the slots of a DFT ring
+    std::vector<double> rot(omega.size() * 2 * kStageSteps);
+    for (size_t f = 0; f < omega.size(); ++f)
+      for (int sl = 0; sl < kStageSteps; ++sl) {
+        const double ph = omega[f] * ((double)sl * J->g.dt);
+        rot[(f * kStageSteps + sl) * 2] = std::cos(ph);
+        rot[(f * kStageSteps + sl) * 2 + 1] = std::sin(ph);
+      }
+    if ((rc = alloc_dev(J, (void **)&J->d_rot, rot.size() * sizeof(double)))) return rc;
+    CK(cudaMemcpy(J->d_rot, rot.data(), rot.size() * sizeof(double), cudaMemcpyHostToDevice));
+    J->h2d += rot.size() * sizeof(double);
     J->h2d += omega.size() * sizeof(double);
   }
   if ((rc = alloc_dev(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
@@ -1115,6 +1127,7 @@ int dft_fold(fdtd_job *J) {
     d.nmon = (int)J->mon_dev.size();
     for (int q = 0; q < d.nmon; ++q) d.mon[q] = J->mon_dev[q];
     d.omega = J->d_omega;
+    d.rot = (const double2 *)J->d_rot;
     d.acc_re = J->d_acc_re;
     d.acc_im = J->d_acc_im;
     d.dt = J->g.dt;
@@ -1347,6 +1360,7 @@ int ring_graph(fdtd_job *J) {
     d.nmon = (int)J->mon_dev.size();
     for (int q = 0; q < d.nmon; ++q) d.mon[q] = J->mon_dev[q];
     d.omega = J->d_omega;
+    d.rot = (const double2 *)J->d_rot;
     d.acc_re = J->d_acc_re;
     d.acc_im = J->d_acc_im;
     d.dt = J->g.dt;
@@ -1686,6 +1700,7 @@ int pack_capture(fdtd::Pack *P) {
     d.nmon = (int)J->mon_dev.size();
     for (int m = 0; m < d.nmon; ++m) d.mon[m] = J->mon_dev[m];
     d.omega = J->d_omega;
+    d.rot = (const double2 *)J->d_rot;
     d.acc_re = J->d_acc_re;
     d.acc_im = J->d_acc_im;
     d.dt = J->g.dt;
@@ -2193,7 +2208,8 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
   }
   for (auto &M : J->mons) {
     const uint64_t smp = (uint64_t)M.ncomp * M.ncell;
-    b += smp * (J->dim == 1 ? 4096 : kStageSteps) * w + 2 * smp * M.d.nfreq * 8 + (uint64_t)M.d.nfreq * 8;
+    b += smp * (J->dim == 1 ? 4096 : kStageSteps) * w + 2 * smp * M.d.nfreq * 8 + (uint64_t)M.d.nfreq * 8 +
+         (uint64_t)M.d.nfreq * kStageSteps * 16;
   }
   for (auto &P : J->probes) b += 1024ull * P.ncomp * 8;
   *bytes = b + (1ull << 20);  // coefficient tables, source table, step counter

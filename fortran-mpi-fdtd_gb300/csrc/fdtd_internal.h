@@ -220,6 +220,8 @@ struct DftParams {
   int nmon;
   Monitor mon[kMaxMon];
   const double *omega;     // all monitors' frequencies
+  const double2 *rot;      // per frequency, e^{i w s dt} for s < kStageSteps;
+                           // null: one sincos per (frequency, slot)
   double *acc_re, *acc_im; // FP64 accumulators
   int nslots;              // valid slots in this fold (0..kStageSteps)
   int n0;                  // step number of slot 0 (eager launches)

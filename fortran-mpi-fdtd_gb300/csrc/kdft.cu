@@ -9,7 +9,12 @@
 // frequencies adds sum_s cos(w t_s) F_s (and sin) into the FP64
 // accumulators.  Phases are computed in FP64 (sincos of w*t); the products
 // and the ring sum run in the job's precision; the accumulators are FP64.
-// Slots outside a monitor's [n_first, n_last] get zero weight.
+// Slots outside a monitor's [n_first, n_last] get zero weight.  With the
+// job's rotation table the phases of a ring come from one FP64 sincos per
+// frequency, e^{i w t0}, times the table's e^{i w s dt}:
+// cos(w (t0 + s dt)) = cos(w t0) cos(w s dt) - sin(w t0) sin(w s dt).
+// Without it (the allocation-free entry point) each (frequency, slot) takes
+// its own sincos.
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.h"
@@ -41,13 +46,30 @@ __global__ void __launch_bounds__(kDftThreads) dft_kernel(const __grid_constant_
   if (nlast < m.n_first || n0 > m.n_last) return;
   const int fc = b / sblocks, sb = b % sblocks;
   const int f0 = fc * kFreqChunk;
+  __shared__ double bc[kFreqChunk], bs[kFreqChunk];
+  if (d.rot) {
+    if (threadIdx.x < kFreqChunk) {
+      double c = 1.0, sn = 0.0;
+      if (f0 + (int)threadIdx.x < m.nfreq)
+        sincos(d.omega[m.freq_off + f0 + threadIdx.x] * ((double)(n0 - 1) * d.dt), &sn, &c);
+      bc[threadIdx.x] = c;
+      bs[threadIdx.x] = sn;
+    }
+    __syncthreads();
+  }
   for (int t = threadIdx.x; t < kFreqChunk * kStageSteps; t += kDftThreads) {
     const int f = t / kStageSteps, s = t % kStageSteps;
     double c = 0.0, sn = 0.0;
     const int n = n0 + s;
     if (f0 + f < m.nfreq && s < d.nslots && n >= m.n_first && n <= m.n_last) {
-      const double tt = (double)(n - 1) * d.dt;          // t=real(n-1,8)*dt
-      sincos(d.omega[m.freq_off + f0 + f] * tt, &sn, &c);
+      if (d.rot) {
+        const double2 r = d.rot[(long long)(m.freq_off + f0 + f) * kStageSteps + s];
+        c = bc[f] * r.x - bs[f] * r.y;
+        sn = bs[f] * r.x + bc[f] * r.y;
+      } else {
+        const double tt = (double)(n - 1) * d.dt;          // t=real(n-1,8)*dt
+        sincos(d.omega[m.freq_off + f0 + f] * tt, &sn, &c);
+      }
     }
     cw[f][s] = T(c);
     sw[f][s] = T(sn);
