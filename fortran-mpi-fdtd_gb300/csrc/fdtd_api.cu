@@ -186,6 +186,12 @@ struct fdtd_job {
   int *d_edge = nullptr;
   cudaStream_t side[2] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {};
+  // 2D: programmatic events of the last two core kernels; prog_prev indexes
+  // the one the next half step's side kernels may wait on (-1: none, after
+  // any other kernel on the job's stream)
+  cudaEvent_t ev_prog[2] = {};
+  int prog_prev = -1;
+  bool join_rec[2] = {false, false};
 };
 
 namespace {
@@ -371,6 +377,7 @@ int make_branches(fdtd_job *J) {
   for (int q = 0; q < 2; ++q) {
     CK(cudaStreamCreateWithFlags(&J->side[q], cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&J->ev_join[q], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&J->ev_prog[q], cudaEventDisableTiming));
   }
   CK(cudaEventCreateWithFlags(&J->ev_fork, cudaEventDisableTiming));
   return FDTD_OK;
@@ -1146,6 +1153,7 @@ int dft_fold(fdtd_job *J) {
   }
   J->stage_n0 += J->stage_fill;
   J->stage_fill = 0;
+  J->prog_prev = -1;
   return FDTD_OK;
 }
 
@@ -1159,8 +1167,9 @@ enum { ST_E = 1, ST_H = 2, ST_SAMPLE = 4 };
 // runs launch them one after another so that each part's events time that
 // part alone.
 template <typename T>
-int launch_part(const fdtd_job *J, const StepParams<T> &p, int part, bool e_half, cudaStream_t s) {
-  if (J->dim == 2) return e_half ? launch_e2d<T>(p, part, s) : launch_h2d<T>(p, part, s);
+int launch_part(const fdtd_job *J, const StepParams<T> &p, int part, bool e_half, cudaStream_t s,
+                cudaEvent_t prog_event = nullptr) {
+  if (J->dim == 2) return e_half ? launch_e2d<T>(p, part, s, prog_event) : launch_h2d<T>(p, part, s, prog_event);
   return e_half ? launch_e3d<T>(p, part, s) : launch_h3d<T>(p, part, s);
 }
 
@@ -1173,28 +1182,44 @@ int run_parts(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], bool e
   for (int q = 0; q < 3; ++q)
     if (want[q] && units[q] > 0) use[nuse++] = q;
   const bool par = !J->prof && nuse > 1;
+  // 2D: the side kernels of this half step wait on the previous core
+  // kernel's programmatic event rather than on its completion, so that they
+  // are ready together with this half's core kernel (they wait for the
+  // previous core kernel in their own pdl_wait), and fully on the side
+  // streams' previous kernels; otherwise they fork off the job's stream.
+  const bool chain = par && J->dim == 2 && use[0] == K2D_CORE;
+  const bool prog = chain && J->prog_prev >= 0;
   cudaStream_t st[3] = {J->stream, J->stream, J->stream};
   if (par) {
-    CK(cudaEventRecord(J->ev_fork, J->stream));
+    if (!prog) CK(cudaEventRecord(J->ev_fork, J->stream));
     for (int b = 1; b < nuse; ++b) {
       st[b] = J->side[b - 1];
-      CK(cudaStreamWaitEvent(st[b], J->ev_fork, 0));
+      if (prog) {
+        CK(cudaStreamWaitEvent(st[b], J->ev_prog[J->prog_prev], 0));
+        for (int c = 0; c < 2; ++c)
+          if (c != b - 1 && J->join_rec[c]) CK(cudaStreamWaitEvent(st[b], J->ev_join[c], 0));
+      } else {
+        CK(cudaStreamWaitEvent(st[b], J->ev_fork, 0));
+      }
     }
   }
+  const int cur = J->prog_prev == 0 ? 1 : 0;
   for (int b = 0; b < nuse; ++b) {
     const int q = use[b];
     const int k = q == K2D_CORE ? (e_half ? FDTD_KERNEL_E : FDTD_KERNEL_H) : kind[q];
     if (!graph) ev_record(J, k, true);
-    J->launches += launch_part<T>(J, p, q, e_half, st[b]);
+    J->launches += launch_part<T>(J, p, q, e_half, st[b], chain && q == K2D_CORE ? J->ev_prog[cur] : nullptr);
     if (!graph) ev_record(J, k, false);
   }
   CK(cudaGetLastError());
   if (par) {
     for (int b = 1; b < nuse; ++b) {
       CK(cudaEventRecord(J->ev_join[b - 1], st[b]));
+      J->join_rec[b - 1] = true;
       CK(cudaStreamWaitEvent(J->stream, J->ev_join[b - 1], 0));
     }
   }
+  J->prog_prev = chain ? cur : -1;
   return FDTD_OK;
 }
 
@@ -1270,6 +1295,7 @@ int tfsf_part(fdtd_job *J, const StepParams<T> &p, bool e_half, bool graph) {
   if (!graph) ev_record(J, FDTD_KERNEL_EDGE, true);
   J->launches += launch_tfsf<T>(p, e_half, J->stream);
   if (!graph) ev_record(J, FDTD_KERNEL_EDGE, false);
+  J->prog_prev = -1;
   CK(cudaGetLastError());
   return FDTD_OK;
 }
@@ -1315,6 +1341,7 @@ int sample_sep(fdtd_job *J, int n, int slot = -1, bool graph = false) {
   p.slot = slot >= 0 ? slot : J->stage_fill;
   p.d_base = graph ? J->d_base : nullptr;
   J->launches += launch_gather<T>(p, J->stream);
+  J->prog_prev = -1;
   CK(cudaGetLastError());
   return FDTD_OK;
 }
@@ -1348,6 +1375,7 @@ int ring_graph(fdtd_job *J) {
   if (!J->d_base && (rc = alloc_dev(J, (void **)&J->d_base, sizeof(int)))) return rc;
   CK(cudaStreamSynchronize(J->stream));
   const long long launches0 = J->launches;
+  J->prog_prev = -1;  // events recorded outside the capture cannot be waited on inside it
   CK(cudaStreamBeginCapture(J->stream, cudaStreamCaptureModeThreadLocal));
   int bad = FDTD_OK;
   for (int s = 0; s < kStageSteps && !bad; ++s) {
@@ -1373,6 +1401,7 @@ int ring_graph(fdtd_job *J) {
   }
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(J->stream, &g);
+  J->prog_prev = -1;
   J->graph_kernels = (int)(J->launches - launches0);
   J->launches = launches0;
   if (bad) { if (g) cudaGraphDestroy(g); return bad; }
@@ -1390,6 +1419,7 @@ int replay_ring(fdtd_job *J, int n0) {
   set_base_kernel<<<1, 1, 0, J->stream>>>(J->d_base, n0);
   CK(cudaGetLastError());
   CK(cudaGraphLaunch(J->graph_exec, J->stream));
+  J->prog_prev = -1;
   J->launches += 1 + J->graph_kernels;
   J->stage_n0 = n0 + kStageSteps;
   J->last_n = n0 + kStageSteps - 1;
@@ -1887,6 +1917,7 @@ int fdtd_destroy(fdtd_job *J) {
   for (int q = 0; q < 2; ++q) {
     if (J->side[q]) cudaStreamDestroy(J->side[q]);
     if (J->ev_join[q]) cudaEventDestroy(J->ev_join[q]);
+    if (J->ev_prog[q]) cudaEventDestroy(J->ev_prog[q]);
   }
   if (J->ev_fork) cudaEventDestroy(J->ev_fork);
   if (J->own_stream) cudaStreamDestroy(J->own_stream);

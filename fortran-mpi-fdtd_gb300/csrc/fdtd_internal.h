@@ -193,7 +193,8 @@ constexpr int kAdeFields = 2 * kMaxPoles;
 // launchers (defined in k2d.cu / k3d.cu / k1d.cu / kdft.cu)
 // 2D half steps: the parts of one half step are independent launches
 enum K2dPart { K2D_CORE = 0, K2D_EDGE = 1, K2D_ADE = 2 };
-template <typename T> int launch_e2d(const StepParams<T> &p, int part, void *stream);
+// prog_event: the core kernel records it as a programmatic event (or null)
+template <typename T> int launch_e2d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
 
 // packs of 2D jobs: one launch runs one part of every job's half step
 constexpr int kMaxPack = 32;
@@ -205,7 +206,7 @@ struct PackLaunch {
 };
 template <typename T>
 int launch_pack2d(const PackLaunch<T> &a, int layout, int vec, bool e_half, int part, void *stream);
-template <typename T> int launch_h2d(const StepParams<T> &p, int part, void *stream);
+template <typename T> int launch_h2d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
 template <typename T> int launch_e3d(const StepParams<T> &p, int part, void *stream);
 template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *stream);
 

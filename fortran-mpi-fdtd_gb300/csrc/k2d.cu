@@ -545,22 +545,26 @@ __global__ void __launch_bounds__(NT) h2d_core(const __grid_constant__ StepParam
 // dispersive-cell kernels, which run beside them, launch plainly: releasing
 // their successors early measured slower).
 template <typename T, int L, int V, int NT>
-void launch_core2(const StepParams<T> &p, bool e_half, cudaStream_t s) {
+void launch_core2(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
   const int blocks = (p.ncore + NT - 1) / NT;
-  if (e_half) launch_pdl(e2d_core<T, L, V, NT>, blocks, NT, s, p);
-  else launch_pdl(h2d_core<T, L, V, NT>, blocks, NT, s, p);
+  if (e_half) launch_pdl(e2d_core<T, L, V, NT>, blocks, NT, s, p, ev);
+  else launch_pdl(h2d_core<T, L, V, NT>, blocks, NT, s, p, ev);
 }
 
 // tile 0: 128 threads, 1: 256, 2: 512
 template <typename T, int L, int V>
-void launch_core2_tiled(const StepParams<T> &p, bool e_half, cudaStream_t s) {
-  if (p.tile == 0) launch_core2<T, L, V, 128>(p, e_half, s);
-  else if (p.tile == 2) launch_core2<T, L, V, 512>(p, e_half, s);
-  else launch_core2<T, L, V, 256>(p, e_half, s);
+void launch_core2_tiled(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
+  if (p.tile == 0) launch_core2<T, L, V, 128>(p, e_half, s, ev);
+  else if (p.tile == 2) launch_core2<T, L, V, 512>(p, e_half, s, ev);
+  else launch_core2<T, L, V, 256>(p, e_half, s, ev);
 }
 
+// The edge and dispersive-cell kernels may be launched early, off the
+// previous core kernel's programmatic event (run_parts): they wait for it
+// here first (a no-op without such a dependency).
 template <typename T, int L, int V>
 __global__ void __launch_bounds__(256) e2d_edge(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
   const int t = blockIdx.x * 256 + threadIdx.x;
   if (t >= p.nedge) return;
   K2<T, L, V>::unit_e(p, __ldg(p.edge_units + t), step_n(p));
@@ -568,6 +572,7 @@ __global__ void __launch_bounds__(256) e2d_edge(const __grid_constant__ StepPara
 
 template <typename T, int L, int V>
 __global__ void __launch_bounds__(256) h2d_edge(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
   const int t = blockIdx.x * 256 + threadIdx.x;
   if (t >= p.nedge) return;
   K2<T, L, V>::unit_h(p, __ldg(p.edge_units + t), step_n(p));
@@ -575,48 +580,53 @@ __global__ void __launch_bounds__(256) h2d_edge(const __grid_constant__ StepPara
 
 template <typename T, int L>
 __global__ void __launch_bounds__(256) e2d_ade(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
   const int s = blockIdx.x * 256 + threadIdx.x;
   if (s < p.nade) ade_e2<T, L>(p, s, step_n(p));
 }
 
 // V: cells per unit along x; 4 (float) / 2 (double) when the row length
 // allows aligned vector access, else 1.  Returns the kernels launched (0/1).
+// `ev`: the core kernel's programmatic event (see launch_pdl), or null; side
+// kernels launch with the device's top priority
 template <typename T, int L, int V>
-int launch_e2d_v(const StepParams<T> &p, int part, cudaStream_t s) {
+int launch_e2d_v(const StepParams<T> &p, int part, cudaStream_t s, cudaEvent_t ev) {
   const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge : p.nade;
   if (units <= 0) return 0;
   const int blocks = (units + 255) / 256;
-  if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, true, s);
-  else if (part == K2D_EDGE) e2d_edge<T, L, V><<<blocks, 256, 0, s>>>(p);
-  else e2d_ade<T, L><<<blocks, 256, 0, s>>>(p);
+  if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, true, s, ev);
+  else if (part == K2D_EDGE) launch_side(e2d_edge<T, L, V>, blocks, 256, s, p);
+  else launch_side(e2d_ade<T, L>, blocks, 256, s, p);
   return 1;
 }
 template <typename T, int L, int V>
-int launch_h2d_v(const StepParams<T> &p, int part, cudaStream_t s) {
+int launch_h2d_v(const StepParams<T> &p, int part, cudaStream_t s, cudaEvent_t ev) {
   const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge : 0;
   if (units <= 0) return 0;
   const int blocks = (units + 255) / 256;
-  if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, false, s);
-  else h2d_edge<T, L, V><<<blocks, 256, 0, s>>>(p);
+  if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, false, s, ev);
+  else launch_side(h2d_edge<T, L, V>, blocks, 256, s, p);
   return 1;
 }
 
 template <typename T>
-int launch_e2d(const StepParams<T> &p, int part, void *stream) {
+int launch_e2d(const StepParams<T> &p, int part, void *stream, void *prog_event) {
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t ev = (cudaEvent_t)prog_event;
   if (p.layout == 3)
-    return p.vec == VW ? launch_e2d_v<T, 3, VW>(p, part, s) : launch_e2d_v<T, 3, 1>(p, part, s);
-  return p.vec == VW ? launch_e2d_v<T, 2, VW>(p, part, s) : launch_e2d_v<T, 2, 1>(p, part, s);
+    return p.vec == VW ? launch_e2d_v<T, 3, VW>(p, part, s, ev) : launch_e2d_v<T, 3, 1>(p, part, s, ev);
+  return p.vec == VW ? launch_e2d_v<T, 2, VW>(p, part, s, ev) : launch_e2d_v<T, 2, 1>(p, part, s, ev);
 }
 
 template <typename T>
-int launch_h2d(const StepParams<T> &p, int part, void *stream) {
+int launch_h2d(const StepParams<T> &p, int part, void *stream, void *prog_event) {
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t ev = (cudaEvent_t)prog_event;
   if (p.layout == 3)
-    return p.vec == VW ? launch_h2d_v<T, 3, VW>(p, part, s) : launch_h2d_v<T, 3, 1>(p, part, s);
-  return p.vec == VW ? launch_h2d_v<T, 2, VW>(p, part, s) : launch_h2d_v<T, 2, 1>(p, part, s);
+    return p.vec == VW ? launch_h2d_v<T, 3, VW>(p, part, s, ev) : launch_h2d_v<T, 3, 1>(p, part, s, ev);
+  return p.vec == VW ? launch_h2d_v<T, 2, VW>(p, part, s, ev) : launch_h2d_v<T, 2, 1>(p, part, s, ev);
 }
 
 // ---- packs: one launch runs the same part of many jobs' half steps ---------
@@ -717,9 +727,9 @@ int launch_pack2d(const PackLaunch<T> &a, int layout, int vec, bool e_half, int 
 template int launch_pack2d<float>(const PackLaunch<float> &, int, int, bool, int, void *);
 template int launch_pack2d<double>(const PackLaunch<double> &, int, int, bool, int, void *);
 
-template int launch_e2d<float>(const StepParams<float> &, int, void *);
-template int launch_e2d<double>(const StepParams<double> &, int, void *);
-template int launch_h2d<float>(const StepParams<float> &, int, void *);
-template int launch_h2d<double>(const StepParams<double> &, int, void *);
+template int launch_e2d<float>(const StepParams<float> &, int, void *, void *);
+template int launch_e2d<double>(const StepParams<double> &, int, void *, void *);
+template int launch_h2d<float>(const StepParams<float> &, int, void *, void *);
+template int launch_h2d<double>(const StepParams<double> &, int, void *, void *);
 
 }  // namespace fdtd

@@ -21,16 +21,53 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 __device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // launch a step kernel with a programmatic dependency on the kernel before it
-// on the stream (the kernel starts with pdl_wait)
+// on the stream (the kernel starts with pdl_wait).  With `ev`, the launch also
+// records ev as a programmatic event that fires once every block has started:
+// kernels on other streams that wait on it may launch early and then wait in
+// their own pdl_wait for this kernel's completion.
 template <typename K, typename P>
-inline void launch_pdl(K kernel, int blocks, int threads, cudaStream_t s, const P &p) {
+inline void launch_pdl(K kernel, int blocks, int threads, cudaStream_t s, const P &p, cudaEvent_t ev = nullptr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(threads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  int na = 1;
+  if (ev) {
+    at[1].id = cudaLaunchAttributeProgrammaticEvent;
+    at[1].val.programmaticEvent.event = ev;
+    at[1].val.programmaticEvent.flags = 0;
+    at[1].val.programmaticEvent.triggerAtBlockStart = 1;
+    na = 2;
+  }
+  cfg.attrs = at;
+  cfg.numAttrs = na;
+  cudaLaunchKernelEx(&cfg, kernel, p);
+}
+
+// launch a small kernel that runs beside a large one with the device's
+// highest scheduling priority, so that its blocks are dispatched ahead of the
+// large kernel's pending blocks
+inline int side_priority() {
+  static int prio = [] {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
+    return greatest;
+  }();
+  return prio;
+}
+
+template <typename K, typename P>
+inline void launch_side(K kernel, int blocks, int threads, cudaStream_t s, const P &p) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
   cfg.blockDim = dim3(threads);
   cfg.stream = s;
   cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = side_priority();
   cfg.attrs = at;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, kernel, p);
