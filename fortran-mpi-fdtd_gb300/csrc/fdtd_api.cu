@@ -186,7 +186,7 @@ struct fdtd_job {
   int *d_edge = nullptr;
   cudaStream_t side[2] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {};
-  // 2D: programmatic events of the last two core kernels; prog_prev indexes
+  // programmatic events of the last two core kernels; prog_prev indexes
   // the one the next half step's side kernels may wait on (-1: none, after
   // any other kernel on the job's stream)
   cudaEvent_t ev_prog[2] = {};
@@ -1170,7 +1170,7 @@ template <typename T>
 int launch_part(const fdtd_job *J, const StepParams<T> &p, int part, bool e_half, cudaStream_t s,
                 cudaEvent_t prog_event = nullptr) {
   if (J->dim == 2) return e_half ? launch_e2d<T>(p, part, s, prog_event) : launch_h2d<T>(p, part, s, prog_event);
-  return e_half ? launch_e3d<T>(p, part, s) : launch_h3d<T>(p, part, s);
+  return e_half ? launch_e3d<T>(p, part, s, prog_event) : launch_h3d<T>(p, part, s, prog_event);
 }
 
 template <typename T>
@@ -1182,12 +1182,12 @@ int run_parts(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], bool e
   for (int q = 0; q < 3; ++q)
     if (want[q] && units[q] > 0) use[nuse++] = q;
   const bool par = !J->prof && nuse > 1;
-  // 2D: the side kernels of this half step wait on the previous core
+  // The side kernels of this half step wait on the previous core
   // kernel's programmatic event rather than on its completion, so that they
   // are ready together with this half's core kernel (they wait for the
   // previous core kernel in their own pdl_wait), and fully on the side
   // streams' previous kernels; otherwise they fork off the job's stream.
-  const bool chain = par && J->dim == 2 && use[0] == K2D_CORE;
+  const bool chain = par && use[0] == K2D_CORE;
   const bool prog = chain && J->prog_prev >= 0;
   cudaStream_t st[3] = {J->stream, J->stream, J->stream};
   if (par) {

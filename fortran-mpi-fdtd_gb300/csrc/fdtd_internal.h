@@ -207,8 +207,8 @@ struct PackLaunch {
 template <typename T>
 int launch_pack2d(const PackLaunch<T> &a, int layout, int vec, bool e_half, int part, void *stream);
 template <typename T> int launch_h2d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
-template <typename T> int launch_e3d(const StepParams<T> &p, int part, void *stream);
-template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *stream);
+template <typename T> int launch_e3d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
+template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
 
 // separate gather (per-procedure API, or monitors inside reference slabs)
 // returns the kernels launched

@@ -458,9 +458,11 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
 }
 
 // general launch: blockIdx selects edge units, reference slab cells, then
-// dispersive cells
+// dispersive cells.  It may be launched early, off the previous core kernel's
+// programmatic event, and then waits for that kernel here first.
 template <typename T, int V>
 __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
   const int n = step_n(p);
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
@@ -482,6 +484,7 @@ __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepPa
 
 template <typename T, int V>
 __global__ void __launch_bounds__(256) h3d_kernel(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
     const int t = b * 256 + threadIdx.x;
@@ -574,61 +577,63 @@ __global__ void __launch_bounds__(32 * RY) h3d_core(const __grid_constant__ Step
 }
 
 template <typename T, int V, int RY>
-void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s) {
+void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
   const int blocks = ((p.cw + 31) / 32) * ((p.ch + RY - 1) / RY) * p.cd;
-  if (e_half) launch_pdl(e3d_core<T, V, RY>, blocks, 32 * RY, s, p);
-  else launch_pdl(h3d_core<T, V, RY>, blocks, 32 * RY, s, p);
+  if (e_half) launch_pdl(e3d_core<T, V, RY>, blocks, 32 * RY, s, p, ev);
+  else launch_pdl(h3d_core<T, V, RY>, blocks, 32 * RY, s, p, ev);
 }
 
 // tile 0: 4 rows of 32 x-vectors, 1: 8 rows, 2: 16 rows
 template <typename T>
-void launch_core3_tiled(const StepParams<T> &p, bool e_half, cudaStream_t s) {
+void launch_core3_tiled(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   if (p.vec == VW) {
-    if (p.tile == 0) launch_core3<T, VW, 4>(p, e_half, s);
-    else if (p.tile == 2) launch_core3<T, VW, 16>(p, e_half, s);
-    else launch_core3<T, VW, 8>(p, e_half, s);
+    if (p.tile == 0) launch_core3<T, VW, 4>(p, e_half, s, ev);
+    else if (p.tile == 2) launch_core3<T, VW, 16>(p, e_half, s, ev);
+    else launch_core3<T, VW, 8>(p, e_half, s, ev);
   } else {
-    if (p.tile == 0) launch_core3<T, 1, 4>(p, e_half, s);
-    else if (p.tile == 2) launch_core3<T, 1, 16>(p, e_half, s);
-    else launch_core3<T, 1, 8>(p, e_half, s);
+    if (p.tile == 0) launch_core3<T, 1, 4>(p, e_half, s, ev);
+    else if (p.tile == 2) launch_core3<T, 1, 16>(p, e_half, s, ev);
+    else launch_core3<T, 1, 8>(p, e_half, s, ev);
   }
 }
 
+// `prog_event`: the core kernel's programmatic event (see launch_pdl), or
+// null; the general kernel launches with the device's top priority
 template <typename T>
-int launch_e3d(const StepParams<T> &p, int part, void *stream) {
+int launch_e3d(const StepParams<T> &p, int part, void *stream, void *prog_event) {
   cudaStream_t s = (cudaStream_t)stream;
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   if (part == K2D_CORE) {
     if (p.ncore <= 0) return 0;
-    launch_core3_tiled<T>(p, true, s);
+    launch_core3_tiled<T>(p, true, s, (cudaEvent_t)prog_event);
     return 1;
   }
   const int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
   if (blocks <= 0) return 0;
-  if (p.vec == VW) e3d_kernel<T, VW><<<blocks, 256, 0, s>>>(p);
-  else e3d_kernel<T, 1><<<blocks, 256, 0, s>>>(p);
+  if (p.vec == VW) launch_side(e3d_kernel<T, VW>, blocks, 256, s, p);
+  else launch_side(e3d_kernel<T, 1>, blocks, 256, s, p);
   return 1;
 }
 template <typename T>
-int launch_h3d(const StepParams<T> &p, int part, void *stream) {
+int launch_h3d(const StepParams<T> &p, int part, void *stream, void *prog_event) {
   cudaStream_t s = (cudaStream_t)stream;
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   if (part == K2D_CORE) {
     if (p.ncore <= 0) return 0;
-    launch_core3_tiled<T>(p, false, s);
+    launch_core3_tiled<T>(p, false, s, (cudaEvent_t)prog_event);
     return 1;
   }
   const int blocks = p.ntile_blocks + p.nslab_blocks;
   if (blocks <= 0) return 0;
-  if (p.vec == VW) h3d_kernel<T, VW><<<blocks, 256, 0, s>>>(p);
-  else h3d_kernel<T, 1><<<blocks, 256, 0, s>>>(p);
+  if (p.vec == VW) launch_side(h3d_kernel<T, VW>, blocks, 256, s, p);
+  else launch_side(h3d_kernel<T, 1>, blocks, 256, s, p);
   return 1;
 }
 
-template int launch_e3d<float>(const StepParams<float> &, int, void *);
-template int launch_e3d<double>(const StepParams<double> &, int, void *);
-template int launch_h3d<float>(const StepParams<float> &, int, void *);
-template int launch_h3d<double>(const StepParams<double> &, int, void *);
+template int launch_e3d<float>(const StepParams<float> &, int, void *, void *);
+template int launch_e3d<double>(const StepParams<double> &, int, void *, void *);
+template int launch_h3d<float>(const StepParams<float> &, int, void *, void *);
+template int launch_h3d<double>(const StepParams<double> &, int, void *, void *);
 
 }  // namespace fdtd
