@@ -150,6 +150,8 @@ struct fdtd_job {
   int stage_fill = 0, stage_n0 = 1;
   double *d_omega = nullptr, *d_acc_re = nullptr, *d_acc_im = nullptr;
   double *d_rot = nullptr;  // per frequency and ring slot: cos, sin of w s dt
+  double *d_mean_part = nullptr;   // mean monitors: partial sums per block
+  unsigned *d_mean_ctr = nullptr;  // mean monitors: blocks done per component
   long long acc_total = 0;
   bool gather_fused = true;
   int dft_blocks = 0;
@@ -830,6 +832,7 @@ int commit_impl(fdtd_job *J) {
   int foff = 0;
   std::vector<double> omega;
   bool touches_slab = false, has_mean = false;
+  int mean_slots = 0;
   for (auto &M : J->mons) {
     Monitor m{};
     for (int a = 0; a < 3; ++a) { m.lo[a] = M.d.lo[a]; m.hi[a] = M.d.hi[a]; }
@@ -844,7 +847,16 @@ int commit_impl(fdtd_job *J) {
     m.freq_off = foff;
     m.mean = M.d.reduce == FDTD_MONITOR_MEAN;
     m.boxcells = (int)M.boxcells;
-    if (m.mean) has_mean = true;
+    if (m.mean) {
+      has_mean = true;
+      // blocks of about 4096 cells: whole x-rows of the box
+      const int wx = m.hi[0] - m.lo[0] + 1;
+      const int rows = (m.hi[1] - m.lo[1] + 1) * (m.hi[2] - m.lo[2] + 1);
+      m.mrows = std::max(1, 4096 / wx);
+      m.mchunks = (rows + m.mrows - 1) / m.mrows;
+      m.mpart = mean_slots;
+      mean_slots += m.ncomp * m.mchunks;
+    }
     base += (long long)M.ncomp * M.ncell;
     acc += (long long)M.ncomp * M.d.nfreq * M.ncell;
     foff += M.d.nfreq;
@@ -857,6 +869,10 @@ int commit_impl(fdtd_job *J) {
   for (auto &P : J->probes)
     if (ref && J->dim == 3 && J->slab_rows > 0 && (P.d.cell[1] <= J->slab_rows - 1 || P.d.cell[1] >= ny - J->slab_rows))
       touches_slab = true;
+  if (mean_slots > 0) {
+    if ((rc = alloc_dev(J, (void **)&J->d_mean_part, (size_t)mean_slots * sizeof(double)))) return rc;
+    if ((rc = alloc_dev(J, (void **)&J->d_mean_ctr, (size_t)mean_slots * sizeof(unsigned)))) return rc;
+  }
   if (J->has_tfbox && (rc = check_tfbox(J, mat))) return rc;
   // 2D samples fused into the H edge rows unless a monitor reduces its box
   // (the reduction runs in the stand-alone gather) or a TFSF box adds face
@@ -1014,6 +1030,8 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   for (int q = 0; q < p.nmon; ++q) p.mon[q] = J->mon_dev[q];
   p.stage = (T *)J->d_stage;
   p.stage_row = J->stage_row;
+  p.mean_part = J->d_mean_part;
+  p.mean_ctr = J->d_mean_ctr;
   p.nprobe = (int)J->probes.size();
   for (int q = 0; q < p.nprobe; ++q) {
     const ProbeRec &P = J->probes[q];
@@ -2241,6 +2259,8 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
     const uint64_t smp = (uint64_t)M.ncomp * M.ncell;
     b += smp * (J->dim == 1 ? 4096 : kStageSteps) * w + 2 * smp * M.d.nfreq * 8 + (uint64_t)M.d.nfreq * 8 +
          (uint64_t)M.d.nfreq * kStageSteps * 16;
+    if (M.d.reduce == FDTD_MONITOR_MEAN)  // partial sums and counters: at most one block per x-row
+      b += (uint64_t)M.ncomp * ((uint64_t)(M.d.hi[1] - M.d.lo[1] + 1) * (M.d.hi[2] - M.d.lo[2] + 1) + 1) * 12;
   }
   for (auto &P : J->probes) b += 1024ull * P.ncomp * 8;
   *bytes = b + (1ull << 20);  // coefficient tables, source table, step counter

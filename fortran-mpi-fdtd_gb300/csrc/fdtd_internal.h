@@ -81,6 +81,10 @@ struct Monitor {
   int freq_off;            // offset into the omega table
   int mean;                // 1: one sample per component, the box mean
   int boxcells;            // cells of the box
+  int mrows;               // mean: x-rows of the box summed per block
+  int mchunks;             // mean: blocks per component (ceil(rows / mrows))
+  int mpart;               // mean: first partial-sum slot (and counter) of
+                           // this monitor's components, mchunks per component
 };
 
 struct Probe {
@@ -164,6 +168,8 @@ struct StepParams {
   const int *d_base;       // graph replays: step number of ring slot 0 on the
                            // device; then n = *d_base + slot
   int vec;                 // cells per thread along x in the 2D tile path
+  double *mean_part;       // mean monitors: FP64 partial sums per block
+  unsigned *mean_ctr;      // mean monitors: blocks done per component
   // 2D/3D total-field/scattered-field box (plane wave along +y)
   int tf_on;
   int tf_lo[3], tf_hi[3];  // total-field box, inclusive cells

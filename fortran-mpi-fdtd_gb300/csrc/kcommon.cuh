@@ -47,6 +47,21 @@ inline void launch_pdl(K kernel, int blocks, int threads, cudaStream_t s, const 
   cudaLaunchKernelEx(&cfg, kernel, p);
 }
 
+// launch_pdl for a kernel of two parameters
+template <typename K, typename P, typename Q>
+inline void launch_pdl2(K kernel, int blocks, int threads, cudaStream_t s, const P &p, const Q &q) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(threads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, p, q);
+}
+
 // launch a small kernel that runs beside a large one with the device's
 // highest scheduling priority, so that its blocks are dispatched ahead of the
 // large kernel's pending blocks

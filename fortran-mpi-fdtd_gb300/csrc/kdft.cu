@@ -106,12 +106,13 @@ void launch_dft(const DftParams &d, const T *stage, void *stream) {
 template void launch_dft<float>(const DftParams &, const float *, void *);
 template void launch_dft<double>(const DftParams &, const double *, void *);
 
+constexpr int kMeanThreads = 256;  // threads per block of the gather launch
+
 // Stand-alone gather of the monitored cells and probes after the H update:
 // one thread per monitored (component, cell) sample, plus one per probe.
 template <typename T>
-__global__ void gather_kernel(const __grid_constant__ StepParams<T> p) {
+__device__ __forceinline__ void gather_cells(const StepParams<T> &p, long long t) {
   const int n = step_n(p);
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const T *F[6] = {p.ex, p.ey, p.ez, p.hx, p.hy, p.hz};
   for (int q = 0; q < p.nmon; ++q) {
     const Monitor &m = p.mon[q];
@@ -144,41 +145,84 @@ __global__ void gather_kernel(const __grid_constant__ StepParams<T> p) {
   }
 }
 
-// Mean monitors: one block per (monitor, component) sums the box in FP64 --
-// each thread a strided subset in order, then a warp-shuffle tree and the
-// warps' partial sums in order, so the result does not depend on timing --
-// and stages the mean as the component's one sample.
-constexpr int kMeanThreads = 256;
-
+// Mean monitors: the box is cut into blocks of m.mrows whole x-rows.  Each
+// block sums its cells in FP64 -- each thread the cells threadIdx.x,
+// threadIdx.x + 256, ... of its rows taken row after row (eight loads issued
+// before they are added, in that order), then a warp-shuffle tree and the
+// warps' sums in order -- into its partial-sum slot.  The last block of a
+// component to finish (a per-component counter) adds the partial sums in
+// block order, stages the mean as the component's one sample and resets the
+// counter.  The result depends on neither which block finishes last nor
+// timing.
 template <typename T>
-__global__ void __launch_bounds__(kMeanThreads) gather_mean_kernel(const __grid_constant__ StepParams<T> p) {
+__device__ __forceinline__ void gather_mean(const StepParams<T> &p, int b) {
   __shared__ double part[kMeanThreads / 32];
-  int b = blockIdx.x, q = 0;
+  __shared__ int last;
+  int q = 0;
   for (; q < p.nmon; ++q) {
     if (!p.mon[q].mean) continue;
-    if (b < p.mon[q].ncomp) break;
-    b -= p.mon[q].ncomp;
+    const int nb = p.mon[q].ncomp * p.mon[q].mchunks;
+    if (b < nb) break;
+    b -= nb;
   }
   if (q >= p.nmon) return;  // uniform over the block
   const Monitor &m = p.mon[q];
+  const int u = b / m.mchunks, chunk = b % m.mchunks;
   const T *F[6] = {p.ex, p.ey, p.ez, p.hx, p.hy, p.hz};
-  const T *f = F[m.comps[b]];
+  const T *f = F[m.comps[u]];
   const int wx = m.hi[0] - m.lo[0] + 1, wy = m.hi[1] - m.lo[1] + 1;
+  const int rows = wy * (m.hi[2] - m.lo[2] + 1);
+  const int r0 = chunk * m.mrows, r1 = min(rows, r0 + m.mrows);
+  const int ne = (r1 - r0) * wx;  // the block's cells, row after row
   double sum = 0.0;
   if (f)
-    for (int c = threadIdx.x; c < m.boxcells; c += kMeanThreads) {
-      const int i = m.lo[0] + c % wx, j = m.lo[1] + (c / wx) % wy, k = m.lo[2] + c / (wx * wy);
-      sum += (double)f[(long long)i + (long long)p.nx * (j + (long long)p.ny * k)];
+    for (int e0 = threadIdx.x; e0 < ne; e0 += 8 * kMeanThreads) {
+      T v[8];  // eight loads in flight, then added in order
+#pragma unroll
+      for (int q8 = 0; q8 < 8; ++q8) {
+        const int e = e0 + q8 * kMeanThreads;
+        v[q8] = T(0);
+        if (e < ne) {
+          const int r = r0 + e / wx, i = e % wx;
+          const int j = m.lo[1] + r % wy, k = m.lo[2] + r / wy;
+          v[q8] = f[(long long)(m.lo[0] + i) + (long long)p.nx * (j + (long long)p.ny * k)];
+        }
+      }
+#pragma unroll
+      for (int q8 = 0; q8 < 8; ++q8) sum += (double)v[q8];
     }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
   if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = sum;
   __syncthreads();
+  const int slot = m.mpart + u * m.mchunks;
   if (threadIdx.x == 0) {
     double tot = 0.0;
     for (int w = 0; w < kMeanThreads / 32; ++w) tot += part[w];
-    p.stage[(long long)p.slot * p.stage_row + m.base + b] = T(tot / (double)m.boxcells);
+    p.mean_part[slot + chunk] = tot;
+    __threadfence();
+    last = atomicAdd(p.mean_ctr + slot, 1u) == (unsigned)(m.mchunks - 1);
   }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double tot = 0.0;
+    for (int c = 0; c < m.mchunks; ++c) tot += __ldcg(p.mean_part + slot + c);
+    p.stage[(long long)p.slot * p.stage_row + m.base + u] = T(tot / (double)m.boxcells);
+    p.mean_ctr[slot] = 0u;
+  }
+}
+
+// One launch for both: the first blocks stage monitored cells and probes,
+// the rest reduce the mean monitors.  It follows the H half step with a
+// programmatic dependency and releases the next kernel at once, so the next
+// E half's launch overlaps it.
+template <typename T>
+__global__ void __launch_bounds__(kMeanThreads) gather_kernel(const __grid_constant__ StepParams<T> p, int cell_blocks) {
+  pdl_wait();
+  pdl_release();
+  if ((int)blockIdx.x < cell_blocks) gather_cells<T>(p, (long long)blockIdx.x * kMeanThreads + threadIdx.x);
+  else gather_mean<T>(p, (int)blockIdx.x - cell_blocks);
 }
 
 template <typename T>
@@ -187,20 +231,12 @@ int launch_gather(const StepParams<T> &p, void *stream) {
   int nmean = 0;
   for (int q = 0; q < p.nmon; ++q) {
     total += (long long)p.mon[q].ncomp * p.mon[q].ncell;
-    if (p.mon[q].mean) nmean += p.mon[q].ncomp;
+    if (p.mon[q].mean) nmean += p.mon[q].ncomp * p.mon[q].mchunks;
   }
-  int launched = 0;
-  if (total > 0) {
-    const int threads = 256;
-    const long long blocks = (total + threads - 1) / threads;
-    gather_kernel<T><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(p);
-    ++launched;
-  }
-  if (nmean > 0) {
-    gather_mean_kernel<T><<<nmean, kMeanThreads, 0, (cudaStream_t)stream>>>(p);
-    ++launched;
-  }
-  return launched;
+  const int cell_blocks = (int)((total + kMeanThreads - 1) / kMeanThreads);
+  if (cell_blocks + nmean <= 0) return 0;
+  launch_pdl2(gather_kernel<T>, cell_blocks + nmean, kMeanThreads, (cudaStream_t)stream, p, cell_blocks);
+  return 1;
 }
 
 template int launch_gather<float>(const StepParams<float> &, void *);
