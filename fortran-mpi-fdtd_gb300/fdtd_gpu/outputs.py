@@ -21,6 +21,15 @@ RTA_2Dfdtd.data (3D/.../transforms/calR_Sy.f90:16-35).
 Free-format records use a full-precision exponent form that Fortran
 list-directed input reads; the fixed-format records follow the reference's
 edit descriptors (E30.19, F30.19, F15.5, E20.10).
+
+``write_reference_3d`` does the same for the 3D program
+(3D/.../program.f90:355-378, 436-690; fileid_tracks.txt): per-step records of
+all six components at the incident, reflected and transmitted points
+(7E30.19), the Sy spectra, the tf_r products of the row k = kc
+(2F15.5,4E20.10) and the timesLiney frames along y at (ic, kc) (7F10.5),
+over its six y-ranks.  The program's maps and VTK frames are switched off
+(printTimesMap, printTimesVTK = .false., program.f90:13-15) and so are not
+written.
 """
 import math
 import os
@@ -169,3 +178,75 @@ def cal_r_sy(transforms_dir, inc=0, ref=0, tras=2, out_name="RTA_2Dfdtd.data"):
         for row in rows:
             fh.write(free(*row) + "\n")
     return rows
+
+
+def poynting_3d_ordered(re, im, ds):
+    """Sy per frequency in the program's summation order (k outer, i inner;
+    program.f90:613-685); re/im: (4, nfreq, ncell) with (Ex, Ez, Hx, Hz)."""
+    ex, ez, hx, hz = 0, 1, 2, 3
+    nf, nc = re.shape[1], re.shape[2]
+    out = np.zeros(nf)
+    for m in range(nf):
+        s = 0.0
+        for c in range(nc):
+            s = s + ((re[hx, m, c] * re[ez, m, c]) + (im[hx, m, c] * im[ez, m, c]) -
+                     (re[hz, m, c] * re[ex, m, c]) - (im[hz, m, c] * im[ex, m, c])) * ds
+        out[m] = s
+    return out
+
+
+def write_reference_3d(outdir, meta, monitors, probes, lines, nranks=6):
+    """Writes the reference 3D program's files under ``outdir``.
+
+    meta      the meta dict of ``problems.reference_3d()``
+    monitors  [(re, im)] of its three plane monitors (incident, reflected,
+              transmitted), each (4, nfreq, nx*nz) for (Ex, Ez, Hx, Hz)
+    probes    [samples] of its three probes (infld, tfld, rfld), each
+              (steps, 6) for (Ex, Ey, Ez, Hx, Hy, Hz), from the probe's first
+              step (meta["probe_first"])
+    lines     {frame: (6, ny)} the six components along y at (ic, kc) at
+              step frame*dn
+    """
+    ds, dt = meta["ds"], meta["dt"]
+    nx, ny, nz = meta["nx"], meta["ny"], meta["nz"]
+    rows = rank_rows(ny, nranks)
+    tr = os.path.join(outdir, "transforms")
+    os.makedirs(tr, exist_ok=True)
+    os.makedirs(os.path.join(outdir, "timesLiney"), exist_ok=True)
+    firsts = meta["probe_first"]
+    ptiny, ptty, kc = meta["ptiny"] - 1, meta["ptty"] - 1, meta["kc"] - 1
+
+    # ---- per-step records: write(2|3|4,'(7E30.19)') n*dt, ex..hz (:445-520) ----
+    for q, (name, j) in enumerate((("infld", ptiny), ("tfld", ptty), ("rfld", ptiny))):
+        k = owner(rows, j)
+        with open(os.path.join(tr, f"r{k}{name}.dat"), "w") as fh:
+            for s, vals in enumerate(probes[q]):
+                n = firsts[q] + s
+                fh.write(fortran_e(n * dt, 30, 19) + "".join(fortran_e(v, 30, 19) for v in vals) + "\n")
+
+    # ---- spectra and tf_r (:613-685) ----
+    lam = 2.0 * math.pi * problems.C0 / np.asarray(meta["arg"]) / NANO
+    sy = [poynting_3d_ordered(re, im, ds) for re, im in monitors]
+    for q, (name, j) in enumerate((("Syin", ptiny), ("Syr", ptiny), ("Syt", ptty))):
+        with open(os.path.join(tr, f"r{owner(rows, j)}{name}.dat"), "w") as fh:
+            for m in range(len(lam)):
+                fh.write(free(lam[m], sy[q][m]) + "\n")
+    re, im = monitors[1]
+    ex, ez, hx, hz = 0, 1, 2, 3
+    with open(os.path.join(tr, f"r{owner(rows, ptiny)}tf_r.dat"), "w") as fh:
+        for m in range(len(lam)):
+            for i in range(nx):
+                c = i + nx * kc
+                fh.write(fortran_f(lam[m], 15, 5) + fortran_f((i + 1) * ds / NANO, 15, 5) +
+                         fortran_e(re[hx, m, c] * re[ez, m, c], 20, 10) + fortran_e(im[hx, m, c] * im[ez, m, c], 20, 10) +
+                         fortran_e(re[hz, m, c] * re[ex, m, c], 20, 10) + fortran_e(im[hz, m, c] * im[ex, m, c], 20, 10) +
+                         "\n")
+            fh.write("\n")
+
+    # ---- frames along y at (ic, kc): write(400+frame,'(7F10.5)') (:563-583) ----
+    for f, line in lines.items():
+        for k, (a, b) in enumerate(rows):
+            with open(os.path.join(outdir, "timesLiney", f"r{k}E_time{f}.dat"), "w") as fh:
+                for j in range(a, b):
+                    fh.write(fortran_f((j + 1) * ds / NANO, 10, 5) +
+                             "".join(fortran_f(line[u][j], 10, 5) for u in range(6)) + "\n")

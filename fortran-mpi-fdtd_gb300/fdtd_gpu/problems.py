@@ -274,10 +274,13 @@ def reference_3d(precision=abi.F64, nt=None):
     spec.add_monitor(*plane(ptiny), comps, arg, tfinStop + 1, 2 ** 31 - 1)
     spec.add_monitor(*plane(ptty), comps, arg, 1, 2 ** 31 - 1)
     six = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    # the per-step records of infld, tfld and rfld (program.f90:441-520)
     spec.add_probe((ic - 1, ptiny - 1, kc - 1), six, 1, tfinStop - 1)
     spec.add_probe((ic - 1, ptty - 1, kc - 1), six, 1, 2 ** 31 - 1)
+    spec.add_probe((ic - 1, ptiny - 1, kc - 1), six, tfinStop + 1, 2 ** 31 - 1)
     meta = dict(sigmam=sigmam, dt=dt, ds=ds, Nt=Nt if nt is None else nt, tfinStop=tfinStop, ic=ic, kc=kc,
-                ptty=ptty, arg=arg, nx=nx, ny=ny, nz=nz)
+                ptty=ptty, ptiny=ptiny, arg=arg, nx=nx, ny=ny, nz=nz, dn=int(Nt / 20.0), Ymax=Ymax,
+                probe_first=(1, 1, tfinStop + 1))
     return spec, meta
 
 

@@ -483,3 +483,35 @@ def test_tfsf_scatterer_vs_oracle(gpu, oracle_lib, prec, layout, periodic_x, n, 
         assert rel_l2(J.get_field(abi.H_INC), O.get_field(abi.H_INC)) <= TOL64
     else:
         assert err <= TOL32_DFT
+
+
+def test_3d_reference_output_files(gpu, tmp_path):
+    """The 3D program run on the GPU and written as its per-rank files: the
+    records hold the run's values, the record counts follow the program's
+    gates, and calR_Sy on the files gives finite R, T, A within [-0.05, 1.05]."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden_2d import load_table
+    from fdtd_gpu import outputs
+    spec, meta = problems.reference_3d()
+    six = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    J = gpu.Job(spec)
+    ic, kc = meta["ic"] - 1, meta["kc"] - 1
+    lines, n = {}, 0
+    for f in range(1, 21):
+        target = f * meta["dn"]
+        J.step(n + 1, target - n)
+        n = target
+        lines[f] = np.stack([J.get_field(c)[kc, :, ic] for c in six])
+    J.step(n + 1, meta["Nt"] - n)
+    mons = [J.get_monitor(q) for q in range(3)]
+    probes = [J.get_probe(q) for q in range(3)]
+    assert [len(p) for p in probes] == [meta["tfinStop"] - 1, meta["Nt"], meta["Nt"] - meta["tfinStop"]]
+    outputs.write_reference_3d(str(tmp_path), meta, mons, probes, lines)
+    tr = tmp_path / "transforms"
+    np.testing.assert_array_equal(load_table(str(tr / "r5tfld.dat"))[:, 1:], probes[1])
+    rows = outputs.cal_r_sy(str(tr), inc=0, ref=0, tras=5, out_name="RTA_3Dfdtd.data")
+    assert np.all(np.isfinite(rows))
+    assert rows[:, 1:].min() > -0.05 and rows[:, 1:3].max() < 1.05
+    line = np.concatenate([load_table(str(tmp_path / "timesLiney" / f"r{k}E_time20.dat")) for k in range(6)])
+    np.testing.assert_allclose(line[:, 1:].T, lines[20], atol=5.01e-6)

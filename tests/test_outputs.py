@@ -67,3 +67,40 @@ def test_cal_r_sy_on_written_spectra(tmp_path):
     np.testing.assert_array_equal(rows[:, 1:], np.stack([r, t, a], 1))
     back = load_table(str(tmp_path / "transforms" / "RTA_2Dfdtd.data"))
     np.testing.assert_array_equal(back, rows)
+
+
+def test_write_read_round_trip_3d(tmp_path):
+    """The 3D program's files: per-step records (7E30.19, exact for doubles),
+    Sy spectra in the program's summation order, tf_r at k = kc, the y-line
+    frames (7F10.5) split over the six y-ranks, and calR_Sy's RTA on them."""
+    spec, meta = problems.reference_3d()
+    rng = np.random.default_rng(2)
+    nf, nx, ny, nz = len(meta["arg"]), meta["nx"], meta["ny"], meta["nz"]
+    mons = [(rng.standard_normal((4, nf, nx * nz)), rng.standard_normal((4, nf, nx * nz))) for _ in range(3)]
+    probes = [rng.standard_normal((n, 6)) for n in (5, 7, 3)]
+    lines = {2: rng.uniform(-1, 1, (6, ny))}
+    outputs.write_reference_3d(str(tmp_path), meta, mons, probes, lines)
+    tr = tmp_path / "transforms"
+    assert outputs.rank_rows(ny, 6)[0] == (0, 211)
+    for name, q, k in (("infld", 0, 0), ("tfld", 1, 5), ("rfld", 2, 0)):
+        t = load_table(str(tr / f"r{k}{name}.dat"))
+        np.testing.assert_array_equal(t[:, 1:], probes[q])
+        first = meta["probe_first"][q]
+        np.testing.assert_allclose(t[:, 0], np.arange(first, first + len(probes[q])) * meta["dt"], rtol=1e-15)
+    for name, q, k in (("Syin", 0, 0), ("Syr", 1, 0), ("Syt", 2, 5)):
+        t = load_table(str(tr / f"r{k}{name}.dat"))
+        np.testing.assert_array_equal(t[:, 1], outputs.poynting_3d_ordered(*mons[q], meta["ds"]))
+    np.testing.assert_allclose(outputs.poynting_3d_ordered(*mons[0], meta["ds"]),
+                               problems.poynting_3d_y(*mons[0], meta["ds"]), rtol=1e-12)
+    tf = load_table(str(tr / "r0tf_r.dat"))
+    assert tf.shape == (nf * nx, 6)
+    re, im = mons[1]
+    c = np.arange(nx) + nx * (meta["kc"] - 1)
+    np.testing.assert_allclose(tf[:nx, 2], re[2, 0, c] * re[1, 0, c], rtol=5.01e-10)
+    np.testing.assert_allclose(tf[:nx, 5], im[3, 0, c] * im[0, 0, c], rtol=5.01e-10)
+    line = np.concatenate([load_table(str(tmp_path / "timesLiney" / f"r{k}E_time2.dat")) for k in range(6)])
+    assert line.shape == (ny, 7)
+    np.testing.assert_allclose(line[:, 1:].T, lines[2], atol=5.01e-6)
+    rows = outputs.cal_r_sy(str(tr), inc=0, ref=0, tras=5, out_name="RTA_3Dfdtd.data")
+    sy = [outputs.poynting_3d_ordered(*m, meta["ds"]) for m in mons]
+    np.testing.assert_array_equal(rows[:, 1:], np.stack(outputs.rta(*sy), 1))
