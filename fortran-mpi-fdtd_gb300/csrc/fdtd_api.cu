@@ -1280,7 +1280,8 @@ int tune_tiles(fdtd_job *J) {
   CK(cudaEventCreate(&b));
   float best = 3.0e38f;
   int choice = 1;
-  for (int c = 0; c < 3; ++c) {
+  const int nshapes = J->dim == 3 ? 6 : 3;  // 3D: also the z-marching kernels
+  for (int c = 0; c < nshapes; ++c) {
     p.tile = c;
     for (int w = 0; w < 2; ++w) {
       launch_part<T>(J, p, K2D_CORE, true, J->stream);
@@ -2295,7 +2296,8 @@ int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
 int fdtd_set_tile(fdtd_job *J, int32_t tile) {
   int rc = check_job(J, false);
   if (rc) return rc;
-  if (tile < 0 || tile > 3) return set_err(FDTD_EINVAL, "tile must be 0 (tune) or 1..3");
+  const int maxt = J->dim == 3 ? 6 : 3;
+  if (tile < 0 || tile > maxt) return set_err(FDTD_EINVAL, "tile must be 0 (tune) or 1..%d", maxt);
   J->tile_req = tile;
   return FDTD_OK;
 }

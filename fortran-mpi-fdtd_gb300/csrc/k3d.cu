@@ -576,6 +576,138 @@ __global__ void __launch_bounds__(32 * RY) h3d_core(const __grid_constant__ Step
   vst<T, V>(p.hz + c, hz);
 }
 
+// ---- z-marching core kernels: one thread owns an x-vector of one row and
+// walks KZ planes upward.  The E half keeps Hx, Hy of the plane below from
+// the previous plane's loads, the H half takes Ex, Ey of the plane above as
+// the next plane's own values, so each cell reads two vectors fewer.  The
+// arithmetic per cell is that of e3d_core / h3d_core, term for term.
+template <typename T, int V, int RY, int KZ>
+struct Core3z {
+  int j, k0, k1, i0;
+  bool live;
+  __device__ __forceinline__ Core3z(const StepParams<T> &p) {
+    const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
+    const int bx = (p.cw + 31) >> 5, by = (p.ch + RY - 1) / RY;
+    const int b = blockIdx.x, tx = b % bx, t2 = b / bx, ty = t2 % by, tz = t2 / by;
+    const int v = tx * 32 + lane, r = ty * RY + wy;
+    k0 = p.cz0 + tz * KZ;
+    k1 = min(p.cz0 + p.cd, k0 + KZ);
+    live = v < p.cw && r < p.ch && k0 < k1;
+    j = p.cy0 + r;
+    i0 = (p.cv0 + v) * V;
+  }
+};
+
+template <typename T, int V, int RY, int KZ>
+__global__ void __launch_bounds__(32 * RY) e3d_corez(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
+  pdl_release();
+  const Core3z<T, V, RY, KZ> u(p);
+  if (!u.live) return;
+  const long long plane = (long long)p.nx * p.ny;
+  long long c = ((long long)u.k0 * p.ny + u.j) * p.nx + u.i0;
+  T hyb[V], hxb[V];
+  nb_vec<T, V>(p, p.hy, c, u.j, u.k0, 0, -1, hyb);
+  nb_vec<T, V>(p, p.hx, c, u.j, u.k0, 0, -1, hxb);
+  for (int k = u.k0; k < u.k1; ++k, c += plane) {
+    T hx[V], hy[V], hz[V], hzd[V], hxd[V], ex[V], ey[V], ez[V];
+    uint8_t id[V];
+    vld_ro<T, V>(p.hx + c, hx);
+    vld_ro<T, V>(p.hy + c, hy);
+    vld_ro<T, V>(p.hz + c, hz);
+    nb_vec<T, V>(p, p.hz, c, u.j, k, -1, 0, hzd);
+    nb_vec<T, V>(p, p.hx, c, u.j, k, -1, 0, hxd);
+    const T hzl = nb_x<T, V>(p, p.hz, c, u.i0, -1), hyl = nb_x<T, V>(p, p.hy, c, u.i0, -1);
+    vld<T, V>(p.ex + c, ex);
+    vld<T, V>(p.ey + c, ey);
+    vld<T, V>(p.ez + c, ez);
+    vld_ids<V>(p.mat + c, id);
+    if (!__ldg(p.rowflag + (long long)k * p.ny + u.j)) {  // source rows: general launch
+      bool uni = true;
+#pragma unroll
+      for (int q = 0; q < V; ++q) uni &= id[q] == p.id0;
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        const T ca = uni ? p.ca0 : coef_ca3(p, id[q]);
+        const T curlhzy = hz[q] - hzd[q], curlhyz = -hy[q] + hyb[q];
+        const T curlhxz = hx[q] - hxb[q], curlhzx = -hz[q] + (q ? hz[q - 1] : hzl);
+        const T curlhyx = hy[q] - (q ? hy[q - 1] : hyl), curlhxy = -hx[q] + hxd[q];
+        ex[q] = ex[q] + ca * (curlhzy + curlhyz);
+        ey[q] = ey[q] + ca * (curlhxz + curlhzx);
+        ez[q] = ez[q] + ca * (curlhyx + curlhxy);
+      }
+      if (uni) {
+        vst<T, V>(p.ex + c, ex);
+        vst<T, V>(p.ey + c, ey);
+        vst<T, V>(p.ez + c, ez);
+      } else {  // dispersive cells belong to the ADE blocks
+        st_guard3<T, V>(p.ex + c, ex, id);
+        st_guard3<T, V>(p.ey + c, ey, id);
+        st_guard3<T, V>(p.ez + c, ez, id);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      hyb[q] = hy[q];
+      hxb[q] = hx[q];
+    }
+  }
+}
+
+template <typename T, int V, int RY, int KZ>
+__global__ void __launch_bounds__(32 * RY) h3d_corez(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
+  pdl_release();
+  const Core3z<T, V, RY, KZ> u(p);
+  if (!u.live) return;
+  const long long plane = (long long)p.nx * p.ny;
+  long long c = ((long long)u.k0 * p.ny + u.j) * p.nx + u.i0;
+  T ex[V], ey[V];
+  vld_ro<T, V>(p.ex + c, ex);
+  vld_ro<T, V>(p.ey + c, ey);
+  for (int k = u.k0; k < u.k1; ++k, c += plane) {
+    T ez[V], ezu[V], exu[V], exa[V], eya[V], hx[V], hy[V], hz[V];
+    vld_ro<T, V>(p.ez + c, ez);
+    nb_vec<T, V>(p, p.ez, c, u.j, k, 1, 0, ezu);
+    nb_vec<T, V>(p, p.ex, c, u.j, k, 1, 0, exu);
+    nb_vec<T, V>(p, p.ex, c, u.j, k, 0, 1, exa);
+    nb_vec<T, V>(p, p.ey, c, u.j, k, 0, 1, eya);
+    const T ezr = nb_x<T, V>(p, p.ez, c, u.i0, 1), eyr = nb_x<T, V>(p, p.ey, c, u.i0, 1);
+    vld<T, V>(p.hx + c, hx);
+    vld<T, V>(p.hy + c, hy);
+    vld<T, V>(p.hz + c, hz);
+    if (!__ldg(p.rowflag + (long long)k * p.ny + u.j)) {
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        const T rz = q < V - 1 ? ez[q + 1] : ezr, ry = q < V - 1 ? ey[q + 1] : eyr;
+        const T curleyz = eya[q] - ey[q], curlezy = -ezu[q] + ez[q];
+        const T curlezx = rz - ez[q], curlexz = -exa[q] + ex[q];
+        const T curlexy = exu[q] - ex[q], curleyx = -ry + ey[q];
+        hx[q] = hx[q] + p.ku * (curleyz + curlezy);
+        hy[q] = hy[q] + p.ku * (curlezx + curlexz);
+        hz[q] = hz[q] + p.ku * (curlexy + curleyx);
+      }
+      vst<T, V>(p.hx + c, hx);
+      vst<T, V>(p.hy + c, hy);
+      vst<T, V>(p.hz + c, hz);
+    }
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      ex[q] = exa[q];
+      ey[q] = eya[q];
+    }
+  }
+}
+
+constexpr int kCoreZ = 8;  // planes per thread of the z-marching kernels
+
+template <typename T, int V, int RY>
+void launch_core3z(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
+  const int blocks = ((p.cw + 31) / 32) * ((p.ch + RY - 1) / RY) * ((p.cd + kCoreZ - 1) / kCoreZ);
+  if (e_half) launch_pdl(e3d_corez<T, V, RY, kCoreZ>, blocks, 32 * RY, s, p, ev);
+  else launch_pdl(h3d_corez<T, V, RY, kCoreZ>, blocks, 32 * RY, s, p, ev);
+}
+
 template <typename T, int V, int RY>
 void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
   const int blocks = ((p.cw + 31) / 32) * ((p.ch + RY - 1) / RY) * p.cd;
@@ -583,19 +715,25 @@ void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent
   else launch_pdl(h3d_core<T, V, RY>, blocks, 32 * RY, s, p, ev);
 }
 
-// tile 0: 4 rows of 32 x-vectors, 1: 8 rows, 2: 16 rows
+// tile 0: 4 rows of 32 x-vectors, 1: 8 rows, 2: 16 rows, one plane per
+// thread; tiles 3, 4, 5: the same shapes marching kCoreZ planes per thread
+template <typename T, int V>
+void launch_core3_v(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
+  switch (p.tile) {
+    case 0: launch_core3<T, V, 4>(p, e_half, s, ev); break;
+    case 2: launch_core3<T, V, 16>(p, e_half, s, ev); break;
+    case 3: launch_core3z<T, V, 4>(p, e_half, s, ev); break;
+    case 4: launch_core3z<T, V, 8>(p, e_half, s, ev); break;
+    case 5: launch_core3z<T, V, 16>(p, e_half, s, ev); break;
+    default: launch_core3<T, V, 8>(p, e_half, s, ev); break;
+  }
+}
+
 template <typename T>
 void launch_core3_tiled(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
-  if (p.vec == VW) {
-    if (p.tile == 0) launch_core3<T, VW, 4>(p, e_half, s, ev);
-    else if (p.tile == 2) launch_core3<T, VW, 16>(p, e_half, s, ev);
-    else launch_core3<T, VW, 8>(p, e_half, s, ev);
-  } else {
-    if (p.tile == 0) launch_core3<T, 1, 4>(p, e_half, s, ev);
-    else if (p.tile == 2) launch_core3<T, 1, 16>(p, e_half, s, ev);
-    else launch_core3<T, 1, 8>(p, e_half, s, ev);
-  }
+  if (p.vec == VW) launch_core3_v<T, VW>(p, e_half, s, ev);
+  else launch_core3_v<T, 1>(p, e_half, s, ev);
 }
 
 // `prog_event`: the core kernel's programmatic event (see launch_pdl), or

@@ -325,7 +325,9 @@ int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms)
  * (the default) lets commit time the candidates on the job's own grid and
  * keep the fastest (cached per kind of grid; environment FDTD_TUNE=0 skips
  * the timing); 1..3 pins a candidate: 2D 128 / 256 / 512 threads per block,
- * 3D 4 / 8 / 16 rows of 32 x-vectors.  Results do not depend on the shape.
+ * 3D 4 / 8 / 16 rows of 32 x-vectors, one plane per thread; 3D also 4..6:
+ * the same shapes with each thread walking 8 planes and keeping the
+ * neighbour plane in registers.  Results do not depend on the shape.
  * fdtd_get_tile returns the shape in use (0: the job has no core kernels). */
 int fdtd_set_tile(fdtd_job *job, int32_t tile);
 int fdtd_get_tile(const fdtd_job *job, int32_t *tile);
