@@ -72,6 +72,18 @@ def lorentz_eps(p, omega):
     return eps
 
 
+def drude2cp_eps(p, omega):
+    """Analytic Drude + 2 critical points permittivity, gold_ep of
+    Mm/my_matfunctions_mod.f90:8-31 (exp(-i omega t) convention):
+    eps_inf - wD^2/(w^2 + i gD w) + sum A W (e^{i phi}/(W - w - i G) +
+    e^{-i phi}/(W + w + i G))."""
+    w = np.asarray(omega, dtype=np.float64)
+    eps = p["eps_inf"] - (p["omega_d"] * p["omega_d"]) / (w * w + 1j * p["gamma_d"] * w)
+    for a, ph, om, g in zip(p["amp"], p["phi"], p["omega"], p["gamma"]):
+        eps = eps + a * om * (np.exp(1j * ph) / (om - w - 1j * g) + np.exp(-1j * ph) / (om + w + 1j * g))
+    return eps
+
+
 def slab_rt(eps, d, omega):
     """|r|^2 and |t|^2 of a slab of permittivity eps and thickness d in
     vacuum at normal incidence (Airy formulas)."""

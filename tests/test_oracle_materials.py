@@ -1,4 +1,11 @@
-"""The oracle's Lorentz-pole materials, checked on the CPU.
+"""The oracle's dispersive materials against physics, checked on the CPU.
+
+0. Gold, Drude + 2 critical points: the FDTD reflectance and transmittance
+   of the 1D line's 50 nm slab match the Airy formulas with the reference's
+   analytic permittivity gold_ep (Mm/my_matfunctions_mod.f90:8-31) within
+   the discretisation error of 1 nm cells (about 1e-2).
+
+The Lorentz-pole materials:
 
 1. The reference codes one recursion twice: the polarisation-current form of
    the *LorentzJp modules (E-form: E += Ku/eps_inf (curl H - ds sum Jp)) and
@@ -107,3 +114,17 @@ def test_titanium_fit_has_a_growing_pole():
     nu = problems.TI_JP["gamma"][0]
     dt = problems.config_1d_gold()[1]["dt"]
     assert nu < 0 and (1.0 - nu * dt) / (1.0 + nu * dt) > 1.0
+
+
+def test_gold_slab_rt_matches_analytic_drude2cp(oracle_lib):
+    spec, meta = problems.config_1d_gold(precision=abi.F64)
+    O = oracle_lib.OracleJob(spec)
+    O.step(1, meta["Nt"])
+    sy = [problems.poynting_1d(*O.get_monitor(q), meta["ds"]) for q in range(3)]
+    O.close()
+    R, T = -sy[1] / sy[0], sy[2] / sy[0]
+    eps = problems.drude2cp_eps(problems.GOLD_CONFIG, meta["arg"])
+    assert eps.imag.min() > 0  # lossy in the exp(-i omega t) convention
+    Ra, Ta = problems.slab_rt(eps, 50e-9, meta["arg"])
+    assert np.max(np.abs(R - Ra)) <= 2e-2
+    assert np.max(np.abs(T - Ta)) <= 2e-2
