@@ -590,10 +590,17 @@ int commit_impl(fdtd_job *J) {
     }
     int lo[3], hi[3];
     region_bounds(J, R, lo, hi);
+    const bool is_box = R.region.kind == FDTD_REGION_BOX;  // every cell of its bounds: whole row runs
     for (int k = lo[2]; k <= hi[2]; ++k)
-      for (int j = lo[1]; j <= hi[1]; ++j)
+      for (int j = lo[1]; j <= hi[1]; ++j) {
+        uint8_t *row = mat.data() + (size_t)nx * ((size_t)j + (size_t)ny * k);
+        if (is_box) {
+          if (hi[0] >= lo[0]) std::fill(row + lo[0], row + hi[0] + 1, (uint8_t)mid[m]);
+          continue;
+        }
         for (int i = lo[0]; i <= hi[0]; ++i)
-          if (inside(J, R, i, j, k)) mat[(size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)] = (uint8_t)mid[m];
+          if (inside(J, R, i, j, k)) row[i] = (uint8_t)mid[m];
+      }
   }
   std::vector<MatCoef<T>> mc(kMaxMat);
   std::vector<AdeCoef<T>> ac;
@@ -720,7 +727,7 @@ int commit_impl(fdtd_job *J) {
   std::vector<uint8_t> ade_mat;
   for (long long c = 0; c < N; ++c) {
     const uint8_t id = mat[(size_t)c];
-    if (!id || !is_ade_kind(mc[id].kind)) continue;
+    if (id < kAdeId) continue;  // ids >= kAdeId are exactly the dispersive materials
     const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((long long)nx * ny));
     if (in_shell(i, j, k)) continue;
     if (!(i >= J->g.main_lo[0] && i <= J->g.main_hi[0] && j >= J->g.main_lo[1] && j <= J->g.main_hi[1] &&
@@ -741,8 +748,15 @@ int commit_impl(fdtd_job *J) {
   if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)kAdeFields * 3 * std::max(32, J->ade_stride)))) return rc;
   {
     // most common constant-dielectric material: its Ku/eps is a kernel parameter
-    std::vector<long long> cnt(kMaxMat, 0);
-    for (long long c2 = 0; c2 < N; ++c2) cnt[mat[(size_t)c2]]++;
+    // eight interleaved sub-histograms: runs of one id would otherwise chain
+    // every increment on the same counter
+    std::vector<long long> sub(8 * kMaxMat, 0), cnt(kMaxMat, 0);
+    long long c2 = 0;
+    for (; c2 + 8 <= N; c2 += 8)
+      for (int u = 0; u < 8; ++u) sub[u * kMaxMat + mat[(size_t)(c2 + u)]]++;
+    for (; c2 < N; ++c2) sub[mat[(size_t)c2]]++;
+    for (int u = 0; u < 8; ++u)
+      for (int t = 0; t < kMaxMat; ++t) cnt[t] += sub[u * kMaxMat + t];
     int best = 0;
     for (int t = 1; t < kAdeId; ++t) if (cnt[t] > cnt[best]) best = t;
     J->id0 = best;
