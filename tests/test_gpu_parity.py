@@ -515,3 +515,33 @@ def test_3d_reference_output_files(gpu, tmp_path):
     assert rows[:, 1:].min() > -0.05 and rows[:, 1:3].max() < 1.05
     line = np.concatenate([load_table(str(tmp_path / "timesLiney" / f"r{k}E_time20.dat")) for k in range(6)])
     np.testing.assert_allclose(line[:, 1:].T, lines[20], atol=5.01e-6)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_chained_branches_equal_serialised_run(gpu, dim):
+    """The replayed step -- core kernels with programmatic dependencies, side
+    kernels released by the previous core kernel's programmatic event -- gives
+    the fields of the same job run with profiling on, where every kernel runs
+    on its own after the previous one has finished.  Bit for bit: a side
+    kernel that read a field before its writer finished would show here."""
+    if dim == 2:
+        spec, _ = problems.config_2d_tmz(precision=abi.F32, n=512, ncyl=6, nfreq=8)
+        comps, steps = (abi.EZ, abi.HX, abi.HY), 640
+    else:
+        spec, _ = problems.config_3d_sphere(precision=abi.F32, n=96, nfreq=4, npml=8, radius=40.0, half=20)
+        comps, steps = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ), 320
+    runs = []
+    for serial in (False, True):
+        J = gpu.Job(spec, tile=1)
+        if serial:
+            J.profile(True)
+        J.step(1, steps)
+        runs.append(([J.get_field(c) for c in comps], [J.get_monitor(q) for q in range(len(spec.monitors))]))
+        J.close()
+    (fa, ma), (fb, mb) = runs
+    assert any(np.abs(x).max() > 0 for x in fa)
+    for x, y in zip(fa, fb):
+        np.testing.assert_array_equal(x, y)
+    for (ra, ia), (rb, ib) in zip(ma, mb):
+        np.testing.assert_array_equal(ra, rb)
+        np.testing.assert_array_equal(ia, ib)
