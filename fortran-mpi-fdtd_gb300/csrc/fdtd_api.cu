@@ -690,6 +690,19 @@ int commit_impl(fdtd_job *J) {
       AdeCoef<T> a{};
       a.kind = MK_LORENTZ;
       a.normal = -1;
+      if (p.sheet) {  // SLG_3LJp1nm: the thin axis is the normal (vacuum) component
+        const int n3[3] = {nx, ny, nz};
+        for (int ax = 0; ax < 3; ++ax)
+          if (R.region.lo[ax] == R.region.hi[ax] && n3[ax] > 1) { a.normal = ax; break; }
+      }
+      a.nl = p.chi3 != 0.0;
+      if (a.nl) {  // Kerr term of pole 0 (3D/graphene3LorentzJp1nm_mod.f90:74-77, 89-91)
+        const double den = 1.0 + p.gamma_nl * dt;
+        a.lk = T(((p.omega[0] * dt) * (p.omega[0] * dt) / (1.0 + p.gamma[0] * dt)) * p.chi3);
+        a.lqv = T(2.0 * p.gamma_nl * dt / den);
+        a.lqs = T((p.w_nl * dt) * (p.w_nl * dt) / den);
+        a.escale = T(p.e_scale);
+      }
       a.ga = T(1.0 / p.eps_inf);
       a.npoles = p.npoles;
       for (int l = 0; l < kMaxPoles; ++l) {
@@ -2015,6 +2028,14 @@ int fdtd_add_lorentz(fdtd_job *J, const fdtd_region *r, const fdtd_lorentz_desc 
   if (p->npoles < 1 || p->npoles > FDTD_LORENTZ_MAX_POLES)
     return set_err(FDTD_EINVAL, "npoles %d outside 1..%d", p->npoles, FDTD_LORENTZ_MAX_POLES);
   if (!(p->eps_inf != 0.0) || !std::isfinite(p->eps_inf)) return set_err(FDTD_EINVAL, "eps_inf must be finite and nonzero");
+  if (p->chi3 != 0.0 && (p->form != FDTD_LORENTZ_JP || p->npoles > 3))
+    return set_err(FDTD_EINVAL, "the Kerr term needs the JP form and at most 3 poles");
+  if (p->sheet) {
+    if (!r || r->kind != FDTD_REGION_BOX) return set_err(FDTD_EINVAL, "a Lorentz sheet needs a one-cell-thick box");
+    bool thin = false;
+    for (int a = 0; a < 3; ++a) if (r->lo[a] == r->hi[a] && J && J->g.n[a] > 1) thin = true;
+    if (!thin) return set_err(FDTD_EINVAL, "a Lorentz sheet must be one cell thick");
+  }
   MatRec m{};
   m.kind = MK_LORENTZ;
   m.lz = *p;

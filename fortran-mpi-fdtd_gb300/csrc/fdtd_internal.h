@@ -62,6 +62,9 @@ struct AdeCoef {
   T lv[kMaxPoles];         //   v += -lv v + (le E - ls p);  p += v
   T ls[kMaxPoles];         //   lv = 2 nu dt/(1+nu dt), ls = (w dt)^2/(1+nu dt),
   T le[kMaxPoles];         //   le = deps ls
+  int nl;                  // Lorentz sheet with a Kerr term on pole 0:
+  T lk;                    //   drive of pole 0 += lk Q E, lk = ls[0] chi3
+  T lqv, lqs, escale;      //   g += -lqv g + lqs ((escale E)^2 - Q);  Q += g
 };
 
 struct Source {
@@ -193,7 +196,8 @@ enum Role : int {
 
 // ADE state layout: state[(f*3 + comp)*stride + slot] with fields
 // 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:S_R 3:V = S_R(n)-S_R(n-1);
-// Lorentz: 2l: p_l, 2l+1: v_l for pole l < kMaxPoles)
+// Lorentz: 2l: p_l, 2l+1: v_l for pole l < kMaxPoles; with a Kerr term
+// (at most 3 poles) 6: Q, 7: g = Q(n)-Q(n-1))
 constexpr int kAdeFields = 2 * kMaxPoles;
 
 // launchers (defined in k2d.cu / k3d.cu / k1d.cu / kdft.cu)

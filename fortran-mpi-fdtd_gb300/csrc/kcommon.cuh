@@ -228,6 +228,9 @@ __device__ __forceinline__ bool sample_row(const StepParams<T> &p, int j, int k)
 //   recursion S_R(n) = r1 S_R(n-1) + r2 S_R(n-2) + r0 E^2 in velocity form.
 // Lorentz poles (3D/goldLorentzJp_mod.f90:60-86, 3D/si_mod.f90:55-60):
 //   E += ga (inc - sum_l v_l);  v_l += -lv v_l + (le E - ls p_l);  p_l += v_l
+// On a Lorentz-Jp sheet (3D/graphene3LorentzJp1nm_mod.f90:42-100) the normal
+// component is vacuum, and the Kerr term adds lk Q E to pole 0's drive with
+//   g += -lqv g + lqs ((escale E)^2 - Q);  Q += g.
 template <typename T>
 __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int comp, const AdeCoef<T> &a,
                                                T inc, T eold) {
@@ -236,6 +239,7 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
   T *f2 = st + (2 * 3 + comp) * (long long)stride + slot;
   T *f3 = st + (3 * 3 + comp) * (long long)stride + slot;
   if (a.kind == MK_LORENTZ) {
+    if (comp == a.normal) return eold + inc;  // sheet: the normal component is vacuum
     T pl[kMaxPoles], vl[kMaxPoles];
     T sv = T(0);
 #pragma unroll
@@ -247,13 +251,24 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
       }
     }
     const T e = eold + a.ga * (inc - sv);
+    T *qk = st + (6 * 3 + comp) * (long long)stride + slot, *gk = st + (7 * 3 + comp) * (long long)stride + slot;
+    const T qv = a.nl ? *qk : T(0);
 #pragma unroll
     for (int l = 0; l < kMaxPoles; ++l) {
       if (l < a.npoles) {
-        const T nv = vl[l] + ((a.le[l] * e - a.ls[l] * pl[l]) - a.lv[l] * vl[l]);
+        T drive = a.le[l] * e;
+        if (l == 0 && a.nl) drive = drive + a.lk * (qv * e);
+        const T nv = vl[l] + ((drive - a.ls[l] * pl[l]) - a.lv[l] * vl[l]);
         st[((2 * l + 1) * 3 + comp) * (long long)stride + slot] = nv;
         st[(2 * l * 3 + comp) * (long long)stride + slot] = pl[l] + nv;
       }
+    }
+    if (a.nl) {
+      const T es = a.escale * e;
+      const T g = *gk;
+      const T ng = g + (a.lqs * (es * es - qv) - a.lqv * g);
+      *gk = ng;
+      *qk = qv + ng;
     }
     return e;
   }

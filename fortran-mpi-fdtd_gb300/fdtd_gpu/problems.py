@@ -61,6 +61,26 @@ TI_JP = _lorentz(abi.LORENTZ_JP, 1.1, (-12.74873, 0.9605442, 67.66233, 55.0525),
                  (4.36014, -1.261863, 0.4063879, -2.176176), (-5.825585, 0.2087635, 1.246245, 8.059584))
 
 
+# Graphene sheet, 3-Lorentz 1 nm fit (M3/graphene3LorentzJp1nm_mod.f90:27-31).  The
+# module's Kerr parameters are public variables a program would set (none
+# does); the values here are a test choice: chi3 1e-18 m^2/V^2, a 40 THz
+# line of 1 ps damping, fields scaled by z0 as the module does.
+GRAPHENE_3LJP = dict(_lorentz(abi.LORENTZ_JP, 1.023242, (4.957366, 4.455092, 1.905429),
+                              (0.573075, 1.713164, 4.598546), (0.368926, 2.42099, 1.35581)),
+                     sheet=1, chi3=1e-18, w_nl=2.0 * PI * 40e12, gamma_nl=1e12, e_scale=Z0)
+
+
+def swap_graphene(spec, material):
+    """A copy of ``spec`` whose graphene (Drude) sheets are replaced by the
+    Lorentz material ``material`` on the same boxes."""
+    import copy
+    from .spec import Material
+    s = copy.deepcopy(spec)
+    s.materials = [Material("lorentz", m.region, params=dict(material)) if m.kind == "graphene" else m
+                   for m in s.materials]
+    return s
+
+
 def lorentz_eps(p, omega):
     """Continuous-time permittivity of the Lorentz recursion (both codings):
     P'' + 2 nu P' + w^2 P = w^2 deps E, so eps = eps_inf + sum deps w^2 /

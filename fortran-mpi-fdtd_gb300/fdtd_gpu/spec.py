@@ -173,6 +173,11 @@ def lorentz_struct(p):
         d.delta_eps[q] = p["delta_eps"][q]
         d.omega[q] = p["omega"][q]
         d.gamma[q] = p["gamma"][q]
+    d.sheet = int(p.get("sheet", 0))
+    d.chi3 = p.get("chi3", 0.0)
+    d.w_nl = p.get("w_nl", 0.0)
+    d.gamma_nl = p.get("gamma_nl", 0.0)
+    d.e_scale = p.get("e_scale", 1.0)
     return d
 
 

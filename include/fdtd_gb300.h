@@ -139,7 +139,17 @@ typedef struct fdtd_graphene_desc {
  *                    gc = deps (w dt)^2/(1 + nu dt)
  * delta_eps is xi1 / dep, omega is w0l / wp and gamma is dnu0l / dnup, all
  * angular [rad/s].  Signs are taken as given (the reference's fits have
- * negative w0 and nu for some poles). */
+ * negative w0 and nu for some poles).
+ *
+ * sheet = 1 makes it the Lorentz-Jp graphene sheet of SLG_3LJp1nm
+ * (3D/graphene3LorentzJp1nm_mod.f90:42-100, 2D/graphene3LorentzJp1nm_mod.f90:
+ * 42-80): the region is a one-cell-thick box, its in-plane components take
+ * the Jp update and its normal component the vacuum one (E += Ku curl H).
+ * chi3 != 0 adds the delayed Kerr term of its first pole (JP form, at most
+ * 3 poles): P0_1 = (xi1 + chi3 Q) E/c0, with
+ *   G = g1NL G + g2NL ((e_scale E)^2 - Q);  Q += dt G,
+ * g1NL, g2NL built from w_nl and gamma_nl like g1, g2 (xi3, wNL, dnuNL, and
+ * z0 for e_scale, in the reference). */
 enum { FDTD_LORENTZ_JP = 0, FDTD_LORENTZ_S = 1 };
 #define FDTD_LORENTZ_MAX_POLES 4
 typedef struct fdtd_lorentz_desc {
@@ -149,6 +159,11 @@ typedef struct fdtd_lorentz_desc {
   double delta_eps[FDTD_LORENTZ_MAX_POLES];
   double omega[FDTD_LORENTZ_MAX_POLES];
   double gamma[FDTD_LORENTZ_MAX_POLES];
+  int32_t sheet;         /* 1: one-cell-thick sheet, in-plane update only */
+  int32_t reserved;
+  double chi3;           /* xi3 [m^2/V^2]; 0: linear                      */
+  double w_nl, gamma_nl; /* wNL, dnuNL [rad/s]                            */
+  double e_scale;        /* V/m per normalised field unit (z0)            */
 } fdtd_lorentz_desc;
 
 /* ---- PML ---------------------------------------------------------------- */

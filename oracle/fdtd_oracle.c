@@ -80,6 +80,9 @@ typedef struct {
   double sa[NPOLE], sb[NPOLE], sc[NPOLE];         /* ga_l, gb_l, gc_l      */
   double *P[3][NPOLE], *Jp[3][NPOLE], *JpT[3];    /* JP state              */
   double *Sm1[3][NPOLE], *Sm2[3][NPOLE];          /* S state: S(n-1), S(n-2) */
+  int l_sheet, l_normal;                          /* SLG_3LJp1nm sheet      */
+  double chi3, g1N, g2N, escale;                  /* xi3, Kerr recursion, z0 */
+  double *Qk[3], *Gk[3];                          /* Q, G per component      */
   fdtd_region region;                  /* painted at commit              */
   double *centers;                     /* owned copy for SPHERES         */
   uint8_t *mask;                       /* owned copy for MASK            */
@@ -197,7 +200,7 @@ void ora_destroy(ora_job *J) {
     omat *M = &J->mat[m];
     free(M->cells); free(M->centers); free(M->mask);
     for (int c = 0; c < 3; c++) { free(M->I[c]); free(M->S[c]); free(M->g1[c]); free(M->g2[c]);
-      free(M->SR[c]); free(M->SRm1[c]); free(M->SRm2[c]); free(M->JpT[c]);
+      free(M->SR[c]); free(M->SRm1[c]); free(M->SRm2[c]); free(M->JpT[c]); free(M->Qk[c]); free(M->Gk[c]);
       for (int l = 0; l < NPOLE; l++) { free(M->P[c][l]); free(M->Jp[c][l]); free(M->Sm1[c][l]); free(M->Sm2[c][l]); } }
   }
   for (int q = 0; q < J->nmon; q++) { free(J->mon[q].omega); free(J->mon[q].re); free(J->mon[q].im); }
@@ -312,11 +315,24 @@ int ora_add_lorentz(ora_job *J, const fdtd_region *r, const fdtd_lorentz_desc *p
   if (p->npoles < 1 || p->npoles > NPOLE) FAIL("npoles must be 1..%d", NPOLE);
   if (p->form != FDTD_LORENTZ_JP && p->form != FDTD_LORENTZ_S) FAIL("bad Lorentz form");
   if (!(p->eps_inf != 0.0)) FAIL("eps_inf must be nonzero");
+  int normal = -1;
+  if (p->sheet) {
+    if (r->kind != FDTD_REGION_BOX) FAIL("a Lorentz sheet needs a one-cell-thick box");
+    for (int a = 0; a < 3; a++)
+      if (r->lo[a] == r->hi[a] && J->g.n[a] > 1) { normal = a; break; }
+    if (normal < 0) FAIL("a Lorentz sheet must be one cell thick");
+  }
+  if (p->chi3 != 0.0 && (p->form != FDTD_LORENTZ_JP || p->npoles > 3)) FAIL("the Kerr term needs the JP form and at most 3 poles");
   omat *M; int id = add_material(J, r, &M); if (id < 0) return id;
   M->kind = p->form == FDTD_LORENTZ_JP ? MAT_LORENTZ_JP : MAT_LORENTZ_S;
   M->npoles = p->npoles;
   M->l_ga = 1.0 / p->eps_inf;
   double dt = J->g.dt;
+  /* SLG_3LJp1nm: (1-dnuNL dt)/(1+dnuNL dt), wNL^2 dt/(1+dnuNL dt) (M3/graphene3LorentzJp1nm_mod.f90:89-91) */
+  M->l_sheet = p->sheet != 0; M->l_normal = normal;
+  M->chi3 = p->chi3; M->escale = p->e_scale;
+  M->g1N = (1.0 - p->gamma_nl * dt) / (1.0 + p->gamma_nl * dt);
+  M->g2N = (p->w_nl * p->w_nl) * dt / (1.0 + p->gamma_nl * dt);
   for (int l = 0; l < p->npoles; l++) {
     double w = p->omega[l], nu = p->gamma[l];
     M->xi[l] = p->delta_eps[l];
@@ -669,7 +685,7 @@ int ora_commit(ora_job *J) {
       }
     } else if (M->kind == MAT_LORENTZ_JP || M->kind == MAT_LORENTZ_S) {
       for (int c = 0; c < 3; c++) {
-        M->JpT[c] = zalloc(cnt);
+        M->JpT[c] = zalloc(cnt); M->Qk[c] = zalloc(cnt); M->Gk[c] = zalloc(cnt);
         for (int l = 0; l < M->npoles; l++) {
           M->P[c][l] = zalloc(cnt); M->Jp[c][l] = zalloc(cnt);
           M->Sm1[c][l] = zalloc(cnt); M->Sm2[c][l] = zalloc(cnt);
@@ -931,23 +947,36 @@ static void materials_update_E(ora_job *J, int n) {
       /* E += Ku ga (curl - ds JpT); JpT = sum_l Jp_l with
          Jp_l = gamma1L Jp_l + gamma2L (xi_l E/c0 - P_l), P_l += dt Jp_l
          (M3/goldLorentzJp_mod.f90:60-86, M2/siLorentzJp_mod.f90:57-77) */
+      /* the sheet's normal component: Ey += Ku (curlhxz + curlhzx), vacuum
+         (M3/graphene3LorentzJp1nm_mod.f90:66, M2/...:60); the Kerr term of
+         pole 1 (:74-77) and its G, Q recursion (:89-95) */
       const double Ku = J->g.ku, ds = J->g.ds, dt = J->g.dt;
       for (int64_t q = 0; q < M->ncell; q++) {
         int64_t c = M->cells[q];
         for (int u = 0; u < nc; u++) {
           int a = ncomp_list[u];
+          if (M->l_sheet && a == M->l_normal) {
+            E[a][c] = E[a][c] + Ku * curl_at(J, a, c) + d_extra_at(J, n, a, c);
+            continue;
+          }
           double e = E[a][c] + Ku * M->l_ga * (curl_at(J, a, c) - ds * M->JpT[a][q]);
           e = e + M->l_ga * d_extra_at(J, n, a, c);
           E[a][c] = e;
           double jt = 0.0;
           for (int l = 0; l < M->npoles; l++) {
             double p0 = M->xi[l] * e / K_C0;
+            if (l == 0 && M->chi3 != 0.0) p0 = p0 + M->chi3 * M->Qk[a][q] * e / K_C0;
             double jp = M->g1L[l] * M->Jp[a][l][q] + M->g2L[l] * (p0 - M->P[a][l][q]);
             M->Jp[a][l][q] = jp;
             M->P[a][l][q] = M->P[a][l][q] + dt * jp;
             jt = jt + jp;
           }
           M->JpT[a][q] = jt;
+          if (M->chi3 != 0.0) {
+            const double ez = M->escale * e;
+            M->Gk[a][q] = M->g1N * M->Gk[a][q] + M->g2N * ((ez * ez) - M->Qk[a][q]);
+            M->Qk[a][q] = M->Qk[a][q] + dt * M->Gk[a][q];
+          }
         }
       }
     } else if (M->kind == MAT_LORENTZ_S) {

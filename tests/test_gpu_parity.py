@@ -545,3 +545,29 @@ def test_chained_branches_equal_serialised_run(gpu, dim):
     for (ra, ia), (rb, ib) in zip(ma, mb):
         np.testing.assert_array_equal(ra, rb)
         np.testing.assert_array_equal(ia, ib)
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("case", ["3d", "2d_te", "2d_tm"])
+def test_lorentz_sheet_vs_oracle(gpu, oracle_lib, prec, case):
+    """The Lorentz-Jp graphene sheet (SLG_3LJp1nm) with its Kerr term: in 3D
+    the graphene configuration's column with this sheet in place of the Drude
+    one; in 2D a sheet across the cylinder workload (TE: Ex in-plane and Ey
+    the vacuum normal component; TM: Ez in-plane)."""
+    from fdtd_gpu.spec import box
+    if case == "3d":
+        spec, _ = problems.config_3d_graphene(precision=prec, nxy=8, nz=384, nfreq=32)
+        spec = problems.swap_graphene(spec, dict(problems.GRAPHENE_3LJP, chi3=1e-12, e_scale=1.0))
+        steps, nmon = 3000, 1
+    else:
+        spec, _ = problems.config_2d_tmz(precision=prec, n=384, ncyl=4, nfreq=16)
+        if case == "2d_te":
+            spec = problems.as_te(spec)
+        spec.add_lorentz(box((24, 150, 0), (359, 150, 0)), dict(problems.GRAPHENE_3LJP, chi3=1e-2, e_scale=1.0))
+        steps, nmon = 2500, 3
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, nmon)
+    assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)

@@ -128,3 +128,32 @@ def test_gold_slab_rt_matches_analytic_drude2cp(oracle_lib):
     Ra, Ta = problems.slab_rt(eps, 50e-9, meta["arg"])
     assert np.max(np.abs(R - Ra)) <= 2e-2
     assert np.max(np.abs(T - Ta)) <= 2e-2
+
+
+def _sheet_spec(chi3, layout=None):
+    """The graphene configuration (8 x 8 laterally periodic column) with the
+    Lorentz-Jp sheet in place of the Drude sheet; the configuration's fields
+    are in V/m, so e_scale = 1."""
+    spec, meta = problems.config_3d_graphene(precision=abi.F64, nxy=8, nz=384, nfreq=32)
+    mat = dict(problems.GRAPHENE_3LJP, chi3=chi3, e_scale=1.0)
+    return problems.swap_graphene(spec, mat), meta
+
+
+def test_lorentz_sheet_kerr_term_scales_with_chi3(oracle_lib):
+    """The Kerr term of the Lorentz-Jp sheet changes the transmitted spectrum
+    in proportion to chi3 for small chi3 (doubling chi3 doubles the change),
+    and the sheet's normal component stays that of vacuum."""
+    res = {}
+    for chi3 in (0.0, 1e-12, 2e-12):  # the early pulse edge is ~3e4 V/m at the sheet
+        spec, _ = _sheet_spec(chi3)
+        O = oracle_lib.OracleJob(spec, nthreads=4)
+        O.step(1, 2500)
+        re, im = O.get_monitor(0)
+        res[chi3] = np.concatenate([re.ravel(), im.ravel()])
+        ex, ez = O.get_field(abi.EX), O.get_field(abi.EZ)
+        O.close()
+    d1 = res[1e-12] - res[0.0]
+    d2 = res[2e-12] - res[0.0]
+    assert np.linalg.norm(d1) > 1e-9 * np.linalg.norm(res[0.0])  # far above rounding (1e-16)
+    assert abs(np.linalg.norm(d2) / np.linalg.norm(d1) - 2.0) < 0.05
+    assert np.abs(ez).max() <= 1e-12 * np.abs(ex).max()  # normal incidence: the normal component stays empty
