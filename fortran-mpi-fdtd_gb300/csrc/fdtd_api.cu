@@ -718,6 +718,20 @@ int commit_impl(fdtd_job *J) {
       ac.push_back(a);
     }
   }
+  if (split && nadem > 0) {
+    // the split-field update owns every shell cell, whatever is painted
+    // there; a dispersive id would make the kernels leave the cell to an ADE
+    // slot, and shell cells have none, so they keep no dispersive id
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j) {
+        uint8_t *row = mat.data() + (size_t)nx * ((size_t)j + (size_t)ny * k);
+        const bool whole = in_shell(J->slo[0], j, k);
+        for (int i = 0; i < nx; ++i) {
+          if (!whole && i == J->slo[0]) i = J->shi[0] + 1;
+          if (i < nx && row[i] >= kAdeId) row[i] = 0;
+        }
+      }
+  }
   if ((rc = alloc_dev(J, (void **)&J->d_mat, (size_t)N))) return rc;
   CK(cudaMemcpy(J->d_mat, mat.data(), (size_t)N, cudaMemcpyHostToDevice));
   J->h2d += (uint64_t)N;
