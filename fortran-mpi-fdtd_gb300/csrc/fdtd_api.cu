@@ -64,6 +64,7 @@ struct MatRec {
   fdtd_drude2cp gold;
   fdtd_graphene_desc gr;
   fdtd_lorentz_desc lz;
+  fdtd_graphene_cp_desc gcp;
   fdtd_region region;
   std::vector<double> centers;
   std::vector<uint8_t> mask;
@@ -127,7 +128,7 @@ struct fdtd_job {
   uint8_t *d_mat = nullptr;
   void *d_mc = nullptr, *d_ac = nullptr, *d_mca = nullptr, *d_mcs = nullptr;
   uint8_t *d_rowflag = nullptr;
-  int nade = 0, ade_stride = 0, id0 = 0;
+  int nade = 0, ade_stride = 0, ade_nf = 0, id0 = 0;
   std::vector<double> mca_host;
   std::vector<char> ac_host;  // AdeCoef<T> table, host copy
   int *d_ade_cell = nullptr;
@@ -634,11 +635,11 @@ int commit_impl(fdtd_job *J) {
       a.hb = T((p.omega_d * p.omega_d) * dt / p.gamma_d);
       a.dha = T(-std::expm1(-p.gamma_d * dt));
       const cd d1 = expm1c(-p.gamma[0] * dt, p.omega[0] * dt), d2 = expm1c(-p.gamma[1] * dt, p.omega[1] * dt);
-      a.d1r = T(d1.real()); a.d1i = T(d1.imag());
-      a.d2r = T(d2.real()); a.d2i = T(d2.imag());
+      a.dr[0] = T(d1.real()); a.di[0] = T(d1.imag());
+      a.dr[1] = T(d2.real()); a.di[1] = T(d2.imag());
       (void)gb;
-      a.gc1r = T(gc[0].real()); a.gc1i = T(gc[0].imag());
-      a.gc2r = T(gc[1].real()); a.gc2i = T(gc[1].imag());
+      a.gcr[0] = T(gc[0].real()); a.gci[0] = T(gc[0].imag());
+      a.gcr[1] = T(gc[1].real()); a.gci[1] = T(gc[1].imag());
       a.wr = T(w.real()); a.wi = T(w.imag());
       c.ade = (int)ac.size();
       c.ca = T(Ku);
@@ -673,6 +674,55 @@ int commit_impl(fdtd_job *J) {
       a.rv = T(1.0 - c2);
       a.rs = T(c1 + c2);
       a.kerr = T((1.0 - p.raman_frac) * chi3n);
+      c.ade = (int)ac.size();
+      c.ca = T(Ku);
+      c.cs = T(1);
+      ac.push_back(a);
+    } else if (R.kind == MK_GRAPHENE_CP) {
+      // Graphene%initialize_GrapheneVars (3D/graphene_mod.f90:202-283,
+      // 2D/graphene_mod.f90:163-236): the amplitudes and the Drude weight
+      // scaled by s = Graphenewidth/ds (scaleParams), gb_p carried as gb_p - 1
+      typedef std::complex<double> cd;
+      const fdtd_graphene_cp_desc &p = R.gcp;
+      const double sc = p.width / J->g.ds;
+      AdeCoef<T> a{};
+      a.kind = MK_GRAPHENE_CP;
+      a.normal = p.normal_axis;
+      a.ha = T(std::exp(-p.drude_gamma * dt));
+      a.hb = T(sc * (p.drude_omega * p.drude_omega) * dt / p.drude_gamma);
+      a.dha = T(-std::expm1(-p.drude_gamma * dt));
+      cd ga = cd(p.eps_inf, 0.0);
+      for (int q = 0; q < kMaxCp; ++q) {
+        const cd d = expm1c(-p.gamma[q] * dt, p.omega[q] * dt);
+        const cd gc = cd(0.0, dt * 2.0 * (sc * p.amp[q]) * p.omega[q]) * std::exp(cd(0.0, -p.phi[q]));
+        ga -= gc;
+        a.dr[q] = T(d.real()); a.di[q] = T(d.imag());
+        a.gcr[q] = T(gc.real()); a.gci[q] = T(gc.imag());
+      }
+      a.gar = T(ga.real());
+      a.gai = T(ga.imag());
+      // Raman S_R(n) = r1 S_R(n-1) + r2 S_R(n-2) + r0 E^2 in velocity form:
+      // V = rv V + rs S_R + r0 E^2, S_R += V, with rv = -r2 and rs = r1 - 1 + r2
+      // from c1 = r1 - 2 and c2 = 1 + r2 computed without cancellation
+      double r0 = 0.0, c1 = 0.0, c2 = 0.0;
+      if (p.chi3 != 0.0) {
+        const double wdt = p.w_nl * dt, gdt = p.gamma_nl * dt;
+        if (p.raman_form == FDTD_RAMAN_CENTRAL) {  // 2D/graphene_mod.f90:210-212
+          r0 = p.chi3 * (wdt * wdt) / (1.0 + gdt);
+          c1 = -(wdt * wdt + 2.0 * gdt) / (1.0 + gdt);
+          c2 = 2.0 * gdt / (1.0 + gdt);
+        } else {  // 3D/graphene_mod.f90:216-218, 256-258
+          const double alfaR = 0.5 * p.gamma_nl, betaR = std::sqrt(p.w_nl * p.w_nl - alfaR * alfaR);
+          const double omegaR = (p.w_nl * p.w_nl) / betaR;
+          r0 = p.chi3 * omegaR * dt * std::exp(-alfaR * dt) * std::sin(betaR * dt);
+          const double sb = std::sin(0.5 * betaR * dt);
+          c1 = 2.0 * (std::expm1(-alfaR * dt) * std::cos(betaR * dt) - 2.0 * sb * sb);
+          c2 = -std::expm1(-2.0 * alfaR * dt);
+        }
+      }
+      a.r0 = T(r0);
+      a.rv = T(1.0 - c2);
+      a.rs = T(c1 + c2);
       c.ade = (int)ac.size();
       c.ca = T(Ku);
       c.cs = T(1);
@@ -772,7 +822,11 @@ int commit_impl(fdtd_job *J) {
     CK(cudaMemcpy(J->d_ade_mat, ade_mat.data(), J->nade, cudaMemcpyHostToDevice));
     J->h2d += (uint64_t)J->nade * (sizeof(int) + 1);
   }
-  if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)kAdeFields * 3 * std::max(32, J->ade_stride)))) return rc;
+  J->ade_nf = 0;
+  for (const MatRec &R : J->mats)
+    J->ade_nf = std::max(J->ade_nf, ade_fields(R.kind, R.lz.npoles, R.lz.chi3 != 0.0));
+  if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)std::max(1, J->ade_nf) * 3 * std::max(32, J->ade_stride))))
+    return rc;
   {
     // most common constant-dielectric material: its Ku/eps is a kernel parameter
     // eight interleaved sub-histograms: runs of one id would otherwise chain
@@ -1509,6 +1563,7 @@ int line_run(fdtd_job *J, int n_first, int n_steps, int stages) {
   p.ade_mat = J->d_ade_mat;
   p.ade_state = (T *)J->d_ade_state;
   p.ade_stride = J->ade_stride;
+  p.ade_nf = J->ade_nf;
   p.ja = J->ja;
   p.jb = J->jb;
   for (int s = 0; s < 2; ++s) {
@@ -2036,6 +2091,27 @@ int fdtd_add_graphene(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_des
   return add_mat(J, r, m, id);
 }
 
+int fdtd_add_graphene_cp(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_cp_desc *p, int32_t *id) {
+  if (!p) return set_err(FDTD_EINVAL, "null graphene parameters");
+  bool ok = std::isfinite(p->eps_inf) && std::isfinite(p->drude_omega) && p->drude_gamma > 0 && p->width > 0;
+  for (int q = 0; q < 4; ++q)
+    ok = ok && std::isfinite(p->amp[q]) && std::isfinite(p->phi[q]) && std::isfinite(p->omega[q]) && std::isfinite(p->gamma[q]);
+  if (!ok) return set_err(FDTD_EINVAL, "graphene needs finite parameters, drude_gamma > 0 and width > 0");
+  if (p->normal_axis < -1 || p->normal_axis > 2) return set_err(FDTD_EINVAL, "normal_axis %d outside -1..2", p->normal_axis);
+  if (p->chi3 != 0.0) {
+    if (p->raman_form != FDTD_RAMAN_EXACT && p->raman_form != FDTD_RAMAN_CENTRAL)
+      return set_err(FDTD_EINVAL, "bad Raman form %d", p->raman_form);
+    if (!std::isfinite(p->chi3) || !(p->gamma_nl >= 0) || !std::isfinite(p->w_nl))
+      return set_err(FDTD_EINVAL, "bad Raman parameters");
+    if (p->raman_form == FDTD_RAMAN_EXACT && !(p->w_nl > 0.5 * p->gamma_nl))
+      return set_err(FDTD_EINVAL, "the exact Raman form needs w_nl > gamma_nl/2");
+  }
+  MatRec m{};
+  m.kind = MK_GRAPHENE_CP;
+  m.gcp = *p;
+  return add_mat(J, r, m, id);
+}
+
 int fdtd_add_lorentz(fdtd_job *J, const fdtd_region *r, const fdtd_lorentz_desc *p, int32_t *id) {
   if (!p) return set_err(FDTD_EINVAL, "null Lorentz parameters");
   if (p->form != FDTD_LORENTZ_JP && p->form != FDTD_LORENTZ_S) return set_err(FDTD_EINVAL, "bad Lorentz form %d", p->form);
@@ -2292,7 +2368,10 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
     }
   }
   nade = std::min(nade, N);
-  b += nade * ((uint64_t)kAdeFields * 3 * w + 5) + 32ull * kAdeFields * 3 * w;
+  int nf = 0;
+  for (auto &m : J->mats) nf = std::max(nf, ade_fields(m.kind, m.lz.npoles, m.lz.chi3 != 0.0));
+  nf = std::max(nf, 1);
+  b += nade * ((uint64_t)nf * 3 * w + 5) + 32ull * nf * 3 * w;
   if (J->has_pml && J->pml.mode == FDTD_PML_SPLIT) {
     b += (uint64_t)(J->dim == 3 ? 6 : 1) * (w == 8 ? 2 : 1) * N * w;
     b += 4ull * (nx + ny + nz) * w;

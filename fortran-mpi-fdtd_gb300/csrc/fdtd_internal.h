@@ -30,9 +30,12 @@ constexpr int kMaxMon = 16;
 constexpr int kMaxProbe = 16;
 constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
 
-enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3, MK_LORENTZ = 4 };
+enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3, MK_LORENTZ = 4, MK_GRAPHENE_CP = 5 };
 constexpr int kMaxPoles = FDTD_LORENTZ_MAX_POLES;
-__host__ __device__ constexpr bool is_ade_kind(int k) { return k == MK_GOLD || k == MK_GRAPHENE || k == MK_LORENTZ; }
+constexpr int kMaxCp = 4;  // critical points of the reference's graphene
+__host__ __device__ constexpr bool is_ade_kind(int k) {
+  return k == MK_GOLD || k == MK_GRAPHENE || k == MK_LORENTZ || k == MK_GRAPHENE_CP;
+}
 
 // per material id, in the job's precision
 template <typename T>
@@ -52,9 +55,10 @@ struct AdeCoef {
   int kind;
   int normal;              // graphene sheet normal axis (in-plane comps updated)
   T ha, hb, dha;           // Drude: S += hb*E - dha*S (dha = 1-ha), Q -= hb*E
-  T d1r, d1i, d2r, d2i;    // CP: g += (gb-1)*g + gc*E, d = gb-1
-  T gc1r, gc1i, gc2r, gc2i;// CP drive
-  T wr, wi;                // 1/ga (E = Re(num * (wr + i wi)))
+  T dr[kMaxCp], di[kMaxCp];   // CP p: g += (gb-1)*g + gc*E, d = gb-1
+  T gcr[kMaxCp], gci[kMaxCp]; // CP drive (gold: p < 2)
+  T wr, wi;                // gold: 1/ga (E = Re(num * (wr + i wi)))
+  T gar, gai;              // 4-CP graphene: ga, E = Re(num / (ga + S_R))
   T r0, rv, rs, kerr, ga;  // graphene Raman in velocity form: V = rv*V + rs*SR + r0*E^2,
                            // SR += V (rv = 1-(1+r2), rs = (r1-2)+(1+r2)); Kerr; eps
                            // (Lorentz: ga = 1/eps_inf)
@@ -197,8 +201,17 @@ enum Role : int {
 // ADE state layout: state[(f*3 + comp)*stride + slot] with fields
 // 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:S_R 3:V = S_R(n)-S_R(n-1);
 // Lorentz: 2l: p_l, 2l+1: v_l for pole l < kMaxPoles; with a Kerr term
-// (at most 3 poles) 6: Q, 7: g = Q(n)-Q(n-1))
-constexpr int kAdeFields = 2 * kMaxPoles;
+// (at most 3 poles) 6: Q, 7: g = Q(n)-Q(n-1); 4-CP graphene: 2+2p, 3+2p:
+// g_p for p < 4, 10: S_R, 11: V).  A job allocates the fields its materials
+// use (ade_fields), at most kAdeFields.
+constexpr int kAdeFields = 12;
+constexpr int ade_fields(int kind, int npoles, int nl) {
+  return kind == MK_GOLD ? 6
+       : kind == MK_GRAPHENE ? 4
+       : kind == MK_GRAPHENE_CP ? 12
+       : kind == MK_LORENTZ ? (nl ? 8 : 2 * npoles)
+       : 0;
+}
 
 // launchers (defined in k2d.cu / k3d.cu / k1d.cu / kdft.cu)
 // 2D half steps: the parts of one half step are independent launches
@@ -261,6 +274,7 @@ struct LineParams {
   const uint8_t *ade_mat;
   T *ade_state;
   int ade_stride;
+  int ade_nf;              // state fields per component in use
   // reference PML, per side and line (0 main, 1 incident)
   int slab_on[2];
   int ja, jb;              // 0-based: low slab rows [0, ja], high [jb, N-1]

@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kLineThreads, 1) line1d_kernel(const __grid_co
         const MatCoef<T> mc = p.mc[p.ade_mat[q]];
         T inc = ku * (hz[j] - hz[j - 1]) + line_src(p, s, 0, j);
         if (exi && j == bd) inc -= ku * hzi[bd - 1];
-        ex[j] = ade_update_state<T>(p.ade_state, p.ade_stride, q, 0, p.ac[mc.ade], inc, ex[j]);
+        ex[j] = ade_update_state<T>(p.ade_state, p.ade_stride, q, 0, p.ac[mc.ade], p.ac + mc.ade, inc, ex[j]);
       }
       for (int side = 0; side < 2; ++side) {
         if (!p.slab_on[side]) continue;
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(1024, 1) line1d_cluster_kernel(const __grid_co
   AdeCoef<T> *ac = (AdeCoef<T> *)sm.take(p.nac * sizeof(AdeCoef<T>));
   int *ade_cell = (int *)sm.take(p.nade * sizeof(int));
   uint8_t *ade_mat = (uint8_t *)sm.take(p.nade);
-  T *state = (T *)sm.take((size_t)kAdeFields * 3 * p.ade_stride * sizeof(T));
+  T *state = (T *)sm.take((size_t)p.ade_nf * 3 * p.ade_stride * sizeof(T));
   // the launch's source values: all of them when they fit, else this and
   // the next step's
   const bool all_src = (long long)p.n_steps * p.nsrc <= kLineSrcAll;
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(1024, 1) line1d_cluster_kernel(const __grid_co
     ade_cell[q] = p.ade_cell[q];
     ade_mat[q] = p.ade_mat[q];
   }
-  for (int q = tid; q < kAdeFields * 3 * p.ade_stride; q += nth) state[q] = p.ade_state[q];
+  for (int q = tid; q < p.ade_nf * 3 * p.ade_stride; q += nth) state[q] = p.ade_state[q];
 #pragma unroll
   for (int l = 0; l < 2; ++l)
 #pragma unroll
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(1024, 1) line1d_cluster_kernel(const __grid_co
         const MatCoef<T> m = mc[ade_mat[q]];
         T d = ku * (hz[j - c0] - h_at(hz, hz_l, j - 1)) + src(0, j, s);
         if (inc && j == bd) d -= ku * h_at(hzi, hzi_l, bd - 1);
-        ex[j - c0] = ade_update_state<T>(state, p.ade_stride, q, 0, ac[m.ade], d, ex[j - c0]);
+        ex[j - c0] = ade_update_state<T>(state, p.ade_stride, q, 0, ac[m.ade], ac + m.ade, d, ex[j - c0]);
       }
 #pragma unroll
       for (int sd = 0; sd < 2; ++sd)
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(1024, 1) line1d_cluster_kernel(const __grid_co
   for (int q = tid; q < p.nade; q += nth) {
     const int j = ade_cell[q];
     if (j < c0 || j >= c1) continue;
-    for (int f = 0; f < kAdeFields * 3; ++f)
+    for (int f = 0; f < p.ade_nf * 3; ++f)
       p.ade_state[(long long)f * p.ade_stride + q] = state[(long long)f * p.ade_stride + q];
   }
 #pragma unroll
@@ -435,7 +435,7 @@ template <typename T>
 size_t line_cluster_bytes(const LineParams<T> &p, int W) {
   auto r = [](size_t b) { return (b + 15) & ~size_t(15); };
   size_t b = (p.exi ? 4 : 2) * r(W * sizeof(T)) + r(W) + r(kMaxMat * sizeof(MatCoef<T>)) + r(p.nac * sizeof(AdeCoef<T>));
-  b += r(p.nade * sizeof(int)) + r(p.nade) + r((size_t)kAdeFields * 3 * p.ade_stride * sizeof(T));
+  b += r(p.nade * sizeof(int)) + r(p.nade) + r((size_t)p.ade_nf * 3 * p.ade_stride * sizeof(T));
   const bool all_src = (long long)p.n_steps * p.nsrc <= kLineSrcAll;
   b += r((all_src ? p.n_steps * p.nsrc : 2 * kMaxSrc) * sizeof(double));
   for (int l = 0; l < 2; ++l)

@@ -404,19 +404,20 @@ __device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
   const int nx = p.nx, ny = p.ny;
   const int i = cell % nx, j = cell / nx;
   const AdeCoef<T> a = ade_coef(p, p.ade_mat[s]);
+  const AdeCoef<T> *am = p.ac + (p.ade_mat[s] - kAdeId);
   if (L == 3) {
     T curl = (p.hy[cell] - ld_x(p.hy, i - 1, j, nx, p.per[0])) +
              (-p.hx[cell] + ld_y(p.hx, i, j - 1, nx, ny, p.per[1]));
     T inc = p.ku * curl + src_sum<T>(p, n, 2, i, j, 0);
-    p.ez[cell] = ade_update<T>(p, a, s, 0, inc, p.ez[cell]);
+    p.ez[cell] = ade_update<T>(p, a, am, s, 0, inc, p.ez[cell]);
   } else {
     T hzc = p.hz[cell];
     T curlhx = hzc - ld_x(p.hz, i - 1, j, nx, p.per[0]);
     T curlhy = hzc - ld_y(p.hz, i, j - 1, nx, ny, p.per[1]);
     T incx = p.ku * curlhy + src_sum<T>(p, n, 0, i, j, 0);
     T incy = -(p.ku * curlhx) + src_sum<T>(p, n, 1, i, j, 0);
-    p.ex[cell] = ade_update<T>(p, a, s, 0, incx, p.ex[cell]);
-    p.ey[cell] = ade_update<T>(p, a, s, 1, incy, p.ey[cell]);
+    p.ex[cell] = ade_update<T>(p, a, am, s, 0, incx, p.ex[cell]);
+    p.ey[cell] = ade_update<T>(p, a, am, s, 1, incy, p.ey[cell]);
   }
 }
 

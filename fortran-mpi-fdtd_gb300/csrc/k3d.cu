@@ -445,6 +445,7 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
   const int i = cell % nx, j = (cell / nx) % ny, k = cell / (nx * ny);
   F3<T> f(p);
   const AdeCoef<T> a = ade_coef(p, p.ade_mat[s]);
+  const AdeCoef<T> *am = p.ac + (p.ade_mat[s] - kAdeId);
   const T hxc = p.hx[cell], hyc = p.hy[cell], hzc = p.hz[cell];
   const T curlhzy = hzc - f.ly(p.hz, i, j - 1, k), curlhyz = -hyc + f.lz(p.hy, i, j, k - 1);
   const T curlhxz = hxc - f.lz(p.hx, i, j, k - 1), curlhzx = -hzc + f.lx(p.hz, i - 1, j, k);
@@ -452,9 +453,9 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
   const T ix_ = p.ku * (curlhzy + curlhyz) + src_sum<T>(p, n, 0, i, j, k);
   const T iy_ = p.ku * (curlhxz + curlhzx) + src_sum<T>(p, n, 1, i, j, k);
   const T iz_ = p.ku * (curlhyx + curlhxy) + src_sum<T>(p, n, 2, i, j, k);
-  p.ex[cell] = ade_update<T>(p, a, s, 0, ix_, p.ex[cell]);
-  p.ey[cell] = ade_update<T>(p, a, s, 1, iy_, p.ey[cell]);
-  p.ez[cell] = ade_update<T>(p, a, s, 2, iz_, p.ez[cell]);
+  p.ex[cell] = ade_update<T>(p, a, am, s, 0, ix_, p.ex[cell]);
+  p.ey[cell] = ade_update<T>(p, a, am, s, 1, iy_, p.ey[cell]);
+  p.ez[cell] = ade_update<T>(p, a, am, s, 2, iz_, p.ez[cell]);
 }
 
 // general launch: blockIdx selects edge units, reference slab cells, then

@@ -233,7 +233,7 @@ __device__ __forceinline__ bool sample_row(const StepParams<T> &p, int j, int k)
 //   g += -lqv g + lqs ((escale E)^2 - Q);  Q += g.
 template <typename T>
 __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int comp, const AdeCoef<T> &a,
-                                               T inc, T eold) {
+                                               const AdeCoef<T> *am, T inc, T eold) {
   T *q_ = st + (0 * 3 + comp) * (long long)stride + slot;
   T *s_ = st + (1 * 3 + comp) * (long long)stride + slot;
   T *f2 = st + (2 * 3 + comp) * (long long)stride + slot;
@@ -279,17 +279,53 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
     T *f5 = st + (5 * 3 + comp) * (long long)stride + slot;
     const T g1r = *f2, g1i = *f3, g2r = *f4, g2i = *f5;
     // gb*g = g + (gb-1)*g
-    const T p1r = g1r + (a.d1r * g1r - a.d1i * g1i), p1i = g1i + (a.d1r * g1i + a.d1i * g1r);
-    const T p2r = g2r + (a.d2r * g2r - a.d2i * g2i), p2i = g2i + (a.d2r * g2i + a.d2i * g2r);
+    const T p1r = g1r + (a.dr[0] * g1r - a.di[0] * g1i), p1i = g1i + (a.dr[0] * g1i + a.di[0] * g1r);
+    const T p2r = g2r + (a.dr[1] * g2r - a.di[1] * g2i), p2i = g2i + (a.dr[1] * g2i + a.di[1] * g2r);
     const T nre = ((Q + a.ha * S) + p1r) + p2r;
     const T nim = p1i + p2i;
     const T e = nre * a.wr - nim * a.wi;
     *q_ = Q - a.hb * e;
     *s_ = S + (a.hb * e - a.dha * S);
-    *f2 = p1r + a.gc1r * e;
-    *f3 = p1i + a.gc1i * e;
-    *f4 = p2r + a.gc2r * e;
-    *f5 = p2i + a.gc2i * e;
+    *f2 = p1r + a.gcr[0] * e;
+    *f3 = p1i + a.gci[0] * e;
+    *f4 = p2r + a.gcr[1] * e;
+    *f5 = p2i + a.gci[1] * e;
+    return e;
+  }
+  if (a.kind == MK_GRAPHENE_CP) {
+    // the reference's Graphene: Re[(Q + ha S + sum_p gb_p g_p) / (ga + S_R)].
+    // Its coefficients are read through am, not the caller's copy a: a copy
+    // of every kind's fields would stay in registers across the components.
+    if (comp == a.normal) return eold + inc;  // the normal component is vacuum (E = D)
+    const long long cs = 3 * (long long)stride;
+    T *g0 = st + (2 * 3 + comp) * (long long)stride + slot;  // g_p: fields 2+2p (re), 3+2p (im)
+    const T ha = am->ha, hb = am->hb, dha = am->dha;
+    T nre = Q + ha * S, nim = T(0);
+#pragma unroll 1  // unrolled, the loads of all four points would stay live together
+    for (int q = 0; q < kMaxCp; ++q) {
+      const T gr = g0[2 * q * cs], gi = g0[(2 * q + 1) * cs];
+      const T dr = am->dr[q], di = am->di[q];
+      nre = nre + (gr + (dr * gr - di * gi));
+      nim = nim + (gi + (dr * gi + di * gr));
+    }
+    T *srp = st + (10 * 3 + comp) * (long long)stride + slot, *vp = st + (11 * 3 + comp) * (long long)stride + slot;
+    const T sr = *srp, v = *vp;
+    const T gai = am->gai, dre = am->gar + sr;
+    const T e = (nre * dre + nim * gai) / (dre * dre + gai * gai);
+    const T nv = am->rv * v + am->rs * sr + am->r0 * (e * e);
+    *vp = nv;
+    *srp = sr + nv;
+    *q_ = Q - hb * e;
+    *s_ = S + (hb * e - dha * S);
+    // g_p = gb_p g_p + gc_p E, with gb_p g_p recomputed from the state (the
+    // same operations as above, so the same values) rather than kept live
+#pragma unroll 1
+    for (int q = 0; q < kMaxCp; ++q) {
+      const T gr = g0[2 * q * cs], gi = g0[(2 * q + 1) * cs];
+      const T dr = am->dr[q], di = am->di[q];
+      g0[2 * q * cs] = (gr + (dr * gr - di * gi)) + am->gcr[q] * e;
+      g0[(2 * q + 1) * cs] = (gi + (dr * gi + di * gr)) + am->gci[q] * e;
+    }
     return e;
   }
   // graphene
@@ -316,10 +352,11 @@ __device__ __forceinline__ AdeCoef<T> ade_coef(const StepParams<T> &p, int id) {
   return ai < kAdeParam ? p.acp[ai] : p.ac[ai];
 }
 
+// a: the coefficients by value; am: the same set in the job's table
 template <typename T>
-__device__ __forceinline__ T ade_update(const StepParams<T> &p, const AdeCoef<T> &a, int slot, int comp, T inc,
-                                         T eold) {
-  return ade_update_state<T>(p.ade_state, p.ade_stride, slot, comp, a, inc, eold);
+__device__ __forceinline__ T ade_update(const StepParams<T> &p, const AdeCoef<T> &a, const AdeCoef<T> *am, int slot,
+                                         int comp, T inc, T eold) {
+  return ade_update_state<T>(p.ade_state, p.ade_stride, slot, comp, a, am, inc, eold);
 }
 
 // vals[c] for a component number known only at run time, by constant-index

@@ -54,6 +54,17 @@ class LorentzDesc(C.Structure):
                 ("chi3", C.c_double), ("w_nl", C.c_double), ("gamma_nl", C.c_double), ("e_scale", C.c_double)]
 
 
+RAMAN_EXACT, RAMAN_CENTRAL = 0, 1
+
+
+class GrapheneCpDesc(C.Structure):
+    _fields_ = [("eps_inf", C.c_double), ("drude_omega", C.c_double), ("drude_gamma", C.c_double),
+                ("amp", C.c_double * 4), ("phi", C.c_double * 4), ("omega", C.c_double * 4),
+                ("gamma", C.c_double * 4), ("width", C.c_double), ("chi3", C.c_double),
+                ("w_nl", C.c_double), ("gamma_nl", C.c_double), ("raman_form", C.c_int32),
+                ("normal_axis", C.c_int32)]
+
+
 class PmlDesc(C.Structure):
     _fields_ = [("mode", C.c_int32), ("npml", (C.c_int32 * 2) * 3),
                 ("eps_lo", C.c_double), ("eps_hi", C.c_double),

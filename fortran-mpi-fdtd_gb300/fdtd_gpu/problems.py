@@ -70,6 +70,48 @@ GRAPHENE_3LJP = dict(_lorentz(abi.LORENTZ_JP, 1.023242, (4.957366, 4.455092, 1.9
                      sheet=1, chi3=1e-18, w_nl=2.0 * PI * 40e12, gamma_nl=1e12, e_scale=Z0)
 
 
+# The reference's Graphene fit (M3/graphene_mod.f90:33-41, the same in M2 and
+# M1): Drude plus four critical points of a 0.34 nm layer, scaled to the cell
+# by width/ds.  xi3, wNL and dnuNL have no defaults there; the Raman term is
+# off here (chi3 = 0) until a caller sets them.
+GRAPHENE_4CP = dict(eps_inf=1.0, drude_omega=5.2796e15, drude_gamma=9e15,
+                    amp=(13.1068, 1.8417, 0.4191, 0.7737), phi=(-1.8391, 0.3505, 3.0565, -0.1199),
+                    omega=(6.1264e14, 6.6843e15, 5.6289e15, 1.118e16),
+                    gamma=(1e14, 7.905e14, 6.7526e14, 1.0005e14),
+                    width=3.4e-10, chi3=0.0, w_nl=0.0, gamma_nl=0.0,
+                    raman_form=abi.RAMAN_EXACT, normal_axis=1)
+
+
+def graphene_cp_eps(p, ds, omega):
+    """Continuous-time permittivity of the Graphene model at cell size ds:
+    the Drude + critical-point form of drude2cp_eps with the amplitudes and
+    the Drude weight scaled by s = width/ds (M3/graphene_mod.f90:264-269)."""
+    s = p["width"] / ds
+    q = dict(eps_inf=p["eps_inf"], omega_d=np.sqrt(s) * p["drude_omega"], gamma_d=p["drude_gamma"],
+             amp=[s * a for a in p["amp"]], phi=p["phi"], omega=p["omega"], gamma=p["gamma"])
+    return drude2cp_eps(q, omega)
+
+
+def as_first_initialised_3d(p):
+    """The 3D module's Graphene as a first initialize_material leaves it:
+    initialize_GrapheneVars copies exp1..4 and expi1..4 into locals before
+    setexp sets them (M3/graphene_mod.f90:221-231), so gb_p = gc_p = 0 and
+    only the Drude and Raman terms act.  Zero amplitudes give the same
+    update (g_p stays 0, gax = eps_inf)."""
+    return dict(p, amp=(0.0, 0.0, 0.0, 0.0))
+
+
+def swap_graphene_cp(spec, material):
+    """A copy of ``spec`` whose graphene (Drude) sheets are replaced by the
+    reference's Graphene ``material`` on the same boxes."""
+    import copy
+    from .spec import Material
+    s = copy.deepcopy(spec)
+    s.materials = [Material("graphene_cp", m.region, params=dict(material)) if m.kind == "graphene" else m
+                   for m in s.materials]
+    return s
+
+
 def swap_graphene(spec, material):
     """A copy of ``spec`` whose graphene (Drude) sheets are replaced by the
     Lorentz material ``material`` on the same boxes."""
@@ -417,10 +459,15 @@ def config_1d_gold(precision=abi.F64, steps=20000):
 
 def config_1d_slab(material, lo=2000, thickness=50, precision=abi.F64, steps=20000):
     """config_1d_gold's line with the gold slab replaced by ``material``
-    (a Lorentz parameter dict) over cells lo .. lo+thickness-1."""
+    (a Lorentz parameter dict, or a Graphene one: it has "drude_omega") over
+    cells lo .. lo+thickness-1."""
     spec, meta = config_1d_gold(precision=precision, steps=steps)
     spec.materials = spec.materials[:1]
-    spec.add_lorentz(box((0, lo, 0), (0, lo + thickness - 1, 0)), material)
+    region = box((0, lo, 0), (0, lo + thickness - 1, 0))
+    if "drude_omega" in material:
+        spec.add_graphene_cp(region, material)
+    else:
+        spec.add_lorentz(region, material)
     spec.name = "config_1d_slab"
     return spec, meta
 

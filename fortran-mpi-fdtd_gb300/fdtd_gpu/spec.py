@@ -18,7 +18,7 @@ Box = Tuple[Tuple[int, int, int], Tuple[int, int, int]]
 
 @dataclass
 class Material:
-    kind: str                      # "dielectric" | "gold" | "graphene" | "lorentz"
+    kind: str                      # "dielectric" | "gold" | "graphene" | "lorentz" | "graphene_cp"
     region: dict                   # {"kind": "box", "lo":..., "hi":...} | spheres | mask
     eps: float = 1.0
     params: Optional[dict] = None
@@ -80,6 +80,14 @@ class JobSpec:
         """params: {"form": abi.LORENTZ_JP | abi.LORENTZ_S, "eps_inf",
         "delta_eps": [...], "omega": [...], "gamma": [...]} (rad/s)."""
         self.materials.append(Material("lorentz", region, params=dict(params)))
+        return len(self.materials)
+
+    def add_graphene_cp(self, region, params):
+        """The reference's Graphene (Drude + 4 critical points + Raman):
+        params {"eps_inf", "drude_omega", "drude_gamma", "amp", "phi", "omega",
+        "gamma" (4 each), "width", "chi3", "w_nl", "gamma_nl", "raman_form",
+        "normal_axis"}."""
+        self.materials.append(Material("graphene_cp", region, params=dict(params)))
         return len(self.materials)
 
     def add_monitor(self, lo, hi, comps, omega, n_first=1, n_last=2 ** 31 - 1, mean=False):
@@ -178,6 +186,25 @@ def lorentz_struct(p):
     d.w_nl = p.get("w_nl", 0.0)
     d.gamma_nl = p.get("gamma_nl", 0.0)
     d.e_scale = p.get("e_scale", 1.0)
+    return d
+
+
+def graphene_cp_struct(p):
+    d = abi.GrapheneCpDesc()
+    d.eps_inf = p["eps_inf"]
+    d.drude_omega = p["drude_omega"]
+    d.drude_gamma = p["drude_gamma"]
+    for q in range(4):
+        d.amp[q] = p["amp"][q]
+        d.phi[q] = p["phi"][q]
+        d.omega[q] = p["omega"][q]
+        d.gamma[q] = p["gamma"][q]
+    d.width = p["width"]
+    d.chi3 = p.get("chi3", 0.0)
+    d.w_nl = p.get("w_nl", 0.0)
+    d.gamma_nl = p.get("gamma_nl", 0.0)
+    d.raman_form = int(p.get("raman_form", abi.RAMAN_EXACT))
+    d.normal_axis = int(p.get("normal_axis", 1))
     return d
 
 

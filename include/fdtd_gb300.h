@@ -166,6 +166,41 @@ typedef struct fdtd_lorentz_desc {
   double e_scale;        /* V/m per normalised field unit (z0)            */
 } fdtd_lorentz_desc;
 
+/* The reference's own graphene, Graphene: Drude plus four critical points,
+ * scaled from the physical layer width to the cell, with a Raman-delayed
+ * third-order term in the denominator (3D/graphene_mod.f90:59-105, 202-283;
+ * 2D/graphene_mod.f90:56-92, 163-236; 1D/graphene_mod.f90:52-71, 126-183):
+ *   E = Re[(D - I + ha S + sum_p gb_p g_p) / (gax + S_R)]
+ *   S_R(n) = r1 S_R(n-1) + r2 S_R(n-2) + r0 E(n)^2
+ *   I += hb E;  S = ha S + hb E;  g_p = gb_p g_p + gc_p E
+ * with s = width/ds, ha = exp(-drude_gamma dt), hb = s drude_omega^2 dt /
+ * drude_gamma, gb_p = exp((-gamma_p + i omega_p) dt),
+ * gc_p = 2 i dt (s amp_p) omega_p exp(-i phi_p), gax = eps_inf - sum_p gc_p.
+ *   FDTD_RAMAN_EXACT    r0 = chi3 wR dt e^{-aR dt} sin(bR dt), r1 = 2 e^{-aR dt}
+ *                       cos(bR dt), r2 = -e^{-2 aR dt}; aR = gamma_nl/2,
+ *                       bR = sqrt(w_nl^2 - aR^2), wR = w_nl^2/bR (3D module)
+ *   FDTD_RAMAN_CENTRAL  r0 = chi3 (w_nl dt)^2/(1 + gamma_nl dt), r1 = (2 -
+ *                       (w_nl dt)^2)/(1 + gamma_nl dt), r2 = -(1 - gamma_nl dt)/
+ *                       (1 + gamma_nl dt) (2D module)
+ * chi3 = 0 drops the Raman term (the 1D module).  chi3 multiplies the
+ * normalised E^2 of the update, as xi3 does in the reference.  The component
+ * along normal_axis is vacuum (E = D): the 2D module sets Ey = Dy, and the 3D
+ * one updates Ex and Ez only, so normal_axis = 1 (y) is the reference's
+ * sheet; -1 updates every component. */
+enum { FDTD_RAMAN_EXACT = 0, FDTD_RAMAN_CENTRAL = 1 };
+typedef struct fdtd_graphene_cp_desc {
+  double eps_inf;                 /* graphene_epinf                          */
+  double drude_omega;             /* graphene_wD [rad/s]                     */
+  double drude_gamma;             /* graphene_dnur [1/s]                     */
+  double amp[4], phi[4];          /* ap, phip                                */
+  double omega[4], gamma[4];      /* omp, rp [rad/s]                         */
+  double width;                   /* Graphenewidth [m]                       */
+  double chi3;                    /* xi3; 0: no Raman term                   */
+  double w_nl, gamma_nl;          /* wNL [rad/s], dnuNL [1/s]                */
+  int32_t raman_form;             /* FDTD_RAMAN_EXACT or FDTD_RAMAN_CENTRAL  */
+  int32_t normal_axis;            /* 0, 1, 2, or -1 for none                 */
+} fdtd_graphene_cp_desc;
+
 /* ---- PML ---------------------------------------------------------------- */
 enum {
   FDTD_PML_REFERENCE = 1, /* the reference's y-slab split-field PML with its
@@ -256,6 +291,10 @@ int fdtd_add_graphene(fdtd_job *job, const fdtd_region *region,
  * 3D/si_mod.f90:84-206).  Every E component of the layout gets the update. */
 int fdtd_add_lorentz(fdtd_job *job, const fdtd_region *region,
                      const fdtd_lorentz_desc *params, int32_t *material_id);
+/* Graphene%initialize_material (3D/graphene_mod.f90:107-283,
+ * 2D/graphene_mod.f90:94-236, 1D/graphene_mod.f90:73-183). */
+int fdtd_add_graphene_cp(fdtd_job *job, const fdtd_region *region,
+                         const fdtd_graphene_cp_desc *params, int32_t *material_id);
 /* pmly%initialize (3D/BERpmly_mod.f90:485-508, 2D/BERpmly_HzExEy_mod.f90:229-247,
  * 1D/BERpmly_ExHz_mod.f90:163-175). */
 int fdtd_add_pml(fdtd_job *job, const fdtd_pml_desc *pml);

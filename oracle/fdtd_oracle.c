@@ -59,7 +59,7 @@ static double cdiv_re(cplx a, cplx b) {
 }
 
 /* ---- job ------------------------------------------------------------------ */
-enum { MAT_DIEL = 1, MAT_GOLD = 2, MAT_GRAPHENE = 3, MAT_LORENTZ_JP = 4, MAT_LORENTZ_S = 5 };
+enum { MAT_DIEL = 1, MAT_GOLD = 2, MAT_GRAPHENE = 3, MAT_LORENTZ_JP = 4, MAT_LORENTZ_S = 5, MAT_GRAPHENE_CP = 6 };
 #define NPOLE FDTD_LORENTZ_MAX_POLES
 #define MAXMAT 250
 
@@ -83,6 +83,11 @@ typedef struct {
   int l_sheet, l_normal;                          /* SLG_3LJp1nm sheet      */
   double chi3, g1N, g2N, escale;                  /* xi3, Kerr recursion, z0 */
   double *Qk[3], *Gk[3];                          /* Q, G per component      */
+  /* the reference's Graphene (M3/graphene_mod.f90:8-44): Drude, 4 critical
+     points, Raman; I, S and the Raman arrays are shared with the above */
+  cplx cgb[4], cgc[4], cgax; double c_ha, c_hb; int c_normal;
+  double c_r0, c_r1, c_r2;
+  cplx *cg[3][4];
   fdtd_region region;                  /* painted at commit              */
   double *centers;                     /* owned copy for SPHERES         */
   uint8_t *mask;                       /* owned copy for MASK            */
@@ -200,6 +205,7 @@ void ora_destroy(ora_job *J) {
     omat *M = &J->mat[m];
     free(M->cells); free(M->centers); free(M->mask);
     for (int c = 0; c < 3; c++) { free(M->I[c]); free(M->S[c]); free(M->g1[c]); free(M->g2[c]);
+      for (int q = 0; q < 4; q++) free(M->cg[c][q]);
       free(M->SR[c]); free(M->SRm1[c]); free(M->SRm2[c]); free(M->JpT[c]); free(M->Qk[c]); free(M->Gk[c]);
       for (int l = 0; l < NPOLE; l++) { free(M->P[c][l]); free(M->Jp[c][l]); free(M->Sm1[c][l]); free(M->Sm2[c][l]); } }
   }
@@ -305,6 +311,56 @@ int ora_add_graphene(ora_job *J, const fdtd_region *r, const fdtd_graphene_desc 
   M->r1 = 2.0 * exp(-alfaR * dt) * cos(betaR * dt);
   M->r2 = -exp(-2.0 * alfaR * dt);
   M->kerr = (1.0 - p->raman_frac) * chi3n;
+  return id;
+}
+
+/* The reference's Graphene%initialize_GrapheneVars (M3/graphene_mod.f90:202-283,
+ * M2/graphene_mod.f90:163-236, M1/graphene_mod.f90:126-183), with setexp and
+ * scaleParams applied first: scaled_ap = (Graphenewidth/ds) ap, scaled_wD =
+ * sqrt(Graphenewidth/ds) wD.  The Raman coefficients follow the 3D module
+ * (exact) or the 2D one (central); chi3 = 0 leaves them zero, as the 1D
+ * module has no Raman term. */
+int ora_add_graphene_cp(ora_job *J, const fdtd_region *r, const fdtd_graphene_cp_desc *p) {
+  if (!(p->drude_gamma > 0) || !(p->width > 0)) FAIL("graphene needs drude_gamma > 0 and width > 0");
+  if (p->normal_axis < -1 || p->normal_axis > 2) FAIL("bad normal_axis");
+  omat *M; int id = add_material(J, r, &M); if (id < 0) return id;
+  M->kind = MAT_GRAPHENE_CP;
+  M->c_normal = p->normal_axis;
+  double dt = J->g.dt;
+  cplx unoi = {0.0, 1.0};
+  double scaleFact = p->width / J->g.ds;
+  double scaled_wD = sqrt(scaleFact) * p->drude_omega;
+  M->c_ha = exp(-p->drude_gamma * dt);
+  M->c_hb = (scaled_wD * scaled_wD) * dt / p->drude_gamma;
+  cplx gax = {p->eps_inf, 0.0};
+  for (int q = 0; q < 4; q++) {
+    cplx a = {-unoi.re * p->phi[q], -unoi.im * p->phi[q]};      /* -unoi*phip */
+    cplx expi = cexp_(a);
+    cplx b = {(-p->gamma[q]) * dt, p->omega[q] * dt};            /* (-rp+unoi*omp)*dt */
+    M->cgb[q] = cexp_(b);
+    /* dt*2.d0*unoi*scaled_ap*omp*expi, evaluated left to right */
+    cplx t = cscale(unoi, dt * 2.0);
+    t = cscale(t, scaleFact * p->amp[q]);
+    t = cscale(t, p->omega[q]);
+    M->cgc[q] = cmul(t, expi);
+    gax = csub(gax, M->cgc[q]);
+  }
+  M->cgax = gax;
+  if (p->chi3 != 0.0) {
+    double xi3 = p->chi3, wNL = p->w_nl, dnuNL = p->gamma_nl;
+    if (p->raman_form == FDTD_RAMAN_CENTRAL) {
+      M->c_r0 = xi3 * ((wNL * dt) * (wNL * dt)) / (1.0 + dnuNL * dt);
+      M->c_r1 = (2.0 - (wNL * dt) * (wNL * dt)) / (1.0 + dnuNL * dt);
+      M->c_r2 = -(1.0 - dnuNL * dt) / (1.0 + dnuNL * dt);
+    } else {
+      double alfaR = 0.5 * dnuNL;
+      double betaR = sqrt((wNL * wNL) - (alfaR * alfaR));
+      double omegaR = (wNL * wNL) / betaR;
+      M->c_r0 = xi3 * omegaR * dt * exp(-alfaR * dt) * sin(betaR * dt);
+      M->c_r1 = 2.0 * exp(-alfaR * dt) * cos(betaR * dt);
+      M->c_r2 = -exp(-2.0 * alfaR * dt);
+    }
+  }
   return id;
 }
 
@@ -676,8 +732,10 @@ int ora_commit(ora_job *J) {
     for (int k = 0; k < nz; k++) for (int j = 0; j < ny; j++) for (int i = 0; i < nx; i++)
       if (J->matid[cell_ix(J, i, j, k)] == m && !(split && in_shell(J, i, j, k)))
         M->cells[cnt++] = cell_ix(J, i, j, k);
-    if (M->kind == MAT_GOLD || M->kind == MAT_GRAPHENE) {
+    if (M->kind == MAT_GOLD || M->kind == MAT_GRAPHENE || M->kind == MAT_GRAPHENE_CP) {
       for (int c = 0; c < 3; c++) {
+        if (M->kind == MAT_GRAPHENE_CP)
+          for (int q = 0; q < 4; q++) M->cg[c][q] = (cplx *)calloc((size_t)(cnt > 0 ? cnt : 1), sizeof(cplx));
         M->I[c] = zalloc(cnt); M->S[c] = zalloc(cnt);
         M->g1[c] = (cplx *)calloc((size_t)(cnt > 0 ? cnt : 1), sizeof(cplx));
         M->g2[c] = (cplx *)calloc((size_t)(cnt > 0 ? cnt : 1), sizeof(cplx));
@@ -941,6 +999,31 @@ static void materials_update_E(ora_job *J, int n) {
           M->SR[a][q] = sr; M->SRm2[a][q] = M->SRm1[a][q]; M->SRm1[a][q] = sr;
           M->I[a][q] = M->I[a][q] + M->g_hb * e;
           M->S[a][q] = M->g_ha * M->S[a][q] + M->g_hb * e;
+        }
+      }
+    } else if (M->kind == MAT_GRAPHENE_CP) {
+      /* E = (D - I + ha S + gb1 g1 + .. + gb4 g4)/(gax + S_R), real part;
+         S_R = r1 S_R(n-1) + r2 S_R(n-2) + r0 E^2; I += hb E; S = ha S + hb E;
+         g_p = gb_p g_p + gc_p E (M3/graphene_mod.f90:70-100, M2/graphene_mod.f90:70-88,
+         M1/graphene_mod.f90:59-68).  The normal component: Ey = Dy
+         (M2/graphene_mod.f90:68; the 3D module leaves Ey to the material
+         updated before it, vacuum for a sheet in air). */
+      for (int64_t q = 0; q < M->ncell; q++) {
+        int64_t c = M->cells[q];
+        for (int u = 0; u < nc; u++) {
+          int a = ncomp_list[u];
+          if (a == M->c_normal) { E[a][c] = D[a][c]; continue; }
+          double r = (D[a][c] - M->I[a][q]) + M->c_ha * M->S[a][q];
+          cplx num = {r, 0.0};
+          for (int p = 0; p < 4; p++) num = cadd(num, cmul(M->cgb[p], M->cg[a][p][q]));
+          cplx den = M->cgax; den.re = den.re + M->SR[a][q];
+          double e = cdiv_re(num, den);
+          E[a][c] = e;
+          double sr = M->c_r1 * M->SRm1[a][q] + M->c_r2 * M->SRm2[a][q] + M->c_r0 * (e * e);
+          M->SR[a][q] = sr; M->SRm2[a][q] = M->SRm1[a][q]; M->SRm1[a][q] = sr;
+          M->I[a][q] = M->I[a][q] + M->c_hb * e;
+          M->S[a][q] = M->c_ha * M->S[a][q] + M->c_hb * e;
+          for (int p = 0; p < 4; p++) M->cg[a][p][q] = cadd(cmul(M->cgb[p], M->cg[a][p][q]), cscale(M->cgc[p], e));
         }
       }
     } else if (M->kind == MAT_LORENTZ_JP) {

@@ -7,6 +7,7 @@ import re
 import pytest
 
 from fdtd_gpu import abi, build, job, problems
+from fdtd_gpu import spec as spec_mod
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -39,14 +40,15 @@ def test_struct_sizes_match_header(built, tmp_path):
                    'sizeof(fdtd_grid_desc),sizeof(fdtd_region),sizeof(fdtd_drude2cp),'
                    'sizeof(fdtd_graphene_desc),sizeof(fdtd_pml_desc),sizeof(fdtd_source_desc),'
                    'sizeof(fdtd_monitor_desc),sizeof(fdtd_probe_desc),sizeof(fdtd_tfsf1d_desc),'
-                   'sizeof(fdtd_lorentz_desc));printf("%zu\\n",sizeof(fdtd_tfsf_desc));return 0;}\n')
+                   'sizeof(fdtd_lorentz_desc));printf("%zu %zu\\n",sizeof(fdtd_tfsf_desc),'
+                   'sizeof(fdtd_graphene_cp_desc));return 0;}\n')
     exe = tmp_path / "sz"
     import subprocess
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     got = [C.sizeof(t) for t in (abi.GridDesc, abi.Region, abi.Drude2CP, abi.GrapheneDesc, abi.PmlDesc,
                                  abi.SourceDesc, abi.MonitorDesc, abi.ProbeDesc, abi.Tfsf1dDesc, abi.LorentzDesc,
-                                 abi.TfsfDesc)]
+                                 abi.TfsfDesc, abi.GrapheneCpDesc)]
     assert [int(x) for x in out] == got
 
 
@@ -76,3 +78,12 @@ def test_bad_arguments_are_rejected(built):
     d.npoles, d.form = 1, 7
     assert L.fdtd_add_lorentz(None, None, C.byref(d), None) == abi.FDTD_EINVAL
     assert "form" in job.last_error()
+    gp = spec_mod.graphene_cp_struct(dict(problems.GRAPHENE_4CP, width=0.0))
+    assert L.fdtd_add_graphene_cp(None, None, C.byref(gp), None) == abi.FDTD_EINVAL
+    assert "width" in job.last_error()
+    gp = spec_mod.graphene_cp_struct(dict(problems.GRAPHENE_4CP, normal_axis=3))
+    assert L.fdtd_add_graphene_cp(None, None, C.byref(gp), None) == abi.FDTD_EINVAL
+    assert "normal_axis" in job.last_error()
+    gp = spec_mod.graphene_cp_struct(dict(problems.GRAPHENE_4CP, chi3=1.0, w_nl=1e12, gamma_nl=4e12))
+    assert L.fdtd_add_graphene_cp(None, None, C.byref(gp), None) == abi.FDTD_EINVAL
+    assert "w_nl" in job.last_error()

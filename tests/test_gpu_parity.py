@@ -571,3 +571,48 @@ def test_lorentz_sheet_vs_oracle(gpu, oracle_lib, prec, case):
     O.step(1, steps)
     err = _dft_err(J, O, nmon)
     assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("case", ["1d", "2d_te", "2d_tm", "3d", "3d_first_init"])
+def test_graphene_cp_vs_oracle(gpu, oracle_lib, prec, case):
+    """The reference's Graphene (Drude + 4 critical points + Raman):
+    1D: a 50 nm slab, every component updated, no Raman (the 1D module);
+    2D TE: a sheet along x with the 3D module's exact Raman coefficients (Ex
+    in-plane, Ey = Dy), crossing the all-face PML shell at both ends;
+    2D TM: the same sheet with the 2D module's central Raman coefficients;
+    3D: the graphene configuration's column with this sheet in place of the
+    Drude one (normal z), and the same with the 3D module's first-initialised
+    coefficients (no critical points)."""
+    from fdtd_gpu.spec import box
+    raman = dict(w_nl=2 * np.pi * 47.4e12, gamma_nl=1e12)
+    if case == "1d":
+        spec, meta = problems.config_1d_slab(dict(problems.GRAPHENE_4CP, normal_axis=-1), precision=prec)
+        steps, nmon, comps = meta["Nt"], 3, (abi.EX, abi.HZ)
+    elif case.startswith("3d"):
+        mat = dict(problems.GRAPHENE_4CP, chi3=1e-18, normal_axis=2, raman_form=abi.RAMAN_EXACT, **raman)
+        if case == "3d_first_init":
+            mat = problems.as_first_initialised_3d(mat)
+        spec, _ = problems.config_3d_graphene(precision=prec, nxy=8, nz=384, nfreq=32)
+        spec = problems.swap_graphene_cp(spec, mat)
+        steps, nmon, comps = 3000, 1, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    else:
+        spec, _ = problems.config_2d_tmz(precision=prec, n=384, ncyl=4, nfreq=16)
+        form = abi.RAMAN_EXACT if case == "2d_te" else abi.RAMAN_CENTRAL
+        comps = (abi.EZ, abi.HX, abi.HY)
+        if case == "2d_te":
+            spec = problems.as_te(spec)
+            comps = (abi.EX, abi.EY, abi.HZ)
+        spec.add_graphene_cp(box((24, 150, 0), (359, 150, 0)),
+                             dict(problems.GRAPHENE_4CP, chi3=1e-2, raman_form=form, **raman))
+        steps, nmon = 2500, 3
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, nmon)
+    if prec == abi.F64:
+        assert err <= TOL64
+        check_state(J, O, comps)
+    else:
+        assert err <= TOL32_DFT

@@ -16,6 +16,17 @@ The Lorentz-pole materials:
 2. Physics: the FDTD reflectance and transmittance of a 50 nm slab match the
    Airy formulas with the analytic permittivity of the fit within the
    discretisation error of 1 nm cells (a few 1e-3).
+
+The reference's own Graphene (Drude + 4 critical points + Raman):
+
+3. A 50 nm slab of the fit, scaled to 1 nm cells by width/ds, against the
+   Airy formulas with the scaled analytic permittivity.  Dropping the
+   critical points, flipping the sign of their phases or leaving out the
+   width scaling each moves R or T by more than 0.2; the FDTD stays within
+   1e-2.
+4. The Raman term: its change of the spectra is linear in chi3 for small
+   chi3, and the 3D module's exact coefficients and the 2D module's central
+   ones agree to O(w_nl dt).
 """
 import numpy as np
 import pytest
@@ -157,3 +168,47 @@ def test_lorentz_sheet_kerr_term_scales_with_chi3(oracle_lib):
     assert np.linalg.norm(d1) > 1e-9 * np.linalg.norm(res[0.0])  # far above rounding (1e-16)
     assert abs(np.linalg.norm(d2) / np.linalg.norm(d1) - 2.0) < 0.05
     assert np.abs(ez).max() <= 1e-12 * np.abs(ex).max()  # normal incidence: the normal component stays empty
+
+
+def test_graphene_cp_slab_rt_matches_analytic_permittivity(oracle_lib):
+    mat = dict(problems.GRAPHENE_4CP, normal_axis=-1)
+    spec, meta = problems.config_1d_slab(mat, thickness=50)
+    O = oracle_lib.OracleJob(spec)
+    O.step(1, meta["Nt"])
+    sy = [problems.poynting_1d(*O.get_monitor(q), meta["ds"]) for q in range(3)]
+    O.close()
+    R, T = -sy[1] / sy[0], sy[2] / sy[0]
+    eps = problems.graphene_cp_eps(mat, meta["ds"], meta["arg"])
+    Ra, Ta = problems.slab_rt(eps, 50 * meta["ds"], meta["arg"])
+    assert np.max(np.abs(R - Ra)) <= 1e-2
+    assert np.max(np.abs(T - Ta)) <= 1e-2
+    # the check tells the model's parts apart: without the critical points
+    # the analytic R/T move far beyond the tolerance
+    R0, T0 = problems.slab_rt(problems.graphene_cp_eps(problems.as_first_initialised_3d(mat), meta["ds"], meta["arg"]),
+                              50 * meta["ds"], meta["arg"])
+    assert max(np.max(np.abs(R0 - Ra)), np.max(np.abs(T0 - Ta))) > 0.1
+
+
+def test_graphene_cp_raman_linear_in_chi3_and_forms_agree(oracle_lib):
+    """A one-cell Graphene sheet on the 1D line (fields ~1e-4 in the line's
+    normalised units): the Raman term changes the spectra by ~1e-8 relative,
+    far above rounding, in proportion to chi3; the exact (3D) and central (2D)
+    Raman coefficients give the same change to O(w_nl dt) ~ 1e-3."""
+    res = {}
+    for form in (abi.RAMAN_EXACT, abi.RAMAN_CENTRAL):
+        for chi3 in (0.0, 1e-3, 2e-3):
+            mat = dict(problems.GRAPHENE_4CP, chi3=chi3, w_nl=2 * np.pi * 47.4e12, gamma_nl=1e12, raman_form=form)
+            spec, _ = problems.config_1d_slab(mat, thickness=1, steps=8000)
+            O = oracle_lib.OracleJob(spec)
+            O.step(1, 8000)
+            res[(form, chi3)] = np.concatenate([np.concatenate([a.ravel(), b.ravel()])
+                                                for a, b in (O.get_monitor(q) for q in range(3))])
+            O.close()
+    d = {}
+    for form in (abi.RAMAN_EXACT, abi.RAMAN_CENTRAL):
+        d1 = res[(form, 1e-3)] - res[(form, 0.0)]
+        d2 = res[(form, 2e-3)] - res[(form, 0.0)]
+        assert np.linalg.norm(d1) > 1e-10 * np.linalg.norm(res[(form, 0.0)])
+        assert abs(np.linalg.norm(d2) / np.linalg.norm(d1) - 2.0) < 1e-3
+        d[form] = d1
+    assert rel_l2(d[abi.RAMAN_CENTRAL], d[abi.RAMAN_EXACT]) < 1e-2
