@@ -65,6 +65,7 @@ struct MatRec {
   fdtd_graphene_desc gr;
   fdtd_lorentz_desc lz;
   fdtd_graphene_cp_desc gcp;
+  double sigma;  // conductive dielectric: eps holds eps_inf
   fdtd_region region;
   std::vector<double> centers;
   std::vector<uint8_t> mask;
@@ -645,6 +646,23 @@ int commit_impl(fdtd_job *J) {
       c.ca = T(Ku);
       c.cs = T(1);
       ac.push_back(a);
+    } else if (R.kind == MK_CONDUCTIVE) {
+      // SiL800 (3D/siL800_mod.f90:85-104): the gold update with no Drude
+      // memory (ha = 0) and no critical points, E = (D - I)/ga, I += gb E
+      const double gb = R.sigma * dt / K.ep0, ga = R.eps + gb;
+      AdeCoef<T> a{};
+      a.kind = MK_GOLD;
+      a.normal = -1;
+      a.ha = T(0);
+      a.hb = T(gb);
+      a.dha = T(1);
+      a.wr = T(1.0 / ga);
+      a.wi = T(0);
+      c.kind = MK_GOLD;
+      c.ade = (int)ac.size();
+      c.ca = T(Ku);
+      c.cs = T(1);
+      ac.push_back(a);
     } else if (R.kind == MK_GRAPHENE) {
       const fdtd_graphene_desc &p = R.gr;
       const double hbar = 6.62607015e-34 / (2.0 * K.pi), kb = 1.380649e-23, qe = 1.602176634e-19;
@@ -746,6 +764,7 @@ int commit_impl(fdtd_job *J) {
           if (R.region.lo[ax] == R.region.hi[ax] && n3[ax] > 1) { a.normal = ax; break; }
       }
       a.nl = p.chi3 != 0.0;
+      a.zx = p.ez_uses_x_current != 0;
       if (a.nl) {  // Kerr term of pole 0 (3D/graphene3LorentzJp1nm_mod.f90:74-77, 89-91)
         const double den = 1.0 + p.gamma_nl * dt;
         a.lk = T(((p.omega[0] * dt) * (p.omega[0] * dt) / (1.0 + p.gamma[0] * dt)) * p.chi3);
@@ -824,7 +843,7 @@ int commit_impl(fdtd_job *J) {
   }
   J->ade_nf = 0;
   for (const MatRec &R : J->mats)
-    J->ade_nf = std::max(J->ade_nf, ade_fields(R.kind, R.lz.npoles, R.lz.chi3 != 0.0));
+    J->ade_nf = std::max(J->ade_nf, ade_fields(R.kind, R.lz.npoles, R.lz.chi3 != 0.0, R.lz.ez_uses_x_current != 0));
   if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)std::max(1, J->ade_nf) * 3 * std::max(32, J->ade_stride))))
     return rc;
   {
@@ -2091,6 +2110,16 @@ int fdtd_add_graphene(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_des
   return add_mat(J, r, m, id);
 }
 
+int fdtd_add_conductive(fdtd_job *J, const fdtd_region *r, double eps_inf, double sigma, int32_t *id) {
+  if (!std::isfinite(eps_inf) || !std::isfinite(sigma) || sigma < 0 || !(eps_inf + sigma > 0))
+    return set_err(FDTD_EINVAL, "a conductive dielectric needs finite eps_inf, sigma >= 0 and eps_inf + sigma dt/eps0 > 0");
+  MatRec m{};
+  m.kind = MK_CONDUCTIVE;
+  m.eps = eps_inf;
+  m.sigma = sigma;
+  return add_mat(J, r, m, id);
+}
+
 int fdtd_add_graphene_cp(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_cp_desc *p, int32_t *id) {
   if (!p) return set_err(FDTD_EINVAL, "null graphene parameters");
   bool ok = std::isfinite(p->eps_inf) && std::isfinite(p->drude_omega) && p->drude_gamma > 0 && p->width > 0;
@@ -2118,8 +2147,10 @@ int fdtd_add_lorentz(fdtd_job *J, const fdtd_region *r, const fdtd_lorentz_desc 
   if (p->npoles < 1 || p->npoles > FDTD_LORENTZ_MAX_POLES)
     return set_err(FDTD_EINVAL, "npoles %d outside 1..%d", p->npoles, FDTD_LORENTZ_MAX_POLES);
   if (!(p->eps_inf != 0.0) || !std::isfinite(p->eps_inf)) return set_err(FDTD_EINVAL, "eps_inf must be finite and nonzero");
-  if (p->chi3 != 0.0 && (p->form != FDTD_LORENTZ_JP || p->npoles > 3))
-    return set_err(FDTD_EINVAL, "the Kerr term needs the JP form and at most 3 poles");
+  if (p->chi3 != 0.0 && p->form != FDTD_LORENTZ_JP) return set_err(FDTD_EINVAL, "the Kerr term needs the JP form");
+  if (p->ez_uses_x_current && (p->form != FDTD_LORENTZ_JP || !J || J->g.layout != FDTD_LAYOUT_3D || !p->sheet ||
+                                !r || r->lo[1] != r->hi[1]))
+    return set_err(FDTD_EINVAL, "ez_uses_x_current needs the JP form and a sheet normal to y on a 3D grid");
   if (p->sheet) {
     if (!r || r->kind != FDTD_REGION_BOX) return set_err(FDTD_EINVAL, "a Lorentz sheet needs a one-cell-thick box");
     bool thin = false;
@@ -2369,7 +2400,7 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
   }
   nade = std::min(nade, N);
   int nf = 0;
-  for (auto &m : J->mats) nf = std::max(nf, ade_fields(m.kind, m.lz.npoles, m.lz.chi3 != 0.0));
+  for (auto &m : J->mats) nf = std::max(nf, ade_fields(m.kind, m.lz.npoles, m.lz.chi3 != 0.0, m.lz.ez_uses_x_current != 0));
   nf = std::max(nf, 1);
   b += nade * ((uint64_t)nf * 3 * w + 5) + 32ull * nf * 3 * w;
   if (J->has_pml && J->pml.mode == FDTD_PML_SPLIT) {

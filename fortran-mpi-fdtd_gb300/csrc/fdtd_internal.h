@@ -30,11 +30,13 @@ constexpr int kMaxMon = 16;
 constexpr int kMaxProbe = 16;
 constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
 
-enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3, MK_LORENTZ = 4, MK_GRAPHENE_CP = 5 };
+// MK_CONDUCTIVE exists on the host only: its cells run the gold update
+enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3, MK_LORENTZ = 4, MK_GRAPHENE_CP = 5,
+                     MK_CONDUCTIVE = 6 };
 constexpr int kMaxPoles = FDTD_LORENTZ_MAX_POLES;
 constexpr int kMaxCp = 4;  // critical points of the reference's graphene
 __host__ __device__ constexpr bool is_ade_kind(int k) {
-  return k == MK_GOLD || k == MK_GRAPHENE || k == MK_LORENTZ || k == MK_GRAPHENE_CP;
+  return k == MK_GOLD || k == MK_GRAPHENE || k == MK_LORENTZ || k == MK_GRAPHENE_CP || k == MK_CONDUCTIVE;
 }
 
 // per material id, in the job's precision
@@ -66,6 +68,7 @@ struct AdeCoef {
   T lv[kMaxPoles];         //   v += -lv v + (le E - ls p);  p += v
   T ls[kMaxPoles];         //   lv = 2 nu dt/(1+nu dt), ls = (w dt)^2/(1+nu dt),
   T le[kMaxPoles];         //   le = deps ls
+  int zx;                  // Lorentz: Ez takes the x current (SLG_LJp)
   int nl;                  // Lorentz sheet with a Kerr term on pole 0:
   T lk;                    //   drive of pole 0 += lk Q E, lk = ls[0] chi3
   T lqv, lqs, escale;      //   g += -lqv g + lqs ((escale E)^2 - Q);  Q += g
@@ -200,16 +203,17 @@ enum Role : int {
 
 // ADE state layout: state[(f*3 + comp)*stride + slot] with fields
 // 0:Q (=D-I)  1:S  2:g1r 3:g1i 4:g2r 5:g2i  (graphene: 2:S_R 3:V = S_R(n)-S_R(n-1);
-// Lorentz: 2l: p_l, 2l+1: v_l for pole l < kMaxPoles; with a Kerr term
-// (at most 3 poles) 6: Q, 7: g = Q(n)-Q(n-1); 4-CP graphene: 2+2p, 3+2p:
+// Lorentz: 2l: p_l, 2l+1: v_l for pole l < npoles; with a Kerr term
+// 2P: Q, 2P+1: g = Q(n)-Q(n-1); with zx, 2P+2 (component 0) holds the x
+// current sum for the z update; 4-CP graphene: 2+2p, 3+2p:
 // g_p for p < 4, 10: S_R, 11: V).  A job allocates the fields its materials
 // use (ade_fields), at most kAdeFields.
 constexpr int kAdeFields = 12;
-constexpr int ade_fields(int kind, int npoles, int nl) {
-  return kind == MK_GOLD ? 6
+constexpr int ade_fields(int kind, int npoles, int nl, int zx) {
+  return kind == MK_GOLD || kind == MK_CONDUCTIVE ? 6
        : kind == MK_GRAPHENE ? 4
        : kind == MK_GRAPHENE_CP ? 12
-       : kind == MK_LORENTZ ? (nl ? 8 : 2 * npoles)
+       : kind == MK_LORENTZ ? (zx ? 2 * npoles + 3 : nl ? 2 * npoles + 2 : 2 * npoles)
        : 0;
 }
 

@@ -231,6 +231,7 @@ __device__ __forceinline__ bool sample_row(const StepParams<T> &p, int j, int k)
 // On a Lorentz-Jp sheet (3D/graphene3LorentzJp1nm_mod.f90:42-100) the normal
 // component is vacuum, and the Kerr term adds lk Q E to pole 0's drive with
 //   g += -lqv g + lqs ((escale E)^2 - Q);  Q += g.
+// The components of a cell are updated in order x, y, z by one thread.
 template <typename T>
 __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int comp, const AdeCoef<T> &a,
                                                const AdeCoef<T> *am, T inc, T eold) {
@@ -250,8 +251,17 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
         sv += vl[l];
       }
     }
+    const int nlf = 2 * a.npoles;  // the Kerr term's Q and g follow the poles
+    if (a.zx) {
+      // SLG_LJp's Ez line subtracts the x current of the previous step
+      // (3D/grapheneLorentzJp_mod.f90:68): the x update leaves its sum in
+      // field nlf+2 (component slot 0) for the z update of the same cell
+      T *xs = st + ((nlf + 2) * 3) * (long long)stride + slot;
+      if (comp == 0) *xs = sv;
+      else if (comp == 2) sv = *xs;
+    }
     const T e = eold + a.ga * (inc - sv);
-    T *qk = st + (6 * 3 + comp) * (long long)stride + slot, *gk = st + (7 * 3 + comp) * (long long)stride + slot;
+    T *qk = st + (nlf * 3 + comp) * (long long)stride + slot, *gk = st + ((nlf + 1) * 3 + comp) * (long long)stride + slot;
     const T qv = a.nl ? *qk : T(0);
 #pragma unroll
     for (int l = 0; l < kMaxPoles; ++l) {

@@ -50,7 +50,7 @@ LORENTZ_MAX_POLES = 4
 class LorentzDesc(C.Structure):
     _fields_ = [("form", C.c_int32), ("npoles", C.c_int32), ("eps_inf", C.c_double),
                 ("delta_eps", C.c_double * LORENTZ_MAX_POLES), ("omega", C.c_double * LORENTZ_MAX_POLES),
-                ("gamma", C.c_double * LORENTZ_MAX_POLES), ("sheet", C.c_int32), ("reserved", C.c_int32),
+                ("gamma", C.c_double * LORENTZ_MAX_POLES), ("sheet", C.c_int32), ("ez_uses_x_current", C.c_int32),
                 ("chi3", C.c_double), ("w_nl", C.c_double), ("gamma_nl", C.c_double), ("e_scale", C.c_double)]
 
 

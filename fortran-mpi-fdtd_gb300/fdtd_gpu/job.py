@@ -18,7 +18,7 @@ _lib = None
 # every entry point declared in include/fdtd_gb300.h
 EXPORTS = [
     "fdtd_create", "fdtd_destroy", "fdtd_last_error", "fdtd_device_count",
-    "fdtd_add_dielectric", "fdtd_add_gold", "fdtd_add_graphene", "fdtd_add_lorentz", "fdtd_add_graphene_cp",
+    "fdtd_add_dielectric", "fdtd_add_gold", "fdtd_add_graphene", "fdtd_add_lorentz", "fdtd_add_graphene_cp", "fdtd_add_conductive",
     "fdtd_add_pml",
     "fdtd_add_tfsf_1d", "fdtd_add_tfsf", "fdtd_add_source", "fdtd_add_monitor", "fdtd_add_probe", "fdtd_commit",
     "fdtd_step", "fdtd_update_DE", "fdtd_pml_update_E", "fdtd_interchange", "fdtd_update_H",
@@ -51,6 +51,7 @@ def lib(path=None):
             "fdtd_add_dielectric": [vp, vp, dbl, C.POINTER(i32)],
             "fdtd_add_gold": [vp, vp, vp, C.POINTER(i32)], "fdtd_add_graphene": [vp, vp, vp, C.POINTER(i32)],
             "fdtd_add_lorentz": [vp, vp, vp, C.POINTER(i32)], "fdtd_add_graphene_cp": [vp, vp, vp, C.POINTER(i32)],
+            "fdtd_add_conductive": [vp, vp, dbl, dbl, C.POINTER(i32)],
             "fdtd_add_pml": [vp, vp], "fdtd_add_tfsf_1d": [vp, vp], "fdtd_add_tfsf": [vp, vp],
             "fdtd_add_source": [vp, vp, C.POINTER(i32)], "fdtd_add_monitor": [vp, vp, C.POINTER(i32)],
             "fdtd_add_probe": [vp, vp, C.POINTER(i32)], "fdtd_commit": [vp],
@@ -140,6 +141,9 @@ class Job:
                 elif m.kind == "lorentz":
                     p = S.lorentz_struct(m.params)
                     check(L.fdtd_add_lorentz(self.h, C.byref(r), C.byref(p), C.byref(mid)))
+                elif m.kind == "conductive":
+                    check(L.fdtd_add_conductive(self.h, C.byref(r), m.params["eps_inf"], m.params["sigma"],
+                                                C.byref(mid)))
                 elif m.kind == "graphene_cp":
                     p = S.graphene_cp_struct(m.params)
                     check(L.fdtd_add_graphene_cp(self.h, C.byref(r), C.byref(p), C.byref(mid)))

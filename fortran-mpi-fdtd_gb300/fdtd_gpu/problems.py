@@ -68,6 +68,16 @@ TI_JP = _lorentz(abi.LORENTZ_JP, 1.1, (-12.74873, 0.9605442, 67.66233, 55.0525),
 GRAPHENE_3LJP = dict(_lorentz(abi.LORENTZ_JP, 1.023242, (4.957366, 4.455092, 1.905429),
                               (0.573075, 1.713164, 4.598546), (0.368926, 2.42099, 1.35581)),
                      sheet=1, chi3=1e-18, w_nl=2.0 * PI * 40e12, gamma_nl=1e12, e_scale=Z0)
+# The same sheet with the poles' weights set to zero: SLG_ndJp
+# (M3/NodispersiveGraphene.f90:27-32), only eps_inf and the Kerr term act.
+GRAPHENE_ND_3LJP = dict(GRAPHENE_3LJP, delta_eps=(0.0, 0.0, 0.0))
+# The 4-Lorentz sheet SLG_LJp (M3/grapheneLorentzJp_mod.f90:27-31), with the
+# same Kerr choice; its Ez line takes the x current (ez_uses_x_current, 3D).
+GRAPHENE_4LJP = dict(_lorentz(abi.LORENTZ_JP, 1.070682, (-0.163673, 0.843432, -0.170024, -0.121134),
+                              (1.642784, 0.807691, 0.934364, 0.525964), (2.267351, 1.018179, 0.621508, 0.033048)),
+                     sheet=1, chi3=1e-18, w_nl=2.0 * PI * 40e12, gamma_nl=1e12, e_scale=Z0, ez_uses_x_current=1)
+# Conductive Si at 800 nm, SiL800 (M3/siL800_mod.f90:16-17): sigma in S/m.
+SI_L800 = dict(eps_inf=3.675 ** 2, sigma=112.8134634)
 
 
 # The reference's Graphene fit (M3/graphene_mod.f90:33-41, the same in M2 and
@@ -144,6 +154,13 @@ def drude2cp_eps(p, omega):
     for a, ph, om, g in zip(p["amp"], p["phi"], p["omega"], p["gamma"]):
         eps = eps + a * om * (np.exp(1j * ph) / (om - w - 1j * g) + np.exp(-1j * ph) / (om + w + 1j * g))
     return eps
+
+
+def conductive_eps(p, omega):
+    """eps_inf + i sigma/(eps0 omega), the permittivity of SiL800's update
+    in the exp(-i omega t) convention."""
+    w = np.asarray(omega, dtype=np.float64)
+    return p["eps_inf"] + 1j * p["sigma"] / (EP0 * w)
 
 
 def slab_rt(eps, d, omega):
@@ -459,26 +476,29 @@ def config_1d_gold(precision=abi.F64, steps=20000):
 
 def config_1d_slab(material, lo=2000, thickness=50, precision=abi.F64, steps=20000):
     """config_1d_gold's line with the gold slab replaced by ``material``
-    (a Lorentz parameter dict, or a Graphene one: it has "drude_omega") over
+    (a Lorentz parameter dict, a Graphene one with "drude_omega" or a
+    conductive one with "sigma") over
     cells lo .. lo+thickness-1."""
     spec, meta = config_1d_gold(precision=precision, steps=steps)
     spec.materials = spec.materials[:1]
     region = box((0, lo, 0), (0, lo + thickness - 1, 0))
     if "drude_omega" in material:
         spec.add_graphene_cp(region, material)
+    elif "sigma" in material:
+        spec.add_conductive(region, material)
     else:
         spec.add_lorentz(region, material)
     spec.name = "config_1d_slab"
     return spec, meta
 
 
-def swap_gold(spec, material):
-    """A copy of ``spec`` whose gold (Drude+2CP) materials are replaced by the
-    Lorentz material ``material`` on the same regions."""
+def swap_gold(spec, material, kind="lorentz"):
+    """A copy of ``spec`` whose gold (Drude+2CP) materials are replaced by
+    ``material`` (of ``kind``, Lorentz by default) on the same regions."""
     import copy
     from .spec import Material
     s = copy.deepcopy(spec)
-    s.materials = [Material("lorentz", m.region, params=dict(material)) if m.kind == "gold" else m
+    s.materials = [Material(kind, m.region, params=dict(material)) if m.kind == "gold" else m
                    for m in s.materials]
     return s
 

@@ -18,7 +18,7 @@ Box = Tuple[Tuple[int, int, int], Tuple[int, int, int]]
 
 @dataclass
 class Material:
-    kind: str                      # "dielectric" | "gold" | "graphene" | "lorentz" | "graphene_cp"
+    kind: str                      # "dielectric" | "gold" | "graphene" | "lorentz" | "graphene_cp" | "conductive"
     region: dict                   # {"kind": "box", "lo":..., "hi":...} | spheres | mask
     eps: float = 1.0
     params: Optional[dict] = None
@@ -80,6 +80,11 @@ class JobSpec:
         """params: {"form": abi.LORENTZ_JP | abi.LORENTZ_S, "eps_inf",
         "delta_eps": [...], "omega": [...], "gamma": [...]} (rad/s)."""
         self.materials.append(Material("lorentz", region, params=dict(params)))
+        return len(self.materials)
+
+    def add_conductive(self, region, params):
+        """A conductive dielectric (SiL800): params {"eps_inf", "sigma" [S/m]}."""
+        self.materials.append(Material("conductive", region, params=dict(params)))
         return len(self.materials)
 
     def add_graphene_cp(self, region, params):
@@ -182,6 +187,7 @@ def lorentz_struct(p):
         d.omega[q] = p["omega"][q]
         d.gamma[q] = p["gamma"][q]
     d.sheet = int(p.get("sheet", 0))
+    d.ez_uses_x_current = int(p.get("ez_uses_x_current", 0))
     d.chi3 = p.get("chi3", 0.0)
     d.w_nl = p.get("w_nl", 0.0)
     d.gamma_nl = p.get("gamma_nl", 0.0)

@@ -145,11 +145,16 @@ typedef struct fdtd_graphene_desc {
  * (3D/graphene3LorentzJp1nm_mod.f90:42-100, 2D/graphene3LorentzJp1nm_mod.f90:
  * 42-80): the region is a one-cell-thick box, its in-plane components take
  * the Jp update and its normal component the vacuum one (E += Ku curl H).
- * chi3 != 0 adds the delayed Kerr term of its first pole (JP form, at most
- * 3 poles): P0_1 = (xi1 + chi3 Q) E/c0, with
+ * chi3 != 0 adds the delayed Kerr term of its first pole (JP form):
+ * P0_1 = (xi1 + chi3 Q) E/c0, with
  *   G = g1NL G + g2NL ((e_scale E)^2 - Q);  Q += dt G,
  * g1NL, g2NL built from w_nl and gamma_nl like g1, g2 (xi3, wNL, dnuNL, and
- * z0 for e_scale, in the reference). */
+ * z0 for e_scale, in the reference).  The 4-pole SLG_LJp
+ * (3D/grapheneLorentzJp_mod.f90:42-100) is the same sheet, except that its
+ * Ez line subtracts JpxT, the x current of the previous step, where the
+ * 3-pole module subtracts JpzT (:68); ez_uses_x_current = 1 reproduces that
+ * (JP form, 3D grids, a sheet normal to y as in the reference: Ex and Ez
+ * in-plane). */
 enum { FDTD_LORENTZ_JP = 0, FDTD_LORENTZ_S = 1 };
 #define FDTD_LORENTZ_MAX_POLES 4
 typedef struct fdtd_lorentz_desc {
@@ -160,7 +165,7 @@ typedef struct fdtd_lorentz_desc {
   double omega[FDTD_LORENTZ_MAX_POLES];
   double gamma[FDTD_LORENTZ_MAX_POLES];
   int32_t sheet;         /* 1: one-cell-thick sheet, in-plane update only */
-  int32_t reserved;
+  int32_t ez_uses_x_current; /* 1: Ez takes JpxT (SLG_LJp)                */
   double chi3;           /* xi3 [m^2/V^2]; 0: linear                      */
   double w_nl, gamma_nl; /* wNL, dnuNL [rad/s]                            */
   double e_scale;        /* V/m per normalised field unit (z0)            */
@@ -291,6 +296,13 @@ int fdtd_add_graphene(fdtd_job *job, const fdtd_region *region,
  * 3D/si_mod.f90:84-206).  Every E component of the layout gets the update. */
 int fdtd_add_lorentz(fdtd_job *job, const fdtd_region *region,
                      const fdtd_lorentz_desc *params, int32_t *material_id);
+/* SiL800%initialize_material (3D/siL800_mod.f90:53-104): a conductive
+ * dielectric, E = (D - I)/ga, I += gb E, ga = eps_inf + sigma dt/eps0,
+ * gb = sigma dt/eps0 (sigma in S/m), on every E component.  The reference's
+ * update_E_inSi writes its Ey pair twice and never Ez (:42-46); the intended
+ * update of all three components is built. */
+int fdtd_add_conductive(fdtd_job *job, const fdtd_region *region, double eps_inf,
+                        double sigma, int32_t *material_id);
 /* Graphene%initialize_material (3D/graphene_mod.f90:107-283,
  * 2D/graphene_mod.f90:94-236, 1D/graphene_mod.f90:73-183). */
 int fdtd_add_graphene_cp(fdtd_job *job, const fdtd_region *region,

@@ -81,6 +81,7 @@ typedef struct {
   double *P[3][NPOLE], *Jp[3][NPOLE], *JpT[3];    /* JP state              */
   double *Sm1[3][NPOLE], *Sm2[3][NPOLE];          /* S state: S(n-1), S(n-2) */
   int l_sheet, l_normal;                          /* SLG_3LJp1nm sheet      */
+  int l_zx;                                       /* SLG_LJp: Ez takes JpxT */
   double chi3, g1N, g2N, escale;                  /* xi3, Kerr recursion, z0 */
   double *Qk[3], *Gk[3];                          /* Q, G per component      */
   /* the reference's Graphene (M3/graphene_mod.f90:8-44): Drude, 4 critical
@@ -281,6 +282,23 @@ int ora_add_gold(ora_job *J, const fdtd_region *r, const fdtd_drude2cp *p) {
   return id;
 }
 
+/* SiL800 (M3/siL800_mod.f90:28-104): E = (D - I)/ga, I += gb E with
+ * ga = ep_inf + sigma dt/ep0, gb = sigma dt/ep0.  It is the gold update with
+ * ha = 0 and no critical points (gb_p = gc_p = 0), which leaves
+ * E = (D - I + 0 S + 0 + 0)/ga and I += hb E.  The reference writes its Ey
+ * pair twice and never Ez (:42-46); every component is updated here. */
+int ora_add_conductive(ora_job *J, const fdtd_region *r, double eps_inf, double sigma) {
+  omat *M; int id = add_material(J, r, &M); if (id < 0) return id;
+  M->kind = MAT_GOLD;
+  double dt = J->g.dt;
+  M->ha = 0.0;
+  M->hb = sigma * dt / K_EP0;
+  cplx zero = {0.0, 0.0}, ga = {eps_inf + sigma * dt / K_EP0, 0.0};
+  for (int q = 0; q < 2; q++) { M->gb[q] = zero; M->gc[q] = zero; }
+  M->ga = ga;
+  return id;
+}
+
 /* Graphene sheet: intraband Drude surface conductivity as an ADE of the
  * Drude form of the gold model (M3/gold_mod.f90:50-88 with no critical
  * points), the Raman recursion of M3/graphene_mod.f90:202-262 in the
@@ -378,14 +396,16 @@ int ora_add_lorentz(ora_job *J, const fdtd_region *r, const fdtd_lorentz_desc *p
       if (r->lo[a] == r->hi[a] && J->g.n[a] > 1) { normal = a; break; }
     if (normal < 0) FAIL("a Lorentz sheet must be one cell thick");
   }
-  if (p->chi3 != 0.0 && (p->form != FDTD_LORENTZ_JP || p->npoles > 3)) FAIL("the Kerr term needs the JP form and at most 3 poles");
+  if (p->chi3 != 0.0 && p->form != FDTD_LORENTZ_JP) FAIL("the Kerr term needs the JP form");
+  if (p->ez_uses_x_current && (p->form != FDTD_LORENTZ_JP || J->dim != 3 || !p->sheet || r->lo[1] != r->hi[1]))
+    FAIL("ez_uses_x_current needs the JP form and a sheet normal to y in 3D");
   omat *M; int id = add_material(J, r, &M); if (id < 0) return id;
   M->kind = p->form == FDTD_LORENTZ_JP ? MAT_LORENTZ_JP : MAT_LORENTZ_S;
   M->npoles = p->npoles;
   M->l_ga = 1.0 / p->eps_inf;
   double dt = J->g.dt;
   /* SLG_3LJp1nm: (1-dnuNL dt)/(1+dnuNL dt), wNL^2 dt/(1+dnuNL dt) (M3/graphene3LorentzJp1nm_mod.f90:89-91) */
-  M->l_sheet = p->sheet != 0; M->l_normal = normal;
+  M->l_sheet = p->sheet != 0; M->l_normal = normal; M->l_zx = p->ez_uses_x_current != 0;
   M->chi3 = p->chi3; M->escale = p->e_scale;
   M->g1N = (1.0 - p->gamma_nl * dt) / (1.0 + p->gamma_nl * dt);
   M->g2N = (p->w_nl * p->w_nl) * dt / (1.0 + p->gamma_nl * dt);
@@ -1033,16 +1053,21 @@ static void materials_update_E(ora_job *J, int n) {
       /* the sheet's normal component: Ey += Ku (curlhxz + curlhzx), vacuum
          (M3/graphene3LorentzJp1nm_mod.f90:66, M2/...:60); the Kerr term of
          pole 1 (:74-77) and its G, Q recursion (:89-95) */
+      /* SLG_LJp's Ez line subtracts JpxT (M3/grapheneLorentzJp_mod.f90:68):
+         the x sum of the previous step, as all E lines of a cell run before
+         its Jp updates (:62-70) */
       const double Ku = J->g.ku, ds = J->g.ds, dt = J->g.dt;
       for (int64_t q = 0; q < M->ncell; q++) {
         int64_t c = M->cells[q];
+        const double jpx_old = M->JpT[0][q];
         for (int u = 0; u < nc; u++) {
           int a = ncomp_list[u];
           if (M->l_sheet && a == M->l_normal) {
             E[a][c] = E[a][c] + Ku * curl_at(J, a, c) + d_extra_at(J, n, a, c);
             continue;
           }
-          double e = E[a][c] + Ku * M->l_ga * (curl_at(J, a, c) - ds * M->JpT[a][q]);
+          const double jt_e = (M->l_zx && a == 2) ? jpx_old : M->JpT[a][q];
+          double e = E[a][c] + Ku * M->l_ga * (curl_at(J, a, c) - ds * jt_e);
           e = e + M->l_ga * d_extra_at(J, n, a, c);
           E[a][c] = e;
           double jt = 0.0;

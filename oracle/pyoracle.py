@@ -33,6 +33,7 @@ def lib():
         L.ora_error.restype = C.c_char_p
         for name in ("ora_add_dielectric",):
             getattr(L, name).argtypes = [vp, vp, C.c_double]
+        L.ora_add_conductive.argtypes = [vp, vp, C.c_double, C.c_double]
         for name in ("ora_add_gold", "ora_add_graphene", "ora_add_lorentz", "ora_add_graphene_cp", "ora_add_pml", "ora_add_tfsf_1d", "ora_add_tfsf",
                      "ora_add_source", "ora_add_monitor", "ora_add_probe"):
             getattr(L, name).argtypes = [vp, vp] if name in ("ora_add_pml", "ora_add_tfsf_1d", "ora_add_tfsf", "ora_add_source",
@@ -71,6 +72,8 @@ class OracleJob:
             elif m.kind == "lorentz":
                 p = S.lorentz_struct(m.params)
                 rc = L.ora_add_lorentz(self.h, C.byref(r), C.byref(p))
+            elif m.kind == "conductive":
+                rc = L.ora_add_conductive(self.h, C.byref(r), m.params["eps_inf"], m.params["sigma"])
             elif m.kind == "graphene_cp":
                 p = S.graphene_cp_struct(m.params)
                 rc = L.ora_add_graphene_cp(self.h, C.byref(r), C.byref(p))

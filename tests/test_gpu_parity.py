@@ -616,3 +616,67 @@ def test_graphene_cp_vs_oracle(gpu, oracle_lib, prec, case):
         check_state(J, O, comps)
     else:
         assert err <= TOL32_DFT
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("case", ["1d", "2d_te", "3d"])
+def test_conductive_vs_oracle(gpu, oracle_lib, prec, case):
+    """SiL800's conductive dielectric (sigma 2e5 S/m, so that the conduction
+    current matters) in place of the gold of the 1D slab, the 2D cylinders
+    (TE) and the 3D sphere.  The state is compared while the pulse is in the
+    material: once it has gone, the conductor keeps a static charge, D and I
+    stay large and nearly equal, and the oracle's E = (D - I)/ga carries the
+    rounding of that difference (~1e-16 |D|), far above the small E left."""
+    mat = dict(problems.SI_L800, sigma=2e5)
+    if case == "1d":
+        spec, meta = problems.config_1d_slab(mat, precision=prec)
+        steps, nmon, comps = meta["Nt"], 3, (abi.EX, abi.HZ)
+    elif case == "2d_te":
+        spec, _ = problems.config_2d_tmz(precision=prec, n=384, ncyl=8, nfreq=24)
+        spec = problems.as_te(problems.swap_gold(spec, mat, kind="conductive"))
+        steps, nmon, comps = 2500, 3, (abi.EX, abi.EY, abi.HZ)
+    else:
+        spec, _ = problems.config_3d_sphere(precision=prec, n=96, nfreq=4, npml=8, radius=120.0, half=30)
+        spec = problems.swap_gold(spec, mat, kind="conductive")
+        steps, nmon, comps = 400, 6, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    mid = 3000 if case == "1d" else steps // 2
+    J.step(1, mid)
+    O.step(1, mid)
+    if prec == abi.F64:
+        check_state(J, O, comps)
+    J.step(mid + 1, steps - mid)
+    O.step(mid + 1, steps - mid)
+    err = _dft_err(J, O, nmon)
+    assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("case", ["4ljp_column", "4ljp_ez_quirk", "nd_column"])
+def test_lorentz_sheet_variants_vs_oracle(gpu, oracle_lib, prec, case):
+    """The other Lorentz-Jp graphene sheets: SLG_LJp's four poles with the
+    Kerr term on the graphene column (normal z); SLG_LJp with its Ez line
+    taking the x current, on a sheet normal to y across a 3D box; SLG_ndJp
+    (zero pole weights) with its Kerr term on the column."""
+    from fdtd_gpu.spec import box
+    if case == "4ljp_ez_quirk":
+        spec, _ = problems.config_3d_sphere(precision=prec, n=48, nfreq=4, npml=6, radius=120.0, half=200)
+        spec.add_lorentz(box((8, 24, 8), (39, 24, 39)),
+                         dict(problems.GRAPHENE_4LJP, chi3=1e-2, e_scale=1.0, ez_uses_x_current=1))
+        steps, nmon, comps = 400, 6, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    else:
+        mat = problems.GRAPHENE_ND_3LJP if case == "nd_column" else dict(problems.GRAPHENE_4LJP, ez_uses_x_current=0)
+        spec, _ = problems.config_3d_graphene(precision=prec, nxy=8, nz=384, nfreq=32)
+        spec = problems.swap_graphene(spec, dict(mat, chi3=1e-12, e_scale=1.0))
+        steps, nmon, comps = 3000, 1, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    J.step(1, steps)
+    O.step(1, steps)
+    err = _dft_err(J, O, nmon)
+    if prec == abi.F64:
+        assert err <= TOL64
+        check_state(J, O, comps)
+    else:
+        assert err <= TOL32_DFT

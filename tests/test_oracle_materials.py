@@ -27,6 +27,15 @@ The reference's own Graphene (Drude + 4 critical points + Raman):
 4. The Raman term: its change of the spectra is linear in chi3 for small
    chi3, and the 3D module's exact coefficients and the 2D module's central
    ones agree to O(w_nl dt).
+
+The smaller variants:
+
+5. SiL800, the conductive dielectric: a 50 nm slab against the Airy formulas
+   with eps_inf + i sigma/(eps0 omega), at the module's sigma and at one
+   large enough that leaving it out would move R/T by more than 0.2.
+6. SLG_LJp, four poles with the Kerr term: linear in chi3 like the 3-pole
+   sheet.  SLG_ndJp (pole weights zero) without the Kerr term is a
+   dielectric of eps_inf for the in-plane field.
 """
 import numpy as np
 import pytest
@@ -212,3 +221,56 @@ def test_graphene_cp_raman_linear_in_chi3_and_forms_agree(oracle_lib):
         assert abs(np.linalg.norm(d2) / np.linalg.norm(d1) - 2.0) < 1e-3
         d[form] = d1
     assert rel_l2(d[abi.RAMAN_CENTRAL], d[abi.RAMAN_EXACT]) < 1e-2
+
+
+@pytest.mark.parametrize("sigma", [problems.SI_L800["sigma"], 2e5])
+def test_conductive_slab_rt_matches_airy_formulas(oracle_lib, sigma):
+    mat = dict(problems.SI_L800, sigma=sigma)
+    spec, meta = problems.config_1d_slab(mat, thickness=50)
+    O = oracle_lib.OracleJob(spec)
+    O.step(1, meta["Nt"])
+    sy = [problems.poynting_1d(*O.get_monitor(q), meta["ds"]) for q in range(3)]
+    O.close()
+    R, T = -sy[1] / sy[0], sy[2] / sy[0]
+    eps = problems.conductive_eps(mat, meta["arg"])
+    Ra, Ta = problems.slab_rt(eps, 50e-9, meta["arg"])
+    assert np.max(np.abs(R - Ra)) <= 2e-3
+    assert np.max(np.abs(T - Ta)) <= 2e-3
+
+
+def test_four_pole_sheet_kerr_term_scales_with_chi3(oracle_lib):
+    res = {}
+    for chi3 in (0.0, 1e-12, 2e-12):
+        spec, meta = problems.config_3d_graphene(precision=abi.F64, nxy=8, nz=384, nfreq=32)
+        spec = problems.swap_graphene(spec, dict(problems.GRAPHENE_4LJP, chi3=chi3, e_scale=1.0, ez_uses_x_current=0))
+        O = oracle_lib.OracleJob(spec, nthreads=4)
+        O.step(1, 2500)
+        re, im = O.get_monitor(0)
+        res[chi3] = np.concatenate([re.ravel(), im.ravel()])
+        O.close()
+    d1 = res[1e-12] - res[0.0]
+    d2 = res[2e-12] - res[0.0]
+    assert np.linalg.norm(d1) > 1e-9 * np.linalg.norm(res[0.0])
+    assert abs(np.linalg.norm(d2) / np.linalg.norm(d1) - 2.0) < 0.05
+
+
+def test_nondispersive_sheet_is_a_dielectric_of_eps_inf(oracle_lib):
+    """SLG_ndJp without its Kerr term: zero pole weights leave every Jp at
+    zero, so under normal incidence (no normal field) the sheet is a
+    dielectric of eps_inf."""
+    out = []
+    for swap in ("nd", "diel"):
+        spec, meta = problems.config_3d_graphene(precision=abi.F64, nxy=8, nz=384, nfreq=32)
+        if swap == "nd":
+            spec = problems.swap_graphene(spec, dict(problems.GRAPHENE_ND_3LJP, chi3=0.0))
+        else:
+            from fdtd_gpu.spec import Material
+            spec.materials = [Material("dielectric", m.region, eps=problems.GRAPHENE_ND_3LJP["eps_inf"])
+                              if m.kind == "graphene" else m for m in spec.materials]
+        O = oracle_lib.OracleJob(spec, nthreads=4)
+        O.step(1, 2500)
+        re, im = O.get_monitor(0)
+        out.append(np.concatenate([re.ravel(), im.ravel(), O.get_field(abi.EX).ravel()]))
+        O.close()
+    assert np.linalg.norm(out[1]) > 0
+    assert rel_l2(out[0], out[1]) <= 1e-12
