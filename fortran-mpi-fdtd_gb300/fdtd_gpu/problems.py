@@ -474,6 +474,40 @@ def config_1d_gold(precision=abi.F64, steps=20000):
     return spec, dict(Nt=steps, tfinStop=tfin, arg=arg, ds=ds, dt=dt)
 
 
+def config_cell(kind, params, precision=abi.F64, steps=8000, lambda0=600e-9, st=0.5e-15, layout=abi.LAYOUT_2D_TM):
+    """A material cell on its own, for its discrete permittivity.  An 8 x 8
+    grid, periodic on both axes, filled with the material and driven by the
+    same soft source on every cell, stays uniform: curl H is 0, so each cell
+    runs only its D -> E update, at the grid's own Ku.  D(n) is the running
+    sum of amp g(t_n), and a probe records E(n) every step; the DFT ratio of
+    their increments is the update's permittivity (cell_eps)."""
+    ds, Ku, n = 1e-9, 0.5, 8
+    dt = Ku * ds / C0
+    comp = abi.EZ if layout == abi.LAYOUT_2D_TM else abi.EX
+    spec = JobSpec(layout=layout, n=(n, n, 1), ku=Ku, dt=dt, ds=ds, periodic=(1, 1, 0),
+                   main_lo=(0, 0, 0), main_hi=(n - 1, n - 1, 0), precision=precision, name="config_cell")
+    getattr(spec, "add_" + kind)(box((0, 0, 0), (n - 1, n - 1, 0)), params)
+    p = _pulse(lambda0)
+    p["st"] = st
+    p["t0"] = 4.0 * st
+    spec.sources.append(dict(component=comp, lo=(0, 0, 0), hi=(n - 1, n - 1, 0), amp=1.0, **p))
+    spec.add_probe((3, 4, 0), (comp,), 1, steps)
+    return spec, dict(Nt=steps, dt=dt, src=p)
+
+
+def cell_eps(e, meta, omega):
+    """The discrete permittivity D(w)/E(w) of a config_cell run, from the
+    probe's E(n) (n = 1..Nt) and the source's increments of D; the
+    increments decay, so the finite DFT does not leak a static tail."""
+    dt, p = meta["dt"], meta["src"]
+    n = np.arange(1, len(e) + 1)
+    t = (n - 1) * dt
+    dd = np.exp(-0.5 * ((t - p["t0"]) / p["st"]) ** 2) * np.sin(p["w0"] * t)
+    de = np.diff(np.concatenate([[0.0], np.asarray(e, dtype=np.float64)]))
+    ph = np.exp(1j * np.outer(np.asarray(omega), t))
+    return (ph @ dd) / (ph @ de)
+
+
 def config_1d_slab(material, lo=2000, thickness=50, precision=abi.F64, steps=20000):
     """config_1d_gold's line with the gold slab replaced by ``material``
     (a Lorentz parameter dict, a Graphene one with "drude_omega" or a

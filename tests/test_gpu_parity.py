@@ -680,3 +680,27 @@ def test_lorentz_sheet_variants_vs_oracle(gpu, oracle_lib, prec, case):
         check_state(J, O, comps)
     else:
         assert err <= TOL32_DFT
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("name", ["gold", "gold_jp", "si_s", "graphene_cp", "conductive"])
+def test_cell_response_vs_oracle(gpu, oracle_lib, prec, name):
+    """Each dispersive update on its own (problems.config_cell: a uniformly
+    driven periodic 8 x 8 grid, so curl H = 0): the GPU's E(n) series against
+    the oracle's (FP64), and the permittivity it implies (FP32)."""
+    params = {"gold": ("gold", problems.GOLD_CONFIG), "gold_jp": ("lorentz", problems.GOLD_JP),
+              "si_s": ("lorentz", problems.SI_S),
+              "graphene_cp": ("graphene_cp", dict(problems.GRAPHENE_4CP, normal_axis=-1)),
+              "conductive": ("conductive", dict(problems.SI_L800, sigma=2e5))}[name]
+    spec, meta = problems.config_cell(*params, precision=prec, steps=20000)
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64))
+    J.step(1, meta["Nt"])
+    O.step(1, meta["Nt"])
+    ej, eo = J.get_probe(0)[:, 0], O.get_probe(0)[:, 0]
+    if prec == abi.F64:
+        assert rel_l2(ej, eo) <= TOL64
+    else:
+        w = problems.dft_omegas(400e-9, 900e-9, 50)
+        ej_eps, eo_eps = problems.cell_eps(ej, meta, w), problems.cell_eps(eo, meta, w)  # complex
+        assert np.linalg.norm(ej_eps - eo_eps) / np.linalg.norm(eo_eps) <= 1e-4

@@ -36,6 +36,17 @@ The smaller variants:
 6. SLG_LJp, four poles with the Kerr term: linear in chi3 like the 3-pole
    sheet.  SLG_ndJp (pole weights zero) without the Kerr term is a
    dielectric of eps_inf for the in-plane field.
+
+The single-cell known-answer test (every dispersive update):
+
+7. A uniformly driven periodic grid runs each cell's D -> E update alone
+   (problems.config_cell).  The DFT ratio of the increments of D and E is
+   the update's discrete permittivity.  It must equal the z-transform of the
+   reference's recursion, derived here independently of the time stepping,
+   to the window's truncation (<= 1e-7).  It must also approach the
+   material's continuous permittivity within the discretisation error:
+   first order in dt for the Drude/critical-point updates, far smaller for
+   the Lorentz ones.
 """
 import numpy as np
 import pytest
@@ -274,3 +285,100 @@ def test_nondispersive_sheet_is_a_dielectric_of_eps_inf(oracle_lib):
         O.close()
     assert np.linalg.norm(out[1]) > 0
     assert rel_l2(out[0], out[1]) <= 1e-12
+
+
+# ---- discrete permittivity of each update, as a z-transform ----------------
+# A delay of one step multiplies a transform sum_n x(n) e^{i w t_n} by
+# zi = e^{i w dt}.  The critical-point terms are complex recursions driven by
+# the real E, and E takes the real part of the quotient, so each of their
+# transfers splits into the parts of its coefficients (K + conj-K)/2 and
+# (K - conj-K)/2i.
+
+def _eps_drude_cp(eps_inf, wd, gd, amp, phi, om, gam, dt, w):
+    """E = Re[(D - I + ha S + sum gb_p g_p)/ga]; I += hb E, S = ha S + hb E,
+    g_p = gb_p g_p + gc_p E (M3/gold_mod.f90:61-82, M3/graphene_mod.f90:70-100)."""
+    zi = np.exp(1j * np.asarray(w) * dt)
+    ha, hb = np.exp(-gd * dt), wd * wd * dt / gd
+    ga = eps_inf + 0j
+    A = -zi * hb / (1 - zi) + ha * hb * zi / (1 - ha * zi)
+    B = 0.0
+    for a, ph, o, g in zip(amp, phi, om, gam):
+        gb, gc = np.exp((-g + 1j * o) * dt), 1j * dt * 2.0 * a * o * np.exp(-1j * ph)
+        ga = ga - gc
+        K = gb * gc * zi / (1 - gb * zi)
+        Kc = np.conj(gb) * np.conj(gc) * zi / (1 - np.conj(gb) * zi)
+        A = A + (K + Kc) / 2
+        B = B + (K - Kc) / 2j
+    wr, wi = (1 / ga).real, (1 / ga).imag
+    return (1 - wr * A + wi * B) / wr
+
+
+def _eps_lorentz(p, dt, w):
+    """JP: E += (1/eps_inf)(dD - c0 dt sum Jp), Jp = g1 Jp + g2 (xi E/c0 - P),
+    P += dt Jp (M3/goldLorentzJp_mod.f90:60-86); S: E = (D - sum S)/eps_inf,
+    S = a S(n-1) + b S(n-2) + c E (M3/si_mod.f90:55-60)."""
+    zi = np.exp(1j * np.asarray(w) * dt)
+    e = p["eps_inf"] + 0j
+    for xi, o, nu in zip(p["delta_eps"], p["omega"], p["gamma"]):
+        if p["form"] == abi.LORENTZ_JP:
+            g1, g2 = (1 - nu * dt) / (1 + nu * dt), o * o * dt / (1 + nu * dt)
+            den = (1 - g1 * zi) + g2 * dt * zi / (1 - zi)
+            e = e + dt * zi * g2 * xi / (den * (1 - zi))
+        else:
+            a, b = (2 - (dt * o) ** 2) / (1 + dt * nu), (dt * nu - 1) / (1 + dt * nu)
+            c = xi * (o * dt) ** 2 / (1 + dt * nu)
+            e = e + zi * c / (1 - a * zi - b * zi * zi)
+    return e
+
+
+def _eps_conductive(p, dt, w):
+    """E = (D - I)/ga, I += gb E (M3/siL800_mod.f90:39-40, 99-100)."""
+    zi = np.exp(1j * np.asarray(w) * dt)
+    gb = p["sigma"] * dt / problems.EP0
+    return p["eps_inf"] + gb + gb * zi / (1 - zi)
+
+
+def _damped(p):
+    """A Lorentz fit with every pole damped (Si's first pole has none), so its
+    response dies out inside the window."""
+    return dict(p, gamma=tuple(max(g, 0.02 * problems._W) for g in p["gamma"]))
+
+
+_GCP = dict(problems.GRAPHENE_4CP, normal_axis=-1)
+_COND = dict(problems.SI_L800, sigma=2e5)
+CELL_CASES = {
+    # name: (kind, params, discrete eps(dt, w), continuous eps(w), tolerance against the continuous one)
+    "gold": ("gold", problems.GOLD_CONFIG,
+             lambda dt, w: _eps_drude_cp(*(problems.GOLD_CONFIG[k] for k in ("eps_inf", "omega_d", "gamma_d", "amp",
+                                                                              "phi", "omega", "gamma")), dt, w),
+             lambda w: problems.drude2cp_eps(problems.GOLD_CONFIG, w), 3e-2),
+    "gold_jp": ("lorentz", problems.GOLD_JP, lambda dt, w: _eps_lorentz(problems.GOLD_JP, dt, w),
+                lambda w: problems.lorentz_eps(problems.GOLD_JP, w), 1e-3),
+    "si_jp": ("lorentz", _damped(problems.SI_JP), lambda dt, w: _eps_lorentz(_damped(problems.SI_JP), dt, w),
+              lambda w: problems.lorentz_eps(_damped(problems.SI_JP), w), 1e-3),
+    "si_s": ("lorentz", _damped(problems.SI_S), lambda dt, w: _eps_lorentz(_damped(problems.SI_S), dt, w),
+             lambda w: problems.lorentz_eps(_damped(problems.SI_S), w), 1e-3),
+    "graphene_cp": ("graphene_cp", _GCP,
+                    lambda dt, w: _eps_drude_cp(_GCP["eps_inf"], np.sqrt(_GCP["width"] / 1e-9) * _GCP["drude_omega"],
+                                                _GCP["drude_gamma"], [_GCP["width"] / 1e-9 * a for a in _GCP["amp"]],
+                                                _GCP["phi"], _GCP["omega"], _GCP["gamma"], dt, w),
+                    lambda w: problems.graphene_cp_eps(_GCP, 1e-9, w), 1.5e-2),
+    "conductive": ("conductive", _COND, lambda dt, w: _eps_conductive(_COND, dt, w),
+                   lambda w: problems.conductive_eps(_COND, w), 2e-3),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CELL_CASES))
+def test_cell_permittivity_known_answer(oracle_lib, name):
+    kind, params, discrete, continuous, tol = CELL_CASES[name]
+    w = problems.dft_omegas(400e-9, 900e-9, 50)
+    spec, meta = problems.config_cell(kind, params, steps=256000)
+    O = oracle_lib.OracleJob(spec)
+    O.step(1, meta["Nt"])
+    e = O.get_probe(0)[:, 0]
+    O.close()
+    eps = problems.cell_eps(e, meta, w)
+    exact = discrete(meta["dt"], w)
+    assert np.max(np.abs(eps - exact) / np.abs(exact)) <= 1e-7
+    cont = continuous(w)
+    assert np.max(np.abs(eps - cont) / np.abs(cont)) <= tol
