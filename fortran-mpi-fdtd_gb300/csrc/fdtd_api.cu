@@ -123,6 +123,13 @@ struct fdtd_job {
   int num_sms = 152;
   cudaStream_t stream = nullptr;
   std::vector<void *> allocs;
+  // the buffers a step changes (fields, split parts, slabs, dispersive
+  // state, DFT sums and ring): what a checkpoint holds, in allocation order
+  struct StateBuf {
+    void *p;
+    size_t bytes;
+  };
+  std::vector<StateBuf> state;
   uint64_t dev_bytes = 0;
   // device state
   void *F[8] = {};  // ex ey ez hx hy hz ex_inc hz_inc
@@ -237,6 +244,14 @@ int alloc_dev(fdtd_job *J, void **p, size_t bytes) {
   // zeroing) before uploads on other streams or the host may touch it
   e = cudaStreamSynchronize(J->stream);
   if (e != cudaSuccess) return set_err(FDTD_ECUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
+  return FDTD_OK;
+}
+
+// a zeroed buffer that the time steps change: registered for checkpoints
+int alloc_state(fdtd_job *J, void **p, size_t bytes) {
+  int rc = alloc_dev(J, p, bytes);
+  if (rc) return rc;
+  J->state.push_back({*p, bytes == 0 ? 16 : bytes});
   return FDTD_OK;
 }
 
@@ -542,15 +557,15 @@ int commit_impl(fdtd_job *J) {
       J->dim == 3 || J->g.layout == FDTD_LAYOUT_2D_TM,
       J->dim == 3 || J->g.layout == FDTD_LAYOUT_2D_TE || J->dim == 1};
   for (int c = 0; c < 6; ++c)
-    if (has[c] && (rc = alloc_dev(J, &J->F[c], (size_t)N * sizeof(T)))) return rc;
+    if (has[c] && (rc = alloc_state(J, &J->F[c], (size_t)N * sizeof(T)))) return rc;
   if (J->has_tfsf) {
-    if ((rc = alloc_dev(J, &J->F[6], (size_t)N * sizeof(T)))) return rc;
-    if ((rc = alloc_dev(J, &J->F[7], (size_t)N * sizeof(T)))) return rc;
+    if ((rc = alloc_state(J, &J->F[6], (size_t)N * sizeof(T)))) return rc;
+    if ((rc = alloc_state(J, &J->F[7], (size_t)N * sizeof(T)))) return rc;
   }
   if (J->has_tfbox) {
-    if ((rc = alloc_dev(J, &J->F[6], (size_t)ny * sizeof(T)))) return rc;
-    if ((rc = alloc_dev(J, &J->F[7], (size_t)ny * sizeof(T)))) return rc;
-    if ((rc = alloc_dev(J, &J->d_tf_abc, 4 * sizeof(T)))) return rc;
+    if ((rc = alloc_state(J, &J->F[6], (size_t)ny * sizeof(T)))) return rc;
+    if ((rc = alloc_state(J, &J->F[7], (size_t)ny * sizeof(T)))) return rc;
+    if ((rc = alloc_state(J, &J->d_tf_abc, 4 * sizeof(T)))) return rc;
   }
   // ---- materials: device ids (constant dielectrics 1..127, dispersive
   // materials kAdeId..255), painted in call order ----
@@ -844,7 +859,7 @@ int commit_impl(fdtd_job *J) {
   J->ade_nf = 0;
   for (const MatRec &R : J->mats)
     J->ade_nf = std::max(J->ade_nf, ade_fields(R.kind, R.lz.npoles, R.lz.chi3 != 0.0, R.lz.ez_uses_x_current != 0));
-  if ((rc = alloc_dev(J, &J->d_ade_state, sizeof(T) * (size_t)std::max(1, J->ade_nf) * 3 * std::max(32, J->ade_stride))))
+  if ((rc = alloc_state(J, &J->d_ade_state, sizeof(T) * (size_t)std::max(1, J->ade_nf) * 3 * std::max(32, J->ade_stride))))
     return rc;
   {
     // most common constant-dielectric material: its Ku/eps is a kernel parameter
@@ -879,8 +894,8 @@ int commit_impl(fdtd_job *J) {
     const int nsp = J->dim == 3 ? 6 : 1;
     const bool two = sizeof(T) == 8;
     for (int q = 0; q < nsp; ++q) {
-      if ((rc = alloc_dev(J, &J->d_sp[q], (size_t)N * sizeof(T)))) return rc;
-      if (two && (rc = alloc_dev(J, &J->d_sp[6 + q], (size_t)N * sizeof(T)))) return rc;
+      if ((rc = alloc_state(J, &J->d_sp[q], (size_t)N * sizeof(T)))) return rc;
+      if (two && (rc = alloc_state(J, &J->d_sp[6 + q], (size_t)N * sizeof(T)))) return rc;
     }
   }
   if (ref && J->dim >= 2) {
@@ -915,7 +930,7 @@ int commit_impl(fdtd_job *J) {
         if ((rc = upload_prof<T>(J, Z, &sc[8], &sc[9], &sc[10], &sc[11]))) return rc;
         const int nf = J->dim == 3 ? 12 : 4;
         for (int q = 0; q < nf; ++q)
-          if ((rc = alloc_dev(J, &J->d_slab[side][q], (size_t)nx * rows * nz * sizeof(T)))) return rc;
+          if ((rc = alloc_state(J, &J->d_slab[side][q], (size_t)nx * rows * nz * sizeof(T)))) return rc;
       }
     }
   }
@@ -935,8 +950,8 @@ int commit_impl(fdtd_job *J) {
           else prof_high(Y, 1, rows, ep, p.sigma_max, p.order, dt, J->g.ds);
           void **lc = J->d_lc[line][side];
           if ((rc = upload_prof<T>(J, Y, &lc[0], &lc[1], &lc[2], &lc[3]))) return rc;
-          if ((rc = alloc_dev(J, &J->d_lex[line][side], (size_t)(rows + 2) * sizeof(T)))) return rc;
-          if ((rc = alloc_dev(J, &J->d_lhz[line][side], (size_t)(rows + 2) * sizeof(T)))) return rc;
+          if ((rc = alloc_state(J, &J->d_lex[line][side], (size_t)(rows + 2) * sizeof(T)))) return rc;
+          if ((rc = alloc_state(J, &J->d_lhz[line][side], (size_t)(rows + 2) * sizeof(T)))) return rc;
         }
       }
     }
@@ -1040,10 +1055,10 @@ int commit_impl(fdtd_job *J) {
     J->h2d += rot.size() * sizeof(double);
     J->h2d += omega.size() * sizeof(double);
   }
-  if ((rc = alloc_dev(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
-  if ((rc = alloc_dev(J, (void **)&J->d_acc_im, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
+  if ((rc = alloc_state(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
+  if ((rc = alloc_state(J, (void **)&J->d_acc_im, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
   J->stage_cap_rows = J->dim == 1 ? 4096 : kStageSteps;
-  if ((rc = alloc_dev(J, &J->d_stage, (size_t)std::max(1LL, base) * J->stage_cap_rows * sizeof(T)))) return rc;
+  if ((rc = alloc_state(J, &J->d_stage, (size_t)std::max(1LL, base) * J->stage_cap_rows * sizeof(T)))) return rc;
   int blocks = 0;
   for (auto &m : J->mon_dev)
     blocks += ((m.ncomp * m.ncell + 255) / 256) * ((m.nfreq + 7) / 8);
@@ -2279,6 +2294,137 @@ int fdtd_step(fdtd_job *J, int32_t n_first, int32_t n_steps) {
   if (n_steps < 0 || n_first < 1) return set_err(FDTD_EINVAL, "bad step range");
   if (n_steps == 0) return FDTD_OK;
   return DISPATCH(J, step_impl)(J, n_first, n_steps);
+}
+
+// ---- checkpoint ----------------------------------------------------------
+// Layout: CkptHeader, then per state buffer its size (uint64), per probe its
+// rows and components (int32 pairs), then the buffers' bytes in allocation
+// order and the probes' rows.  The unfolded part of the DFT ring is part of
+// the stage buffer, with stage_fill and stage_n0 in the header, so a resumed
+// job folds the same rings as the saved one would have.
+struct CkptHeader {
+  char magic[8];
+  uint32_t version;
+  int32_t layout, precision, n[3];
+  uint32_t nbuf, nprobe;
+  int32_t stage_fill, stage_n0, last_n, reserved;
+  uint64_t total;
+};
+constexpr char kCkptMagic[8] = {'F', 'D', 'T', 'D', 'C', 'K', 'P', 'T'};
+
+static uint64_t ckpt_bytes(const fdtd_job *J) {
+  uint64_t b = sizeof(CkptHeader) + J->state.size() * sizeof(uint64_t) + J->probes.size() * 2 * sizeof(int32_t);
+  for (auto &s : J->state) b += s.bytes;
+  for (auto &P : J->probes) b += (uint64_t)P.cap * P.ncomp * sizeof(double);
+  return b;
+}
+
+int fdtd_state_bytes(const fdtd_job *J, uint64_t *bytes) {
+  if (!J || !bytes) return set_err(FDTD_EINVAL, "null argument");
+  if (!J->committed) return set_err(FDTD_ESTATE, "the job is not committed");
+  *bytes = ckpt_bytes(J);
+  return FDTD_OK;
+}
+
+int fdtd_save_state(fdtd_job *J, void *buf, uint64_t bytes) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (!buf) return set_err(FDTD_EINVAL, "null buffer");
+  const uint64_t need = ckpt_bytes(J);
+  if (bytes < need) return set_err(FDTD_ERANGE, "checkpoint needs %llu bytes, got %llu", (unsigned long long)need,
+                                   (unsigned long long)bytes);
+  // the step boundary: everything queued has run; the ring is not folded
+  CK(cudaStreamSynchronize(J->stream));
+  CK(cudaGetLastError());
+  char *o = (char *)buf;
+  CkptHeader h{};
+  memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.layout = J->g.layout;
+  h.precision = J->g.precision;
+  for (int a = 0; a < 3; ++a) h.n[a] = J->g.n[a];
+  h.nbuf = (uint32_t)J->state.size();
+  h.nprobe = (uint32_t)J->probes.size();
+  h.stage_fill = J->stage_fill;
+  h.stage_n0 = J->stage_n0;
+  h.last_n = J->last_n;
+  h.total = need;
+  memcpy(o, &h, sizeof h);
+  o += sizeof h;
+  for (auto &s : J->state) {
+    const uint64_t b = s.bytes;
+    memcpy(o, &b, sizeof b);
+    o += sizeof b;
+  }
+  for (auto &P : J->probes) {
+    const int32_t rc2[2] = {P.cap, P.ncomp};
+    memcpy(o, rc2, sizeof rc2);
+    o += sizeof rc2;
+  }
+  for (auto &s : J->state) {
+    CK(cudaMemcpy(o, s.p, s.bytes, cudaMemcpyDeviceToHost));
+    o += s.bytes;
+  }
+  for (auto &P : J->probes) {
+    const size_t b = (size_t)P.cap * P.ncomp * sizeof(double);
+    if (b) CK(cudaMemcpy(o, P.buf, b, cudaMemcpyDeviceToHost));
+    o += b;
+  }
+  J->d2h += need;
+  return FDTD_OK;
+}
+
+int fdtd_load_state(fdtd_job *J, const void *buf, uint64_t bytes) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (!buf || bytes < sizeof(CkptHeader)) return set_err(FDTD_EINVAL, "null or short checkpoint");
+  const char *in = (const char *)buf;
+  CkptHeader h;
+  memcpy(&h, in, sizeof h);
+  if (memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1) return set_err(FDTD_EINVAL, "not a checkpoint of this library");
+  if (h.total != bytes) return set_err(FDTD_EINVAL, "checkpoint of %llu bytes given as %llu", (unsigned long long)h.total,
+                                       (unsigned long long)bytes);
+  bool same = h.layout == J->g.layout && h.precision == J->g.precision && h.nbuf == J->state.size() &&
+              h.nprobe == J->probes.size();
+  for (int a = 0; a < 3; ++a) same = same && h.n[a] == J->g.n[a];
+  if (!same) return set_err(FDTD_EINVAL, "the checkpoint comes from a job of another layout, precision, size or set-up");
+  const char *sz = in + sizeof h;
+  for (size_t q = 0; q < J->state.size(); ++q) {
+    uint64_t b;
+    memcpy(&b, sz + q * sizeof b, sizeof b);
+    if (b != J->state[q].bytes) return set_err(FDTD_EINVAL, "checkpoint buffer %zu holds %llu bytes, the job %zu", q,
+                                               (unsigned long long)b, J->state[q].bytes);
+  }
+  const char *pr = sz + J->state.size() * sizeof(uint64_t);
+  int n_probe_max = 0;
+  std::vector<int32_t> caps(J->probes.size());
+  for (size_t q = 0; q < J->probes.size(); ++q) {
+    int32_t rc2[2];
+    memcpy(rc2, pr + q * sizeof rc2, sizeof rc2);
+    if (rc2[1] != J->probes[q].ncomp || rc2[0] < 0) return set_err(FDTD_EINVAL, "checkpoint probe %zu does not match", q);
+    caps[q] = rc2[0];
+    if (rc2[0] > 0) n_probe_max = std::max(n_probe_max, J->probes[q].d.n_first + rc2[0] - 1);
+  }
+  CK(cudaStreamSynchronize(J->stream));
+  if (n_probe_max > 0 && (rc = ensure_probe_cap(J, n_probe_max))) return rc;
+  const char *o = pr + J->probes.size() * 2 * sizeof(int32_t);
+  for (auto &s : J->state) {
+    CK(cudaMemcpy(s.p, o, s.bytes, cudaMemcpyHostToDevice));
+    o += s.bytes;
+  }
+  for (size_t q = 0; q < J->probes.size(); ++q) {
+    ProbeRec &P = J->probes[q];
+    const size_t b = (size_t)caps[q] * P.ncomp * sizeof(double);
+    if (P.buf && P.cap > 0) CK(cudaMemset(P.buf, 0, (size_t)P.cap * P.ncomp * sizeof(double)));
+    if (b) CK(cudaMemcpy(P.buf, o, b, cudaMemcpyHostToDevice));
+    o += b;
+  }
+  J->stage_fill = h.stage_fill;
+  J->stage_n0 = h.stage_n0;
+  J->last_n = h.last_n;
+  J->prog_prev = -1;
+  J->h2d += bytes;
+  return FDTD_OK;
 }
 
 int fdtd_update_DE(fdtd_job *J, int32_t n) {

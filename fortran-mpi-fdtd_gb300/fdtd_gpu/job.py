@@ -25,7 +25,7 @@ EXPORTS = [
     "fdtd_pml_update_H", "fdtd_sample", "fdtd_sync", "fdtd_get_field", "fdtd_set_field",
     "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_estimate_bytes", "fdtd_profile",
     "fdtd_kernel_time", "fdtd_kernel_cells", "fdtd_set_tile", "fdtd_get_tile", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
-    "fdtd_dft_sample_noalloc",
+    "fdtd_dft_sample_noalloc", "fdtd_state_bytes", "fdtd_save_state", "fdtd_load_state",
     "fdtd_server_create", "fdtd_server_submit", "fdtd_server_wait", "fdtd_server_job", "fdtd_server_times",
     "fdtd_server_release", "fdtd_server_stats", "fdtd_server_destroy",
 ]
@@ -52,6 +52,8 @@ def lib(path=None):
             "fdtd_add_gold": [vp, vp, vp, C.POINTER(i32)], "fdtd_add_graphene": [vp, vp, vp, C.POINTER(i32)],
             "fdtd_add_lorentz": [vp, vp, vp, C.POINTER(i32)], "fdtd_add_graphene_cp": [vp, vp, vp, C.POINTER(i32)],
             "fdtd_add_conductive": [vp, vp, dbl, dbl, C.POINTER(i32)],
+            "fdtd_state_bytes": [vp, C.POINTER(C.c_uint64)], "fdtd_save_state": [vp, vp, C.c_uint64],
+            "fdtd_load_state": [vp, vp, C.c_uint64],
             "fdtd_add_pml": [vp, vp], "fdtd_add_tfsf_1d": [vp, vp], "fdtd_add_tfsf": [vp, vp],
             "fdtd_add_source": [vp, vp, C.POINTER(i32)], "fdtd_add_monitor": [vp, vp, C.POINTER(i32)],
             "fdtd_add_probe": [vp, vp, C.POINTER(i32)], "fdtd_commit": [vp],
@@ -240,6 +242,19 @@ class Job:
         out = np.empty(max(1, cnt.value * ncomp))
         check(lib().fdtd_get_probe(self.h, int(pid), out.ctypes.data, C.byref(cnt)))
         return out[: cnt.value * ncomp].reshape(cnt.value, ncomp)
+
+    def save_state(self):
+        """The job's evolving state at this step boundary (fdtd_save_state)."""
+        n = C.c_uint64()
+        check(lib().fdtd_state_bytes(self.h, C.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        check(lib().fdtd_save_state(self.h, buf.ctypes.data, n.value))
+        return buf
+
+    def load_state(self, buf):
+        """Restore a state saved from a job of the same description."""
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        check(lib().fdtd_load_state(self.h, buf.ctypes.data, buf.size))
 
     def device_bytes(self):
         b = C.c_uint64()

@@ -357,6 +357,18 @@ int fdtd_update_H(fdtd_job *job, int32_t n);
 int fdtd_pml_update_H(fdtd_job *job, int32_t n);
 int fdtd_sample(fdtd_job *job, int32_t n);
 
+/* Checkpoint and resume.  fdtd_save_state writes the job's evolving state at
+ * a step boundary into one host buffer of fdtd_state_bytes bytes: the field
+ * arrays (with an incident line), the split-PML parts and reference slabs,
+ * the dispersive state, the DFT sums with the not yet folded part of the
+ * sample ring, and the probe records.  fdtd_load_state puts it into a job
+ * committed from the same description; the job then continues bit for bit
+ * as the saved one would have, from the step after the last one that ran.
+ * The reference keeps no checkpoints. */
+int fdtd_state_bytes(const fdtd_job *job, uint64_t *bytes);
+int fdtd_save_state(fdtd_job *job, void *buf, uint64_t bytes);
+int fdtd_load_state(fdtd_job *job, const void *buf, uint64_t bytes);
+
 /* ---- results ------------------------------------------------------------- */
 int fdtd_sync(fdtd_job *job);
 /* n[0]*n[1]*n[2] values of one component, x fastest. */

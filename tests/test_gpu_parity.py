@@ -704,3 +704,60 @@ def test_cell_response_vs_oracle(gpu, oracle_lib, prec, name):
         w = problems.dft_omegas(400e-9, 900e-9, 50)
         ej_eps, eo_eps = problems.cell_eps(ej, meta, w), problems.cell_eps(eo, meta, w)  # complex
         assert np.linalg.norm(ej_eps - eo_eps) / np.linalg.norm(eo_eps) <= 1e-4
+
+
+@pytest.mark.parametrize("case", ["2d_tmz", "2d_ref", "3d_ref", "1d_ref", "tfsf_3d"])
+def test_checkpoint_resume_is_bitwise(gpu, case):
+    """A job saved at a step boundary inside a DFT ring and loaded into a new
+    job of the same description continues bit for bit as the uninterrupted
+    run: fields, DFT sums and probes.  The cases cover the gold ADE, the
+    all-face and the reference PML, the 1D TFSF line and the 2D/3D box."""
+    if case == "2d_tmz":
+        spec, _ = problems.config_2d_tmz(precision=abi.F32, n=256, ncyl=4, nfreq=8)
+        comps, n1, n2 = (abi.EZ, abi.HX, abi.HY), 333, 700
+    elif case == "2d_ref":
+        spec, _ = problems.reference_2d()
+        comps, n1, n2 = (abi.EX, abi.EY, abi.HZ), 1001, 2000
+    elif case == "3d_ref":
+        spec, _ = problems.reference_3d()
+        comps, n1, n2 = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ), 150, 300
+    elif case == "1d_ref":
+        spec, _ = problems.reference_1d()
+        comps, n1, n2 = (abi.EX, abi.HZ, abi.EX_INC, abi.HZ_INC), 2501, 5000
+    else:
+        spec, _ = problems.config_tfsf(layout=abi.LAYOUT_3D, precision=abi.F64, n=64, scatterer="gold", radius=8.0)
+        comps, n1, n2 = (abi.EX, abi.EY, abi.EZ, abi.E_INC, abi.H_INC), 101, 260
+    whole = gpu.Job(spec)
+    whole.step(1, n2)
+    first = gpu.Job(spec)
+    first.step(1, n1)
+    state = first.save_state()
+    first.close()
+    resumed = gpu.Job(spec)
+    resumed.load_state(state)
+    resumed.step(n1 + 1, n2 - n1)
+    for c in comps:
+        np.testing.assert_array_equal(resumed.get_field(c), whole.get_field(c))
+    for q in range(len(spec.monitors)):
+        for x, y in zip(resumed.get_monitor(q), whole.get_monitor(q)):
+            np.testing.assert_array_equal(x, y)
+    for q in range(len(spec.probes)):
+        np.testing.assert_array_equal(resumed.get_probe(q), whole.get_probe(q))
+    whole.close()
+    resumed.close()
+
+
+def test_checkpoint_from_another_job_is_refused(gpu):
+    a, _ = problems.config_2d_tmz(precision=abi.F32, n=256, ncyl=4, nfreq=8)
+    b, _ = problems.config_2d_tmz(precision=abi.F32, n=512, ncyl=4, nfreq=8)
+    ja, jb = gpu.Job(a), gpu.Job(b)
+    ja.step(1, 10)
+    state = ja.save_state()
+    with pytest.raises(gpu.FdtdError) as e:
+        jb.load_state(state)
+    assert e.value.code == abi.FDTD_EINVAL
+    state[:8] = 0
+    with pytest.raises(gpu.FdtdError):
+        ja.load_state(state)
+    ja.close()
+    jb.close()
