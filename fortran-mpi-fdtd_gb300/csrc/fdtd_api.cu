@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -128,6 +129,7 @@ struct fdtd_job {
   struct StateBuf {
     void *p;
     size_t bytes;
+    int esz;  // element size: 4 float, 8 double
   };
   std::vector<StateBuf> state;
   uint64_t dev_bytes = 0;
@@ -174,6 +176,7 @@ struct fdtd_job {
   int nsrc_dev = 0;
   // CUDA graph of one ring of kStageSteps steps + its DFT fold
   int *d_base = nullptr;
+  unsigned long long *d_count = nullptr;  // fdtd_check_finite
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_kernels = 0;
@@ -223,7 +226,17 @@ void keep_pool_memory(int dev) {
   });
 }
 
+// fdtd_debug_fail_alloc: the number of job allocations that still succeed
+// before one fails (-1: none fails)
+std::atomic<long long> g_fail_after{-1};
+
 cudaError_t pool_alloc(fdtd_job *J, void **p, size_t bytes) {
+  long long left = g_fail_after.load();
+  while (left >= 0 && !g_fail_after.compare_exchange_weak(left, left - 1)) {}
+  if (left == 0) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
   keep_pool_memory(J->device);
   return cudaMallocAsync(p, bytes, J->stream);
 }
@@ -247,11 +260,13 @@ int alloc_dev(fdtd_job *J, void **p, size_t bytes) {
   return FDTD_OK;
 }
 
-// a zeroed buffer that the time steps change: registered for checkpoints
-int alloc_state(fdtd_job *J, void **p, size_t bytes) {
+// a zeroed buffer that the time steps change, of float or double elements
+// (esz 0: the job's precision): registered for checkpoints and for
+// fdtd_check_finite
+int alloc_state(fdtd_job *J, void **p, size_t bytes, int esz = 0) {
   int rc = alloc_dev(J, p, bytes);
   if (rc) return rc;
-  J->state.push_back({*p, bytes == 0 ? 16 : bytes});
+  J->state.push_back({*p, bytes == 0 ? size_t(16) : bytes, esz ? esz : (int)J->esz});
   return FDTD_OK;
 }
 
@@ -1055,8 +1070,8 @@ int commit_impl(fdtd_job *J) {
     J->h2d += rot.size() * sizeof(double);
     J->h2d += omega.size() * sizeof(double);
   }
-  if ((rc = alloc_state(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
-  if ((rc = alloc_state(J, (void **)&J->d_acc_im, (size_t)std::max(1LL, acc) * sizeof(double)))) return rc;
+  if ((rc = alloc_state(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double), 8))) return rc;
+  if ((rc = alloc_state(J, (void **)&J->d_acc_im, (size_t)std::max(1LL, acc) * sizeof(double), 8))) return rc;
   J->stage_cap_rows = J->dim == 1 ? 4096 : kStageSteps;
   if ((rc = alloc_state(J, &J->d_stage, (size_t)std::max(1LL, base) * J->stage_cap_rows * sizeof(T)))) return rc;
   int blocks = 0;
@@ -1212,17 +1227,21 @@ int ensure_srctab(fdtd_job *J, int n_max) {
   J->nsrc_dev = nsrc;
   if (nsrc == 0 || n_max <= J->srctab_steps) return FDTD_OK;
   const long long old_steps = J->srctab_steps;
+  // a larger device table first: if it cannot be had, nothing has changed
+  double *nb = nullptr;
+  long long cap = J->srctab_cap_steps;
+  if (n_max > J->srctab_cap_steps) {
+    cap = std::max<long long>(2 * J->srctab_cap_steps, std::max(n_max, 4096));
+    cudaError_t e = pool_alloc(J, (void **)&nb, (size_t)cap * nsrc * sizeof(double));
+    if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "source table: %s", cudaGetErrorString(e));
+  }
   for (long long n = old_steps + 1; n <= n_max; ++n) {
     const double t = (double)(n - 1) * J->g.dt;           // t=real(n-1,8)*dt
     for (auto &s : J->srcs)
       if (src_on_device(J, s)) J->srctab.push_back(gauss_t(s, t) * s.amp);
   }
   J->srctab_steps = n_max;
-  if (n_max > J->srctab_cap_steps) {
-    long long cap = std::max<long long>(2 * J->srctab_cap_steps, std::max(n_max, 4096));
-    double *nb = nullptr;
-    cudaError_t e = pool_alloc(J, (void **)&nb, (size_t)cap * nsrc * sizeof(double));
-    if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "source table: %s", cudaGetErrorString(e));
+  if (nb) {
     CK(cudaStreamSynchronize(J->stream));
     if (J->d_srctab) { pool_free(J, J->d_srctab); J->dev_bytes -= (uint64_t)J->srctab_cap_steps * nsrc * sizeof(double); }
     J->d_srctab = nb;
@@ -1636,10 +1655,15 @@ int line_run(fdtd_job *J, int n_first, int n_steps, int stages) {
       }
     }
     if ((long long)v.size() > J->srcval_cap) {
+      // the new buffer first: if it cannot be had, the old one stays
+      const long long cap = std::max<long long>((long long)v.size(), 4096);
+      double *nb = nullptr;
+      cudaError_t e = pool_alloc(J, (void **)&nb, cap * sizeof(double));
+      if (e != cudaSuccess) return set_err(FDTD_ENOMEM, "source values: %s", cudaGetErrorString(e));
       if (J->d_srcval) { pool_free(J, J->d_srcval); J->dev_bytes -= J->srcval_cap * sizeof(double); }
-      J->srcval_cap = std::max<long long>((long long)v.size(), 4096);
-      CK(pool_alloc(J, (void **)&J->d_srcval, J->srcval_cap * sizeof(double)));
-      J->dev_bytes += J->srcval_cap * sizeof(double);
+      J->d_srcval = nb;
+      J->srcval_cap = cap;
+      J->dev_bytes += cap * sizeof(double);
     }
     CK(cudaMemcpyAsync(J->d_srcval, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, J->stream));
     CK(cudaStreamSynchronize(J->stream));  // v is a temporary
@@ -2294,6 +2318,34 @@ int fdtd_step(fdtd_job *J, int32_t n_first, int32_t n_steps) {
   if (n_steps < 0 || n_first < 1) return set_err(FDTD_EINVAL, "bad step range");
   if (n_steps == 0) return FDTD_OK;
   return DISPATCH(J, step_impl)(J, n_first, n_steps);
+}
+
+// ---- health checks ---------------------------------------------------------
+int fdtd_check_finite(fdtd_job *J, int64_t *count) {
+  int rc = check_job(J, true);
+  if (rc) return rc;
+  if (!count) return set_err(FDTD_EINVAL, "null count");
+  if (!J->d_count && (rc = alloc_dev(J, (void **)&J->d_count, sizeof(unsigned long long)))) return rc;
+  CK(cudaMemsetAsync(J->d_count, 0, sizeof(unsigned long long), J->stream));
+  for (auto &s : J->state)
+    if (launch_count_nonfinite(s.p, s.bytes, s.esz, J->d_count, J->num_sms, J->stream))
+      return set_err(FDTD_ECUDA, "non-finite count launch failed");
+  for (auto &P : J->probes)
+    if (P.buf && launch_count_nonfinite(P.buf, (size_t)P.cap * P.ncomp * sizeof(double), 8, J->d_count, J->num_sms,
+                                        J->stream))
+      return set_err(FDTD_ECUDA, "non-finite count launch failed");
+  J->launches += J->state.size() + J->probes.size();
+  unsigned long long h = 0;
+  CK(cudaMemcpyAsync(&h, J->d_count, sizeof h, cudaMemcpyDeviceToHost, J->stream));
+  CK(cudaStreamSynchronize(J->stream));
+  J->prog_prev = -1;
+  *count = (int64_t)h;
+  return FDTD_OK;
+}
+
+int fdtd_debug_fail_alloc(int32_t after) {
+  g_fail_after.store(after < 0 ? -1 : (long long)after);
+  return FDTD_OK;
 }
 
 // ---- checkpoint ----------------------------------------------------------

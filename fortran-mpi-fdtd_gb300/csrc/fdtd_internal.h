@@ -241,6 +241,8 @@ template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *str
 // returns the kernels launched
 template <typename T> int launch_gather(const StepParams<T> &p, void *stream);
 // total-field/scattered-field box: incident line and face terms of a half step
+// kcheck.cu: count the non-finite float (esz 4) or double (esz 8) values of a buffer
+int launch_count_nonfinite(const void *p, size_t bytes, int esz, unsigned long long *out, int num_sms, void *stream);
 template <typename T> int launch_tfsf(const StepParams<T> &p, bool e_half, void *stream);
 
 // DFT fold: acc += sum over valid ring slots of e^{i w t} * sample * dt

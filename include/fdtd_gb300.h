@@ -369,6 +369,17 @@ int fdtd_state_bytes(const fdtd_job *job, uint64_t *bytes);
 int fdtd_save_state(fdtd_job *job, void *buf, uint64_t bytes);
 int fdtd_load_state(fdtd_job *job, const void *buf, uint64_t bytes);
 
+/* Health.  fdtd_check_finite counts the NaN and infinite values in the same
+ * buffers a checkpoint holds (one reduction pass over them, on the job's
+ * stream; a caller checks every so many steps).  The reference checks
+ * nothing.
+ * fdtd_debug_fail_alloc makes the device allocation that follows `after`
+ * further successful ones fail as an out-of-memory would, for any job of the
+ * process (-1 switches it off): it lets a caller exercise its recovery from
+ * FDTD_ENOMEM at every allocation of set-up and stepping. */
+int fdtd_check_finite(fdtd_job *job, int64_t *count);
+int fdtd_debug_fail_alloc(int32_t after);
+
 /* ---- results ------------------------------------------------------------- */
 int fdtd_sync(fdtd_job *job);
 /* n[0]*n[1]*n[2] values of one component, x fastest. */

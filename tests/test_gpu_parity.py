@@ -761,3 +761,62 @@ def test_checkpoint_from_another_job_is_refused(gpu):
         ja.load_state(state)
     ja.close()
     jb.close()
+
+
+def test_nonfinite_values_are_counted(gpu):
+    """A NaN written into one cell on the host spreads through the update,
+    and fdtd_check_finite sees it; a clean run counts none."""
+    spec, _ = problems.config_2d_tmz(precision=abi.F32, n=256, ncyl=4, nfreq=8)
+    J = gpu.Job(spec)
+    J.step(1, 100)
+    assert J.count_nonfinite() == 0
+    ez = J.get_field(abi.EZ)
+    ez[0, 128, 128] = np.nan
+    J.set_field(abi.EZ, ez)
+    assert J.count_nonfinite() == 1
+    J.step(101, 40)
+    assert J.count_nonfinite() > 100
+    J.close()
+
+
+def test_allocation_failures_are_reported_and_recovered(gpu):
+    """Every device allocation of set-up and stepping fails once in turn
+    (fdtd_debug_fail_alloc): each failure comes back as FDTD_ENOMEM with the
+    job still usable, and a job whose step failed runs correctly when
+    stepped again."""
+    spec, _ = problems.config_2d_tmz(precision=abi.F32, n=256, ncyl=4, nfreq=8)
+    spec.add_probe((128, 128, 0), (abi.EZ,))
+    ref = gpu.Job(spec)
+    ref.step(1, 100)
+    want = [ref.get_field(c) for c in (abi.EZ, abi.HX, abi.HY)], ref.get_probe(0)
+    ref.close()
+    failed_setup = failed_step = 0
+    try:
+        for k in range(400):
+            gpu.fail_alloc_after(k)
+            try:
+                J = gpu.Job(spec)
+            except gpu.FdtdError as e:
+                assert e.code == abi.FDTD_ENOMEM, str(e)
+                failed_setup += 1
+                continue
+            try:
+                J.step(1, 100)
+                done = True
+            except gpu.FdtdError as e:
+                assert e.code == abi.FDTD_ENOMEM, str(e)
+                failed_step += 1
+                done = False
+            gpu.fail_alloc_after(-1)
+            if not done:
+                J.step(1, 100)  # a failed step ran nothing: the same call again
+            got = [J.get_field(c) for c in (abi.EZ, abi.HX, abi.HY)], J.get_probe(0)
+            J.close()
+            for x, y in zip(got[0], want[0]):
+                np.testing.assert_array_equal(x, y)
+            np.testing.assert_array_equal(got[1], want[1])
+            if done:
+                break
+    finally:
+        gpu.fail_alloc_after(-1)
+    assert failed_setup >= 10 and failed_step >= 2
