@@ -6,7 +6,9 @@
 // reference's formulas and operation order) and then only launches kernels.
 // There is no CPU compute path: without an sm_103 device every call that
 // needs one fails with FDTD_ENODEV.
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <atomic>
@@ -25,6 +27,16 @@
 #include "fdtd_internal.h"
 
 using namespace fdtd;
+
+// an NVTX range over a host entry point: profilers (ncu --nvtx, nsys) can
+// pick the engine's calls by name; without a profiler attached it costs a
+// predictable branch
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 namespace {
 
@@ -177,6 +189,11 @@ struct fdtd_job {
   // CUDA graph of one ring of kStageSteps steps + its DFT fold
   int *d_base = nullptr;
   unsigned long long *d_count = nullptr;  // fdtd_check_finite
+  // the TMA-staged 3D E core: tensor maps of Hx, Hy, Hz, and the flag its
+  // bounded waits set when they give up
+  TmaMaps tma{};
+  bool tma_ok = false;
+  int *d_err = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_kernels = 0;
@@ -258,6 +275,17 @@ int alloc_dev(fdtd_job *J, void **p, size_t bytes) {
   e = cudaStreamSynchronize(J->stream);
   if (e != cudaSuccess) return set_err(FDTD_ECUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
   return FDTD_OK;
+}
+
+// the device flag of bounded waits (after the stream has drained): a wait
+// that gave up is reported once as FDTD_ECUDA
+int kernel_flag(fdtd_job *J) {
+  if (!J->d_err) return FDTD_OK;
+  int h = 0;
+  CK(cudaMemcpy(&h, J->d_err, sizeof h, cudaMemcpyDeviceToHost));
+  if (!h) return FDTD_OK;
+  CK(cudaMemset(J->d_err, 0, sizeof h));
+  return set_err(FDTD_ECUDA, "a bounded wait in the TMA core kernel gave up");
 }
 
 // a zeroed buffer that the time steps change, of float or double elements
@@ -495,6 +523,7 @@ int split_3d(fdtd_job *J, const std::vector<uint8_t> &rf) {
 
 template <typename T>
 int tune_tiles(fdtd_job *J);
+int setup_tma(fdtd_job *J);
 
 // The TFSF box: faces, and the cells its face terms touch (the box widened by
 // one cell across each face) inside the grid, the main range and the PML's
@@ -1079,7 +1108,9 @@ int commit_impl(fdtd_job *J) {
     blocks += ((m.ncomp * m.ncell + 255) / 256) * ((m.nfreq + 7) / 8);
   J->dft_blocks = blocks;
   CK(cudaStreamSynchronize(J->stream));
+  if ((rc = setup_tma(J))) return rc;
   if ((rc = tune_tiles<T>(J))) return rc;
+  if ((rc = kernel_flag(J))) return rc;
   J->committed = true;
   return FDTD_OK;
 }
@@ -1091,9 +1122,54 @@ double gauss_t(const fdtd_source_desc &s, double t) {
   return std::exp(-0.5 * (a * a)) * std::sin(s.w0 * t);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }();
+  return fn;
+}
+
+// The TMA-staged E core (FP32, 4-cell vectors) needs every neighbour of the
+// core box inside the grid: the box starts at least one cell in on each
+// axis.  Its tensor maps cover the H arrays as nx x ny x nz floats with
+// one-plane boxes of the kernel's tile: 128 cells along x (Hy, Hz: plus a
+// 4-float halo), 8 rows (Hx, Hz: plus the row below).
+int setup_tma(fdtd_job *J) {
+  J->tma_ok = false;
+  if (J->dim != 3 || J->esz != 4 || J->vec != 4 || J->ncore <= 0) return FDTD_OK;
+  if (J->cv0 < 1 || J->cy0 < 1 || J->cz0 < 1) return FDTD_OK;
+  if (getenv("FDTD_NO_TMA")) return FDTD_OK;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return FDTD_OK;
+  const cuuint64_t dim[3] = {(cuuint64_t)J->nx, (cuuint64_t)J->ny, (cuuint64_t)J->nz};
+  const cuuint64_t stride[2] = {(cuuint64_t)J->nx * 4, (cuuint64_t)J->nx * J->ny * 4};
+  const cuuint32_t es[3] = {1, 1, 1};
+  auto make = [&](CUtensorMap *m, void *base, cuuint32_t bx, cuuint32_t by) {
+    const cuuint32_t box[3] = {bx, by, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dim, stride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  if (!make(&J->tma.hx, J->F[3], 128, 9) || !make(&J->tma.hy, J->F[4], 132, 8) || !make(&J->tma.hz, J->F[5], 132, 9))
+    return FDTD_OK;  // not offered
+  int rc;
+  if (!J->d_err && (rc = alloc_dev(J, (void **)&J->d_err, sizeof(int)))) return rc;
+  J->tma_ok = true;
+  return FDTD_OK;
+}
+
 template <typename T>
 void fill_common(fdtd_job *J, StepParams<T> &p) {
   memset(&p, 0, sizeof p);
+  p.tma = J->tma_ok ? &J->tma : nullptr;
+  p.err = J->d_err;
   p.layout = J->g.layout;
   p.nx = J->nx; p.ny = J->ny; p.nz = J->nz;
   for (int a = 0; a < 3; ++a) {
@@ -1402,6 +1478,8 @@ int tune_tiles(fdtd_job *J) {
   if (J->dim < 2 || J->ncore <= 0) return FDTD_OK;
   if (J->tile_req > 0) {
     J->tile = J->tile_req - 1;
+    if (J->tile == 6 && !J->tma_ok)
+      return set_err(FDTD_EINVAL, "tile 7 (the TMA core) needs FP32, 4-cell vectors and a core box inside the grid");
     return FDTD_OK;
   }
   const char *off = getenv("FDTD_TUNE");
@@ -1411,7 +1489,8 @@ int tune_tiles(fdtd_job *J) {
   }
   int lg = 0;
   for (long long c = J->ncore; c > 1; c >>= 1) ++lg;
-  const long long key = ((((long long)J->dim * 8 + J->g.layout) * 4 + J->g.precision) * 8 + J->vec) * 64 + lg;
+  const long long key = (((((long long)J->dim * 8 + J->g.layout) * 4 + J->g.precision) * 8 + J->vec) * 64 + lg) * 2 +
+                        (J->tma_ok ? 1 : 0);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -1428,7 +1507,8 @@ int tune_tiles(fdtd_job *J) {
   CK(cudaEventCreate(&b));
   float best = 3.0e38f;
   int choice = 1;
-  const int nshapes = J->dim == 3 ? 6 : 3;  // 3D: also the z-marching kernels
+  // 3D: also the z-marching kernels and, where set up, the TMA-staged E core
+  const int nshapes = J->dim == 3 ? (J->tma_ok ? 7 : 6) : 3;
   for (int c = 0; c < nshapes; ++c) {
     p.tile = c;
     for (int w = 0; w < 2; ++w) {
@@ -2306,6 +2386,7 @@ int fdtd_add_probe(fdtd_job *J, const fdtd_probe_desc *p, int32_t *id) {
 }
 
 int fdtd_commit(fdtd_job *J) {
+  NvtxRange nvtx_("fdtd_commit");
   int rc = check_job(J, false);
   if (rc) return rc;
   if (J->dim == 1 && J->has_pml && J->pml.npml[1][0] < 1) return set_err(FDTD_EINVAL, "1D PML needs npmly >= 1");
@@ -2313,6 +2394,7 @@ int fdtd_commit(fdtd_job *J) {
 }
 
 int fdtd_step(fdtd_job *J, int32_t n_first, int32_t n_steps) {
+  NvtxRange nvtx_("fdtd_step");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (n_steps < 0 || n_first < 1) return set_err(FDTD_EINVAL, "bad step range");
@@ -2322,6 +2404,7 @@ int fdtd_step(fdtd_job *J, int32_t n_first, int32_t n_steps) {
 
 // ---- health checks ---------------------------------------------------------
 int fdtd_check_finite(fdtd_job *J, int64_t *count) {
+  NvtxRange nvtx_("fdtd_check_finite");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (!count) return set_err(FDTD_EINVAL, "null count");
@@ -2379,6 +2462,7 @@ int fdtd_state_bytes(const fdtd_job *J, uint64_t *bytes) {
 }
 
 int fdtd_save_state(fdtd_job *J, void *buf, uint64_t bytes) {
+  NvtxRange nvtx_("fdtd_save_state");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (!buf) return set_err(FDTD_EINVAL, "null buffer");
@@ -2427,6 +2511,7 @@ int fdtd_save_state(fdtd_job *J, void *buf, uint64_t bytes) {
 }
 
 int fdtd_load_state(fdtd_job *J, const void *buf, uint64_t bytes) {
+  NvtxRange nvtx_("fdtd_load_state");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (!buf || bytes < sizeof(CkptHeader)) return set_err(FDTD_EINVAL, "null or short checkpoint");
@@ -2480,10 +2565,12 @@ int fdtd_load_state(fdtd_job *J, const void *buf, uint64_t bytes) {
 }
 
 int fdtd_update_DE(fdtd_job *J, int32_t n) {
+  NvtxRange nvtx_("fdtd_update_DE");
   int rc = check_job(J, true);
   return rc ? rc : DISPATCH(J, proc_call)(J, n, 0);
 }
 int fdtd_pml_update_E(fdtd_job *J, int32_t n) {
+  NvtxRange nvtx_("fdtd_pml_update_E");
   int rc = check_job(J, true);
   return rc ? rc : DISPATCH(J, proc_call)(J, n, 1);
 }
@@ -2494,28 +2581,33 @@ int fdtd_interchange(fdtd_job *J, int32_t which) {
   return FDTD_OK;  // one domain: the halo is the neighbouring cell
 }
 int fdtd_update_H(fdtd_job *J, int32_t n) {
+  NvtxRange nvtx_("fdtd_update_H");
   int rc = check_job(J, true);
   return rc ? rc : DISPATCH(J, proc_call)(J, n, 2);
 }
 int fdtd_pml_update_H(fdtd_job *J, int32_t n) {
+  NvtxRange nvtx_("fdtd_pml_update_H");
   int rc = check_job(J, true);
   return rc ? rc : DISPATCH(J, proc_call)(J, n, 3);
 }
 int fdtd_sample(fdtd_job *J, int32_t n) {
+  NvtxRange nvtx_("fdtd_sample");
   int rc = check_job(J, true);
   return rc ? rc : DISPATCH(J, proc_call)(J, n, 4);
 }
 
 int fdtd_sync(fdtd_job *J) {
+  NvtxRange nvtx_("fdtd_sync");
   int rc = check_job(J, true);
   if (rc) return rc;
   if ((rc = DISPATCH(J, dft_fold)(J))) return rc;
   CK(cudaStreamSynchronize(J->stream));
   CK(cudaGetLastError());
-  return FDTD_OK;
+  return kernel_flag(J);
 }
 
 int fdtd_get_field(fdtd_job *J, int32_t comp, double *host) {
+  NvtxRange nvtx_("fdtd_get_field");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (!host) return set_err(FDTD_EINVAL, "null buffer");
@@ -2523,6 +2615,7 @@ int fdtd_get_field(fdtd_job *J, int32_t comp, double *host) {
 }
 
 int fdtd_set_field(fdtd_job *J, int32_t comp, const double *host) {
+  NvtxRange nvtx_("fdtd_set_field");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (!host) return set_err(FDTD_EINVAL, "null buffer");
@@ -2530,6 +2623,7 @@ int fdtd_set_field(fdtd_job *J, int32_t comp, const double *host) {
 }
 
 int fdtd_get_monitor(fdtd_job *J, int32_t id, double *re, double *im) {
+  NvtxRange nvtx_("fdtd_get_monitor");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (id < 0 || id >= (int)J->mons.size()) return set_err(FDTD_ERANGE, "bad monitor id");
@@ -2543,6 +2637,7 @@ int fdtd_get_monitor(fdtd_job *J, int32_t id, double *re, double *im) {
 }
 
 int fdtd_get_probe(fdtd_job *J, int32_t id, double *host, int32_t *count) {
+  NvtxRange nvtx_("fdtd_get_probe");
   int rc = check_job(J, true);
   if (rc) return rc;
   if (id < 0 || id >= (int)J->probes.size()) return set_err(FDTD_ERANGE, "bad probe id");
@@ -2653,7 +2748,7 @@ int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
 int fdtd_set_tile(fdtd_job *J, int32_t tile) {
   int rc = check_job(J, false);
   if (rc) return rc;
-  const int maxt = J->dim == 3 ? 6 : 3;
+  const int maxt = J->dim == 3 ? 7 : 3;
   if (tile < 0 || tile > maxt) return set_err(FDTD_EINVAL, "tile must be 0 (tune) or 1..%d", maxt);
   J->tile_req = tile;
   return FDTD_OK;

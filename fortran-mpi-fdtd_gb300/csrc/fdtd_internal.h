@@ -16,6 +16,7 @@
 //   * DFT: samples of the monitored cells are staged per step in a ring of
 //     kStageSteps slots and folded into FP64 accumulators once per ring.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -23,6 +24,13 @@
 #include "fdtd_gb300.h"
 
 namespace fdtd {
+
+// tensor maps of the 3D H arrays (FP32) for the TMA-staged E core: boxes of
+// one plane, Hx 128 x 9 rows from (x0, y0-1), Hy 132 x 8 from (x0-4, y0),
+// Hz 132 x 9 from (x0-4, y0-1)
+struct TmaMaps {
+  CUtensorMap hx, hy, hz;
+};
 
 constexpr int kMaxMat = 256;
 constexpr int kMaxSrc = 8;
@@ -164,7 +172,9 @@ struct StepParams {
   // 3D: the core box is vectors [cv0, cv0+cw) x rows [cy0, cy0+ch) x planes
   // [cz0, cz0+cd); edge_units are then x-vectors (k*ny + j)*nx/V + vector
   int ch, cz0, cd;
-  int tile;                // block shape of the core kernels (0..2, tuned)
+  int tile;                // block shape of the core kernels (tuned; 3D 6: the TMA-staged E core)
+  const struct TmaMaps *tma;  // host copy of the H planes' tensor maps, for the launcher (or null)
+  int *err;                // device flag: a bounded wait of a kernel gave up (nonzero)
   // sampling fused into the H kernel
   int gather;              // 1: tile threads write the stage row / probes
   int nmon;

@@ -700,6 +700,173 @@ __global__ void __launch_bounds__(32 * RY) h3d_corez(const __grid_constant__ Ste
   }
 }
 
+// ---- TMA-staged E core (FP32) ----------------------------------------------
+// A block owns a tile of kTmaX cells along x by kTmaY rows and marches up to
+// kTmaZ planes of the core box along z (more blocks than planes per block:
+// a block's planes run one after another).  For every plane one thread issues
+// three tiled bulk copies (cp.async.bulk.tensor) of the H planes into shared
+// memory: Hx with the row below, Hy with the four cells to its left (a copy's
+// x must start on a 16-byte boundary, so the halo is four floats wide, of
+// which the kernel uses one), Hz with both.  The previous plane's Hx and Hy
+// are still in shared memory for the z differences.  Three stages rotate:
+// the plane below, this plane, and the next plane in flight.  E, the material
+// ids and the stores are the threads' own vector accesses, as in e3d_core,
+// whose arithmetic this kernel repeats term for term.  It runs only where the
+// core box starts at least one cell inside the grid on every axis, so every
+// neighbour it reads is a cell of the grid (no wrap, no zero fill).
+constexpr int kTmaX = 128, kTmaY = 8, kTmaZ = 8;
+constexpr int kTmaHx = (kTmaY + 1) * kTmaX;             // floats of one stage's Hx
+constexpr int kTmaHy = kTmaY * (kTmaX + 4);
+constexpr int kTmaHz = (kTmaY + 1) * (kTmaX + 4);
+constexpr int kTmaHzPad = ((kTmaHz * 4 + 127) / 128) * 32;  // Hz rounded up to 128 bytes
+constexpr int kTmaStage = kTmaHx + kTmaHy + kTmaHzPad;     // floats per stage
+constexpr unsigned kTmaBytes = (unsigned)(kTmaHx + kTmaHy + kTmaHz) * 4u;  // bytes a stage receives
+constexpr int kTmaSmem = 3 * kTmaStage * 4 + 128;           // dynamic shared bytes (+ alignment)
+static_assert((kTmaHx * 4) % 128 == 0 && (kTmaHy * 4) % 128 == 0 && (kTmaStage * 4) % 128 == 0,
+              "TMA destinations are 128-byte aligned");
+constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait gives up
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// bounded wait for the phase of the given parity to complete
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, unsigned parity) {
+  for (unsigned it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(32 * kTmaY) e3d_core_tma(const __grid_constant__ StepParams<float> p,
+                                                           const __grid_constant__ TmaMaps m) {
+  extern __shared__ unsigned char sm_raw[];
+  __shared__ __align__(8) unsigned long long bar[3];
+  pdl_wait();
+  pdl_release();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int bx = (p.cw + 31) >> 5, by = (p.ch + kTmaY - 1) / kTmaY;
+  const int tx = blockIdx.x % bx, t2 = blockIdx.x / bx, ty = t2 % by, tz = t2 / by;
+  const int x0 = (p.cv0 + tx * 32) * 4, y0 = p.cy0 + ty * kTmaY;
+  const int kz0 = p.cz0 + tz * kTmaZ, kz1 = min(kz0 + kTmaZ, p.cz0 + p.cd);
+  const bool live = tx * 32 + lane < p.cw && ty * kTmaY + w < p.ch;
+  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(sm_raw);
+  const uint32_t sbase = (raw + 127u) & ~127u;
+  const float *gbase = (const float *)(sm_raw + (sbase - raw));
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(bar);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 3; ++s) mbar_init(bar0 + 8 * s, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // load number u (plane kz0 - 1 + u) goes to stage u % 3, whose (u / 3)-th
+  // phase it completes
+  auto issue = [&](int u) {
+    const int s = u % 3, plane = kz0 - 1 + u;
+    const uint32_t st = sbase + (uint32_t)(s * kTmaStage * 4), b = bar0 + 8 * s;
+    mbar_expect_tx(b, kTmaBytes);
+    tma_load_3d(st, &m.hx, x0, y0 - 1, plane, b);
+    tma_load_3d(st + kTmaHx * 4, &m.hy, x0 - 4, y0, plane, b);
+    tma_load_3d(st + (kTmaHx + kTmaHy) * 4, &m.hz, x0 - 4, y0 - 1, plane, b);
+  };
+  const int nload = kz1 - kz0 + 1;
+  if (threadIdx.x == 0) {
+    issue(0);
+    if (nload > 1) issue(1);
+  }
+  int issued = nload > 1 ? 2 : 1, waited = 0;
+  bool ok = __syncthreads_and(mbar_wait(bar0, 0));
+  waited = 1;
+  // this thread's E, material ids and row flag of the first plane; later
+  // planes' are loaded before the barrier that ends the previous plane, so
+  // their latency overlaps the wait for the H copies
+  const int j = y0 + w, xr = 4 * lane;
+  float ex[4] = {}, ey[4] = {}, ez[4] = {};
+  uint8_t id[4] = {};
+  bool skip = true;
+  auto load_e = [&](int k) {
+    skip = !live || __ldg(p.rowflag + (long long)k * p.ny + j);
+    if (skip) return;
+    const long long c = ((long long)k * p.ny + j) * p.nx + x0 + xr;
+    vld<float, 4>(p.ex + c, ex);
+    vld<float, 4>(p.ey + c, ey);
+    vld<float, 4>(p.ez + c, ez);
+    vld_ids<4>(p.mat + c, id);
+  };
+  load_e(kz0);
+  for (int k = kz0; ok && k < kz1; ++k) {
+    const int u = k - kz0 + 1;  // this plane's load number
+    // the next plane goes into the stage the plane k - 2 held: every thread
+    // finished reading it before the barrier that ended the last round
+    if (threadIdx.x == 0 && u + 1 < nload) issue(u + 1);
+    if (u + 1 < nload) issued = u + 2;
+    ok = __syncthreads_and(mbar_wait(bar0 + 8 * (u % 3), (unsigned)(u / 3) & 1u));
+    if (!ok) break;
+    waited = u + 1;
+    if (!skip) {
+      const float *Hx = gbase + (u % 3) * kTmaStage, *Hy = Hx + kTmaHx, *Hz = Hy + kTmaHy;
+      const float *Hxp = gbase + ((u + 2) % 3) * kTmaStage, *Hyp = Hxp + kTmaHx;
+      const int yr = (kTmaX + 4) * w + 4 + xr, zr = (kTmaX + 4) * (w + 1) + 4 + xr;
+      const float4 hx4 = *(const float4 *)(Hx + kTmaX * (w + 1) + xr);
+      const float4 hxd4 = *(const float4 *)(Hx + kTmaX * w + xr);
+      const float4 hxb4 = *(const float4 *)(Hxp + kTmaX * (w + 1) + xr);
+      const float4 hy4 = *(const float4 *)(Hy + yr), hyb4 = *(const float4 *)(Hyp + yr);
+      const float4 hz4 = *(const float4 *)(Hz + zr), hzd4 = *(const float4 *)(Hz + zr - (kTmaX + 4));
+      const float hyl = Hy[yr - 1], hzl = Hz[zr - 1];
+      const float hx[4] = {hx4.x, hx4.y, hx4.z, hx4.w}, hxd[4] = {hxd4.x, hxd4.y, hxd4.z, hxd4.w};
+      const float hxb[4] = {hxb4.x, hxb4.y, hxb4.z, hxb4.w}, hy[4] = {hy4.x, hy4.y, hy4.z, hy4.w};
+      const float hyb[4] = {hyb4.x, hyb4.y, hyb4.z, hyb4.w}, hz[4] = {hz4.x, hz4.y, hz4.z, hz4.w};
+      const float hzd[4] = {hzd4.x, hzd4.y, hzd4.z, hzd4.w};
+      const long long c = ((long long)k * p.ny + j) * p.nx + x0 + xr;
+      bool uni = true;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) uni &= id[q] == p.id0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float ca = uni ? p.ca0 : coef_ca3(p, id[q]);
+        const float curlhzy = hz[q] - hzd[q], curlhyz = -hy[q] + hyb[q];
+        const float curlhxz = hx[q] - hxb[q], curlhzx = -hz[q] + (q ? hz[q - 1] : hzl);
+        const float curlhyx = hy[q] - (q ? hy[q - 1] : hyl), curlhxy = -hx[q] + hxd[q];
+        ex[q] = ex[q] + ca * (curlhzy + curlhyz);
+        ey[q] = ey[q] + ca * (curlhxz + curlhzx);
+        ez[q] = ez[q] + ca * (curlhyx + curlhxy);
+      }
+      if (uni) {
+        vst<float, 4>(p.ex + c, ex);
+        vst<float, 4>(p.ey + c, ey);
+        vst<float, 4>(p.ez + c, ez);
+      } else {  // dispersive cells belong to the ADE blocks
+        st_guard3<float, 4>(p.ex + c, ex, id);
+        st_guard3<float, 4>(p.ey + c, ey, id);
+        st_guard3<float, 4>(p.ez + c, ez, id);
+      }
+    }
+    if (k + 1 < kz1) load_e(k + 1);
+    __syncthreads();
+  }
+  if (!ok) {
+    // a wait gave up: report it, and let the copies already issued land
+    // (each wait bounded) before the block's shared memory goes away
+    if (threadIdx.x == 0) atomicExch(p.err, 1);
+    for (int u = waited; u < issued; ++u) mbar_wait(bar0 + 8 * (u % 3), (unsigned)(u / 3) & 1u);
+  }
+}
+
 constexpr int kCoreZ = 8;  // planes per thread of the z-marching kernels
 
 template <typename T, int V, int RY>
@@ -716,10 +883,44 @@ void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent
   else launch_pdl(h3d_core<T, V, RY>, blocks, 32 * RY, s, p, ev);
 }
 
+// the TMA-staged E core: one block per tile of kTmaX x kTmaY cells and
+// kTmaZ planes, kTmaSmem bytes of dynamic shared memory
+inline void launch_core3_tma(const StepParams<float> &p, cudaStream_t s, cudaEvent_t ev) {
+  const int blocks = ((p.cw + 31) / 32) * ((p.ch + kTmaY - 1) / kTmaY) * ((p.cd + kTmaZ - 1) / kTmaZ);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(32 * kTmaY);
+  cfg.dynamicSmemBytes = kTmaSmem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  int na = 1;
+  if (ev) {
+    at[1].id = cudaLaunchAttributeProgrammaticEvent;
+    at[1].val.programmaticEvent.event = ev;
+    at[1].val.programmaticEvent.flags = 0;
+    at[1].val.programmaticEvent.triggerAtBlockStart = 1;
+    na = 2;
+  }
+  cfg.attrs = at;
+  cfg.numAttrs = na;
+  cudaLaunchKernelEx(&cfg, e3d_core_tma, p, *p.tma);
+}
+
 // tile 0: 4 rows of 32 x-vectors, 1: 8 rows, 2: 16 rows, one plane per
-// thread; tiles 3, 4, 5: the same shapes marching kCoreZ planes per thread
+// thread; tiles 3, 4, 5: the same shapes marching kCoreZ planes per thread;
+// tile 6 (FP32 with 4-cell vectors, where the host set up the tensor maps):
+// the TMA-staged E core, with tile 1's H core
 template <typename T, int V>
 void launch_core3_v(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
+  if constexpr (sizeof(T) == 4 && V == 4) {
+    if (p.tile == 6 && p.tma) {
+      if (e_half) launch_core3_tma(p, s, ev);
+      else launch_core3<T, V, 8>(p, false, s, ev);
+      return;
+    }
+  }
   switch (p.tile) {
     case 0: launch_core3<T, V, 4>(p, e_half, s, ev); break;
     case 2: launch_core3<T, V, 16>(p, e_half, s, ev); break;
