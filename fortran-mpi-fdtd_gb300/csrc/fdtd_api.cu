@@ -150,6 +150,8 @@ struct fdtd_job {
   uint8_t *d_mat = nullptr;
   void *d_mc = nullptr, *d_ac = nullptr, *d_mca = nullptr, *d_mcs = nullptr;
   uint8_t *d_rowflag = nullptr;
+  uint32_t *d_uni = nullptr;  // per x-vector: all ids id0 (see StepParams::uni)
+  int uni_words = 0;
   int nade = 0, ade_stride = 0, ade_nf = 0, id0 = 0;
   std::vector<double> mca_host;
   std::vector<char> ac_host;  // AdeCoef<T> table, host copy
@@ -1081,6 +1083,28 @@ int commit_impl(fdtd_job *J) {
     J->h2d += rf.size();
     if ((rc = split_3d(J, rf))) return rc;
   }
+  if (J->dim == 3) {
+    // per x-vector of vec cells: 1 where every id is id0, so that the 3D E
+    // cores (DRAM-bound) need not load the vector's ids; the 2D cores, which
+    // run from L2, issue the id load with their field loads instead
+    const int V = J->vec, nvec = nx / V, words = (nvec + 31) / 32;
+    const long long rows = (long long)ny * nz;
+    std::vector<uint32_t> bits((size_t)rows * words, 0u);
+    const uint8_t id0 = (uint8_t)J->id0;
+    for (long long r = 0; r < rows; ++r) {
+      const uint8_t *row = mat.data() + (size_t)r * nx;
+      uint32_t *wd = bits.data() + (size_t)r * words;
+      for (int v = 0; v < nvec; ++v) {
+        bool u = true;
+        for (int q = 0; q < V; ++q) u = u && row[v * V + q] == id0;
+        if (u) wd[v >> 5] |= 1u << (v & 31);
+      }
+    }
+    if ((rc = alloc_dev(J, (void **)&J->d_uni, bits.size() * sizeof(uint32_t)))) return rc;
+    CK(cudaMemcpy(J->d_uni, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    J->h2d += bits.size() * sizeof(uint32_t);
+    J->uni_words = words;
+  }
   J->stage_row = base;
   J->acc_total = acc;
   if (!omega.empty()) {
@@ -1170,6 +1194,8 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   memset(&p, 0, sizeof p);
   p.tma = J->tma_ok ? &J->tma : nullptr;
   p.err = J->d_err;
+  p.uni = J->d_uni;
+  p.uni_words = J->uni_words;
   p.layout = J->g.layout;
   p.nx = J->nx; p.ny = J->ny; p.nz = J->nz;
   for (int a = 0; a < 3; ++a) {

@@ -131,6 +131,8 @@ struct StepParams {
   int id0;                 // most common material id of the main cells and
   T ca0;                   //   its Ku/eps (no table lookup for it)
   const uint8_t *rowflag;  // per x-row, ROW_* bits: 2D [j], 3D [k*ny + j]
+  const uint32_t *uni;     // 3D, per x-vector of vec cells: bit v of word [row*uni_words + v/32] is 1
+  int uni_words;           //   when every cell of the vector has id id0 (its ids need no load)
   // ADE slots
   int nade;
   const int *ade_cell;     // linear cell index

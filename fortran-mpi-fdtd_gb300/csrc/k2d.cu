@@ -436,7 +436,7 @@ __device__ __forceinline__ void core_e(const StepParams<T> &p, int j, int i0) {
   else if (p.per[1]) vld_ro<T, V>(ydc + (long long)(ny - 1) * nx + i0, below);
   vld_ro<T, V>(xdc + c, a0);
   const T left = i0 > 0 ? __ldg(xdc + c - 1) : (p.per[0] ? __ldg(xdc + c + nx - 1) : T(0));
-  vld_ids<V>(p.mat + c, id);
+  vld_ids<V>(p.mat + c, id);  // issued with the field loads: a bitmap test first costs a round trip here
   if (L == 3) {
     T a1[V];
     vld_ro<T, V>(p.hx + c, a1);

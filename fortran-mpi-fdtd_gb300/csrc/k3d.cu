@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(32 * RY) e3d_core(const __grid_constant__ Step
   vld<T, V>(p.ex + c, ex);
   vld<T, V>(p.ey + c, ey);
   vld<T, V>(p.ez + c, ez);
-  vld_ids<V>(p.mat + c, id);
+  vec_ids<T, V>(p, (long long)u.k * p.ny + u.j, u.i0 / V, p.mat + c, id);
   if (__ldg(p.rowflag + (long long)u.k * p.ny + u.j)) return;  // source rows: general launch
   bool uni = true;
 #pragma unroll
@@ -622,7 +622,7 @@ __global__ void __launch_bounds__(32 * RY) e3d_corez(const __grid_constant__ Ste
     vld<T, V>(p.ex + c, ex);
     vld<T, V>(p.ey + c, ey);
     vld<T, V>(p.ez + c, ez);
-    vld_ids<V>(p.mat + c, id);
+    vec_ids<T, V>(p, (long long)k * p.ny + u.j, u.i0 / V, p.mat + c, id);
     if (!__ldg(p.rowflag + (long long)k * p.ny + u.j)) {  // source rows: general launch
       bool uni = true;
 #pragma unroll
@@ -806,7 +806,7 @@ __global__ void __launch_bounds__(32 * kTmaY) e3d_core_tma(const __grid_constant
     vld<float, 4>(p.ex + c, ex);
     vld<float, 4>(p.ey + c, ey);
     vld<float, 4>(p.ez + c, ez);
-    vld_ids<4>(p.mat + c, id);
+    vec_ids<float, 4>(p, (long long)k * p.ny + j, (x0 + xr) / 4, p.mat + c, id);
   };
   load_e(kz0);
   for (int k = kz0; ok && k < kz1; ++k) {

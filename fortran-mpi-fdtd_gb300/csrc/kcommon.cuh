@@ -355,6 +355,19 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
   return e;
 }
 
+// the ids of the x-vector v of a row: id0 throughout when the uniformity
+// bitmap says so, else loaded
+template <typename T, int V>
+__device__ __forceinline__ void vec_ids(const StepParams<T> &p, long long row, int v, const uint8_t *mat,
+                                        uint8_t (&id)[V]) {
+  if (p.uni && ((__ldg(p.uni + row * p.uni_words + (v >> 5)) >> (v & 31)) & 1u)) {
+#pragma unroll
+    for (int q = 0; q < V; ++q) id[q] = (uint8_t)p.id0;
+  } else {
+    vld_ids<V>(mat, id);
+  }
+}
+
 // coefficients of a dispersive material id (>= kAdeId)
 template <typename T>
 __device__ __forceinline__ AdeCoef<T> ade_coef(const StepParams<T> &p, int id) {
