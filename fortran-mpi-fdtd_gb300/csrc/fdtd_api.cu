@@ -79,6 +79,7 @@ struct MatRec {
   fdtd_lorentz_desc lz;
   fdtd_graphene_cp_desc gcp;
   double sigma;  // conductive dielectric: eps holds eps_inf
+  fdtd_graphene_nk_desc gnk;
   fdtd_region region;
   std::vector<double> centers;
   std::vector<uint8_t> mask;
@@ -720,6 +721,39 @@ int commit_impl(fdtd_job *J) {
       a.wr = T(1.0 / ga);
       a.wi = T(0);
       c.kind = MK_GOLD;
+      c.ade = (int)ac.size();
+      c.ca = T(Ku);
+      c.cs = T(1);
+      ac.push_back(a);
+    } else if (R.kind == MK_GRAPHENE_NK) {
+      // graphene633 (1D/graphene633_mod.f90:48-105): the graphene update with
+      // no Drude memory (ha = 0), ga = eps_inf + sigma dt/eps0, I += gb E,
+      // Kerr chi3 alpha, Raman (1 - alpha) chi3 damped by gamma_nl
+      const fdtd_graphene_nk_desc &p = R.gnk;
+      const double sigma = std::sqrt(p.scale) * 4.0 * K.pi * p.n * p.k * K.c0 * K.ep0 / p.wavelength;
+      const double eps_inf = p.scale * (p.n * p.n - p.k * p.k);
+      const double gb = sigma * dt / K.ep0;
+      AdeCoef<T> a{};
+      a.kind = MK_GRAPHENE;
+      a.normal = -1;
+      a.ha = T(0);
+      a.hb = T(gb);
+      a.dha = T(1);
+      a.ga = T(eps_inf + gb);
+      a.kerr = T(p.alpha * p.chi3);
+      double r0 = 0.0, c1 = 0.0, c2 = 0.0;
+      if (p.chi3 != 0.0) {
+        const double betaR = std::sqrt(p.w_nl * p.w_nl - p.gamma_nl * p.gamma_nl);
+        const double omegaR = (p.w_nl * p.w_nl) / betaR;
+        r0 = (1.0 - p.alpha) * p.chi3 * omegaR * dt * std::exp(-p.gamma_nl * dt) * std::sin(betaR * dt);
+        const double sb = std::sin(0.5 * betaR * dt);
+        c1 = 2.0 * (std::expm1(-p.gamma_nl * dt) * std::cos(betaR * dt) - 2.0 * sb * sb);
+        c2 = -std::expm1(-2.0 * p.gamma_nl * dt);
+      }
+      a.r0 = T(r0);
+      a.rv = T(1.0 - c2);
+      a.rs = T(c1 + c2);
+      c.kind = MK_GRAPHENE;
       c.ade = (int)ac.size();
       c.ca = T(Ku);
       c.cs = T(1);
@@ -2252,6 +2286,19 @@ int fdtd_add_graphene(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_des
   MatRec m{};
   m.kind = MK_GRAPHENE;
   m.gr = *p;
+  return add_mat(J, r, m, id);
+}
+
+int fdtd_add_graphene_nk(fdtd_job *J, const fdtd_region *r, const fdtd_graphene_nk_desc *p, int32_t *id) {
+  if (!p) return set_err(FDTD_EINVAL, "null graphene parameters");
+  if (!std::isfinite(p->n) || !std::isfinite(p->k) || !(p->wavelength > 0) || !(p->scale >= 0) ||
+      !std::isfinite(p->chi3) || !std::isfinite(p->alpha))
+    return set_err(FDTD_EINVAL, "graphene_nk needs finite n, k, chi3, alpha, wavelength > 0 and scale >= 0");
+  if (p->chi3 != 0.0 && !(p->w_nl > p->gamma_nl && p->gamma_nl >= 0))
+    return set_err(FDTD_EINVAL, "the Raman term needs w_nl > gamma_nl >= 0");
+  MatRec m{};
+  m.kind = MK_GRAPHENE_NK;
+  m.gnk = *p;
   return add_mat(J, r, m, id);
 }
 

@@ -38,13 +38,15 @@ constexpr int kMaxMon = 16;
 constexpr int kMaxProbe = 16;
 constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
 
-// MK_CONDUCTIVE exists on the host only: its cells run the gold update
+// MK_CONDUCTIVE and MK_GRAPHENE_NK exist on the host only: their cells run
+// the gold and the graphene update
 enum MatKind : int { MK_NONE = 0, MK_DIEL = 1, MK_GOLD = 2, MK_GRAPHENE = 3, MK_LORENTZ = 4, MK_GRAPHENE_CP = 5,
-                     MK_CONDUCTIVE = 6 };
+                     MK_CONDUCTIVE = 6, MK_GRAPHENE_NK = 7 };
 constexpr int kMaxPoles = FDTD_LORENTZ_MAX_POLES;
 constexpr int kMaxCp = 4;  // critical points of the reference's graphene
 __host__ __device__ constexpr bool is_ade_kind(int k) {
-  return k == MK_GOLD || k == MK_GRAPHENE || k == MK_LORENTZ || k == MK_GRAPHENE_CP || k == MK_CONDUCTIVE;
+  return k == MK_GOLD || k == MK_GRAPHENE || k == MK_LORENTZ || k == MK_GRAPHENE_CP || k == MK_CONDUCTIVE ||
+         k == MK_GRAPHENE_NK;
 }
 
 // per material id, in the job's precision
@@ -223,7 +225,7 @@ enum Role : int {
 constexpr int kAdeFields = 12;
 constexpr int ade_fields(int kind, int npoles, int nl, int zx) {
   return kind == MK_GOLD || kind == MK_CONDUCTIVE ? 6
-       : kind == MK_GRAPHENE ? 4
+       : kind == MK_GRAPHENE || kind == MK_GRAPHENE_NK ? 4
        : kind == MK_GRAPHENE_CP ? 12
        : kind == MK_LORENTZ ? (zx ? 2 * npoles + 3 : nl ? 2 * npoles + 2 : 2 * npoles)
        : 0;

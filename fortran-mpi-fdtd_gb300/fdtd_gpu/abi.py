@@ -57,6 +57,11 @@ class LorentzDesc(C.Structure):
 RAMAN_EXACT, RAMAN_CENTRAL = 0, 1
 
 
+class GrapheneNkDesc(C.Structure):
+    _fields_ = [("n", C.c_double), ("k", C.c_double), ("wavelength", C.c_double), ("scale", C.c_double),
+                ("chi3", C.c_double), ("alpha", C.c_double), ("w_nl", C.c_double), ("gamma_nl", C.c_double)]
+
+
 class GrapheneCpDesc(C.Structure):
     _fields_ = [("eps_inf", C.c_double), ("drude_omega", C.c_double), ("drude_gamma", C.c_double),
                 ("amp", C.c_double * 4), ("phi", C.c_double * 4), ("omega", C.c_double * 4),

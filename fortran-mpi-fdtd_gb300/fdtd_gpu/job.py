@@ -18,7 +18,7 @@ _lib = None
 # every entry point declared in include/fdtd_gb300.h
 EXPORTS = [
     "fdtd_create", "fdtd_destroy", "fdtd_last_error", "fdtd_device_count",
-    "fdtd_add_dielectric", "fdtd_add_gold", "fdtd_add_graphene", "fdtd_add_lorentz", "fdtd_add_graphene_cp", "fdtd_add_conductive",
+    "fdtd_add_dielectric", "fdtd_add_gold", "fdtd_add_graphene", "fdtd_add_lorentz", "fdtd_add_graphene_cp", "fdtd_add_conductive", "fdtd_add_graphene_nk",
     "fdtd_add_pml",
     "fdtd_add_tfsf_1d", "fdtd_add_tfsf", "fdtd_add_source", "fdtd_add_monitor", "fdtd_add_probe", "fdtd_commit",
     "fdtd_step", "fdtd_update_DE", "fdtd_pml_update_E", "fdtd_interchange", "fdtd_update_H",
@@ -53,6 +53,7 @@ def lib(path=None):
             "fdtd_add_gold": [vp, vp, vp, C.POINTER(i32)], "fdtd_add_graphene": [vp, vp, vp, C.POINTER(i32)],
             "fdtd_add_lorentz": [vp, vp, vp, C.POINTER(i32)], "fdtd_add_graphene_cp": [vp, vp, vp, C.POINTER(i32)],
             "fdtd_add_conductive": [vp, vp, dbl, dbl, C.POINTER(i32)],
+            "fdtd_add_graphene_nk": [vp, vp, vp, C.POINTER(i32)],
             "fdtd_state_bytes": [vp, C.POINTER(C.c_uint64)], "fdtd_save_state": [vp, vp, C.c_uint64],
             "fdtd_load_state": [vp, vp, C.c_uint64],
             "fdtd_check_finite": [vp, C.POINTER(C.c_int64)], "fdtd_debug_fail_alloc": [i32],
@@ -151,6 +152,9 @@ class Job:
                 elif m.kind == "lorentz":
                     p = S.lorentz_struct(m.params)
                     check(L.fdtd_add_lorentz(self.h, C.byref(r), C.byref(p), C.byref(mid)))
+                elif m.kind == "graphene_nk":
+                    p = S.graphene_nk_struct(m.params)
+                    check(L.fdtd_add_graphene_nk(self.h, C.byref(r), C.byref(p), C.byref(mid)))
                 elif m.kind == "conductive":
                     check(L.fdtd_add_conductive(self.h, C.byref(r), m.params["eps_inf"], m.params["sigma"],
                                                 C.byref(mid)))

@@ -76,6 +76,19 @@ GRAPHENE_ND_3LJP = dict(GRAPHENE_3LJP, delta_eps=(0.0, 0.0, 0.0))
 GRAPHENE_4LJP = dict(_lorentz(abi.LORENTZ_JP, 1.070682, (-0.163673, 0.843432, -0.170024, -0.121134),
                               (1.642784, 0.807691, 0.934364, 0.525964), (2.267351, 1.018179, 0.621508, 0.033048)),
                      sheet=1, chi3=1e-18, w_nl=2.0 * PI * 40e12, gamma_nl=1e12, e_scale=Z0, ez_uses_x_current=1)
+# The 1D graphene at 633 nm, graphene633 (M1/graphene633_mod.f90:50): its n, k;
+# scaleFactor, xi3, alpha, wNL and dnuNL are set by a program (none does): the
+# values here are a test choice (no scaling, linear).
+GRAPHENE_633 = dict(n=2.731108, k=1.357, wavelength=633e-9, scale=1.0, chi3=0.0, alpha=0.0, w_nl=0.0, gamma_nl=0.0)
+
+
+def graphene_nk_eps(p, omega):
+    """The permittivity of graphene633's linear update: eps_inf + i sigma/(eps0 w)
+    with its sigma and eps_inf from n, k (M1/graphene633_mod.f90:51-52)."""
+    sigma = math.sqrt(p["scale"]) * 4.0 * PI * p["n"] * p["k"] * C0 * EP0 / p["wavelength"]
+    return conductive_eps(dict(eps_inf=p["scale"] * (p["n"] ** 2 - p["k"] ** 2), sigma=sigma), omega)
+
+
 # Conductive Si at 800 nm, SiL800 (M3/siL800_mod.f90:16-17): sigma in S/m.
 SI_L800 = dict(eps_inf=3.675 ** 2, sigma=112.8134634)
 
@@ -518,6 +531,8 @@ def config_1d_slab(material, lo=2000, thickness=50, precision=abi.F64, steps=200
     region = box((0, lo, 0), (0, lo + thickness - 1, 0))
     if "drude_omega" in material:
         spec.add_graphene_cp(region, material)
+    elif "wavelength" in material:
+        spec.add_graphene_nk(region, material)
     elif "sigma" in material:
         spec.add_conductive(region, material)
     else:

@@ -19,6 +19,7 @@ Box = Tuple[Tuple[int, int, int], Tuple[int, int, int]]
 @dataclass
 class Material:
     kind: str                      # "dielectric" | "gold" | "graphene" | "lorentz" | "graphene_cp" | "conductive"
+    #                                  | "graphene_nk"
     region: dict                   # {"kind": "box", "lo":..., "hi":...} | spheres | mask
     eps: float = 1.0
     params: Optional[dict] = None
@@ -85,6 +86,12 @@ class JobSpec:
     def add_conductive(self, region, params):
         """A conductive dielectric (SiL800): params {"eps_inf", "sigma" [S/m]}."""
         self.materials.append(Material("conductive", region, params=dict(params)))
+        return len(self.materials)
+
+    def add_graphene_nk(self, region, params):
+        """The reference's 1D graphene at 633 nm (graphene633): params {"n",
+        "k", "wavelength", "scale", "chi3", "alpha", "w_nl", "gamma_nl"}."""
+        self.materials.append(Material("graphene_nk", region, params=dict(params)))
         return len(self.materials)
 
     def add_graphene_cp(self, region, params):
@@ -193,6 +200,11 @@ def lorentz_struct(p):
     d.gamma_nl = p.get("gamma_nl", 0.0)
     d.e_scale = p.get("e_scale", 1.0)
     return d
+
+
+def graphene_nk_struct(p):
+    return abi.GrapheneNkDesc(p["n"], p["k"], p["wavelength"], p["scale"], p.get("chi3", 0.0), p.get("alpha", 0.0),
+                              p.get("w_nl", 0.0), p.get("gamma_nl", 0.0))
 
 
 def graphene_cp_struct(p):

@@ -192,6 +192,27 @@ typedef struct fdtd_lorentz_desc {
  * along normal_axis is vacuum (E = D): the 2D module sets Ey = Dy, and the 3D
  * one updates Ex and Ez only, so normal_axis = 1 (y) is the reference's
  * sheet; -1 updates every component. */
+/* The reference's 1D graphene at 633 nm, graphene633 (1D/graphene633_mod.f90:
+ * 26-105): a conductive layer from its refractive index n + ik at one
+ * wavelength, with the linearised Kerr term of an instantaneous fraction
+ * alpha of chi3 and a Raman-delayed rest:
+ *   E = (D - I + 2 chi3 alpha E^3) / (ga + S_R + 3 chi3 alpha E^2),  I += gb E
+ *   S_R(n) = r1 S_R(n-1) + r2 S_R(n-2) + r0 E(n)^2
+ * where E on the right is the previous step's; sigma = sqrt(s) 4 pi n k c0
+ * eps0 / wavelength, eps_inf = s (n^2 - k^2), ga = eps_inf + sigma dt/eps0,
+ * gb = sigma dt/eps0 (s = scale), and r0 = (1 - alpha) chi3 wR dt
+ * e^{-gamma_nl dt} sin(bR dt), r1 = 2 e^{-gamma_nl dt} cos(bR dt),
+ * r2 = -e^{-2 gamma_nl dt}, bR = sqrt(w_nl^2 - gamma_nl^2), wR = w_nl^2/bR
+ * (this module damps with gamma_nl where the 3D Graphene takes gamma_nl/2).
+ * Every E component of the layout takes the update. */
+typedef struct fdtd_graphene_nk_desc {
+  double n, k;              /* refractive index of the layer (the module's 2.731108, 1.357) */
+  double wavelength;        /* [m] (633e-9)                                    */
+  double scale;             /* scaleFactor                                     */
+  double chi3, alpha;       /* xi3 and its instantaneous fraction              */
+  double w_nl, gamma_nl;    /* wNL [rad/s], dnuNL [1/s]                         */
+} fdtd_graphene_nk_desc;
+
 enum { FDTD_RAMAN_EXACT = 0, FDTD_RAMAN_CENTRAL = 1 };
 typedef struct fdtd_graphene_cp_desc {
   double eps_inf;                 /* graphene_epinf                          */
@@ -303,6 +324,9 @@ int fdtd_add_lorentz(fdtd_job *job, const fdtd_region *region,
  * update of all three components is built. */
 int fdtd_add_conductive(fdtd_job *job, const fdtd_region *region, double eps_inf,
                         double sigma, int32_t *material_id);
+/* graphene633%initialize_material (1D/graphene633_mod.f90:48-105). */
+int fdtd_add_graphene_nk(fdtd_job *job, const fdtd_region *region,
+                         const fdtd_graphene_nk_desc *params, int32_t *material_id);
 /* Graphene%initialize_material (3D/graphene_mod.f90:107-283,
  * 2D/graphene_mod.f90:94-236, 1D/graphene_mod.f90:73-183). */
 int fdtd_add_graphene_cp(fdtd_job *job, const fdtd_region *region,

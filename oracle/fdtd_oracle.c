@@ -299,6 +299,32 @@ int ora_add_conductive(ora_job *J, const fdtd_region *r, double eps_inf, double 
   return id;
 }
 
+/* graphene633 (M1/graphene633_mod.f90:26-105), literally: the graphene
+ * update below with no Drude memory (g_ha = 0), g_ga = ep_inf + sigma dt/ep0,
+ * g_hb = sigma dt/ep0, kerr = xi3 alpha, and the module's Raman coefficients
+ * (:101-103), damped by dnuNL itself; every component takes it. */
+int ora_add_graphene_nk(ora_job *J, const fdtd_region *r, const fdtd_graphene_nk_desc *p) {
+  if (!(p->wavelength > 0) || !(p->scale >= 0)) FAIL("graphene_nk needs wavelength > 0 and scale >= 0");
+  omat *M; int id = add_material(J, r, &M); if (id < 0) return id;
+  M->kind = MAT_GRAPHENE;
+  M->normal = -1;
+  double dt = J->g.dt;
+  double sigma = sqrt(p->scale) * 4.0 * K_PI * p->n * p->k * K_C0 * K_EP0 / p->wavelength;
+  double ep_inf = p->scale * ((p->n * p->n) - (p->k * p->k));
+  M->g_ha = 0.0;
+  M->g_hb = sigma * dt / K_EP0;
+  M->g_ga = ep_inf + sigma * dt / K_EP0;
+  M->kerr = p->chi3 * p->alpha;
+  if (p->chi3 != 0.0) {
+    double betaR = sqrt((p->w_nl * p->w_nl) - (p->gamma_nl * p->gamma_nl));
+    double omegaR = (p->w_nl * p->w_nl) / betaR;
+    M->r0 = (1.0 - p->alpha) * p->chi3 * omegaR * dt * exp(-p->gamma_nl * dt) * sin(betaR * dt);
+    M->r1 = 2.0 * exp(-p->gamma_nl * dt) * cos(betaR * dt);
+    M->r2 = -exp(-2.0 * p->gamma_nl * dt);
+  }
+  return id;
+}
+
 /* Graphene sheet: intraband Drude surface conductivity as an ADE of the
  * Drude form of the gold model (M3/gold_mod.f90:50-88 with no critical
  * points), the Raman recursion of M3/graphene_mod.f90:202-262 in the

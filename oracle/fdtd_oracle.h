@@ -33,6 +33,7 @@ int ora_add_graphene(ora_job *job, const fdtd_region *region, const fdtd_graphen
 int ora_add_lorentz(ora_job *job, const fdtd_region *region, const fdtd_lorentz_desc *p);
 int ora_add_graphene_cp(ora_job *job, const fdtd_region *region, const fdtd_graphene_cp_desc *p);
 int ora_add_conductive(ora_job *job, const fdtd_region *region, double eps_inf, double sigma);
+int ora_add_graphene_nk(ora_job *job, const fdtd_region *region, const fdtd_graphene_nk_desc *p);
 int ora_add_pml(ora_job *job, const fdtd_pml_desc *pml);
 int ora_add_tfsf_1d(ora_job *job, const fdtd_tfsf1d_desc *tfsf);
 int ora_add_tfsf(ora_job *job, const fdtd_tfsf_desc *tfsf);

@@ -34,7 +34,8 @@ def lib():
         for name in ("ora_add_dielectric",):
             getattr(L, name).argtypes = [vp, vp, C.c_double]
         L.ora_add_conductive.argtypes = [vp, vp, C.c_double, C.c_double]
-        for name in ("ora_add_gold", "ora_add_graphene", "ora_add_lorentz", "ora_add_graphene_cp", "ora_add_pml", "ora_add_tfsf_1d", "ora_add_tfsf",
+        for name in ("ora_add_gold", "ora_add_graphene", "ora_add_lorentz", "ora_add_graphene_cp", "ora_add_graphene_nk",
+                     "ora_add_pml", "ora_add_tfsf_1d", "ora_add_tfsf",
                      "ora_add_source", "ora_add_monitor", "ora_add_probe"):
             getattr(L, name).argtypes = [vp, vp] if name in ("ora_add_pml", "ora_add_tfsf_1d", "ora_add_tfsf", "ora_add_source",
                                                               "ora_add_monitor", "ora_add_probe") else [vp, vp, vp]
@@ -72,6 +73,9 @@ class OracleJob:
             elif m.kind == "lorentz":
                 p = S.lorentz_struct(m.params)
                 rc = L.ora_add_lorentz(self.h, C.byref(r), C.byref(p))
+            elif m.kind == "graphene_nk":
+                p = S.graphene_nk_struct(m.params)
+                rc = L.ora_add_graphene_nk(self.h, C.byref(r), C.byref(p))
             elif m.kind == "conductive":
                 rc = L.ora_add_conductive(self.h, C.byref(r), m.params["eps_inf"], m.params["sigma"])
             elif m.kind == "graphene_cp":

@@ -684,7 +684,7 @@ def test_lorentz_sheet_variants_vs_oracle(gpu, oracle_lib, prec, case):
 
 
 @pytest.mark.parametrize("prec", [abi.F64, abi.F32])
-@pytest.mark.parametrize("name", ["gold", "gold_jp", "si_s", "graphene_cp", "conductive"])
+@pytest.mark.parametrize("name", ["gold", "gold_jp", "si_s", "graphene_cp", "conductive", "graphene_633"])
 def test_cell_response_vs_oracle(gpu, oracle_lib, prec, name):
     """Each dispersive update on its own (problems.config_cell: a uniformly
     driven periodic 8 x 8 grid, so curl H = 0): the GPU's E(n) series against
@@ -692,7 +692,8 @@ def test_cell_response_vs_oracle(gpu, oracle_lib, prec, name):
     params = {"gold": ("gold", problems.GOLD_CONFIG), "gold_jp": ("lorentz", problems.GOLD_JP),
               "si_s": ("lorentz", problems.SI_S),
               "graphene_cp": ("graphene_cp", dict(problems.GRAPHENE_4CP, normal_axis=-1)),
-              "conductive": ("conductive", dict(problems.SI_L800, sigma=2e5))}[name]
+              "conductive": ("conductive", dict(problems.SI_L800, sigma=2e5)),
+              "graphene_633": ("graphene_nk", problems.GRAPHENE_633)}[name]
     spec, meta = problems.config_cell(*params, precision=prec, steps=20000)
     J = gpu.Job(spec)
     O = oracle_lib.OracleJob(spec.with_precision(abi.F64))
@@ -821,3 +822,42 @@ def test_allocation_failures_are_reported_and_recovered(gpu):
     finally:
         gpu.fail_alloc_after(-1)
     assert failed_setup >= 10 and failed_step >= 2
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+@pytest.mark.parametrize("case", ["1d", "2d_te", "3d"])
+def test_graphene_nk_vs_oracle(gpu, oracle_lib, prec, case):
+    """The reference's 1D graphene at 633 nm (graphene633), Kerr and Raman on:
+    a 10-cell layer of the 1D line; a 3-row layer across the 2D TE cylinder
+    workload; the graphene column of the 3D configuration (fields in V/m)."""
+    from fdtd_gpu.spec import Material, box
+    raman = dict(alpha=0.7, w_nl=2 * np.pi * 47.4e12, gamma_nl=1e12)
+    if case == "1d":
+        spec, meta = problems.config_1d_slab(dict(problems.GRAPHENE_633, chi3=1.0, **raman), thickness=10,
+                                             precision=prec)
+        steps, nmon, comps = meta["Nt"], 3, (abi.EX, abi.HZ)
+    elif case == "2d_te":
+        spec, _ = problems.config_2d_tmz(precision=prec, n=384, ncyl=4, nfreq=16)
+        spec = problems.as_te(spec)
+        spec.add_graphene_nk(box((40, 150, 0), (343, 152, 0)), dict(problems.GRAPHENE_633, chi3=1e-2, **raman))
+        steps, nmon, comps = 2500, 3, (abi.EX, abi.EY, abi.HZ)
+    else:
+        spec, _ = problems.config_3d_graphene(precision=prec, nxy=8, nz=384, nfreq=32)
+        mat = dict(problems.GRAPHENE_633, scale=0.17, chi3=1e-18, **raman)
+        spec.materials = [Material("graphene_nk", m.region, params=dict(mat)) if m.kind == "graphene" else m
+                          for m in spec.materials]
+        steps, nmon, comps = 3000, 1, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    # the state is compared mid-run: afterwards the conducting layer keeps a
+    # static charge, and the oracle's (D - I) carries rounding of ~1e-16 |D|
+    # far above the small E left (as in test_conductive_vs_oracle)
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    mid = 3000 if case == "1d" else steps // 2
+    J.step(1, mid)
+    O.step(1, mid)
+    if prec == abi.F64:
+        check_state(J, O, comps)
+    J.step(mid + 1, steps - mid)
+    O.step(mid + 1, steps - mid)
+    err = _dft_err(J, O, nmon)
+    assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)

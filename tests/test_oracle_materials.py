@@ -345,6 +345,10 @@ def _damped(p):
 
 
 _GCP = dict(problems.GRAPHENE_4CP, normal_axis=-1)
+_G633 = problems.GRAPHENE_633
+_G633_LIN = dict(eps_inf=_G633["scale"] * (_G633["n"] ** 2 - _G633["k"] ** 2),
+                 sigma=np.sqrt(_G633["scale"]) * 4.0 * np.pi * _G633["n"] * _G633["k"] * problems.C0 * problems.EP0
+                 / _G633["wavelength"])
 _COND = dict(problems.SI_L800, sigma=2e5)
 CELL_CASES = {
     # name: (kind, params, discrete eps(dt, w), continuous eps(w), tolerance against the continuous one)
@@ -365,6 +369,10 @@ CELL_CASES = {
                     lambda w: problems.graphene_cp_eps(_GCP, 1e-9, w), 1.5e-2),
     "conductive": ("conductive", _COND, lambda dt, w: _eps_conductive(_COND, dt, w),
                    lambda w: problems.conductive_eps(_COND, w), 2e-3),
+    # the conduction term's O(dt) offset: ga carries sigma dt/eps0 of which a
+    # centred update would hold half (here ~0.018 in eps ~ 7-12)
+    "graphene_633": ("graphene_nk", _G633, lambda dt, w: _eps_conductive(_G633_LIN, dt, w),
+                     lambda w: problems.graphene_nk_eps(_G633, w), 3e-3),
 }
 
 
@@ -382,3 +390,25 @@ def test_cell_permittivity_known_answer(oracle_lib, name):
     assert np.max(np.abs(eps - exact) / np.abs(exact)) <= 1e-7
     cont = continuous(w)
     assert np.max(np.abs(eps - cont) / np.abs(cont)) <= tol
+
+
+def test_graphene_633_kerr_and_raman_linear_in_chi3(oracle_lib):
+    """graphene633's Kerr (alpha) and Raman (1 - alpha) parts on a one-cell
+    layer of the 1D line: the change of the spectra is linear in chi3, and
+    the instantaneous and delayed parts both act."""
+    res = {}
+    for alpha in (0.0, 1.0):
+        for chi3 in (0.0, 1.0, 2.0):  # changes of ~1e-5 (Raman) and ~5e-4 (Kerr): linear
+            mat = dict(problems.GRAPHENE_633, chi3=chi3, alpha=alpha, w_nl=2 * np.pi * 47.4e12, gamma_nl=1e12)
+            spec, _ = problems.config_1d_slab(mat, thickness=1, steps=8000)
+            O = oracle_lib.OracleJob(spec)
+            O.step(1, 8000)
+            res[(alpha, chi3)] = np.concatenate([np.concatenate([a.ravel(), b.ravel()])
+                                                 for a, b in (O.get_monitor(q) for q in range(3))])
+            O.close()
+    for alpha in (0.0, 1.0):
+        d1 = res[(alpha, 1.0)] - res[(alpha, 0.0)]
+        d2 = res[(alpha, 2.0)] - res[(alpha, 0.0)]
+        assert np.linalg.norm(d1) > 1e-10 * np.linalg.norm(res[(alpha, 0.0)])
+        assert abs(np.linalg.norm(d2) / np.linalg.norm(d1) - 2.0) < 1e-3
+    assert rel_l2(res[(1.0, 1.0)] - res[(1.0, 0.0)], res[(0.0, 1.0)] - res[(0.0, 0.0)]) > 0.1
