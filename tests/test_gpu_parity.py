@@ -861,3 +861,16 @@ def test_graphene_nk_vs_oracle(gpu, oracle_lib, prec, case):
     O.step(mid + 1, steps - mid)
     err = _dft_err(J, O, nmon)
     assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)
+
+
+def test_tma_core_only_where_the_core_box_lies_inside(gpu):
+    """Tile 7 (the TMA-staged E core) needs every neighbour of the core box
+    inside the grid: the laterally periodic graphene column refuses it at
+    commit, and its tuner picks among the other shapes."""
+    spec, _ = problems.config_3d_graphene(precision=abi.F32, nxy=8, nz=384, nfreq=8)
+    with pytest.raises(gpu.FdtdError) as e:
+        gpu.Job(spec, tile=7)
+    assert e.value.code == abi.FDTD_EINVAL
+    J = gpu.Job(spec)
+    assert J.tile() in range(1, 7)
+    J.close()
