@@ -465,7 +465,8 @@ int split_2d(fdtd_job *J, const std::vector<uint8_t> &rf) {
   J->cv0 = cv0;
   J->cw = cv1 - cv0;
   J->cy0 = ylo;
-  J->ncore = J->cw * (cy1 - ylo);
+  J->ch = cy1 - ylo;
+  J->ncore = J->cw * J->ch;
   std::vector<int> edge;
   edge.reserve((size_t)nvec * ny - (size_t)J->ncore + (size_t)nvec * 8);
   for (int j = 0; j < ny; ++j) {
@@ -1278,6 +1279,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     p.cv0 = J->cv0;
     p.cw = J->cw;
     p.cy0 = J->cy0;
+    p.ch = J->ch;
     p.ncore = J->ncore;
     p.tile = J->tile;
     p.nedge = J->nedge;

@@ -724,35 +724,6 @@ constexpr unsigned kTmaBytes = (unsigned)(kTmaHx + kTmaHy + kTmaHz) * 4u;  // by
 constexpr int kTmaSmem = 3 * kTmaStage * 4 + 128;           // dynamic shared bytes (+ alignment)
 static_assert((kTmaHx * 4) % 128 == 0 && (kTmaHy * 4) % 128 == 0 && (kTmaStage * 4) % 128 == 0,
               "TMA destinations are 128-byte aligned");
-constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait gives up
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-// bounded wait for the phase of the given parity to complete
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, unsigned parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(dst),
-      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
-      : "memory");
-}
-
 __global__ void __launch_bounds__(32 * kTmaY) e3d_core_tma(const __grid_constant__ StepParams<float> p,
                                                            const __grid_constant__ TmaMaps m) {
   extern __shared__ unsigned char sm_raw[];
