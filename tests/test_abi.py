@@ -40,15 +40,15 @@ def test_struct_sizes_match_header(built, tmp_path):
                    'sizeof(fdtd_grid_desc),sizeof(fdtd_region),sizeof(fdtd_drude2cp),'
                    'sizeof(fdtd_graphene_desc),sizeof(fdtd_pml_desc),sizeof(fdtd_source_desc),'
                    'sizeof(fdtd_monitor_desc),sizeof(fdtd_probe_desc),sizeof(fdtd_tfsf1d_desc),'
-                   'sizeof(fdtd_lorentz_desc));printf("%zu %zu\\n",sizeof(fdtd_tfsf_desc),'
-                   'sizeof(fdtd_graphene_cp_desc));return 0;}\n')
+                   'sizeof(fdtd_lorentz_desc));printf("%zu %zu %zu\\n",sizeof(fdtd_tfsf_desc),'
+                   'sizeof(fdtd_graphene_cp_desc),sizeof(fdtd_graphene_nk_desc));return 0;}\n')
     exe = tmp_path / "sz"
     import subprocess
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     got = [C.sizeof(t) for t in (abi.GridDesc, abi.Region, abi.Drude2CP, abi.GrapheneDesc, abi.PmlDesc,
                                  abi.SourceDesc, abi.MonitorDesc, abi.ProbeDesc, abi.Tfsf1dDesc, abi.LorentzDesc,
-                                 abi.TfsfDesc, abi.GrapheneCpDesc)]
+                                 abi.TfsfDesc, abi.GrapheneCpDesc, abi.GrapheneNkDesc)]
     assert [int(x) for x in out] == got
 
 
@@ -87,3 +87,24 @@ def test_bad_arguments_are_rejected(built):
     gp = spec_mod.graphene_cp_struct(dict(problems.GRAPHENE_4CP, chi3=1.0, w_nl=1e12, gamma_nl=4e12))
     assert L.fdtd_add_graphene_cp(None, None, C.byref(gp), None) == abi.FDTD_EINVAL
     assert "w_nl" in job.last_error()
+
+
+def test_new_entry_points_reject_bad_arguments(built):
+    """Checkpoint, health and graphene entry points answer a null job or bad
+    parameters with an error code, without a device."""
+    L = job.lib()
+    n = C.c_uint64()
+    assert L.fdtd_state_bytes(None, C.byref(n)) == abi.FDTD_EINVAL
+    buf = (C.c_uint8 * 64)()
+    assert L.fdtd_save_state(None, buf, 64) == abi.FDTD_EINVAL
+    assert L.fdtd_load_state(None, buf, 64) == abi.FDTD_EINVAL
+    cnt = C.c_int64()
+    assert L.fdtd_check_finite(None, C.byref(cnt)) == abi.FDTD_EINVAL
+    assert L.fdtd_debug_fail_alloc(-1) == abi.FDTD_OK
+    p = spec_mod.graphene_nk_struct(dict(problems.GRAPHENE_633, wavelength=0.0))
+    assert L.fdtd_add_graphene_nk(None, None, C.byref(p), None) == abi.FDTD_EINVAL
+    assert "wavelength" in job.last_error()
+    p = spec_mod.graphene_nk_struct(dict(problems.GRAPHENE_633, chi3=1.0, w_nl=1e12, gamma_nl=2e12))
+    assert L.fdtd_add_graphene_nk(None, None, C.byref(p), None) == abi.FDTD_EINVAL
+    assert "Raman" in job.last_error()
+    assert L.fdtd_add_conductive(None, None, 1.0, -1.0, None) == abi.FDTD_EINVAL
