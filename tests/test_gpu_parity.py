@@ -874,3 +874,27 @@ def test_tma_core_only_where_the_core_box_lies_inside(gpu):
     J = gpu.Job(spec)
     assert J.tile() in range(1, 7)
     J.close()
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+def test_odd_grid_with_several_dispersive_kinds_vs_oracle(gpu, oracle_lib, prec):
+    """A 203 x 203 TE grid (one cell per vector in both precisions) holding
+    Lorentz-Jp gold cylinders, a 4-critical-point graphene sheet and a
+    conductive block at once: the core and edge kernels' one-cell path beside
+    three kinds of dispersive update in one launch."""
+    from fdtd_gpu.spec import box
+    spec, _ = problems.config_2d_tmz(precision=prec, n=203, ncyl=4, nfreq=8, npml=16)
+    spec = problems.as_te(problems.swap_gold(spec, problems.GOLD_JP))
+    spec.add_graphene_cp(box((20, 120, 0), (182, 120, 0)), dict(problems.GRAPHENE_4CP, chi3=1e-2, w_nl=2 * np.pi * 47.4e12,
+                                                                gamma_nl=1e12))
+    spec.add_conductive(box((60, 150, 0), (90, 160, 0)), dict(problems.SI_L800, sigma=2e5))
+    J = gpu.Job(spec)
+    O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+    J.step(1, 700)
+    O.step(1, 700)
+    if prec == abi.F64:
+        check_state(J, O, (abi.EX, abi.EY, abi.HZ))
+    J.step(701, 800)
+    O.step(701, 800)
+    err = _dft_err(J, O, len(spec.monitors))
+    assert err <= (TOL64 if prec == abi.F64 else TOL32_DFT)
