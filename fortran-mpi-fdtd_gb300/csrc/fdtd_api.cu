@@ -6,6 +6,15 @@
 // reference's formulas and operation order) and then only launches kernels.
 // There is no CPU compute path: without an sm_103 device every call that
 // needs one fails with FDTD_ENODEV.
+//
+// Sections, in order: the job record and its device allocations (state
+// buffers registered for checkpoints); PML coefficient tables; commit
+// (material painting, dispersive coefficients and slots, PML, rows, the core
+// and edge split, the uniformity bitmap, sampling tables, the tensor maps of
+// the TMA-staged core, the block-shape tuner); stepping (the parts of a half
+// step, their streams and programmatic dependencies, the DFT ring, CUDA-graph
+// replay, the 1D line); packs of small 2D jobs; the C entry points, with the
+// health checks and the checkpoint after the getters.
 #include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
