@@ -1227,6 +1227,12 @@ int setup_tma(fdtd_job *J) {
   };
   if (!make(&J->tma.hx, J->F[3], 128, 9) || !make(&J->tma.hy, J->F[4], 132, 8) || !make(&J->tma.hz, J->F[5], 132, 9))
     return FDTD_OK;  // not offered
+  // the H core reads the cells right of, above and beyond the core box: it
+  // also needs the box to end at least one cell before the grid's far side
+  J->tma.h_ok = 0;
+  if ((J->cv0 + J->cw) * 4 <= J->nx - 1 && J->cy0 + J->ch <= J->ny - 1 && J->cz0 + J->cd <= J->nz - 1 &&
+      make(&J->tma.ex, J->F[0], 128, 9) && make(&J->tma.ey, J->F[1], 132, 8) && make(&J->tma.ez, J->F[2], 132, 9))
+    J->tma.h_ok = 1;
   int rc;
   if (!J->d_err && (rc = alloc_dev(J, (void **)&J->d_err, sizeof(int)))) return rc;
   J->tma_ok = true;
@@ -1549,8 +1555,8 @@ int tune_tiles(fdtd_job *J) {
   if (J->dim < 2 || J->ncore <= 0) return FDTD_OK;
   if (J->tile_req > 0) {
     J->tile = J->tile_req - 1;
-    if (J->tile == 6 && !J->tma_ok)
-      return set_err(FDTD_EINVAL, "tile 7 (the TMA core) needs FP32, 4-cell vectors and a core box inside the grid");
+    if ((J->tile == 6 && !J->tma_ok) || (J->tile == 7 && !(J->tma_ok && J->tma.h_ok)))
+      return set_err(FDTD_EINVAL, "tiles 7 and 8 (the TMA cores) need FP32, 4-cell vectors and a core box inside the grid");
     return FDTD_OK;
   }
   const char *off = getenv("FDTD_TUNE");
@@ -1578,8 +1584,8 @@ int tune_tiles(fdtd_job *J) {
   CK(cudaEventCreate(&b));
   float best = 3.0e38f;
   int choice = 1;
-  // 3D: also the z-marching kernels and, where set up, the TMA-staged E core
-  const int nshapes = J->dim == 3 ? (J->tma_ok ? 7 : 6) : 3;
+  // 3D: also the z-marching kernels and, where set up, the TMA-staged cores
+  const int nshapes = J->dim == 3 ? (J->tma_ok ? (J->tma.h_ok ? 8 : 7) : 6) : 3;
   for (int c = 0; c < nshapes; ++c) {
     p.tile = c;
     for (int w = 0; w < 2; ++w) {
@@ -2832,7 +2838,7 @@ int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
 int fdtd_set_tile(fdtd_job *J, int32_t tile) {
   int rc = check_job(J, false);
   if (rc) return rc;
-  const int maxt = J->dim == 3 ? 7 : 3;
+  const int maxt = J->dim == 3 ? 8 : 3;
   if (tile < 0 || tile > maxt) return set_err(FDTD_EINVAL, "tile must be 0 (tune) or 1..%d", maxt);
   J->tile_req = tile;
   return FDTD_OK;

@@ -30,6 +30,10 @@ namespace fdtd {
 // Hz 132 x 9 from (x0-4, y0-1)
 struct TmaMaps {
   CUtensorMap hx, hy, hz;
+  // the H core's E planes: Ex 128 x 9 rows from (x0, y0), Ey 132 x 8 and Ez
+  // 132 x 9 from (x0, y0) (the cell to the right, the row above); h_ok when set
+  CUtensorMap ex, ey, ez;
+  int h_ok;
 };
 
 constexpr int kMaxMat = 256;

@@ -838,6 +838,105 @@ __global__ void __launch_bounds__(32 * kTmaY) e3d_core_tma(const __grid_constant
   }
 }
 
+// The TMA-staged H core: the same tiles march up the core box, each plane's
+// Ex (with the row above), Ey (with the cell to the right) and Ez (with both)
+// copied into the 3-stage ring; the plane above is the next round's plane.
+// The arithmetic is h3d_core's, term for term.  It runs only where the core
+// box ends at least one cell before the far side of the grid on every axis.
+__global__ void __launch_bounds__(32 * kTmaY) h3d_core_tma(const __grid_constant__ StepParams<float> p,
+                                                           const __grid_constant__ TmaMaps m) {
+  extern __shared__ unsigned char sm_raw[];
+  __shared__ __align__(8) unsigned long long bar[3];
+  pdl_wait();
+  pdl_release();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int bx = (p.cw + 31) >> 5, by = (p.ch + kTmaY - 1) / kTmaY;
+  const int tx = blockIdx.x % bx, t2 = blockIdx.x / bx, ty = t2 % by, tz = t2 / by;
+  const int x0 = (p.cv0 + tx * 32) * 4, y0 = p.cy0 + ty * kTmaY;
+  const int kz0 = p.cz0 + tz * kTmaZ, kz1 = min(kz0 + kTmaZ, p.cz0 + p.cd);
+  const bool live = tx * 32 + lane < p.cw && ty * kTmaY + w < p.ch;
+  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(sm_raw);
+  const uint32_t sbase = (raw + 127u) & ~127u;
+  const float *gbase = (const float *)(sm_raw + (sbase - raw));
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(bar);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 3; ++s) mbar_init(bar0 + 8 * s, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // load number u is plane kz0 + u, in stage u % 3 (phase u / 3)
+  auto issue = [&](int u) {
+    const int s = u % 3, plane = kz0 + u;
+    const uint32_t st = sbase + (uint32_t)(s * kTmaStage * 4), b = bar0 + 8 * s;
+    mbar_expect_tx(b, kTmaBytes);
+    tma_load_3d(st, &m.ex, x0, y0, plane, b);
+    tma_load_3d(st + kTmaHx * 4, &m.ey, x0, y0, plane, b);
+    tma_load_3d(st + (kTmaHx + kTmaHy) * 4, &m.ez, x0, y0, plane, b);
+  };
+  const int nload = kz1 - kz0 + 1;  // the planes kz0 .. kz1 (the last one only as the plane above)
+  if (threadIdx.x == 0) {
+    issue(0);
+    issue(1);
+  }
+  int issued = 2, waited = 0;
+  bool ok = __syncthreads_and(mbar_wait(bar0, 0));
+  waited = 1;
+  const int j = y0 + w, xr = 4 * lane;
+  float hx[4] = {}, hy[4] = {}, hz[4] = {};
+  bool skip = true;
+  auto load_h = [&](int k) {
+    skip = !live || __ldg(p.rowflag + (long long)k * p.ny + j);
+    if (skip) return;
+    const long long c = ((long long)k * p.ny + j) * p.nx + x0 + xr;
+    vld<float, 4>(p.hx + c, hx);
+    vld<float, 4>(p.hy + c, hy);
+    vld<float, 4>(p.hz + c, hz);
+  };
+  load_h(kz0);
+  for (int k = kz0; ok && k < kz1; ++k) {
+    const int u = k - kz0;  // this plane's load number; u + 1 is the plane above
+    if (threadIdx.x == 0 && u + 2 < nload) issue(u + 2);  // into the stage of plane k - 1
+    if (u + 2 < nload) issued = u + 3;
+    ok = __syncthreads_and(mbar_wait(bar0 + 8 * ((u + 1) % 3), (unsigned)((u + 1) / 3) & 1u));
+    if (!ok) break;
+    waited = u + 2;
+    if (!skip) {
+      const float *Ex = gbase + (u % 3) * kTmaStage, *Ey = Ex + kTmaHx, *Ez = Ey + kTmaHy;
+      const float *Exa = gbase + ((u + 1) % 3) * kTmaStage, *Eya = Exa + kTmaHx;
+      const int yr = (kTmaX + 4) * w + xr, zr = (kTmaX + 4) * w + xr;
+      const float4 ex4 = *(const float4 *)(Ex + kTmaX * w + xr), exu4 = *(const float4 *)(Ex + kTmaX * (w + 1) + xr);
+      const float4 exa4 = *(const float4 *)(Exa + kTmaX * w + xr);
+      const float4 ey4 = *(const float4 *)(Ey + yr), eya4 = *(const float4 *)(Eya + yr);
+      const float4 ez4 = *(const float4 *)(Ez + zr), ezu4 = *(const float4 *)(Ez + zr + (kTmaX + 4));
+      const float eyr = Ey[yr + 4], ezr = Ez[zr + 4];
+      const float ex[4] = {ex4.x, ex4.y, ex4.z, ex4.w}, exu[4] = {exu4.x, exu4.y, exu4.z, exu4.w};
+      const float exa[4] = {exa4.x, exa4.y, exa4.z, exa4.w}, ey[4] = {ey4.x, ey4.y, ey4.z, ey4.w};
+      const float eya[4] = {eya4.x, eya4.y, eya4.z, eya4.w}, ez[4] = {ez4.x, ez4.y, ez4.z, ez4.w};
+      const float ezu[4] = {ezu4.x, ezu4.y, ezu4.z, ezu4.w};
+      const long long c = ((long long)k * p.ny + j) * p.nx + x0 + xr;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float rz = q < 3 ? ez[q + 1] : ezr, ry = q < 3 ? ey[q + 1] : eyr;
+        const float curleyz = eya[q] - ey[q], curlezy = -ezu[q] + ez[q];
+        const float curlezx = rz - ez[q], curlexz = -exa[q] + ex[q];
+        const float curlexy = exu[q] - ex[q], curleyx = -ry + ey[q];
+        hx[q] = hx[q] + p.ku * (curleyz + curlezy);
+        hy[q] = hy[q] + p.ku * (curlezx + curlexz);
+        hz[q] = hz[q] + p.ku * (curlexy + curleyx);
+      }
+      vst<float, 4>(p.hx + c, hx);
+      vst<float, 4>(p.hy + c, hy);
+      vst<float, 4>(p.hz + c, hz);
+    }
+    if (k + 1 < kz1) load_h(k + 1);
+    __syncthreads();
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(p.err, 1);
+    for (int u = waited; u < issued; ++u) mbar_wait(bar0 + 8 * (u % 3), (unsigned)(u / 3) & 1u);
+  }
+}
+
 constexpr int kCoreZ = 8;  // planes per thread of the z-marching kernels
 
 template <typename T, int V, int RY>
@@ -856,7 +955,7 @@ void launch_core3(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent
 
 // the TMA-staged E core: one block per tile of kTmaX x kTmaY cells and
 // kTmaZ planes, kTmaSmem bytes of dynamic shared memory
-inline void launch_core3_tma(const StepParams<float> &p, cudaStream_t s, cudaEvent_t ev) {
+inline void launch_core3_tma(const StepParams<float> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
   const int blocks = ((p.cw + 31) / 32) * ((p.ch + kTmaY - 1) / kTmaY) * ((p.cd + kTmaZ - 1) / kTmaZ);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
@@ -876,18 +975,18 @@ inline void launch_core3_tma(const StepParams<float> &p, cudaStream_t s, cudaEve
   }
   cfg.attrs = at;
   cfg.numAttrs = na;
-  cudaLaunchKernelEx(&cfg, e3d_core_tma, p, *p.tma);
+  cudaLaunchKernelEx(&cfg, e_half ? e3d_core_tma : h3d_core_tma, p, *p.tma);
 }
 
 // tile 0: 4 rows of 32 x-vectors, 1: 8 rows, 2: 16 rows, one plane per
 // thread; tiles 3, 4, 5: the same shapes marching kCoreZ planes per thread;
 // tile 6 (FP32 with 4-cell vectors, where the host set up the tensor maps):
-// the TMA-staged E core, with tile 1's H core
+// the TMA-staged E core, with tile 1's H core; tile 7: both TMA-staged cores
 template <typename T, int V>
 void launch_core3_v(const StepParams<T> &p, bool e_half, cudaStream_t s, cudaEvent_t ev) {
   if constexpr (sizeof(T) == 4 && V == 4) {
-    if (p.tile == 6 && p.tma) {
-      if (e_half) launch_core3_tma(p, s, ev);
+    if ((p.tile == 6 || p.tile == 7) && p.tma) {
+      if (e_half || (p.tile == 7 && p.tma->h_ok)) launch_core3_tma(p, e_half, s, ev);
       else launch_core3<T, V, 8>(p, false, s, ev);
       return;
     }

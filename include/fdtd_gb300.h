@@ -442,9 +442,10 @@ int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms)
  * the same shapes with each thread walking 8 planes and keeping the
  * neighbour plane in registers.  FP32 with 4-cell vectors, where the core
  * box lies at least one cell inside the grid, adds 3D 7: the TMA-staged E
- * core (tiled bulk copies into shared memory); pinning it elsewhere fails at
- * commit with FDTD_EINVAL.  Results do not depend on the shape.  Environment
- * FDTD_NO_TMA leaves the TMA-staged kernel out.
+ * core (tiled bulk copies into shared memory), and 8: both TMA-staged cores;
+ * pinning one elsewhere fails at commit with FDTD_EINVAL.  Results do not
+ * depend on the shape.  Environment FDTD_NO_TMA leaves the TMA-staged
+ * kernels out.
  * fdtd_get_tile returns the shape in use (0: the job has no core kernels). */
 int fdtd_set_tile(fdtd_job *job, int32_t tile);
 int fdtd_get_tile(const fdtd_job *job, int32_t *tile);

@@ -279,7 +279,8 @@ def test_core_block_shapes_give_identical_results(gpu, dim):
         comps, steps = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ), 200
     ref = None
     # 3D 4..6: z-marching kernels; 7: the TMA-staged E core (FP32, core box inside the grid)
-    for tile in ((1, 2, 3) if dim == 2 else (1, 2, 3, 4, 5, 6, 7)):
+    # 3D 8: the TMA-staged E and H cores
+    for tile in ((1, 2, 3) if dim == 2 else (1, 2, 3, 4, 5, 6, 7, 8)):
         J = gpu.Job(spec, tile=tile)
         assert J.tile() == tile
         J.step(1, steps)
@@ -292,7 +293,7 @@ def test_core_block_shapes_give_identical_results(gpu, dim):
                 np.testing.assert_array_equal(a, b)
         J.close()
     J = gpu.Job(spec)
-    assert J.tile() in ((1, 2, 3) if dim == 2 else range(1, 8))
+    assert J.tile() in ((1, 2, 3) if dim == 2 else range(1, 9))
     J.close()
 
 
