@@ -1566,8 +1566,9 @@ int tune_tiles(fdtd_job *J) {
   }
   int lg = 0;
   for (long long c = J->ncore; c > 1; c >>= 1) ++lg;
-  const long long key = (((((long long)J->dim * 8 + J->g.layout) * 4 + J->g.precision) * 8 + J->vec) * 64 + lg) * 2 +
-                        (J->tma_ok ? 1 : 0);
+  // which TMA-staged kernels the grid can take is part of the kind of grid
+  const long long key = (((((long long)J->dim * 8 + J->g.layout) * 4 + J->g.precision) * 8 + J->vec) * 64 + lg) * 4 +
+                        (J->tma_ok ? 2 : 0) + (J->tma_ok && J->tma.h_ok ? 1 : 0);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
