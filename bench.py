@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--nt", type=int, default=10000, help="time steps per job")
     ap.add_argument("--n", type=int, default=2048, help="grid cells per side")
     ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-child", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-threads", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the 3D, graphene and 1D runs")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs in the serving run (0: none)")
@@ -170,17 +171,32 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def dft_rel_err(ja, jb, nmon):
+    """Relative L2 distance of job a's monitor sums from job b's, over all
+    monitors together."""
+    import numpy as np
+    num = den = 0.0
+    for q in range(nmon):
+        ra, ia = ja.get_monitor(q)
+        rb, ib = jb.get_monitor(q)
+        num += float(np.sum((ra - rb) ** 2) + np.sum((ia - ib) ** 2))
+        den += float(np.sum(rb ** 2) + np.sum(ib ** 2))
+    return math.sqrt(num / den) if den > 0 else float("nan")
+
+
 def config_runs(stream):
-    """The other named configurations, each timed over a short run after a
-    warm-up (CUDA events on the bench stream): Mcell-updates/s and the step's
-    ideal bytes (each field read and written once, plus the material id:
-    12w+1 per cell in 3D, 4w+1 in 1D) over the measured HBM peak."""
+    """The other named configurations.  The 3D ones run their whole length
+    in FP32 and in FP64 plain (timed with CUDA events on the bench stream
+    after a short warm-up), so that the FP32 spectra can be compared with the
+    FP64 ones of the same run: Mcell-updates/s, the FP32 DFT error, and the
+    step's ideal bytes (each field read and written once, plus the material
+    id: 12w+1 per cell in 3D, 4w+1 in 1D) over the measured HBM peak."""
     import torch
     from fdtd_gpu import abi, problems
     from fdtd_gpu.job import Job
     peak, _ = measured_peaks()
 
-    def timed(spec, warm, k, per_cell):
+    def timed(spec, warm, k, per_cell, keep=False):
         J = Job(spec)
         J.set_stream(stream.cuda_stream)
         J.step(1, warm)
@@ -192,20 +208,28 @@ def config_runs(stream):
         b.record(stream)
         torch.cuda.synchronize()
         ms = a.elapsed_time(b)
-        J.close()
         mc = spec.cells() * k / (ms / 1e3) / 1e6
         w = 4 if spec.precision == abi.F32 else 8
-        return {"mcell_updates_per_s": mc, "ms_per_step": ms / k, "timed_steps": k,
-                "step_bytes_frac_of_hbm": mc * 1e6 * per_cell(w) / (peak * 1e9)}
+        r = {"mcell_updates_per_s": mc, "ms_per_step": ms / k, "timed_steps": k, "tile": J.tile(),
+             "step_bytes_frac_of_hbm": mc * 1e6 * per_cell(w) / (peak * 1e9)}
+        if keep:
+            return r, J
+        J.close()
+        return r
 
     out = {}
-    s32, _ = problems.config_3d_sphere(precision=abi.F32)
-    s64, _ = problems.config_3d_sphere(precision=abi.F64)
-    r32, r64 = timed(s32, 64, 256, lambda w: 12 * w + 1), timed(s64, 32, 96, lambda w: 12 * w + 1)
-    out["3d_sphere_512^3_splitpml16_64freq"] = {"fp32": r32, "fp64_plain": r64,
-                                               "fp32_over_fp64": r32["mcell_updates_per_s"] / r64["mcell_updates_per_s"]}
-    g32, _ = problems.config_3d_graphene(precision=abi.F32)
-    out["3d_graphene_256x256x384_pmlz10_128freq"] = {"fp32": timed(g32, 64, 512, lambda w: 12 * w + 1)}
+    for name, make, nmon in (("3d_sphere_512^3_splitpml16_64freq", problems.config_3d_sphere, 6),
+                             ("3d_graphene_256x256x384_pmlz10_128freq", problems.config_3d_graphene, 1)):
+        s32, meta = make(precision=abi.F32)
+        s64, _ = make(precision=abi.F64)
+        nt, warm = meta["Nt"], 64
+        r32, j32 = timed(s32, warm, nt - warm, lambda w: 12 * w + 1, keep=True)
+        r64, j64 = timed(s64, warm, nt - warm, lambda w: 12 * w + 1, keep=True)
+        out[name] = {"fp32": r32, "fp64_plain": r64, "time_steps": nt,
+                     "fp32_over_fp64": r32["mcell_updates_per_s"] / r64["mcell_updates_per_s"],
+                     "dft_rel_err_fp32_vs_fp64": dft_rel_err(j32, j64, nmon)}
+        j32.close()
+        j64.close()
     o32, _ = problems.config_1d_gold(precision=abi.F32)
     o64, _ = problems.config_1d_gold(precision=abi.F64)
     l32, l64 = timed(o32, 2000, 18000, lambda w: 4 * w + 1), timed(o64, 2000, 18000, lambda w: 4 * w + 1)
@@ -256,62 +280,76 @@ def serving_run(njobs, rate):
     }
 
 
-def cpu_baseline(n, seconds, nthreads=None):
-    """The FP64 oracle (reference algorithm on the CPU) on the host cores over a
-    bounded sample of the same workload: chunks of time steps until `seconds`."""
+CPU_SAMPLE_STEPS = 200  # time steps of the workload in one timed CPU sample
+
+
+def cpu_child(args):
+    """Child process of cpu_measure: the FP64 oracle on the host cores, the
+    OpenMP threads pinned (OMP_PROC_BIND=close, OMP_PLACES=cores, set by the
+    parent before the runtime starts).  Memory is first touched and the
+    thread team started by a few untimed steps; then `warm` untimed and `k`
+    timed samples of CPU_SAMPLE_STEPS steps each, from one running state.
+    Prints one JSON line: the sample times."""
     from fdtd_gpu import abi
     from oracle.pyoracle import OracleJob, build
     build()
-    nth = nthreads or os.cpu_count() or 1
-    spec, meta = workload(n, 10000, abi.F64)
-    O = OracleJob(spec, nthreads=nth)
-    O.step(1, 4)  # touch memory
-    done, t0 = 0, time.perf_counter()
-    while True:
-        O.step(5 + done, 10)
-        done += 10
-        el = time.perf_counter() - t0
-        if el >= seconds or done >= 2000:
-            break
-    value = spec.cells() * done / el / 1e6
+    spec, _ = workload(args.n, 10000, abi.F64)
+    O = OracleJob(spec, nthreads=args.cpu_threads)
+    n = 1
+    O.step(n, 4)
+    n += 4
+    times = []
+    for r in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.step(n, CPU_SAMPLE_STEPS)
+        dt = time.perf_counter() - t0
+        n += CPU_SAMPLE_STEPS
+        if r >= args.warmup:
+            times.append(dt)
+    print(json.dumps({"times": times, "cells": spec.cells()}), flush=True)
+    return 0
+
+
+def cpu_measure(n, warm, k):
+    """The CPU baseline, the same measurement for the GPU line's
+    cpu_baseline and for the reference arm: the FP64 oracle (the reference's
+    algorithm restated in C; the Fortran/MPI reference cannot be built
+    without gfortran and MPI) on all host cores with pinned threads, the
+    median of k samples of CPU_SAMPLE_STEPS time steps of the n x n workload
+    after `warm` untimed ones.  Runs in a child process, so that the OpenMP
+    runtime starts with the pinning settings and without the GPU process's
+    threads."""
+    nth = os.cpu_count() or 1
+    env = dict(os.environ, OMP_PROC_BIND="close", OMP_PLACES="cores", OMP_NUM_THREADS=str(nth))
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-child", "--n", str(n), "--warmup", str(warm),
+           "--steps", str(k), "--cpu-threads", str(nth)]
+    out = subprocess.run(cmd, env=env, capture_output=True, text=True, check=True).stdout
+    d = json.loads(out.strip().splitlines()[-1])
+    med = statistics.median(d["times"])
+    value = d["cells"] * CPU_SAMPLE_STEPS / med / 1e6
+    spread = (max(d["times"]) - min(d["times"])) / med
     return {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-            "sample": f"FP64 oracle, {done} time steps of the {n}x{n} workload on {nth} host threads ({el:.1f} s)"}
+            "sample": f"FP64 oracle (the reference's algorithm in C; the Fortran/MPI reference needs gfortran and "
+                      f"MPI, absent on this box), median of {k} samples of {CPU_SAMPLE_STEPS} time steps of the "
+                      f"{n}x{n} workload after {warm} untimed, {nth} threads pinned "
+                      f"(OMP_PROC_BIND=close, OMP_PLACES=cores)",
+            "sample_seconds": d["times"], "spread": spread}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from fdtd_gpu import abi
-    from oracle.pyoracle import OracleJob, build
-    build()
-    nth = os.cpu_count() or 1
-    spec, meta = workload(args.n, 10000, abi.F64)
-    O = OracleJob(spec, nthreads=nth)
-    per_step = 20  # time steps of the workload per bench step (bounded sample)
-    n = 1
-    for _ in range(args.warmup):
-        O.step(n, per_step)
-        n += per_step
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        O.step(n, per_step)
-        times.append(time.perf_counter() - t0)
-        n += per_step
-    tot = sum(times)
-    value = spec.cells() * per_step * args.steps / tot / 1e6
+    cb = cpu_measure(args.n, args.warmup, args.steps)
+    value = cb["value"]
+    ms = 1e3 * statistics.median(cb["sample_seconds"])
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": workload_name(args.n, args.nt),
-                                            "note": f"each bench step = a sample of {per_step} time steps of "
-                                                    f"the workload, from a state already {args.warmup * per_step} "
-                                                    f"steps in"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-                             "sample": f"FP64 oracle (the reference's algorithm restated in C; the Fortran/MPI "
-                                       f"reference needs gfortran+MPI, absent on this box), {per_step} time steps "
-                                       f"per bench step on {nth} host threads"},
+                                            "note": f"each bench step = a sample of {CPU_SAMPLE_STEPS} time steps "
+                                                    f"of the workload (the median sample is reported)"},
+            "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -319,6 +357,8 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.cpu_child:
+        return cpu_child(args)
     if args.impl == "reference":
         return run_reference(args)
     import numpy as np
@@ -395,13 +435,7 @@ def main():
     value64 = aggregate_mcells(world, cells, args.nt, t64 / 1e3)
 
     # ---- DFT error FP32 vs FP64 (same job, same steps) ----
-    num = den = 0.0
-    for q in range(len(spec32.monitors)):
-        r32, i32 = jobs32[0].get_monitor(q)
-        r64, i64 = jobs64[0].get_monitor(q)
-        num += float(np.sum((r32 - r64) ** 2) + np.sum((i32 - i64) ** 2))
-        den += float(np.sum(r64 ** 2) + np.sum(i64 ** 2))
-    dft_err = math.sqrt(num / den) if den > 0 else float("nan")
+    dft_err = dft_rel_err(jobs32[0], jobs64[0], len(spec32.monitors))
 
     # ---- roofline of the dominant kernel (FP32) ----
     # the interior (core) E and H kernels update nearly all cells; the edge
@@ -464,7 +498,7 @@ def main():
     if rank == 0 and args.serve_jobs > 0:
         out["serving"] = serving_run(args.serve_jobs, args.serve_rate)
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)
+        out["cpu_baseline"] = cpu_measure(args.n, 1, 5)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

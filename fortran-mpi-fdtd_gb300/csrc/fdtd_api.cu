@@ -206,6 +206,7 @@ struct fdtd_job {
   TmaMaps tma{};
   bool tma_ok = false;
   int *d_err = nullptr;
+  unsigned wait_limit = kWaitLimit;  // polls of a TMA core's mbarrier wait (fdtd_debug_wait_limit)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_kernels = 0;
@@ -1244,6 +1245,7 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   memset(&p, 0, sizeof p);
   p.tma = J->tma_ok ? &J->tma : nullptr;
   p.err = J->d_err;
+  p.wait_limit = J->wait_limit;
   p.uni = J->d_uni;
   p.uni_words = J->uni_words;
   p.layout = J->g.layout;
@@ -2517,6 +2519,13 @@ int fdtd_check_finite(fdtd_job *J, int64_t *count) {
   return FDTD_OK;
 }
 
+int fdtd_debug_wait_limit(fdtd_job *J, int32_t rounds) {
+  if (!J) return set_err(FDTD_EINVAL, "null job");
+  J->wait_limit = rounds < 0 ? kWaitLimit : (unsigned)rounds;
+  destroy_graph(J);  // the captured launches hold the old limit
+  return FDTD_OK;
+}
+
 int fdtd_debug_fail_alloc(int32_t after) {
   g_fail_after.store(after < 0 ? -1 : (long long)after);
   return FDTD_OK;
@@ -2616,6 +2625,11 @@ int fdtd_load_state(fdtd_job *J, const void *buf, uint64_t bytes) {
               h.nprobe == J->probes.size();
   for (int a = 0; a < 3; ++a) same = same && h.n[a] == J->g.n[a];
   if (!same) return set_err(FDTD_EINVAL, "the checkpoint comes from a job of another layout, precision, size or set-up");
+  // the size table and the probe records must lie inside the buffer before
+  // they are read; the whole layout they describe must then fill it exactly
+  const uint64_t tables = sizeof h + J->state.size() * sizeof(uint64_t) + J->probes.size() * 2 * sizeof(int32_t);
+  if (bytes < tables) return set_err(FDTD_EINVAL, "checkpoint of %llu bytes is shorter than its tables",
+                                     (unsigned long long)bytes);
   const char *sz = in + sizeof h;
   for (size_t q = 0; q < J->state.size(); ++q) {
     uint64_t b;
@@ -2633,6 +2647,11 @@ int fdtd_load_state(fdtd_job *J, const void *buf, uint64_t bytes) {
     caps[q] = rc2[0];
     if (rc2[0] > 0) n_probe_max = std::max(n_probe_max, J->probes[q].d.n_first + rc2[0] - 1);
   }
+  uint64_t expect = tables;
+  for (auto &st : J->state) expect += st.bytes;
+  for (size_t q = 0; q < J->probes.size(); ++q) expect += (uint64_t)caps[q] * J->probes[q].ncomp * sizeof(double);
+  if (expect != bytes) return set_err(FDTD_EINVAL, "checkpoint of %llu bytes, its tables describe %llu",
+                                      (unsigned long long)bytes, (unsigned long long)expect);
   CK(cudaStreamSynchronize(J->stream));
   if (n_probe_max > 0 && (rc = ensure_probe_cap(J, n_probe_max))) return rc;
   const char *o = pr + J->probes.size() * 2 * sizeof(int32_t);

@@ -41,6 +41,7 @@ constexpr int kMaxSrc = 8;
 constexpr int kMaxMon = 16;
 constexpr int kMaxProbe = 16;
 constexpr int kStageSteps = 32;  // DFT staging ring length (steps per fold)
+constexpr unsigned kWaitLimit = 1u << 22;  // default try_wait rounds before an mbarrier wait gives up
 
 // MK_CONDUCTIVE and MK_GRAPHENE_NK exist on the host only: their cells run
 // the gold and the graphene update
@@ -183,6 +184,7 @@ struct StepParams {
   int tile;                // block shape of the core kernels (tuned; 3D 6: the TMA-staged E core)
   const struct TmaMaps *tma;  // host copy of the H planes' tensor maps, for the launcher (or null)
   int *err;                // device flag: a bounded wait of a kernel gave up (nonzero)
+  unsigned wait_limit;     // polls of an mbarrier before a main-loop wait gives up
   // sampling fused into the H kernel
   int gather;              // 1: tile threads write the stage row / probes
   int nmon;
@@ -279,6 +281,9 @@ struct DftParams {
   int total_work_blocks;
 };
 template <typename T> void launch_dft(const DftParams &d, const T *stage, void *stream);
+// load the DFT fold kernel on the current device now (cudaFuncGetAttributes)
+// rather than at its first launch; 0 on success
+template <typename T> int preload_dft();
 
 // 1D line: persistent single-block kernel running many steps
 template <typename T>

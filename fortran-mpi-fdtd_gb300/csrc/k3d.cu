@@ -761,8 +761,8 @@ __global__ void __launch_bounds__(32 * kTmaY) e3d_core_tma(const __grid_constant
     if (nload > 1) issue(1);
   }
   int issued = nload > 1 ? 2 : 1, waited = 0;
-  bool ok = __syncthreads_and(mbar_wait(bar0, 0));
-  waited = 1;
+  bool ok = __syncthreads_and(mbar_wait(bar0, 0, p.wait_limit));
+  waited = ok ? 1 : 0;  // a first wait that gave up leaves load 0 to the drain below
   // this thread's E, material ids and row flag of the first plane; later
   // planes' are loaded before the barrier that ends the previous plane, so
   // their latency overlaps the wait for the H copies
@@ -786,7 +786,7 @@ __global__ void __launch_bounds__(32 * kTmaY) e3d_core_tma(const __grid_constant
     // finished reading it before the barrier that ended the last round
     if (threadIdx.x == 0 && u + 1 < nload) issue(u + 1);
     if (u + 1 < nload) issued = u + 2;
-    ok = __syncthreads_and(mbar_wait(bar0 + 8 * (u % 3), (unsigned)(u / 3) & 1u));
+    ok = __syncthreads_and(mbar_wait(bar0 + 8 * (u % 3), (unsigned)(u / 3) & 1u, p.wait_limit));
     if (!ok) break;
     waited = u + 1;
     if (!skip) {
@@ -879,8 +879,8 @@ __global__ void __launch_bounds__(32 * kTmaY) h3d_core_tma(const __grid_constant
     issue(1);
   }
   int issued = 2, waited = 0;
-  bool ok = __syncthreads_and(mbar_wait(bar0, 0));
-  waited = 1;
+  bool ok = __syncthreads_and(mbar_wait(bar0, 0, p.wait_limit));
+  waited = ok ? 1 : 0;  // a first wait that gave up leaves load 0 to the drain below
   const int j = y0 + w, xr = 4 * lane;
   float hx[4] = {}, hy[4] = {}, hz[4] = {};
   bool skip = true;
@@ -897,7 +897,7 @@ __global__ void __launch_bounds__(32 * kTmaY) h3d_core_tma(const __grid_constant
     const int u = k - kz0;  // this plane's load number; u + 1 is the plane above
     if (threadIdx.x == 0 && u + 2 < nload) issue(u + 2);  // into the stage of plane k - 1
     if (u + 2 < nload) issued = u + 3;
-    ok = __syncthreads_and(mbar_wait(bar0 + 8 * ((u + 1) % 3), (unsigned)((u + 1) / 3) & 1u));
+    ok = __syncthreads_and(mbar_wait(bar0 + 8 * ((u + 1) % 3), (unsigned)((u + 1) / 3) & 1u, p.wait_limit));
     if (!ok) break;
     waited = u + 2;
     if (!skip) {

@@ -369,7 +369,6 @@ __device__ __forceinline__ void vec_ids(const StepParams<T> &p, long long row, i
 }
 
 // ---- mbarrier and tiled bulk copies (TMA) ------------------------------------
-constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait gives up
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
@@ -377,9 +376,10 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
-// bounded wait for the phase of the given parity to complete
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, unsigned parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it) {
+// bounded wait for the phase of the given parity to complete: at most
+// `limit` polls, then false
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, unsigned parity, unsigned limit = kWaitLimit) {
+  for (unsigned it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"

@@ -1,21 +1,23 @@
 // knoalloc.cu -- the running DFT of one box of a field for callers that
 // cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc while they run.  One kind records its
-// time loop into a CUDA graph by stream capture, where an allocation is not
-// allowed.  Another takes all of its device memory from its own pool and
-// forbids driver allocations, which synchronise the device and fragment the
-// pool.  fdtd_dft_sample_noalloc samples a box of such a caller's own field
-// array at step n and folds the samples into the caller's own FP64
-// accumulators, like a monitor of a job (fdtd_add_monitor) does, without
-// allocating anything.
+// Some callers cannot call cudaMalloc while they run.  One kind takes all of
+// its device memory from its own pool at start-up and forbids driver
+// allocations, which synchronise the device and fragment the pool; another
+// runs under a device-memory budget fixed before its time loop.
+// fdtd_dft_sample_noalloc samples a box of such a caller's own field array at
+// step n and folds the samples into the caller's own FP64 accumulators, like
+// a monitor of a job (fdtd_add_monitor) does, without allocating anything.
 //
 // The samples of the current ring of kStageSteps steps are staged in
 // g_noalloc_stage, a file-scope static device array of
 // FDTD_NOALLOC_STAGE_BYTES on every device that runs it.  On the host the
 // symbol is only a stand-in, so it is never handed to a kernel: the first
-// call on each device looks up its device address with cudaGetSymbolAddress,
-// with that device current, and caches it for later calls.
+// call on each device, with that device current, looks up its device address
+// with cudaGetSymbolAddress and caches it for later calls.  The same set-up
+// loads the two gather kernels and the FP64 DFT fold (cudaFuncGetAttributes),
+// which under lazy module loading would otherwise be loaded, and their code
+// placed in device memory, at their first launch.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -31,6 +33,7 @@ __device__ __align__(256) unsigned char g_noalloc_stage[FDTD_NOALLOC_STAGE_BYTES
 
 constexpr int kMaxDevices = 64;
 double *g_stage_dev[kMaxDevices] = {};
+int g_last_n[kMaxDevices] = {};  // step of the last sampled call per device (0: none)
 std::mutex g_stage_mu;
 
 // gather the box of the field (x fastest) into ring slot `slot`
@@ -53,6 +56,10 @@ int stage_address(double **out) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_stage);
     if (e != cudaSuccess || !p) return fdtd::report_error(FDTD_ECUDA, "cudaGetSymbolAddress of the stage ring failed");
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, noalloc_gather<float>) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, noalloc_gather<double>) != cudaSuccess || fdtd::preload_dft<double>() != 0)
+      return fdtd::report_error(FDTD_ECUDA, "loading the allocation-free DFT kernels failed");
     g_stage_dev[dev] = (double *)p;
   }
   *out = g_stage_dev[dev];
@@ -76,23 +83,28 @@ extern "C" int fdtd_dft_sample_noalloc(const void *field, int32_t precision, int
   for (int a = 0; a < 3; ++a) {
     if (lo[a] < 0 || hi[a] >= n3[a] || lo[a] > hi[a])
       return fdtd::report_error(FDTD_ERANGE, "fdtd_dft_sample_noalloc: box outside the field");
+    // checked after every factor: each is below 2^31 and the product so far
+    // at most the limit, so the product cannot overflow
     ncell *= hi[a] - lo[a] + 1;
+    if (ncell > FDTD_NOALLOC_MAX_CELLS)
+      return fdtd::report_error(FDTD_ERANGE, "fdtd_dft_sample_noalloc: box exceeds the stage ring's %d cells",
+                                (int)FDTD_NOALLOC_MAX_CELLS);
   }
-  if (ncell > FDTD_NOALLOC_MAX_CELLS)
-    return fdtd::report_error(FDTD_ERANGE,
-                              "fdtd_dft_sample_noalloc: box of %lld cells exceeds the stage ring's %d cells",
-                              ncell, (int)FDTD_NOALLOC_MAX_CELLS);
   if (n < n_first || n > n_last) return FDTD_OK;  // outside the window: nothing to sample
   double *stage = nullptr;
   int rc = stage_address(&stage);
   if (rc) return rc;
+  int dev = 0;
+  cudaGetDevice(&dev);  // succeeded in stage_address
   cudaStream_t s = (cudaStream_t)stream;
   const size_t row = (size_t)ncell * sizeof(double);
   // ring slot of step n: steps 1..32 fill slots 0..31, steps 33..64 again 0..31
   const int slot = (n - 1) % fdtd::kStageSteps;
-  // the first step of the window may start mid-ring: the slots before it are
-  // folded with the rest of the ring, so they must hold zeros
-  if (n == n_first && slot > 0 && cudaMemsetAsync(stage, 0, row * slot, s) != cudaSuccess)
+  // A sequence that starts mid-ring (at n_first, or later when a run resumes
+  // inside the window) folds the slots before its first step with the rest of
+  // the ring, and the array still holds an earlier sequence's samples there:
+  // those slots are cleared unless this call follows the previous one's step
+  if (slot > 0 && (n == n_first || g_last_n[dev] != n - 1) && cudaMemsetAsync(stage, 0, row * slot, s) != cudaSuccess)
     return fdtd::report_error(FDTD_ECUDA, "fdtd_dft_sample_noalloc: clearing the stage ring failed");
   const int wx = hi[0] - lo[0] + 1, wy = hi[1] - lo[1] + 1;
   const int threads = 256, blocks = (int)((ncell + threads - 1) / threads);
@@ -104,6 +116,7 @@ extern "C" int fdtd_dft_sample_noalloc(const void *field, int32_t precision, int
                                                      (int)ncell, stage, slot);
   if (cudaGetLastError() != cudaSuccess)
     return fdtd::report_error(FDTD_ECUDA, "fdtd_dft_sample_noalloc: gather launch failed");
+  g_last_n[dev] = n;
   if (slot == fdtd::kStageSteps - 1 || n == n_last || flush) {
     fdtd::DftParams d{};
     d.nmon = 1;

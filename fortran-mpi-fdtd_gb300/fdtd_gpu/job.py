@@ -26,7 +26,7 @@ EXPORTS = [
     "fdtd_get_monitor", "fdtd_get_probe", "fdtd_device_bytes", "fdtd_estimate_bytes", "fdtd_profile",
     "fdtd_kernel_time", "fdtd_kernel_cells", "fdtd_set_tile", "fdtd_get_tile", "fdtd_launch_count", "fdtd_set_stream", "fdtd_transfer_bytes",
     "fdtd_dft_sample_noalloc", "fdtd_state_bytes", "fdtd_save_state", "fdtd_load_state",
-    "fdtd_check_finite", "fdtd_debug_fail_alloc",
+    "fdtd_check_finite", "fdtd_debug_fail_alloc", "fdtd_debug_wait_limit",
     "fdtd_server_create", "fdtd_server_submit", "fdtd_server_wait", "fdtd_server_job", "fdtd_server_times",
     "fdtd_server_release", "fdtd_server_stats", "fdtd_server_destroy",
 ]
@@ -57,6 +57,7 @@ def lib(path=None):
             "fdtd_state_bytes": [vp, C.POINTER(C.c_uint64)], "fdtd_save_state": [vp, vp, C.c_uint64],
             "fdtd_load_state": [vp, vp, C.c_uint64],
             "fdtd_check_finite": [vp, C.POINTER(C.c_int64)], "fdtd_debug_fail_alloc": [i32],
+            "fdtd_debug_wait_limit": [vp, i32],
             "fdtd_add_pml": [vp, vp], "fdtd_add_tfsf_1d": [vp, vp], "fdtd_add_tfsf": [vp, vp],
             "fdtd_add_source": [vp, vp, C.POINTER(i32)], "fdtd_add_monitor": [vp, vp, C.POINTER(i32)],
             "fdtd_add_probe": [vp, vp, C.POINTER(i32)], "fdtd_commit": [vp],
@@ -254,6 +255,11 @@ class Job:
         out = np.empty(max(1, cnt.value * ncomp))
         check(lib().fdtd_get_probe(self.h, int(pid), out.ctypes.data, C.byref(cnt)))
         return out[: cnt.value * ncomp].reshape(cnt.value, ncomp)
+
+    def debug_wait_limit(self, rounds):
+        """fdtd_debug_wait_limit: polls of a TMA core's mbarrier before its
+        wait gives up (-1: the default)."""
+        check(lib().fdtd_debug_wait_limit(self.h, int(rounds)))
 
     def count_nonfinite(self):
         """NaN and infinite values in the job's evolving state."""

@@ -403,6 +403,14 @@ int fdtd_load_state(fdtd_job *job, const void *buf, uint64_t bytes);
  * FDTD_ENOMEM at every allocation of set-up and stepping. */
 int fdtd_check_finite(fdtd_job *job, int64_t *count);
 int fdtd_debug_fail_alloc(int32_t after);
+/* fdtd_debug_wait_limit sets how many polls the TMA-staged 3D core kernels
+ * make of a copy's mbarrier before they give up on it (rounds < 0: the
+ * default, 2^22).  With 0 every wait of the main loop gives up at once: the
+ * kernel sets the job's error flag, lets the copies it issued land, and
+ * returns, and the next fdtd_sync reports FDTD_ECUDA (once).  It lets a
+ * caller exercise that path without a copy that never completes.  No
+ * counterpart in the reference, which has no device code. */
+int fdtd_debug_wait_limit(fdtd_job *job, int32_t rounds);
 
 /* ---- results ------------------------------------------------------------- */
 int fdtd_sync(fdtd_job *job);
@@ -511,9 +519,10 @@ int fdtd_server_destroy(fdtd_server *server);
  * No counterpart in the reference: its DFT sums live inside program.f90's
  * time loop (2D/.../program.f90:383-391, 3D/.../program.f90:441-540).  This
  * entry point serves host codes that keep their own device fields and cannot
- * let a library allocate device memory while they run (a time loop recorded
- * into a CUDA graph by stream capture, or a code that takes every device
- * byte from its own pool).
+ * let a library allocate device memory while they run: a code that takes
+ * every device byte from its own pool at start-up (a driver allocation would
+ * synchronise the device and fragment that pool), or one that runs under a
+ * device-memory budget fixed before its time loop starts.
  *
  * Call it once per step n, after the H update, with the device field array
  * `field` (nx*ny*nz values of `precision`, x fastest) and the box lo..hi
@@ -530,11 +539,16 @@ int fdtd_server_destroy(fdtd_server *server);
  * static device array of FDTD_NOALLOC_STAGE_BYTES that the library holds on
  * every device for the life of the process, so a box may hold at most
  * FDTD_NOALLOC_MAX_CELLS cells (a 512 x 512 plane); a larger box fails with
- * FDTD_ERANGE.  The first call on each device looks up that array's device
- * address (cudaGetSymbolAddress) with the device current; make that first
- * call before any stream capture.  The array is shared by all calls on a
- * device, so one sequence of steps may run at a time per device: calls that
- * overlap (two boxes at once, or two host threads or streams) race on it. */
+ * FDTD_ERANGE.  The first call on each device does the set-up, with the
+ * device current: it looks up that array's device address
+ * (cudaGetSymbolAddress) and loads the kernels it launches, so that no later
+ * call makes the driver load code; make that first call before any stream
+ * capture.  The array is shared by all calls on a device and keeps the last
+ * call's samples, so one sequence of steps may run at a time per device:
+ * calls that overlap on the GPU (two boxes at once, or two host threads or
+ * streams) race on it.  A sequence may start at any step of the window
+ * (a run resumed mid-window, say): the ring slots before its first step are
+ * cleared whenever a call does not follow the previous call's step. */
 #define FDTD_NOALLOC_RING 32
 #define FDTD_NOALLOC_MAX_CELLS 262144
 #define FDTD_NOALLOC_STAGE_BYTES (FDTD_NOALLOC_MAX_CELLS * FDTD_NOALLOC_RING * 8)

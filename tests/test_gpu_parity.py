@@ -19,10 +19,15 @@ TOL32_DFT = 1e-4
 
 
 def rel_l2(a, b):
+    """Relative L2 error of a against b.  A reference that is all zeros
+    passes only a value that is all zeros too (a monitor gated off in both):
+    any nonzero value against it is an infinite error, not a small one."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     nb = np.linalg.norm(b)
-    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+    if nb == 0:
+        return 0.0 if not np.any(a) else float("inf")
+    return np.linalg.norm(a - b) / nb
 
 
 def check_state(J, O, comps, tol=TOL64, per_comp=1e-8):
@@ -32,6 +37,7 @@ def check_state(J, O, comps, tol=TOL64, per_comp=1e-8):
     polarisation, carries rounding noise of the dominant ones)."""
     a = [J.get_field(c) for c in comps]
     b = [O.get_field(c) for c in comps]
+    assert any(np.any(x) for x in b), "the oracle's state is all zeros: nothing was driven"
     tot = rel_l2(np.concatenate([x.ravel() for x in a]), np.concatenate([x.ravel() for x in b]))
     assert tot <= tol, f"state rel L2 {tot:.3e}"
     for c, x, y in zip(comps, a, b):
@@ -163,18 +169,34 @@ def test_2d_reference_deterministic(gpu):
 # 3D and 1D reference programs against the oracle
 # ---------------------------------------------------------------------------
 def test_3d_reference_vs_oracle(gpu, oracle_lib):
+    """The 3D reference program for its whole Nt = 13696 steps: by then the
+    pulse has crossed the gold strip, the SiO2 layer and the Si substrate and
+    has driven the high-y PML slab (setboundayEyb/Hyb, eps_hi = Si), so every
+    monitor and probe, the Si region and the high slab's rows hold nonzero
+    values, and all of them are compared."""
     spec, meta = problems.reference_3d()
-    steps = 700
+    steps = meta["Nt"]
+    assert steps == 13696
     J = gpu.Job(spec)
     O = oracle_lib.OracleJob(spec, nthreads=NTH)
     J.step(1, steps)
     O.step(1, steps)
-    check_state(J, O, (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ))
-    for q in (0, 2):
-        for x, y in zip(J.get_monitor(q), O.get_monitor(q)):
-            assert rel_l2(x, y) <= TOL64
-    for q in range(2):
-        assert rel_l2(J.get_probe(q), O.get_probe(q)) <= TOL64
+    comps = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ)
+    check_state(J, O, comps)
+    # the strip is uniform along z and the source is Ex: the fields are Ex,
+    # Ey and Hz; Ez, Hx and Hy stay exactly zero in both
+    npml, ny = 10, meta["ny"]
+    si_lo = spec.materials[3].region["lo"][1]  # first row of the Si substrate (0-based)
+    for c in (abi.EX, abi.EY, abi.HZ):
+        f = O.get_field(c)                    # [z][y][x]
+        assert np.any(f[:, si_lo:ny - npml, :]), f"component {c}: Si substrate not driven"
+    for c in (abi.EX, abi.HZ):  # the high slab's coupling row takes Exy / Hzy (setboundayEyb/Hyb)
+        assert np.any(O.get_field(c)[:, ny - npml, :]), f"component {c}: high-y PML slab not driven"
+    assert _dft_err(J, O, 3, live=(0, 1, 2)) <= TOL64
+    for q in range(3):
+        p = O.get_probe(q)
+        assert np.any(p), f"probe {q} of the oracle is zero"
+        assert rel_l2(J.get_probe(q), p) <= TOL64
 
 
 def test_1d_reference_vs_oracle(gpu, oracle_lib):
@@ -194,11 +216,20 @@ def test_1d_reference_vs_oracle(gpu, oracle_lib):
 # ---------------------------------------------------------------------------
 # benchmark workloads at reduced size: FP64 plain and FP32 against the oracle
 # ---------------------------------------------------------------------------
-def _dft_err(J, O, nmon):
-    errs = []
+def _dft_err(J, O, nmon, live=None):
+    """Largest relative L2 error of the monitors' sums.  At least one monitor
+    of the oracle must hold nonzero sums; the monitors listed in `live` must
+    each hold them (a monitor gated off for the whole run may stay zero, and
+    then the GPU's must be zero too)."""
+    errs, norms = [], []
     for q in range(nmon):
         (jr, ji), (orr, oi) = J.get_monitor(q), O.get_monitor(q)
-        errs.append(rel_l2(np.concatenate([jr.ravel(), ji.ravel()]), np.concatenate([orr.ravel(), oi.ravel()])))
+        ref = np.concatenate([orr.ravel(), oi.ravel()])
+        norms.append(np.linalg.norm(ref))
+        errs.append(rel_l2(np.concatenate([jr.ravel(), ji.ravel()]), ref))
+    assert max(norms) > 0, "every monitor of the oracle is zero"
+    for q in live or ():
+        assert norms[q] > 0, f"monitor {q} of the oracle is zero"
     return max(errs)
 
 
@@ -295,6 +326,62 @@ def test_core_block_shapes_give_identical_results(gpu, dim):
     J = gpu.Job(spec)
     assert J.tile() in ((1, 2, 3) if dim == 2 else range(1, 9))
     J.close()
+
+
+def test_tma_cores_across_tile_seams(gpu, oracle_lib):
+    """The TMA-staged 3D cores on a grid of several tiles: a 300^3 sphere
+    with a 7-cell PML has a core box of 284 x 286 x 286 cells, so its x-range
+    spans three 128-cell tiles (the last one 28 cells wide) and its y- and
+    z-ranges are not multiples of the 8-row, 8-plane tiles.  The wave
+    crosses the sphere, so the fields vary along every axis at every seam.
+    Each TMA core shape gives the plain shape's fields bit for bit, and the
+    plain shape's spectra match the FP64 oracle to the FP32 tolerance."""
+    spec, _ = problems.config_3d_sphere(precision=abi.F32, n=300, nfreq=4, npml=7, radius=40.0, half=70)
+    comps, steps = (abi.EX, abi.EY, abi.EZ, abi.HX, abi.HY, abi.HZ), 300
+    ref = None
+    for tile in (2, 7, 8):
+        J = gpu.Job(spec, tile=tile)
+        assert J.tile() == tile
+        J.step(1, steps)
+        got = [J.get_field(c) for c in comps]
+        if ref is None:
+            ref = got
+            O = oracle_lib.OracleJob(spec.with_precision(abi.F64), nthreads=NTH)
+            O.step(1, steps)
+            assert _dft_err(J, O, 6) <= TOL32_DFT
+            for c, g in zip(comps, got):
+                assert np.any(g), f"component {c} is zero"
+        else:
+            for c, a, b in zip(comps, ref, got):
+                np.testing.assert_array_equal(a, b, err_msg=f"tile {tile}, component {c}")
+        J.close()
+
+
+@pytest.fixture(scope="module")
+def bench2d_oracle(oracle_lib):
+    """The FP64 oracle on the bench's whole 2D workload: 2048^2 cells, 40
+    cylinders, 10000 steps."""
+    spec, meta = problems.config_2d_tmz(precision=abi.F64)
+    O = oracle_lib.OracleJob(spec, nthreads=NTH)
+    O.step(1, meta["Nt"])
+    return O, meta
+
+
+@pytest.mark.parametrize("prec", [abi.F64, abi.F32])
+def test_2d_bench_workload_full_size_vs_oracle(gpu, bench2d_oracle, prec):
+    """The bench's 2D workload at its full size and length against the FP64
+    oracle: FP64 plain, fields and spectra <= 1e-10; FP32, spectra <= 1e-4
+    (the metric's tolerance)."""
+    O, meta = bench2d_oracle
+    spec, _ = problems.config_2d_tmz(precision=prec)
+    J = gpu.Job(spec)
+    J.step(1, meta["Nt"])
+    err = _dft_err(J, O, 3, live=(0, 1, 2))
+    if prec == abi.F64:
+        assert err <= TOL64
+        check_state(J, O, (abi.EZ, abi.HX, abi.HY))
+    else:
+        assert err <= TOL32_DFT
 
 
 @pytest.mark.parametrize("dim", [1, 3])
@@ -764,6 +851,49 @@ def test_checkpoint_from_another_job_is_refused(gpu):
         ja.load_state(state)
     ja.close()
     jb.close()
+    # damaged checkpoints whose header total agrees with their length: cut
+    # short, or with a probe record that claims more samples than it holds
+    a.add_probe((128, 128, 0), (abi.EZ,))
+    ja = gpu.Job(a)
+    ja.step(1, 10)
+    good = ja.save_state()
+    nbuf = int(good[32:36].view(np.uint32)[0])
+    short = good[:-8].copy()
+    short[56:64] = np.frombuffer(np.uint64(short.size).tobytes(), np.uint8)
+    rec = 64 + 8 * nbuf                       # the probe's (samples, components) record
+    more = good.copy()
+    more[rec:rec + 4] = np.frombuffer(np.int32(good[rec:rec + 4].view(np.int32)[0] + 1).tobytes(), np.uint8)
+    for bad in (short, more):
+        with pytest.raises(gpu.FdtdError) as e:
+            ja.load_state(bad)
+        assert e.value.code == abi.FDTD_EINVAL
+    ja.load_state(good)
+    ja.close()
+
+
+def test_tma_wait_give_up_is_reported_and_recovered(gpu):
+    """The TMA cores' bounded waits, made to run out at once (a wait limit
+    of 0 polls) while every copy still lands: the kernels set the job's flag,
+    let their copies land and return; fdtd_sync reports FDTD_ECUDA once, the
+    context stays usable, and with the default limit the job then steps
+    without error, and a fresh job gives the plain cores' fields."""
+    spec, _ = problems.config_3d_sphere(precision=abi.F32, n=96, nfreq=4, npml=8, radius=40.0, half=20)
+    J = gpu.Job(spec, tile=8)
+    J.debug_wait_limit(0)
+    J.step(1, 3)
+    with pytest.raises(gpu.FdtdError) as e:
+        J.sync()
+    assert e.value.code == abi.FDTD_ECUDA
+    J.sync()                                # reported once
+    J.debug_wait_limit(-1)
+    J.step(4, 40)
+    J.sync()
+    J.close()
+    a, b = gpu.Job(spec, tile=8), gpu.Job(spec, tile=2)
+    a.step(1, 40)
+    b.step(1, 40)
+    for c in (abi.EX, abi.HY):
+        np.testing.assert_array_equal(a.get_field(c), b.get_field(c))
 
 
 def test_nonfinite_values_are_counted(gpu):

@@ -45,22 +45,45 @@ def setup():
     return torch, job, spec, meta, yin, frames, re[0], im[0]
 
 
-def run_sequence(torch, job, meta, yin, frames, precision, flush_at=()):
+def run_sequence(torch, job, meta, yin, frames, precision, flush_at=(), steps=None, acc=None):
+    """Feed the recorded Ez frames of `steps` (default: all) to the entry
+    point, into the accumulators `acc` (default: new zeroed ones)."""
     dev = torch.device("cuda", 0)
     dtype = torch.float64 if precision == abi.F64 else torch.float32
     field = torch.zeros((128, 128), dtype=dtype, device=dev)
     omega = torch.tensor(np.asarray(meta["arg"], np.float64), device=dev)
     nf, ncell = len(meta["arg"]), 128
-    acc_re = torch.zeros(nf * ncell, dtype=torch.float64, device=dev)
-    acc_im = torch.zeros_like(acc_re)
+    if acc is None:
+        acc = (torch.zeros(nf * ncell, dtype=torch.float64, device=dev),
+               torch.zeros(nf * ncell, dtype=torch.float64, device=dev))
+    acc_re, acc_im = acc
     stream = torch.cuda.current_stream(dev).cuda_stream
-    for n in sorted(frames):
+    for n in sorted(frames) if steps is None else steps:
         field.copy_(torch.from_numpy(frames[n]).to(dtype))
         job.dft_sample_noalloc(field.data_ptr(), precision, (128, 128, 1), (0, yin, 0), (127, yin, 0), n, N1, N2,
                                meta["dt"], omega.data_ptr(), nf, acc_re.data_ptr(), acc_im.data_ptr(),
                                flush=n in flush_at, stream=stream)
     torch.cuda.synchronize(dev)
     return acc_re.cpu().numpy().reshape(nf, ncell), acc_im.cpu().numpy().reshape(nf, ncell)
+
+
+def test_noalloc_sequence_resumed_mid_window(setup):
+    """A run that stops inside the window (flushing its last ring) and later
+    resumes mid-ring, after another sequence has filled the shared stage
+    array, still sums to the job's monitor: the slots before the resumed
+    step are cleared, not folded with the other sequence's samples."""
+    torch, job, spec, meta, yin, frames, jre, jim = setup
+    dev = torch.device("cuda", 0)
+    nf, ncell = len(meta["arg"]), 128
+    acc = (torch.zeros(nf * ncell, dtype=torch.float64, device=dev),
+           torch.zeros(nf * ncell, dtype=torch.float64, device=dev))
+    stop = N1 + 39                      # the run stops mid-ring; the resumed step N1 + 40 lies at slot 28
+    assert (stop - 1) % 32 != 31 and stop % 32 == 28
+    run_sequence(torch, job, meta, yin, frames, abi.F64, flush_at=(stop,), steps=range(N1, stop + 1), acc=acc)
+    run_sequence(torch, job, meta, yin, frames, abi.F64)          # another sequence fills the ring
+    re, im = run_sequence(torch, job, meta, yin, frames, abi.F64, steps=range(stop + 1, N2 + 1), acc=acc)
+    assert rel_l2(re, jre) <= TOL64
+    assert rel_l2(im, jim) <= TOL64
 
 
 def test_noalloc_matches_job_monitor_two_sequences(setup):
