@@ -205,6 +205,18 @@ struct fdtd_job {
   // bounded waits set when they give up
   TmaMaps tma{};
   bool tma_ok = false;
+  // the fused 3D step kernel (FP32): a second set of field buffers Fb, the
+  // two sets taking turns as step n and step n+1 (pp: the set that holds the
+  // current step inside fdtd_step; 0, the canonical F, between calls), and
+  // the tensor maps of each set's H arrays
+  bool fused_ok = false;
+  void *Fb[6] = {};
+  int pp = 0;
+  FusedMaps fmaps[2]{};
+  // the persistent 2D step kernel: whole rings in one cooperative launch,
+  // with the grid barrier's counter
+  bool persist_ok = false;
+  unsigned *d_bar = nullptr;
   int *d_err = nullptr;
   unsigned wait_limit = kWaitLimit;  // polls of a TMA core's mbarrier wait (fdtd_debug_wait_limit)
   cudaGraph_t graph = nullptr;
@@ -288,6 +300,18 @@ int alloc_dev(fdtd_job *J, void **p, size_t bytes) {
   e = cudaStreamSynchronize(J->stream);
   if (e != cudaSuccess) return set_err(FDTD_ECUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
   return FDTD_OK;
+}
+
+// give back a buffer of alloc_dev before the job ends
+void free_dev(fdtd_job *J, void *p, size_t bytes) {
+  if (!p) return;
+  for (size_t q = 0; q < J->allocs.size(); ++q)
+    if (J->allocs[q] == p) {
+      J->allocs.erase(J->allocs.begin() + (long)q);
+      break;
+    }
+  pool_free(J, p);
+  J->dev_bytes -= bytes;
 }
 
 // the device flag of bounded waits (after the stream has drained): a wait
@@ -538,6 +562,20 @@ int split_3d(fdtd_job *J, const std::vector<uint8_t> &rf) {
 template <typename T>
 int tune_tiles(fdtd_job *J);
 int setup_tma(fdtd_job *J);
+int setup_fused(fdtd_job *J);
+
+// The persistent 2D step kernel takes the samples in its H edge units (the
+// fused gather), so it needs a job without mean monitors or a TFSF box.
+// Environment FDTD_NO_PERSIST leaves it out.
+int setup_persist(fdtd_job *J) {
+  J->persist_ok = false;
+  if (J->dim != 2 || !J->gather_fused || J->has_tfbox || J->ncore <= 0 || getenv("FDTD_NO_PERSIST")) return FDTD_OK;
+  int rc;
+  if (!J->d_bar && (rc = alloc_dev(J, (void **)&J->d_bar, sizeof(unsigned)))) return rc;
+  if (!J->d_err && (rc = alloc_dev(J, (void **)&J->d_err, sizeof(int)))) return rc;
+  J->persist_ok = true;
+  return FDTD_OK;
+}
 
 // The TFSF box: faces, and the cells its face terms touch (the box widened by
 // one cell across each face) inside the grid, the main range and the PML's
@@ -1178,7 +1216,13 @@ int commit_impl(fdtd_job *J) {
   J->dft_blocks = blocks;
   CK(cudaStreamSynchronize(J->stream));
   if ((rc = setup_tma(J))) return rc;
+  if ((rc = setup_fused(J))) return rc;
+  if ((rc = setup_persist(J))) return rc;
   if ((rc = tune_tiles<T>(J))) return rc;
+  if (J->fused_ok && J->tile != 8) {  // the tuner kept a split shape: no second set of fields
+    for (int c = 0; c < 6; ++c) { free_dev(J, J->Fb[c], (size_t)J->ncell * 4); J->Fb[c] = nullptr; }
+    J->fused_ok = false;
+  }
   if ((rc = kernel_flag(J))) return rc;
   J->committed = true;
   return FDTD_OK;
@@ -1240,6 +1284,41 @@ int setup_tma(fdtd_job *J) {
   return FDTD_OK;
 }
 
+// The fused 3D step kernel needs what the TMA cores need on both sides of the
+// core box, and a grid without reference slabs or a TFSF box (their kernels
+// update fields in place).  Its second set of field buffers is allocated
+// here, before the tuner times the kernel; commit gives it back if the tuner
+// keeps another shape.  Environment FDTD_NO_FUSED leaves the kernel out.
+int setup_fused(fdtd_job *J) {
+  J->fused_ok = false;
+  if (!J->tma_ok || !J->tma.h_ok || J->slab_rows > 0 || J->has_tfbox || getenv("FDTD_NO_FUSED")) return FDTD_OK;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return FDTD_OK;
+  int rc;
+  const size_t bytes = (size_t)J->ncell * 4;
+  for (int c = 0; c < 6; ++c)
+    if (!J->Fb[c] && (rc = alloc_dev(J, &J->Fb[c], bytes))) return rc;
+  const cuuint64_t dim[3] = {(cuuint64_t)J->nx, (cuuint64_t)J->ny, (cuuint64_t)J->nz};
+  const cuuint64_t stride[2] = {(cuuint64_t)J->nx * 4, (cuuint64_t)J->nx * J->ny * 4};
+  const cuuint32_t es[3] = {1, 1, 1};
+  auto make = [&](CUtensorMap *m, void *base, cuuint32_t bx, cuuint32_t by) {
+    const cuuint32_t box[3] = {bx, by, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dim, stride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  for (int b = 0; b < 2; ++b) {
+    void *const *F = b ? J->Fb : J->F;
+    if (!make(&J->fmaps[b].hx, F[3], 128, 10) || !make(&J->fmaps[b].hy, F[4], 132, 9) ||
+        !make(&J->fmaps[b].hz, F[5], 132, 10)) {
+      for (int c = 0; c < 6; ++c) { free_dev(J, J->Fb[c], bytes); J->Fb[c] = nullptr; }
+      return FDTD_OK;  // not offered
+    }
+  }
+  J->fused_ok = true;
+  return FDTD_OK;
+}
+
 template <typename T>
 void fill_common(fdtd_job *J, StepParams<T> &p) {
   memset(&p, 0, sizeof p);
@@ -1260,6 +1339,9 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   p.ku = T(J->g.ku);
   p.ex = (T *)J->F[0]; p.ey = (T *)J->F[1]; p.ez = (T *)J->F[2];
   p.hx = (T *)J->F[3]; p.hy = (T *)J->F[4]; p.hz = (T *)J->F[5];
+  p.exo = p.ex; p.eyo = p.ey; p.ezo = p.ez;  // in place unless a fused step sets a ping-pong pair
+  p.hxo = p.hx; p.hyo = p.hy; p.hzo = p.hz;
+  p.pp = 0;
   p.mat = J->d_mat;
   p.mc = (const MatCoef<T> *)J->d_mc;
   p.mca = (const T *)J->d_mca;
@@ -1559,6 +1641,11 @@ int tune_tiles(fdtd_job *J) {
     J->tile = J->tile_req - 1;
     if ((J->tile == 6 && !J->tma_ok) || (J->tile == 7 && !(J->tma_ok && J->tma.h_ok)))
       return set_err(FDTD_EINVAL, "tiles 7 and 8 (the TMA cores) need FP32, 4-cell vectors and a core box inside the grid");
+    if (J->dim == 3 && J->tile == 8 && !J->fused_ok)
+      return set_err(FDTD_EINVAL, "tile 9 (the fused step kernel) needs FP32, 4-cell vectors, a core box inside the "
+                                  "grid, and no reference slabs or TFSF box");
+    if (J->dim == 2 && J->tile == 3 && !J->persist_ok)
+      return set_err(FDTD_EINVAL, "2D tile 4 (the persistent step kernel) needs a job without mean monitors or a TFSF box");
     return FDTD_OK;
   }
   const char *off = getenv("FDTD_TUNE");
@@ -1569,8 +1656,8 @@ int tune_tiles(fdtd_job *J) {
   int lg = 0;
   for (long long c = J->ncore; c > 1; c >>= 1) ++lg;
   // which TMA-staged kernels the grid can take is part of the kind of grid
-  const long long key = (((((long long)J->dim * 8 + J->g.layout) * 4 + J->g.precision) * 8 + J->vec) * 64 + lg) * 4 +
-                        (J->tma_ok ? 2 : 0) + (J->tma_ok && J->tma.h_ok ? 1 : 0);
+  const long long key = (((((long long)J->dim * 8 + J->g.layout) * 4 + J->g.precision) * 8 + J->vec) * 64 + lg) * 8 +
+                        (J->fused_ok ? 4 : 0) + (J->tma_ok ? 2 : 0) + (J->tma_ok && J->tma.h_ok ? 1 : 0);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -1588,18 +1675,27 @@ int tune_tiles(fdtd_job *J) {
   float best = 3.0e38f;
   int choice = 1;
   // 3D: also the z-marching kernels and, where set up, the TMA-staged cores
-  const int nshapes = J->dim == 3 ? (J->tma_ok ? (J->tma.h_ok ? 8 : 7) : 6) : 3;
+  // and the fused step kernel (one launch in place of an E and an H core)
+  const int nshapes = J->dim == 3 ? (J->fused_ok ? 9 : J->tma_ok ? (J->tma.h_ok ? 8 : 7) : 6) : 3;
+  auto cores = [&](int c) {
+    if constexpr (sizeof(T) == 4) {
+      if (c == 8) {
+        StepParams<float> q = p;
+        q.exo = (float *)J->Fb[0]; q.eyo = (float *)J->Fb[1]; q.ezo = (float *)J->Fb[2];
+        q.hxo = (float *)J->Fb[3]; q.hyo = (float *)J->Fb[4]; q.hzo = (float *)J->Fb[5];
+        q.pp = 1;
+        launch_step3d_fused(q, J->fmaps[0], J->stream);
+        return;
+      }
+    }
+    launch_part<T>(J, p, K2D_CORE, true, J->stream);
+    launch_part<T>(J, p, K2D_CORE, false, J->stream);
+  };
   for (int c = 0; c < nshapes; ++c) {
     p.tile = c;
-    for (int w = 0; w < 2; ++w) {
-      launch_part<T>(J, p, K2D_CORE, true, J->stream);
-      launch_part<T>(J, p, K2D_CORE, false, J->stream);
-    }
+    for (int w = 0; w < 2; ++w) cores(c);
     cudaEventRecord(a, J->stream);
-    for (int r = 0; r < 5; ++r) {
-      launch_part<T>(J, p, K2D_CORE, true, J->stream);
-      launch_part<T>(J, p, K2D_CORE, false, J->stream);
-    }
+    for (int r = 0; r < 5; ++r) cores(c);
     cudaEventRecord(b, J->stream);
     float ms = 0.f;
     if (cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms < best) {
@@ -1682,9 +1778,107 @@ int after_sample(fdtd_job *J, int n) {
   return FDTD_OK;
 }
 
+// A job steps through the fused 3D kernel when the tuner (or fdtd_set_tile)
+// chose it.  The per-procedure entry points keep the split kernels.
+bool fused_mode(const fdtd_job *J) { return J->fused_ok && J->tile == 8; }
+
+// One time step of the fused path, from field set pp to the other: the
+// general E kernel (edge units and ADE cells; E^n and H^n of the current set,
+// E^{n+1} into the other), the fused kernel over the core box, the general H
+// kernel (E^{n+1} and H^{n+1} in the other set), then the samples of the new
+// fields.  The four launches run in this order on the job's stream, each
+// waiting for the one before in its programmatic dependency.
+template <typename T>
+int fused_step(fdtd_job *J, int n, int slot, bool graph) {
+  if constexpr (sizeof(T) != 4) {
+    (void)n; (void)slot; (void)graph;
+    return set_err(FDTD_ESTATE, "the fused step kernel is FP32 only");
+  } else {
+    const int from = J->pp, to = 1 - from;
+    float *A[6], *B[6];
+    for (int c = 0; c < 6; ++c) {
+      A[c] = (float *)(from ? J->Fb[c] : J->F[c]);
+      B[c] = (float *)(to ? J->Fb[c] : J->F[c]);
+    }
+    StepParams<float> p;
+    fill_common<float>(J, p);
+    set_sources<float>(J, p);
+    p.roles = ROLE_MAIN | ROLE_PML | ROLE_ADE;
+    p.n = n;
+    p.slot = slot;
+    p.d_base = graph ? J->d_base : nullptr;
+    p.pp = 1;
+    p.ex = A[0]; p.ey = A[1]; p.ez = A[2]; p.hx = A[3]; p.hy = A[4]; p.hz = A[5];
+    p.exo = B[0]; p.eyo = B[1]; p.ezo = B[2]; p.hxo = B[3]; p.hyo = B[4]; p.hzo = B[5];
+    if (!graph) ev_record(J, FDTD_KERNEL_EDGE, true);
+    J->launches += launch_e3d_general_pdl<float>(p, J->stream);
+    if (!graph) ev_record(J, FDTD_KERNEL_EDGE, false);
+    if (!graph) ev_record(J, FDTD_KERNEL_STEP, true);
+    J->launches += launch_step3d_fused(p, J->fmaps[from], J->stream);
+    if (!graph) ev_record(J, FDTD_KERNEL_STEP, false);
+    p.ex = B[0]; p.ey = B[1]; p.ez = B[2];  // the H half reads E^{n+1}
+    if (!graph) ev_record(J, FDTD_KERNEL_EDGE, true);
+    J->launches += launch_h3d_general_pdl<float>(p, J->stream);
+    if (!graph) ev_record(J, FDTD_KERNEL_EDGE, false);
+    StepParams<float> g;  // samples of the new fields
+    fill_common<float>(J, g);
+    g.ex = g.exo = B[0]; g.ey = g.eyo = B[1]; g.ez = g.ezo = B[2];
+    g.hx = g.hxo = B[3]; g.hy = g.hyo = B[4]; g.hz = g.hzo = B[5];
+    g.n = n;
+    g.slot = slot;
+    g.d_base = graph ? J->d_base : nullptr;
+    J->launches += launch_gather<float>(g, J->stream);
+    J->pp = to;
+    J->prog_prev = -1;
+    CK(cudaGetLastError());
+    return FDTD_OK;
+  }
+}
+
+// After an odd number of fused steps the current fields are in the second
+// set: copy them to the canonical one, where every other entry point and the
+// ring graph (which starts from it) expect them.
+int fused_settle(fdtd_job *J) {
+  if (!J->pp) return FDTD_OK;
+  const size_t bytes = (size_t)J->ncell * 4;
+  for (int c = 0; c < 6; ++c) CK(cudaMemcpyAsync(J->F[c], J->Fb[c], bytes, cudaMemcpyDeviceToDevice, J->stream));
+  J->pp = 0;
+  J->prog_prev = -1;
+  return FDTD_OK;
+}
+
+// 2D jobs whose steps run in the persistent kernel (tile 4)
+bool persist_mode(const fdtd_job *J) { return J->persist_ok && J->tile == 3; }
+
+// One ring of kStageSteps steps in one launch of the persistent 2D kernel:
+// from step n (or, in a graph replay, the device-side ring base) with ring
+// slots 0..kStageSteps-1
+template <typename T>
+int persist_ring(fdtd_job *J, int n, bool graph) {
+  StepParams<T> p;
+  fill_common<T>(J, p);
+  set_sources<T>(J, p);
+  p.roles = ROLE_MAIN | ROLE_PML | ROLE_ADE;
+  p.n = n;
+  p.slot = 0;
+  p.gather = 1;
+  p.d_base = graph ? J->d_base : nullptr;
+  if (!graph) ev_record(J, FDTD_KERNEL_STEP, true);
+  const int r = launch_step2d_persistent<T>(p, J->d_bar, kStageSteps, J->stream);
+  if (!graph) ev_record(J, FDTD_KERNEL_STEP, false);
+  if (r < 0) return set_err(FDTD_ECUDA, "persistent step kernel launch: %s", cudaGetErrorString(cudaGetLastError()));
+  J->launches += r;
+  J->prog_prev = -1;
+  return FDTD_OK;
+}
+
 template <typename T>
 int eager_step(fdtd_job *J, int n) {
   int rc;
+  if (fused_mode(J)) {
+    if ((rc = fused_step<T>(J, n, J->stage_fill, false))) return rc;
+    return after_sample<T>(J, n);
+  }
   if ((rc = half_e<T>(J, n, ROLE_MAIN | ROLE_PML | ROLE_ADE))) return rc;
   if ((rc = half_h<T>(J, n, ROLE_MAIN | ROLE_PML, J->gather_fused))) return rc;
   if (!J->gather_fused && (rc = sample_sep<T>(J, n))) return rc;
@@ -1705,7 +1899,14 @@ int ring_graph(fdtd_job *J) {
   J->prog_prev = -1;  // events recorded outside the capture cannot be waited on inside it
   CK(cudaStreamBeginCapture(J->stream, cudaStreamCaptureModeThreadLocal));
   int bad = FDTD_OK;
-  for (int s = 0; s < kStageSteps && !bad; ++s) {
+  // the fused path alternates the field sets over the ring's even number of
+  // steps, so a replay starts and ends with the canonical set
+  if (persist_mode(J)) bad = persist_ring<T>(J, 0, true);
+  for (int s = 0; s < kStageSteps && !bad && !persist_mode(J); ++s) {
+    if (fused_mode(J)) {
+      bad = fused_step<T>(J, 0, s, true);
+      continue;
+    }
     bad = half_e<T>(J, 0, ROLE_MAIN | ROLE_PML | ROLE_ADE, s, true);
     if (!bad) bad = half_h<T>(J, 0, ROLE_MAIN | ROLE_PML, J->gather_fused, s, true);
     if (!bad && !J->gather_fused) bad = sample_sep<T>(J, 0, s, true);
@@ -1882,15 +2083,26 @@ int step_impl(fdtd_job *J, int n_first, int n_steps) {
   // run the tail eagerly (the per-launch events of fdtd_profile need eager)
   while (n < end && J->stage_fill != 0)
     if ((rc = eager_step<T>(J, n++))) return rc;
-  if (J->use_graph && !J->prof) {
+  if (J->use_graph && !J->prof && end - n >= kStageSteps) {
+    if ((rc = fused_settle(J))) return rc;
     while (end - n >= kStageSteps) {
       if ((rc = replay_ring<T>(J, n))) return rc;
       n += kStageSteps;
     }
   }
+  // profiled runs of the persistent kernel: whole rings as eager launches,
+  // each timed by its events, then the ring's DFT fold
+  while (J->prof && persist_mode(J) && end - n >= kStageSteps) {
+    if ((rc = persist_ring<T>(J, n, false))) return rc;
+    J->stage_n0 = n;
+    J->stage_fill = kStageSteps;
+    J->last_n = n + kStageSteps - 1;
+    if ((rc = dft_fold<T>(J))) return rc;
+    n += kStageSteps;
+  }
   while (n < end)
     if ((rc = eager_step<T>(J, n++))) return rc;
-  return FDTD_OK;
+  return fused_settle(J);
 }
 
 #define DISPATCH(J, call) ((J)->g.precision == FDTD_F32 ? call<float> : call<double>)
@@ -2778,6 +2990,10 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
   const uint64_t N = (uint64_t)J->ncell, w = J->esz;
   const int nx = J->nx, ny = J->ny, nz = J->nz;
   uint64_t b = N * w * (J->dim == 3 ? 6 : J->dim == 2 ? 3 : 2) + N;  // fields, material ids
+  // the fused 3D step kernel's second set of fields (commit may give it back)
+  if (J->dim == 3 && w == 4 && J->nx % 4 == 0 && !J->has_tfbox &&
+      !(J->has_pml && J->pml.mode == FDTD_PML_REFERENCE))
+    b += 6 * N * w;
   if (J->has_tfsf) b += 2 * N * w;
   if (J->has_tfbox) b += 2ull * ny * w + 4 * w;
   // dispersive cells: each region's cells, bounded per sphere / box
@@ -2858,7 +3074,7 @@ int fdtd_kernel_time(fdtd_job *J, int32_t kind, int64_t *launches, double *ms) {
 int fdtd_set_tile(fdtd_job *J, int32_t tile) {
   int rc = check_job(J, false);
   if (rc) return rc;
-  const int maxt = J->dim == 3 ? 8 : 3;
+  const int maxt = J->dim == 3 ? 9 : 4;
   if (tile < 0 || tile > maxt) return set_err(FDTD_EINVAL, "tile must be 0 (tune) or 1..%d", maxt);
   J->tile_req = tile;
   return FDTD_OK;
@@ -2877,6 +3093,8 @@ int fdtd_kernel_cells(const fdtd_job *J, int32_t kind, int64_t *cells) {
   if (!J->committed) return set_err(FDTD_ESTATE, "job not committed");
   int64_t c = 0;
   if (kind == FDTD_KERNEL_E || kind == FDTD_KERNEL_H) c = J->dim >= 2 ? (int64_t)J->ncore * J->vec : 0;
+  else if (kind == FDTD_KERNEL_STEP)
+    c = fused_mode(J) ? (int64_t)J->ncore * J->vec : persist_mode(J) ? (int64_t)J->ncell * kStageSteps : 0;
   else if (kind == FDTD_KERNEL_EDGE)
     c = J->dim >= 2 ? (int64_t)J->nedge * J->vec : 0;
   else if (kind == FDTD_KERNEL_ADE) c = J->dim == 2 ? J->nade : 0;

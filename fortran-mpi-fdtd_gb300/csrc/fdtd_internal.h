@@ -25,6 +25,13 @@
 
 namespace fdtd {
 
+// tensor maps of one buffer's H arrays for the fused 3D step kernel: one-plane
+// boxes of Hx 128 x 10 rows from (x0, y0-1), Hy 132 x 9 from (x0-4, y0), Hz
+// 132 x 10 from (x0-4, y0-1)
+struct FusedMaps {
+  CUtensorMap hx, hy, hz;
+};
+
 // tensor maps of the 3D H arrays (FP32) for the TMA-staged E core: boxes of
 // one plane, Hx 128 x 9 rows from (x0, y0-1), Hy 132 x 8 from (x0-4, y0),
 // Hz 132 x 9 from (x0-4, y0-1)
@@ -131,6 +138,13 @@ struct StepParams {
   T ku;
   // fields (E/H components; null when the layout lacks them)
   T *ex, *ey, *ez, *hx, *hy, *hz;
+  // where the 3D edge, ADE and fused kernels store what they update: the same
+  // arrays (in place), or with pp the other buffer of a ping-pong pair, in
+  // which case every cell a kernel owns is stored, updated or not.  E half:
+  // E^n read from ex.., E^{n+1} stored to exo..; H half: ex.. hold E^{n+1},
+  // H^n read from hx.., H^{n+1} stored to hxo..
+  T *exo, *eyo, *ezo, *hxo, *hyo, *hzo;
+  int pp;
   const uint8_t *mat;      // material id per cell: 0 none, 1..127 constant
                            // dielectric, 128..255 dispersive (ADE slots)
   const MatCoef<T> *mc;
@@ -243,6 +257,12 @@ enum K2dPart { K2D_CORE = 0, K2D_EDGE = 1, K2D_ADE = 2 };
 // prog_event: the core kernel records it as a programmatic event (or null)
 template <typename T> int launch_e2d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
 
+// the persistent 2D step kernel: `nsteps` whole steps (from p.n, or *p.d_base
+// in a graph replay, ring slots from p.slot) in one cooperative launch, with a
+// grid barrier on the counter `ctr` (zeroed by the launcher before the
+// launch) after each half step.  Returns 1, or -1 when the launch failed.
+template <typename T> int launch_step2d_persistent(const StepParams<T> &p, unsigned *ctr, int nsteps, void *stream);
+
 // packs of 2D jobs: one launch runs one part of every job's half step
 constexpr int kMaxPack = 32;
 template <typename T>
@@ -256,6 +276,15 @@ int launch_pack2d(const PackLaunch<T> &a, int layout, int vec, bool e_half, int 
 template <typename T> int launch_h2d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
 template <typename T> int launch_e3d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
 template <typename T> int launch_h3d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
+// the 3D general kernels (edge units, slabs, ADE cells) on the job's stream
+// with a programmatic dependency, for the serial order of a fused step
+template <typename T> int launch_e3d_general_pdl(const StepParams<T> &p, void *stream);
+template <typename T> int launch_h3d_general_pdl(const StepParams<T> &p, void *stream);
+// the fused 3D step kernel (k3f.cu): E^{n+1} and H^{n+1} of the core box in
+// one pass, reading buffer ex.. (maps m) and storing to exo.. (ping-pong)
+int launch_step3d_fused(const StepParams<float> &p, const FusedMaps &m, void *stream);
+// blocks and dynamic shared memory of one launch
+void step3d_fused_shape(const StepParams<float> &p, int *blocks, int *smem);
 
 // separate gather (per-procedure API, or monitors inside reference slabs)
 // returns the kernels launched

@@ -29,14 +29,6 @@ __device__ __forceinline__ T coef_ca3(const StepParams<T> &p, uint8_t id) {
   return id == p.id0 ? p.ca0 : __ldg(p.mca + id);
 }
 
-// store V values, skipping cells whose E belongs to an ADE thread
-template <typename T, int V>
-__device__ __forceinline__ void st_guard3(T *a, const T (&v)[V], const uint8_t (&id)[V]) {
-#pragma unroll
-  for (int q = 0; q < V; ++q)
-    if (id[q] < kAdeId) a[q] = v[q];
-}
-
 template <typename T>
 struct F3 {
   const StepParams<T> &p;
@@ -218,10 +210,10 @@ __device__ __forceinline__ void edge_e3(const StepParams<T> &p, int unit, int n)
       wrote = true;
     }
   }
-  if (wrote) {  // cells not updated store back what they read; ADE cells are skipped
-    st_guard3<T, V>(p.ex + c, ex, id);
-    st_guard3<T, V>(p.ey + c, ey, id);
-    st_guard3<T, V>(p.ez + c, ez, id);
+  if (wrote || p.pp) {  // cells not updated store what they read; ADE cells are skipped
+    st_guard3<T, V>(p.exo + c, ex, id);
+    st_guard3<T, V>(p.eyo + c, ey, id);
+    st_guard3<T, V>(p.ezo + c, ez, id);
   }
   if (pml) {
     vst<T, V>(p.sp[0] + c, s0);
@@ -305,10 +297,10 @@ __device__ __forceinline__ void edge_h3(const StepParams<T> &p, int unit) {
       wrote = true;
     }
   }
-  if (wrote) {
-    vst<T, V>(p.hx + c, hx);
-    vst<T, V>(p.hy + c, hy);
-    vst<T, V>(p.hz + c, hz);
+  if (wrote || p.pp) {
+    vst<T, V>(p.hxo + c, hx);
+    vst<T, V>(p.hyo + c, hy);
+    vst<T, V>(p.hzo + c, hz);
   }
   if (pml) {
     vst<T, V>(p.sp[3] + c, s3);
@@ -453,9 +445,9 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
   const T ix_ = p.ku * (curlhzy + curlhyz) + src_sum<T>(p, n, 0, i, j, k);
   const T iy_ = p.ku * (curlhxz + curlhzx) + src_sum<T>(p, n, 1, i, j, k);
   const T iz_ = p.ku * (curlhyx + curlhxy) + src_sum<T>(p, n, 2, i, j, k);
-  p.ex[cell] = ade_update<T>(p, a, am, s, 0, ix_, p.ex[cell]);
-  p.ey[cell] = ade_update<T>(p, a, am, s, 1, iy_, p.ey[cell]);
-  p.ez[cell] = ade_update<T>(p, a, am, s, 2, iz_, p.ez[cell]);
+  p.exo[cell] = ade_update<T>(p, a, am, s, 0, ix_, p.ex[cell]);
+  p.eyo[cell] = ade_update<T>(p, a, am, s, 1, iy_, p.ey[cell]);
+  p.ezo[cell] = ade_update<T>(p, a, am, s, 2, iz_, p.ez[cell]);
 }
 
 // general launch: blockIdx selects edge units, reference slab cells, then
@@ -1040,6 +1032,29 @@ int launch_h3d(const StepParams<T> &p, int part, void *stream, void *prog_event)
   else launch_side(h3d_kernel<T, 1>, blocks, 256, s, p);
   return 1;
 }
+
+template <typename T>
+int launch_e3d_general_pdl(const StepParams<T> &p, void *stream) {
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+  const int blocks = p.ntile_blocks + p.nslab_blocks + p.nade_blocks;
+  if (blocks <= 0) return 0;
+  if (p.vec == VW) launch_pdl(e3d_kernel<T, VW>, blocks, 256, (cudaStream_t)stream, p);
+  else launch_pdl(e3d_kernel<T, 1>, blocks, 256, (cudaStream_t)stream, p);
+  return 1;
+}
+template <typename T>
+int launch_h3d_general_pdl(const StepParams<T> &p, void *stream) {
+  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
+  const int blocks = p.ntile_blocks + p.nslab_blocks;
+  if (blocks <= 0) return 0;
+  if (p.vec == VW) launch_pdl(h3d_kernel<T, VW>, blocks, 256, (cudaStream_t)stream, p);
+  else launch_pdl(h3d_kernel<T, 1>, blocks, 256, (cudaStream_t)stream, p);
+  return 1;
+}
+template int launch_e3d_general_pdl<float>(const StepParams<float> &, void *);
+template int launch_e3d_general_pdl<double>(const StepParams<double> &, void *);
+template int launch_h3d_general_pdl<float>(const StepParams<float> &, void *);
+template int launch_h3d_general_pdl<double>(const StepParams<double> &, void *);
 
 template int launch_e3d<float>(const StepParams<float> &, int, void *, void *);
 template int launch_e3d<double>(const StepParams<double> &, int, void *, void *);

@@ -355,6 +355,14 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
   return e;
 }
 
+// store V values, skipping cells whose E belongs to an ADE thread
+template <typename T, int V>
+__device__ __forceinline__ void st_guard3(T *a, const T (&v)[V], const uint8_t (&id)[V]) {
+#pragma unroll
+  for (int q = 0; q < V; ++q)
+    if (id[q] < kAdeId) a[q] = v[q];
+}
+
 // the ids of the x-vector v of a row: id0 throughout when the uniformity
 // bitmap says so, else loaded
 template <typename T, int V>

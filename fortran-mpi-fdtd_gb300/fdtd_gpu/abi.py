@@ -10,7 +10,7 @@ COMP_NAMES = {"Ex": EX, "Ey": EY, "Ez": EZ, "Hx": HX, "Hy": HY, "Hz": HZ,
               "Ex_inc": EX_INC, "Hz_inc": HZ_INC}
 REGION_BOX, REGION_SPHERES, REGION_MASK = 0, 1, 2
 PML_REFERENCE, PML_SPLIT = 1, 2
-KERNEL_E, KERNEL_H, KERNEL_DFT, KERNEL_LINE1D, KERNEL_EDGE, KERNEL_ADE, KERNEL_COUNT = range(7)
+KERNEL_E, KERNEL_H, KERNEL_DFT, KERNEL_LINE1D, KERNEL_EDGE, KERNEL_ADE, KERNEL_STEP, KERNEL_COUNT = range(8)
 
 I3 = C.c_int32 * 3
 

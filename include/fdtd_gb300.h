@@ -436,24 +436,34 @@ int fdtd_estimate_bytes(const fdtd_job *job, uint64_t *bytes);
  * the summed device time of kernel class `kind` since the last reset. */
 /* FDTD_KERNEL_E / _H: the 3D half-step kernels, and in 2D the interior
  * (core) kernels; FDTD_KERNEL_EDGE: the 2D kernels for PML cells, the edges
- * of the main range and rows with sources, monitors or reference slabs;
- * FDTD_KERNEL_ADE: the 2D dispersive-cell kernel. */
+ * of the main range and rows with sources, monitors or reference slabs (in
+ * 3D with the fused step kernel: the general E and H kernels);
+ * FDTD_KERNEL_ADE: the 2D dispersive-cell kernel; FDTD_KERNEL_STEP: the
+ * fused 3D step kernel (E and H of the core box in one launch). */
 enum { FDTD_KERNEL_E = 0, FDTD_KERNEL_H = 1, FDTD_KERNEL_DFT = 2, FDTD_KERNEL_LINE1D = 3,
-       FDTD_KERNEL_EDGE = 4, FDTD_KERNEL_ADE = 5, FDTD_KERNEL_COUNT = 6 };
+       FDTD_KERNEL_EDGE = 4, FDTD_KERNEL_ADE = 5, FDTD_KERNEL_STEP = 6, FDTD_KERNEL_COUNT = 7 };
 int fdtd_profile(fdtd_job *job, int32_t enable);
 int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms);
 /* Block shape of the interior (core) kernels.  Before fdtd_commit, tile 0
  * (the default) lets commit time the candidates on the job's own grid and
  * keep the fastest (cached per kind of grid; environment FDTD_TUNE=0 skips
- * the timing); 1..3 pins a candidate: 2D 128 / 256 / 512 threads per block,
+ * the timing); 1..3 pins a candidate: 2D 128 / 256 / 512 threads per block
+ * (2D 4: the persistent step kernel, which runs each ring of 32 steps in one
+ * cooperative launch with a grid barrier after each half step, for jobs
+ * without mean monitors or a TFSF box; environment FDTD_NO_PERSIST leaves it
+ * out),
  * 3D 4 / 8 / 16 rows of 32 x-vectors, one plane per thread; 3D also 4..6:
  * the same shapes with each thread walking 8 planes and keeping the
  * neighbour plane in registers.  FP32 with 4-cell vectors, where the core
  * box lies at least one cell inside the grid, adds 3D 7: the TMA-staged E
  * core (tiled bulk copies into shared memory), and 8: both TMA-staged cores;
- * pinning one elsewhere fails at commit with FDTD_EINVAL.  Results do not
- * depend on the shape.  Environment FDTD_NO_TMA leaves the TMA-staged
- * kernels out.
+ * where the core box also ends at least one cell before the grid's far sides
+ * and the grid has no reference slabs or TFSF box, 9: the fused step kernel,
+ * which takes E and H of the core box from step n to n+1 in one pass over
+ * two sets of field buffers used in turn (the job then holds a second copy
+ * of its six field arrays); pinning one elsewhere fails at commit with
+ * FDTD_EINVAL.  Results do not depend on the shape.  Environment FDTD_NO_TMA
+ * leaves the TMA-staged kernels out, FDTD_NO_FUSED the fused one.
  * fdtd_get_tile returns the shape in use (0: the job has no core kernels). */
 int fdtd_set_tile(fdtd_job *job, int32_t tile);
 int fdtd_get_tile(const fdtd_job *job, int32_t *tile);
