@@ -52,8 +52,11 @@ def parse():
     ap.add_argument("--cpu-threads", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the 3D, graphene and 1D runs")
-    ap.add_argument("--serve-jobs", type=int, default=24, help="jobs in the serving run (0: none)")
-    ap.add_argument("--serve-rate", type=float, default=16.0, help="Poisson arrival rate, jobs/s")
+    ap.add_argument("--serve-jobs", type=int, default=200, help="jobs per arrival rate of the serving sweep (0: none)")
+    ap.add_argument("--serve-rates", default="4,8,16,32", help="Poisson arrival rates of the sweep, jobs/s")
+    ap.add_argument("--serve-arms-jobs", type=int, default=48,
+                    help="jobs of each of the served/sequential x FP32/FP64 arms (0: none)")
+    ap.add_argument("--serve-arms-rate", type=float, default=16.0, help="arrival rate of the arms, jobs/s")
     return ap.parse_args()
 
 
@@ -108,7 +111,8 @@ def measured_peaks():
 
 def profile_traffic(kernel):
     """dram bytes per launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_2d_tmz.md")
+    name = {"STEP": "step2d_fused"}.get(kernel, kernel)
+    path = os.path.join(ROOT, "profiles", f"{name}_2d_tmz.md")
     try:
         txt = open(path).read()
     except OSError:
@@ -190,13 +194,15 @@ def config_runs(stream):
     after a short warm-up), so that the FP32 spectra can be compared with the
     FP64 ones of the same run: Mcell-updates/s, the FP32 DFT error, and the
     step's ideal bytes (each field read and written once, plus the material
-    id: 12w+1 per cell in 3D, 4w+1 in 1D) over the measured HBM peak."""
+    id: 12w+1 per cell in 3D, 4w+1 in 1D) over the measured HBM peak; in 3D
+    also the step's algorithmic bytes with the split-PML shell's stored parts
+    (12w more per shell cell in FP32, 24w in FP64) over the same peak."""
     import torch
     from fdtd_gpu import abi, problems
     from fdtd_gpu.job import Job
     peak, _ = measured_peaks()
 
-    def timed(spec, warm, k, per_cell, keep=False):
+    def timed(spec, warm, k, per_cell, keep=False, shell=False):
         J = Job(spec)
         J.set_stream(stream.cuda_stream)
         J.step(1, warm)
@@ -212,6 +218,14 @@ def config_runs(stream):
         w = 4 if spec.precision == abi.F32 else 8
         r = {"mcell_updates_per_s": mc, "ms_per_step": ms / k, "timed_steps": k, "tile": J.tile(),
              "step_bytes_frac_of_hbm": mc * 1e6 * per_cell(w) / (peak * 1e9)}
+        if shell:
+            # the split-PML shell (cells outside the interior box) also reads
+            # and writes its stored parts: 6 per cell in FP32, 12 in FP64
+            nshell = spec.cells() - J.kernel_cells(abi.KERNEL_E)
+            alg = spec.cells() * per_cell(w) + nshell * (12 if w == 4 else 24) * w
+            r["shell_cells"] = nshell
+            r["step_alg_bytes"] = alg
+            r["step_alg_bytes_frac_of_hbm"] = alg / (ms / k / 1e3) / (peak * 1e9)
         if keep:
             return r, J
         J.close()
@@ -223,8 +237,8 @@ def config_runs(stream):
         s32, meta = make(precision=abi.F32)
         s64, _ = make(precision=abi.F64)
         nt, warm = meta["Nt"], 64
-        r32, j32 = timed(s32, warm, nt - warm, lambda w: 12 * w + 1, keep=True)
-        r64, j64 = timed(s64, warm, nt - warm, lambda w: 12 * w + 1, keep=True)
+        r32, j32 = timed(s32, warm, nt - warm, lambda w: 12 * w + 1, keep=True, shell=True)
+        r64, j64 = timed(s64, warm, nt - warm, lambda w: 12 * w + 1, keep=True, shell=True)
         out[name] = {"fp32": r32, "fp64_plain": r64, "time_steps": nt,
                      "fp32_over_fp64": r32["mcell_updates_per_s"] / r64["mcell_updates_per_s"],
                      "dft_rel_err_fp32_vs_fp64": dft_rel_err(j32, j64, nmon)}
@@ -240,22 +254,30 @@ def config_runs(stream):
     return out
 
 
-def serving_run(njobs, rate):
-    """The serving workload: seeded Poisson arrivals of 2D TMz and 3D sphere
-    jobs, continuously batched by the library's server in FP32, against the
-    same arrivals run one at a time in FP64 plain."""
-    from fdtd_gpu import abi, serve
-    from fdtd_gpu.job import Job
-    mix = serve.poisson_mix(njobs, rate, seed=1)
+def serve_served(mix):
+    """The mix through the library's server (continuous batching, HBM
+    admission, packs of small 2D jobs, graph rings): jobs/s, p50/p99 latency
+    and the pack statistics."""
+    from fdtd_gpu import serve
     S = serve.Server(max_active=16, chunk_steps=256)
     lat, wall = serve.run_mix(S, mix)
     st = S.stats()
     S.close()
     cells = sum(sp.cells() * nst for _, sp, nst in mix)
-    mix64 = serve.poisson_mix(njobs, rate, seed=1, precision=abi.F64)
+    return {"jobs": len(mix), "jobs_per_s": len(mix) / wall, "p50_s": serve.percentile(lat, 50),
+            "p99_s": serve.percentile(lat, 99), "wall_s": wall, "mcell_updates_per_s": cells / wall / 1e6,
+            "hbm_held_max_bytes": st["held_bytes_max"], "packed_rings": st["packed_rings"],
+            "pack_builds": st["pack_builds"], "pack_build_s": st["pack_build_s"]}
+
+
+def serve_sequential(mix):
+    """The same arrivals run one job at a time through the plain job API
+    (each job created, stepped and its spectra read before the next one)."""
+    from fdtd_gpu import serve
+    from fdtd_gpu.job import Job
     t0 = time.perf_counter()
-    lat64 = []
-    for ta, spec, nst in mix64:
+    lat = []
+    for ta, spec, nst in mix:
         idle = ta - (time.perf_counter() - t0)
         if idle > 0:
             time.sleep(idle)
@@ -264,20 +286,38 @@ def serving_run(njobs, rate):
         for q in range(len(spec.monitors)):
             J.get_monitor(q)
         J.close()
-        lat64.append(time.perf_counter() - t0 - ta)
-    wall64 = time.perf_counter() - t0
-    return {
-        "workload": f"{njobs} jobs, Poisson {rate:g}/s, seed 1: 80% 2D TMz N in {{256,512,1024}} with 1-20 "
-                    "cylinders, 20% 3D spheres N in {128,192,256}; 2000-8000 steps, 32-128 frequencies",
-        "served_fp32": {"jobs_per_s": njobs / wall, "p50_s": serve.percentile(lat, 50),
-                        "p99_s": serve.percentile(lat, 99), "wall_s": wall,
-                        "mcell_updates_per_s": cells / wall / 1e6, "max_active": 16, "chunk_steps": 256,
-                        "hbm_held_max_bytes": st["held_bytes_max"]},
-        "sequential_fp64_plain": {"jobs_per_s": njobs / wall64, "p50_s": serve.percentile(lat64, 50),
-                                  "p99_s": serve.percentile(lat64, 99), "wall_s": wall64,
-                                  "mcell_updates_per_s": cells / wall64 / 1e6},
-        "latency": "host time from submission (at the Poisson arrival time) to the job's completion",
-    }
+        lat.append(time.perf_counter() - t0 - ta)
+    wall = time.perf_counter() - t0
+    cells = sum(sp.cells() * nst for _, sp, nst in mix)
+    return {"jobs": len(mix), "jobs_per_s": len(mix) / wall, "p50_s": serve.percentile(lat, 50),
+            "p99_s": serve.percentile(lat, 99), "wall_s": wall, "mcell_updates_per_s": cells / wall / 1e6}
+
+
+def serving_run(njobs, rates, arms_jobs, arms_rate):
+    """The serving workload: seeded Poisson arrivals of 2D TMz and 3D sphere
+    jobs.  For each arrival rate, `njobs` jobs served in FP32; at `arms_rate`,
+    `arms_jobs` jobs in four arms -- served and one-at-a-time, each in FP32
+    and in FP64 plain -- so that the gain of batching (served vs sequential
+    at one precision) is apart from the gain of precision."""
+    from fdtd_gpu import abi, serve
+    out = {"workload": "Poisson arrivals, numpy default_rng(1): 80% 2D TMz N in {256,512,1024} with 1-20 "
+                       "cylinders, 20% 3D spheres N in {128,192,256}; 2000-8000 steps, 32-128 frequencies",
+           "latency": "host time from submission (at the Poisson arrival time) to the job's completion",
+           "server": {"max_active": 16, "chunk_steps": 256}, "sweep_fp32": []}
+    for rate in rates:
+        r = serve_served(serve.poisson_mix(njobs, rate, seed=1))
+        r["rate_per_s"] = rate
+        out["sweep_fp32"].append(r)
+    if arms_jobs > 0:
+        m32 = serve.poisson_mix(arms_jobs, arms_rate, seed=1)
+        m64 = serve.poisson_mix(arms_jobs, arms_rate, seed=1, precision=abi.F64)
+        out["arms"] = {"rate_per_s": arms_rate, "jobs": arms_jobs,
+                       "served_fp32": serve_served(m32), "sequential_fp32": serve_sequential(m32),
+                       "served_fp64_plain": serve_served(m64), "sequential_fp64_plain": serve_sequential(m64)}
+        a = out["arms"]
+        a["batching_gain_fp32"] = a["served_fp32"]["jobs_per_s"] / a["sequential_fp32"]["jobs_per_s"]
+        a["batching_gain_fp64"] = a["served_fp64_plain"]["jobs_per_s"] / a["sequential_fp64_plain"]["jobs_per_s"]
+    return out
 
 
 CPU_SAMPLE_STEPS = 200  # time steps of the workload in one timed CPU sample
@@ -417,20 +457,21 @@ def main():
         pj.sync()
         kt = {}
         for kind, name in ((abi.KERNEL_E, "E"), (abi.KERNEL_H, "H"), (abi.KERNEL_EDGE, "EDGE"),
-                           (abi.KERNEL_ADE, "ADE"), (abi.KERNEL_DFT, "DFT")):
+                           (abi.KERNEL_ADE, "ADE"), (abi.KERNEL_DFT, "DFT"), (abi.KERNEL_STEP, "STEP")):
             kt[name] = pj.kernel_time(kind) + (pj.kernel_cells(kind),)
+        tile = pj.tile()
         pj.close()
-        return spec, meta, jobs[warm:], ms, launches, kt, clocks
+        return spec, meta, jobs[warm:], ms, launches, kt, clocks, tile
 
     # ---- FP32 (headline) ----
-    spec32, meta, jobs32, ms32, launches, kt32, clocks = timed_jobs(abi.F32, args.steps, args.warmup)
+    spec32, meta, jobs32, ms32, launches, kt32, clocks, tile32 = timed_jobs(abi.F32, args.steps, args.warmup)
     t_step = max(ms32) if False else sum(ms32) / len(ms32)
     t_step = max_over_ranks(t_step, dev, world)
     cells = spec32.cells()
     value = aggregate_mcells(world, cells, args.nt, t_step / 1e3)
 
     # ---- FP64 plain ----
-    spec64, _, jobs64, ms64, _, kt64, _ = timed_jobs(abi.F64, args.fp64_steps, 1)
+    spec64, _, jobs64, ms64, _, kt64, _, tile64 = timed_jobs(abi.F64, args.fp64_steps, 1)
     t64 = max_over_ranks(sum(ms64) / len(ms64), dev, world)
     value64 = aggregate_mcells(world, cells, args.nt, t64 / 1e3)
 
@@ -438,20 +479,29 @@ def main():
     dft_err = dft_rel_err(jobs32[0], jobs64[0], len(spec32.monitors))
 
     # ---- roofline of the dominant kernel (FP32) ----
-    # the interior (core) E and H kernels update nearly all cells; the edge
-    # and dispersive-cell kernels run beside them as parallel graph branches
-    dom = "E" if kt32["E"][1] >= kt32["H"][1] else "H"
+    # with the fused step kernel (the tuner's usual choice here) one launch
+    # per step updates every cell but the dispersive ones, whose kernel runs
+    # beside it; otherwise the interior (core) E and H kernels update nearly
+    # all cells, with the edge and dispersive-cell kernels as parallel branches
+    if kt32["STEP"][0] > 0:
+        dom, kname, per = "STEP", "step2d_fused (TMz, FP32)", "step"
+        note = ("algorithmic bytes = grid cells x (6w+1): Ez, Hx, Hy read and written once and the material id "
+                "read; the two field sets (~0.2 GB) exceed what stays in the 129 MB L2 between steps")
+    else:
+        dom = "E" if kt32["E"][1] >= kt32["H"][1] else "H"
+        kname, per = f"{dom.lower()}2d_core<float,TM,4>", dom
+        note = ("algorithmic bytes = core cells x (4w+1) for E, 5w for H; the working set (~0.1 GB) is "
+                "L2-resident between steps (129 MB L2), so the frac can exceed 1 against HBM")
     cnt, tot, dcells = kt32[dom]
     avg_s = (tot / cnt) / 1e3
-    bpl = dcells * alg_bytes(dom, 4)
+    bpl = dcells * alg_bytes(per, 4)
     achieved = bpl / avg_s / 1e9
     peak, peak_kind = measured_peaks()
     traffic, tr_src = profile_traffic(dom)
-    roof = {"bound": "hbm", "kernel": f"{dom.lower()}2d_core<float,TM,4>", "achieved": achieved, "peak": peak,
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
             "alg_bytes_per_launch": bpl, "cells_per_launch": dcells, "avg_launch_us": avg_s * 1e6,
-            "note": "algorithmic bytes = core cells x (4w+1) for E, 5w for H; the working set (~0.1 GB) is "
-                    "L2-resident between steps (129 MB L2), so the frac can exceed 1 against HBM"}
+            "note": note}
     if tr_src:
         roof["traffic_source"] = tr_src
     step_bw = cells * alg_bytes("step", 4) / (t_step / 1e3 / args.nt) / 1e9
@@ -478,10 +528,13 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload_name(args.n, args.nt), "cells": cells, "time_steps_per_job": args.nt,
                    "bench_step": "one job of the workload from a fresh state",
-                   "launch": "CUDA graph per 32-step ring (E, H and DFT fold kernels)",
+                   "launch": ("CUDA graph per 32-step ring: the dispersive-cell and fused step kernels per step, "
+                              "the DFT fold per ring" if kt32["STEP"][0] > 0 else
+                              "CUDA graph per 32-step ring (E, H and DFT fold kernels)"),
+                   "tile": tile32,
                    "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed jobs",
                    "parallelism": f"replicas x{world}"},
-        "fp64_plain": {"value": value64, "ms_per_step": t64, "steps": len(ms64)},
+        "fp64_plain": {"value": value64, "ms_per_step": t64, "steps": len(ms64), "tile": tile64},
         "fp32_over_fp64": value / value64,
         "dft_rel_err_fp32_vs_fp64": dft_err,
         "step_bandwidth_gbs": step_bw,
@@ -496,7 +549,8 @@ def main():
     if rank == 0 and not args.no_configs:
         out["configs"] = config_runs(stream)
     if rank == 0 and args.serve_jobs > 0:
-        out["serving"] = serving_run(args.serve_jobs, args.serve_rate)
+        out["serving"] = serving_run(args.serve_jobs, [float(x) for x in args.serve_rates.split(",") if x],
+                                     args.serve_arms_jobs, args.serve_arms_rate)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_measure(args.n, 1, 5)
     if rank == 0:

@@ -205,18 +205,16 @@ struct fdtd_job {
   // bounded waits set when they give up
   TmaMaps tma{};
   bool tma_ok = false;
-  // the fused 3D step kernel (FP32): a second set of field buffers Fb, the
-  // two sets taking turns as step n and step n+1 (pp: the set that holds the
-  // current step inside fdtd_step; 0, the canonical F, between calls), and
-  // the tensor maps of each set's H arrays
+  // the fused step kernels (FP32): a second set of field buffers Fb (and of
+  // the stored split-PML parts, spb, in 2D), the two sets taking turns as
+  // step n and step n+1 (pp: the set that holds the current step inside
+  // fdtd_step; 0, the canonical F, between calls), and in 3D the tensor maps
+  // of each set's H arrays
   bool fused_ok = false;
   void *Fb[6] = {};
+  void *spb[3] = {};
   int pp = 0;
   FusedMaps fmaps[2]{};
-  // the persistent 2D step kernel: whole rings in one cooperative launch,
-  // with the grid barrier's counter
-  bool persist_ok = false;
-  unsigned *d_bar = nullptr;
   int *d_err = nullptr;
   unsigned wait_limit = kWaitLimit;  // polls of a TMA core's mbarrier wait (fdtd_debug_wait_limit)
   cudaGraph_t graph = nullptr;
@@ -564,18 +562,9 @@ int tune_tiles(fdtd_job *J);
 int setup_tma(fdtd_job *J);
 int setup_fused(fdtd_job *J);
 
-// The persistent 2D step kernel takes the samples in its H edge units (the
-// fused gather), so it needs a job without mean monitors or a TFSF box.
-// Environment FDTD_NO_PERSIST leaves it out.
-int setup_persist(fdtd_job *J) {
-  J->persist_ok = false;
-  if (J->dim != 2 || !J->gather_fused || J->has_tfbox || J->ncore <= 0 || getenv("FDTD_NO_PERSIST")) return FDTD_OK;
-  int rc;
-  if (!J->d_bar && (rc = alloc_dev(J, (void **)&J->d_bar, sizeof(unsigned)))) return rc;
-  if (!J->d_err && (rc = alloc_dev(J, (void **)&J->d_err, sizeof(int)))) return rc;
-  J->persist_ok = true;
-  return FDTD_OK;
-}
+void free_fused(fdtd_job *J);
+// the tile (0-based) that selects the fused step kernel
+int fused_tile(const fdtd_job *J) { return J->dim == 3 ? 8 : 3; }
 
 // The TFSF box: faces, and the cells its face terms touch (the box widened by
 // one cell across each face) inside the grid, the main range and the PML's
@@ -1217,12 +1206,8 @@ int commit_impl(fdtd_job *J) {
   CK(cudaStreamSynchronize(J->stream));
   if ((rc = setup_tma(J))) return rc;
   if ((rc = setup_fused(J))) return rc;
-  if ((rc = setup_persist(J))) return rc;
   if ((rc = tune_tiles<T>(J))) return rc;
-  if (J->fused_ok && J->tile != 8) {  // the tuner kept a split shape: no second set of fields
-    for (int c = 0; c < 6; ++c) { free_dev(J, J->Fb[c], (size_t)J->ncell * 4); J->Fb[c] = nullptr; }
-    J->fused_ok = false;
-  }
+  if (J->fused_ok && J->tile != fused_tile(J)) free_fused(J);  // the tuner kept a split shape
   if ((rc = kernel_flag(J))) return rc;
   J->committed = true;
   return FDTD_OK;
@@ -1284,14 +1269,43 @@ int setup_tma(fdtd_job *J) {
   return FDTD_OK;
 }
 
+// The second set of fields (and split parts) of a fused step kernel, with
+// the accounting of its bytes
+void free_fused(fdtd_job *J) {
+  const size_t bytes = (size_t)J->ncell * 4;
+  for (int c = 0; c < 6; ++c) { free_dev(J, J->Fb[c], bytes); J->Fb[c] = nullptr; }
+  for (int q = 0; q < 3; ++q) { free_dev(J, J->spb[q], bytes); J->spb[q] = nullptr; }
+  J->fused_ok = false;
+}
+
+// The fused 2D step kernel (TMz, FP32) handles every cell of the grid itself,
+// dispersive cells aside: it needs 4-cell vectors, no periodic axis, no
+// reference slabs, no TFSF box and no mean monitors (the samples are taken
+// in the kernel).  Its second set of Ez, Hx, Hy (and Ezx) is allocated here,
+// before the tuner times the kernel.
+int setup_fused2(fdtd_job *J) {
+  if (J->g.layout != FDTD_LAYOUT_2D_TM || J->esz != 4 || J->vec != 4 || J->g.periodic[0] || J->g.periodic[1] ||
+      J->slab_rows > 0 || J->has_tfbox || !J->gather_fused)
+    return FDTD_OK;
+  int rc;
+  const size_t bytes = (size_t)J->ncell * 4;
+  for (int c = 2; c <= 4; ++c)
+    if (!J->Fb[c] && (rc = alloc_dev(J, &J->Fb[c], bytes))) return rc;
+  if (J->d_sp[0] && !J->spb[0] && (rc = alloc_dev(J, &J->spb[0], bytes))) return rc;
+  J->fused_ok = true;
+  return FDTD_OK;
+}
+
 // The fused 3D step kernel needs what the TMA cores need on both sides of the
 // core box, and a grid without reference slabs or a TFSF box (their kernels
 // update fields in place).  Its second set of field buffers is allocated
 // here, before the tuner times the kernel; commit gives it back if the tuner
-// keeps another shape.  Environment FDTD_NO_FUSED leaves the kernel out.
+// keeps another shape.  Environment FDTD_NO_FUSED leaves the kernels out.
 int setup_fused(fdtd_job *J) {
   J->fused_ok = false;
-  if (!J->tma_ok || !J->tma.h_ok || J->slab_rows > 0 || J->has_tfbox || getenv("FDTD_NO_FUSED")) return FDTD_OK;
+  if (getenv("FDTD_NO_FUSED") || J->ncore <= 0) return FDTD_OK;
+  if (J->dim == 2) return setup_fused2(J);
+  if (J->dim != 3 || !J->tma_ok || !J->tma.h_ok || J->slab_rows > 0 || J->has_tfbox) return FDTD_OK;
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return FDTD_OK;
   int rc;
@@ -1311,7 +1325,7 @@ int setup_fused(fdtd_job *J) {
     void *const *F = b ? J->Fb : J->F;
     if (!make(&J->fmaps[b].hx, F[3], 128, 10) || !make(&J->fmaps[b].hy, F[4], 132, 9) ||
         !make(&J->fmaps[b].hz, F[5], 132, 10)) {
-      for (int c = 0; c < 6; ++c) { free_dev(J, J->Fb[c], bytes); J->Fb[c] = nullptr; }
+      free_fused(J);
       return FDTD_OK;  // not offered
     }
   }
@@ -1644,8 +1658,9 @@ int tune_tiles(fdtd_job *J) {
     if (J->dim == 3 && J->tile == 8 && !J->fused_ok)
       return set_err(FDTD_EINVAL, "tile 9 (the fused step kernel) needs FP32, 4-cell vectors, a core box inside the "
                                   "grid, and no reference slabs or TFSF box");
-    if (J->dim == 2 && J->tile == 3 && !J->persist_ok)
-      return set_err(FDTD_EINVAL, "2D tile 4 (the persistent step kernel) needs a job without mean monitors or a TFSF box");
+    if (J->dim == 2 && J->tile == 3 && !J->fused_ok)
+      return set_err(FDTD_EINVAL, "2D tile 4 (the fused step kernel) needs TMz, FP32, nx a multiple of 4, no periodic "
+                                  "axis, and no reference slabs, TFSF box or mean monitors");
     return FDTD_OK;
   }
   const char *off = getenv("FDTD_TUNE");
@@ -1675,16 +1690,21 @@ int tune_tiles(fdtd_job *J) {
   float best = 3.0e38f;
   int choice = 1;
   // 3D: also the z-marching kernels and, where set up, the TMA-staged cores
-  // and the fused step kernel (one launch in place of an E and an H core)
-  const int nshapes = J->dim == 3 ? (J->fused_ok ? 9 : J->tma_ok ? (J->tma.h_ok ? 8 : 7) : 6) : 3;
+  // and the fused step kernel (one launch in place of an E and an H core).
+  // 2D: also the fused step kernel, against the E and H cores alone (in a
+  // step the edge and dispersive-cell kernels run beside the cores, and
+  // their work is a small part of a grid large enough for the fused kernel)
+  const int nshapes = J->dim == 3 ? (J->fused_ok ? 9 : J->tma_ok ? (J->tma.h_ok ? 8 : 7) : 6) : J->fused_ok ? 4 : 3;
   auto cores = [&](int c) {
     if constexpr (sizeof(T) == 4) {
-      if (c == 8) {
+      if (c == fused_tile(J)) {
         StepParams<float> q = p;
         q.exo = (float *)J->Fb[0]; q.eyo = (float *)J->Fb[1]; q.ezo = (float *)J->Fb[2];
         q.hxo = (float *)J->Fb[3]; q.hyo = (float *)J->Fb[4]; q.hzo = (float *)J->Fb[5];
+        q.spo[0] = (float *)J->spb[0];
         q.pp = 1;
-        launch_step3d_fused(q, J->fmaps[0], J->stream);
+        if (J->dim == 3) launch_step3d_fused(q, J->fmaps[0], J->stream);
+        else launch_step2d_fused(q, J->stream);
         return;
       }
     }
@@ -1778,9 +1798,46 @@ int after_sample(fdtd_job *J, int n) {
   return FDTD_OK;
 }
 
-// A job steps through the fused 3D kernel when the tuner (or fdtd_set_tile)
+// A job steps through a fused step kernel when the tuner (or fdtd_set_tile)
 // chose it.  The per-procedure entry points keep the split kernels.
-bool fused_mode(const fdtd_job *J) { return J->fused_ok && J->tile == 8; }
+bool fused_mode(const fdtd_job *J) { return J->fused_ok && J->tile == fused_tile(J); }
+
+// One time step of the fused 2D path, from field set pp to the other: the
+// dispersive cells' E (E^n and H^n of the current set, E^{n+1} into the
+// other), then the fused kernel over the whole grid, which takes the samples
+// of the new fields itself.  The fused kernel follows e2d_ade with a
+// programmatic dependency and waits for it only at dispersive cells.
+int fused_step2(fdtd_job *J, int n, int slot, bool graph) {
+  const int from = J->pp, to = 1 - from;
+  float *A[6] = {}, *B[6] = {};
+  for (int c = 0; c < 6; ++c) {
+    A[c] = (float *)(from ? J->Fb[c] : J->F[c]);
+    B[c] = (float *)(to ? J->Fb[c] : J->F[c]);
+  }
+  StepParams<float> p;
+  fill_common<float>(J, p);
+  set_sources<float>(J, p);
+  p.roles = ROLE_MAIN | ROLE_PML | ROLE_ADE;
+  p.n = n;
+  p.slot = slot;
+  p.d_base = graph ? J->d_base : nullptr;
+  p.gather = 1;
+  p.pp = 1;
+  p.ez = A[2]; p.hx = A[3]; p.hy = A[4];
+  p.ezo = B[2]; p.hxo = B[3]; p.hyo = B[4];
+  p.sp[0] = (float *)(from ? J->spb[0] : J->d_sp[0]);
+  p.spo[0] = (float *)(to ? J->spb[0] : J->d_sp[0]);
+  if (!graph) ev_record(J, FDTD_KERNEL_ADE, true);
+  J->launches += launch_e2d_ade_pdl<float>(p, J->stream);
+  if (!graph) ev_record(J, FDTD_KERNEL_ADE, false);
+  if (!graph) ev_record(J, FDTD_KERNEL_STEP, true);
+  J->launches += launch_step2d_fused(p, J->stream);
+  if (!graph) ev_record(J, FDTD_KERNEL_STEP, false);
+  J->pp = to;
+  J->prog_prev = -1;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
 
 // One time step of the fused path, from field set pp to the other: the
 // general E kernel (edge units and ADE cells; E^n and H^n of the current set,
@@ -1794,6 +1851,7 @@ int fused_step(fdtd_job *J, int n, int slot, bool graph) {
     (void)n; (void)slot; (void)graph;
     return set_err(FDTD_ESTATE, "the fused step kernel is FP32 only");
   } else {
+    if (J->dim == 2) return fused_step2(J, n, slot, graph);
     const int from = J->pp, to = 1 - from;
     float *A[6], *B[6];
     for (int c = 0; c < 6; ++c) {
@@ -1841,33 +1899,11 @@ int fused_step(fdtd_job *J, int n, int slot, bool graph) {
 int fused_settle(fdtd_job *J) {
   if (!J->pp) return FDTD_OK;
   const size_t bytes = (size_t)J->ncell * 4;
-  for (int c = 0; c < 6; ++c) CK(cudaMemcpyAsync(J->F[c], J->Fb[c], bytes, cudaMemcpyDeviceToDevice, J->stream));
+  for (int c = 0; c < 6; ++c)
+    if (J->Fb[c]) CK(cudaMemcpyAsync(J->F[c], J->Fb[c], bytes, cudaMemcpyDeviceToDevice, J->stream));
+  for (int q = 0; q < 3; ++q)
+    if (J->spb[q]) CK(cudaMemcpyAsync(J->d_sp[q], J->spb[q], bytes, cudaMemcpyDeviceToDevice, J->stream));
   J->pp = 0;
-  J->prog_prev = -1;
-  return FDTD_OK;
-}
-
-// 2D jobs whose steps run in the persistent kernel (tile 4)
-bool persist_mode(const fdtd_job *J) { return J->persist_ok && J->tile == 3; }
-
-// One ring of kStageSteps steps in one launch of the persistent 2D kernel:
-// from step n (or, in a graph replay, the device-side ring base) with ring
-// slots 0..kStageSteps-1
-template <typename T>
-int persist_ring(fdtd_job *J, int n, bool graph) {
-  StepParams<T> p;
-  fill_common<T>(J, p);
-  set_sources<T>(J, p);
-  p.roles = ROLE_MAIN | ROLE_PML | ROLE_ADE;
-  p.n = n;
-  p.slot = 0;
-  p.gather = 1;
-  p.d_base = graph ? J->d_base : nullptr;
-  if (!graph) ev_record(J, FDTD_KERNEL_STEP, true);
-  const int r = launch_step2d_persistent<T>(p, J->d_bar, kStageSteps, J->stream);
-  if (!graph) ev_record(J, FDTD_KERNEL_STEP, false);
-  if (r < 0) return set_err(FDTD_ECUDA, "persistent step kernel launch: %s", cudaGetErrorString(cudaGetLastError()));
-  J->launches += r;
   J->prog_prev = -1;
   return FDTD_OK;
 }
@@ -1901,8 +1937,7 @@ int ring_graph(fdtd_job *J) {
   int bad = FDTD_OK;
   // the fused path alternates the field sets over the ring's even number of
   // steps, so a replay starts and ends with the canonical set
-  if (persist_mode(J)) bad = persist_ring<T>(J, 0, true);
-  for (int s = 0; s < kStageSteps && !bad && !persist_mode(J); ++s) {
+  for (int s = 0; s < kStageSteps && !bad; ++s) {
     if (fused_mode(J)) {
       bad = fused_step<T>(J, 0, s, true);
       continue;
@@ -2089,16 +2124,6 @@ int step_impl(fdtd_job *J, int n_first, int n_steps) {
       if ((rc = replay_ring<T>(J, n))) return rc;
       n += kStageSteps;
     }
-  }
-  // profiled runs of the persistent kernel: whole rings as eager launches,
-  // each timed by its events, then the ring's DFT fold
-  while (J->prof && persist_mode(J) && end - n >= kStageSteps) {
-    if ((rc = persist_ring<T>(J, n, false))) return rc;
-    J->stage_n0 = n;
-    J->stage_fill = kStageSteps;
-    J->last_n = n + kStageSteps - 1;
-    if ((rc = dft_fold<T>(J))) return rc;
-    n += kStageSteps;
   }
   while (n < end)
     if ((rc = eager_step<T>(J, n++))) return rc;
@@ -2994,6 +3019,10 @@ int fdtd_estimate_bytes(const fdtd_job *J, uint64_t *bytes) {
   if (J->dim == 3 && w == 4 && J->nx % 4 == 0 && !J->has_tfbox &&
       !(J->has_pml && J->pml.mode == FDTD_PML_REFERENCE))
     b += 6 * N * w;
+  // the fused 2D step kernel's: Ez, Hx, Hy and the stored PML part
+  if (J->g.layout == FDTD_LAYOUT_2D_TM && w == 4 && J->nx % 4 == 0 && !J->has_tfbox &&
+      !(J->has_pml && J->pml.mode == FDTD_PML_REFERENCE))
+    b += 4 * N * w;
   if (J->has_tfsf) b += 2 * N * w;
   if (J->has_tfbox) b += 2ull * ny * w + 4 * w;
   // dispersive cells: each region's cells, bounded per sphere / box
@@ -3094,7 +3123,7 @@ int fdtd_kernel_cells(const fdtd_job *J, int32_t kind, int64_t *cells) {
   int64_t c = 0;
   if (kind == FDTD_KERNEL_E || kind == FDTD_KERNEL_H) c = J->dim >= 2 ? (int64_t)J->ncore * J->vec : 0;
   else if (kind == FDTD_KERNEL_STEP)
-    c = fused_mode(J) ? (int64_t)J->ncore * J->vec : persist_mode(J) ? (int64_t)J->ncell * kStageSteps : 0;
+    c = !fused_mode(J) ? 0 : J->dim == 3 ? (int64_t)J->ncore * J->vec : (int64_t)J->ncell;
   else if (kind == FDTD_KERNEL_EDGE)
     c = J->dim >= 2 ? (int64_t)J->nedge * J->vec : 0;
   else if (kind == FDTD_KERNEL_ADE) c = J->dim == 2 ? J->nade : 0;

@@ -175,6 +175,8 @@ struct StepParams {
                            // 2D TM: Ezx; 2D TE: Hzx).  FP64 also stores the
                            // other parts in sp[6+q] (Exz Eyx Ezy Hxz Hyx Hzy /
                            // Ezy / Hzy); FP32 takes them as total - part.
+  T *spo[3];               // the fused 2D step: where sp[0..2] of step n+1 go
+                           // (the other buffer of a ping-pong pair)
   // reference y-slabs (2D: Ex Ey Hzx Hzy; 3D: 12 split arrays) per side
   int slab_on[2];
   int slab_j0[2];          // first 0-based row of the slab
@@ -257,11 +259,13 @@ enum K2dPart { K2D_CORE = 0, K2D_EDGE = 1, K2D_ADE = 2 };
 // prog_event: the core kernel records it as a programmatic event (or null)
 template <typename T> int launch_e2d(const StepParams<T> &p, int part, void *stream, void *prog_event = nullptr);
 
-// the persistent 2D step kernel: `nsteps` whole steps (from p.n, or *p.d_base
-// in a graph replay, ring slots from p.slot) in one cooperative launch, with a
-// grid barrier on the counter `ctr` (zeroed by the launcher before the
-// launch) after each half step.  Returns 1, or -1 when the launch failed.
-template <typename T> int launch_step2d_persistent(const StepParams<T> &p, unsigned *ctr, int nsteps, void *stream);
+// the dispersive cells' E update with a programmatic dependency on the kernel
+// before it (the first launch of a fused 2D step); returns the kernels launched
+template <typename T> int launch_e2d_ade_pdl(const StepParams<T> &p, void *stream);
+// the fused 2D step kernel (k2f.cu, TMz, FP32): E^{n+1} and H^{n+1} of every
+// cell in one pass, reading ez, hx, hy, sp[0] and storing to ezo, hxo, hyo,
+// spo[0]; returns the kernels launched
+int launch_step2d_fused(const StepParams<float> &p, void *stream);
 
 // packs of 2D jobs: one launch runs one part of every job's half step
 constexpr int kMaxPack = 32;

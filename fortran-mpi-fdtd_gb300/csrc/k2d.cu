@@ -167,8 +167,8 @@ struct K2 {
           if (do_pml) {
             // Ez = Ezx + Ezy (3D/BERpmly_mod.f90:151,153 with d/dz = 0)
             const T py = kTwoParts<T> ? ezy[q] : e0[q] - ezx[q];
-            const T nezx = f1x[q] * ezx[q] + f2x[q] * dxp[q];
-            const T nezy = f1y * py + f2y * dyp[q];
+            const T nezx = lin2(f1x[q], ezx[q], f2x[q], dxp[q]);
+            const T nezy = lin2(f1y, py, f2y, dyp[q]);
             ezx[q] = nezx;
             ezy[q] = nezy;
             e0[q] = nezx + nezy;
@@ -309,8 +309,8 @@ struct K2 {
         const T rgt = q < V - 1 ? cur[q + 1] : right;
         if (split && (i < p.slo[0] || i > p.shi[0] || shell_y)) {
           if (do_pml) {
-            h0[q] = g1y * h0[q] + g2y * (-up[q] + cur[q]);
-            h1[q] = g1x[q] * h1[q] + g2x[q] * (rgt - cur[q]);
+            h0[q] = lin2(g1y, h0[q], g2y, -up[q] + cur[q]);
+            h1[q] = lin2(g1x[q], h1[q], g2x[q], rgt - cur[q]);
             wrote = true;
           }
         } else if (do_main && main_y && i >= p.mlo[0] && i <= p.mhi[0]) {
@@ -409,15 +409,15 @@ __device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
     T curl = (p.hy[cell] - ld_x(p.hy, i - 1, j, nx, p.per[0])) +
              (-p.hx[cell] + ld_y(p.hx, i, j - 1, nx, ny, p.per[1]));
     T inc = p.ku * curl + src_sum<T>(p, n, 2, i, j, 0);
-    p.ez[cell] = ade_update<T>(p, a, am, s, 0, inc, p.ez[cell]);
+    p.ezo[cell] = ade_update<T>(p, a, am, s, 0, inc, p.ez[cell]);
   } else {
     T hzc = p.hz[cell];
     T curlhx = hzc - ld_x(p.hz, i - 1, j, nx, p.per[0]);
     T curlhy = hzc - ld_y(p.hz, i, j - 1, nx, ny, p.per[1]);
     T incx = p.ku * curlhy + src_sum<T>(p, n, 0, i, j, 0);
     T incy = -(p.ku * curlhx) + src_sum<T>(p, n, 1, i, j, 0);
-    p.ex[cell] = ade_update<T>(p, a, am, s, 0, incx, p.ex[cell]);
-    p.ey[cell] = ade_update<T>(p, a, am, s, 1, incy, p.ey[cell]);
+    p.exo[cell] = ade_update<T>(p, a, am, s, 0, incx, p.ex[cell]);
+    p.eyo[cell] = ade_update<T>(p, a, am, s, 1, incy, p.ey[cell]);
   }
 }
 
@@ -579,9 +579,13 @@ __global__ void __launch_bounds__(256) h2d_edge(const __grid_constant__ StepPara
   K2<T, L, V>::unit_h(p, __ldg(p.edge_units + t), step_n(p));
 }
 
+// The fused 2D step kernel follows this one with a programmatic dependency
+// and waits for it only where it meets a dispersive cell: it may start once
+// every block here has passed its own wait (and with it, the previous step).
 template <typename T, int L>
 __global__ void __launch_bounds__(256) e2d_ade(const __grid_constant__ StepParams<T> p) {
   pdl_wait();
+  pdl_release();
   const int s = blockIdx.x * 256 + threadIdx.x;
   if (s < p.nade) ade_e2<T, L>(p, s, step_n(p));
 }
@@ -621,6 +625,15 @@ int launch_e2d(const StepParams<T> &p, int part, void *stream, void *prog_event)
 }
 
 template <typename T>
+int launch_e2d_ade_pdl(const StepParams<T> &p, void *stream) {
+  if (p.nade <= 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p.layout == 3) launch_pdl(e2d_ade<T, 3>, (p.nade + 255) / 256, 256, s, p);
+  else launch_pdl(e2d_ade<T, 2>, (p.nade + 255) / 256, 256, s, p);
+  return 1;
+}
+
+template <typename T>
 int launch_h2d(const StepParams<T> &p, int part, void *stream, void *prog_event) {
   constexpr int VW = sizeof(T) == 4 ? 4 : 2;
   cudaStream_t s = (cudaStream_t)stream;
@@ -629,134 +642,6 @@ int launch_h2d(const StepParams<T> &p, int part, void *stream, void *prog_event)
     return p.vec == VW ? launch_h2d_v<T, 3, VW>(p, part, s, ev) : launch_h2d_v<T, 3, 1>(p, part, s, ev);
   return p.vec == VW ? launch_h2d_v<T, 2, VW>(p, part, s, ev) : launch_h2d_v<T, 2, 1>(p, part, s, ev);
 }
-
-// ---- persistent step kernel: whole rings of steps in one launch --------------
-// One cooperative launch (every block resident at once) runs `nsteps` steps.
-// Each half step is the same units as the split launches -- core units, edge
-// units, dispersive cells -- taken by the blocks in grid-stride order; a grid
-// barrier ends each half step.  The units of a half step write disjoint
-// cells and read only the other half's fields, as for the parallel branches
-// of the split path, so the order in which blocks take them does not matter
-// and every cell gets the split path's value bit for bit.  The barrier is a
-// counter in device memory (zeroed before the launch) that each block
-// increments once per barrier and then polls until all blocks have arrived;
-// its polls are bounded: a block that gives up sets the job's error flag and
-// returns, and so, in turn, do the others.
-constexpr int kPThreads = 512;
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *a) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
-  return v;
-}
-
-// all blocks of the grid past this point, or false (every thread) when the
-// wait gave up
-__device__ __forceinline__ bool grid_barrier(unsigned *ctr, unsigned target, unsigned limit, int *err) {
-  __shared__ int gave_up;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    gave_up = 0;
-    __threadfence();  // this block's stores before its arrival
-    atomicAdd(ctr, 1u);
-    for (unsigned it = 0; ld_acquire_u32(ctr) < target; ++it) {
-      if (it >= limit) {
-        gave_up = 1;
-        atomicExch(err, 1);
-        break;
-      }
-      __nanosleep(64);
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return !gave_up;
-}
-
-// the edge and dispersive-cell units, kept out of line: their register needs
-// would otherwise set the whole kernel's, and with it how many warps the core
-// units (nearly all of the work) run with
-template <typename T, int L, int V>
-__device__ __noinline__ void persist_edge_e(const StepParams<T> &p, int unit, int n) { K2<T, L, V>::unit_e(p, unit, n); }
-template <typename T, int L, int V>
-__device__ __noinline__ void persist_edge_h(const StepParams<T> &p, int unit, int n) { K2<T, L, V>::unit_h(p, unit, n); }
-template <typename T, int L>
-__device__ __noinline__ void persist_ade(const StepParams<T> &p, int s, int n) { ade_e2<T, L>(p, s, n); }
-
-template <typename T, int L, int V>
-__global__ void __launch_bounds__(kPThreads, 2) step2d_persistent(const __grid_constant__ StepParams<T> p, unsigned *ctr,
-                                                                int nsteps) {
-  // the job's parameters with this step's number and ring slot, in shared
-  // memory (the unit functions read p.slot and the step number)
-  static_assert(sizeof(StepParams<T>) % 8 == 0, "StepParams is copied in 8-byte words");
-  __shared__ unsigned long long sm[sizeof(StepParams<T>) / 8];
-  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&p);
-  for (int w = threadIdx.x; w < (int)(sizeof(StepParams<T>) / 8); w += blockDim.x) sm[w] = src[w];
-  StepParams<T> &ps = *reinterpret_cast<StepParams<T> *>(sm);
-  const int n0 = p.d_base ? *p.d_base : p.n;
-  const int nthr = gridDim.x * kPThreads, tid = blockIdx.x * kPThreads + threadIdx.x;
-  unsigned target = 0;
-  for (int s = 0; s < nsteps; ++s) {
-    const int n = n0 + s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      ps.slot = p.slot + s;
-      ps.n = n;
-      ps.d_base = nullptr;
-    }
-    __syncthreads();
-    for (int t = tid; t < ps.ncore; t += nthr) core_e<T, L, V>(ps, ps.cy0 + t / ps.cw, (ps.cv0 + t % ps.cw) * V);
-    for (int t = tid; t < ps.nedge; t += nthr) persist_edge_e<T, L, V>(ps, __ldg(ps.edge_units + t), n);
-    for (int t = tid; t < ps.nade; t += nthr) persist_ade<T, L>(ps, t, n);
-    target += gridDim.x;
-    if (!grid_barrier(ctr, target, p.wait_limit, p.err)) return;
-    for (int t = tid; t < ps.ncore; t += nthr) core_h<T, L, V>(ps, ps.cy0 + t / ps.cw, (ps.cv0 + t % ps.cw) * V);
-    for (int t = tid; t < ps.nedge; t += nthr) persist_edge_h<T, L, V>(ps, __ldg(ps.edge_units + t), n);
-    target += gridDim.x;
-    if (!grid_barrier(ctr, target, p.wait_limit, p.err)) return;
-  }
-}
-
-template <typename T, int L, int V>
-int launch_persist_v(const StepParams<T> &p, unsigned *ctr, int nsteps, cudaStream_t s) {
-  auto kern = step2d_persistent<T, L, V>;
-  static int per_sm = [&] {
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kPThreads, 0) != cudaSuccess) b = 0;
-    return b;
-  }();
-  static int nsm = [] {
-    int d = 0, c = 0;
-    if (cudaGetDevice(&d) != cudaSuccess || cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, d) != cudaSuccess)
-      c = 0;
-    return c;
-  }();
-  if (per_sm <= 0 || nsm <= 0) return -1;
-  if (cudaMemsetAsync(ctr, 0, sizeof(unsigned), s) != cudaSuccess) return -1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(per_sm * nsm);
-  cfg.blockDim = dim3(kPThreads);
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeCooperative;
-  at[0].val.cooperative = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, kern, p, ctr, nsteps) != cudaSuccess) return -1;
-  return 1;
-}
-
-template <typename T>
-int launch_step2d_persistent(const StepParams<T> &p, unsigned *ctr, int nsteps, void *stream) {
-  constexpr int VW = sizeof(T) == 4 ? 4 : 2;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (p.layout == 3)
-    return p.vec == VW ? launch_persist_v<T, 3, VW>(p, ctr, nsteps, s) : launch_persist_v<T, 3, 1>(p, ctr, nsteps, s);
-  return p.vec == VW ? launch_persist_v<T, 2, VW>(p, ctr, nsteps, s) : launch_persist_v<T, 2, 1>(p, ctr, nsteps, s);
-}
-
-template int launch_step2d_persistent<float>(const StepParams<float> &, unsigned *, int, void *);
-template int launch_step2d_persistent<double>(const StepParams<double> &, unsigned *, int, void *);
 
 // ---- packs: one launch runs the same part of many jobs' half steps ---------
 // Block b belongs to the job q with bstart[q] <= b < bstart[q+1]; the job's
@@ -860,5 +745,7 @@ template int launch_e2d<float>(const StepParams<float> &, int, void *, void *);
 template int launch_e2d<double>(const StepParams<double> &, int, void *, void *);
 template int launch_h2d<float>(const StepParams<float> &, int, void *, void *);
 template int launch_h2d<double>(const StepParams<double> &, int, void *, void *);
+template int launch_e2d_ade_pdl<float>(const StepParams<float> &, void *);
+template int launch_e2d_ade_pdl<double>(const StepParams<double> &, void *);
 
 }  // namespace fdtd

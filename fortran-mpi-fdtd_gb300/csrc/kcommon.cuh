@@ -20,6 +20,16 @@ constexpr bool kTwoParts = sizeof(T) == 8;
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// a*b + c*d with one fixed rounding: a*b fused into the add, c*d rounded
+// first.  Left to the compiler, the contraction of a sum of two products may
+// fuse either one, and differently in different kernels; the split-field PML
+// updates use this form wherever two kernels compute the same cell, so that
+// their results agree bit for bit.
+__device__ __forceinline__ float lin2(float a, float b, float c, float d) { return __fmaf_rn(a, b, __fmul_rn(c, d)); }
+__device__ __forceinline__ double lin2(double a, double b, double c, double d) {
+  return __fma_rn(a, b, __dmul_rn(c, d));
+}
+
 // launch a step kernel with a programmatic dependency on the kernel before it
 // on the stream (the kernel starts with pdl_wait).  With `ev`, the launch also
 // records ev as a programmatic event that fires once every block has started:

@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB_DIR = os.path.join(PKG, "lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB = os.path.join(LIB_DIR, "libfdtd_gb300.so")
-SOURCES = ["fdtd_api.cu", "fdtd_server.cu", "k2d.cu", "k3d.cu", "k3f.cu", "k1d.cu", "kdft.cu", "knoalloc.cu", "ktfsf.cu", "kcheck.cu"]
+SOURCES = ["fdtd_api.cu", "fdtd_server.cu", "k2d.cu", "k3d.cu", "k3f.cu", "k2f.cu", "k1d.cu", "kdft.cu", "knoalloc.cu", "ktfsf.cu", "kcheck.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -36,9 +36,12 @@ def main(argv=None):
     J.profile(True)
     J.step(1, a.steps)
     J.sync()
-    kinds = {"E": abi.KERNEL_E, "H": abi.KERNEL_H, "EDGE": abi.KERNEL_EDGE}
+    kinds = {"E": abi.KERNEL_E, "H": abi.KERNEL_H, "EDGE": abi.KERNEL_EDGE, "ADE": abi.KERNEL_ADE,
+             "STEP": abi.KERNEL_STEP, "DFT": abi.KERNEL_DFT}
     out = {k: dict(zip(("launches", "ms"), J.kernel_time(v))) for k, v in kinds.items()}
-    print(json.dumps(dict(case=a.case, n=a.n, tile=J.tile(), core_cells=J.kernel_cells(abi.KERNEL_E), kernels=out)))
+    print(json.dumps(dict(case=a.case, n=a.n, tile=J.tile(), core_cells=J.kernel_cells(abi.KERNEL_E),
+                          edge_cells=J.kernel_cells(abi.KERNEL_EDGE), step_cells=J.kernel_cells(abi.KERNEL_STEP),
+                          kernels=out)))
     J.close()
 
 

@@ -439,7 +439,8 @@ int fdtd_estimate_bytes(const fdtd_job *job, uint64_t *bytes);
  * of the main range and rows with sources, monitors or reference slabs (in
  * 3D with the fused step kernel: the general E and H kernels);
  * FDTD_KERNEL_ADE: the 2D dispersive-cell kernel; FDTD_KERNEL_STEP: the
- * fused 3D step kernel (E and H of the core box in one launch). */
+ * fused step kernels (3D: E and H of the core box in one launch; 2D: E and
+ * H of the whole grid, dispersive cells aside, in one launch). */
 enum { FDTD_KERNEL_E = 0, FDTD_KERNEL_H = 1, FDTD_KERNEL_DFT = 2, FDTD_KERNEL_LINE1D = 3,
        FDTD_KERNEL_EDGE = 4, FDTD_KERNEL_ADE = 5, FDTD_KERNEL_STEP = 6, FDTD_KERNEL_COUNT = 7 };
 int fdtd_profile(fdtd_job *job, int32_t enable);
@@ -448,10 +449,11 @@ int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms)
  * (the default) lets commit time the candidates on the job's own grid and
  * keep the fastest (cached per kind of grid; environment FDTD_TUNE=0 skips
  * the timing); 1..3 pins a candidate: 2D 128 / 256 / 512 threads per block
- * (2D 4: the persistent step kernel, which runs each ring of 32 steps in one
- * cooperative launch with a grid barrier after each half step, for jobs
- * without mean monitors or a TFSF box; environment FDTD_NO_PERSIST leaves it
- * out),
+ * (2D 4: the fused step kernel, which takes Ez, Hx and Hy of every cell
+ * from step n to n+1 in one pass over two sets of field buffers used in
+ * turn, for TMz FP32 jobs with nx a multiple of 4, no periodic axis and no
+ * reference slabs, TFSF box or mean monitors; the job then holds a second
+ * copy of its fields and of the stored PML part),
  * 3D 4 / 8 / 16 rows of 32 x-vectors, one plane per thread; 3D also 4..6:
  * the same shapes with each thread walking 8 planes and keeping the
  * neighbour plane in registers.  FP32 with 4-cell vectors, where the core
@@ -463,7 +465,7 @@ int fdtd_kernel_time(fdtd_job *job, int32_t kind, int64_t *launches, double *ms)
  * two sets of field buffers used in turn (the job then holds a second copy
  * of its six field arrays); pinning one elsewhere fails at commit with
  * FDTD_EINVAL.  Results do not depend on the shape.  Environment FDTD_NO_TMA
- * leaves the TMA-staged kernels out, FDTD_NO_FUSED the fused one.
+ * leaves the TMA-staged kernels out, FDTD_NO_FUSED the fused ones.
  * fdtd_get_tile returns the shape in use (0: the job has no core kernels). */
 int fdtd_set_tile(fdtd_job *job, int32_t tile);
 int fdtd_get_tile(const fdtd_job *job, int32_t *tile);

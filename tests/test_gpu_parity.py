@@ -4,6 +4,7 @@ against the reference's own shipped 2D outputs.
 FP64 plain path: relative L2 <= 1e-10 on fields, DFT sums and spectra.
 FP32 path: DFT spectra relative L2 <= 1e-4 against the FP64 oracle.
 """
+import math
 import os
 
 import numpy as np
@@ -34,13 +35,16 @@ def check_state(J, O, comps, tol=TOL64, per_comp=1e-8):
     """A field snapshot is the whole state vector (all components): its
     relative L2 must be <= tol.  Each component on its own must be within
     per_comp (a component far smaller than the others, e.g. Hx under x
-    polarisation, carries rounding noise of the dominant ones)."""
+    polarisation, carries rounding noise of the dominant ones: per_comp=None
+    checks the whole state only)."""
     a = [J.get_field(c) for c in comps]
     b = [O.get_field(c) for c in comps]
     assert any(np.any(x) for x in b), "the oracle's state is all zeros: nothing was driven"
     tot = rel_l2(np.concatenate([x.ravel() for x in a]), np.concatenate([x.ravel() for x in b]))
     assert tot <= tol, f"state rel L2 {tot:.3e}"
     for c, x, y in zip(comps, a, b):
+        if per_comp is None:
+            break
         e = rel_l2(x, y)
         assert e <= per_comp, f"component {c}: rel L2 {e:.3e}"
 
@@ -181,7 +185,8 @@ def test_3d_reference_vs_oracle(gpu, oracle_lib):
     coupling (only Exy/Ezy are copied back to the main grid,
     3D/BERpmly_mod.f90:200-278) amplifies the last-bit differences that the
     E-form dielectric and gold updates make by design.  The slab rows are
-    held to 1e-7 of the field's norm at Nt."""
+    held to 1e-7 of the state's norm at Nt (and each driven component to
+    1e-7 of its own)."""
     spec, meta = problems.reference_3d()
     assert meta["Nt"] == 13696
     J = gpu.Job(spec)
@@ -190,9 +195,12 @@ def test_3d_reference_vs_oracle(gpu, oracle_lib):
     mid = 4500
     J.step(1, mid)
     O.step(1, mid)
-    check_state(J, O, comps)
     # the strip is uniform along z and the source is Ex: the fields are Ex,
-    # Ey and Hz; Ez, Hx and Hy stay exactly zero in both
+    # Ey and Hz, each held to 1e-8 on its own; Ez, Hx and Hy carry only the
+    # rounding noise of those, far below them, which the whole-state
+    # tolerance holds
+    check_state(J, O, comps, per_comp=None)  # whole state <= 1e-10
+    check_state(J, O, (abi.EX, abi.EY, abi.HZ))
     npml, ny = 10, meta["ny"]
     si_lo = spec.materials[3].region["lo"][1]  # first row of the Si substrate (0-based)
     for c in (abi.EX, abi.EY, abi.HZ):
@@ -205,11 +213,16 @@ def test_3d_reference_vs_oracle(gpu, oracle_lib):
     a = np.concatenate([J.get_field(c)[:, npml:ny - npml, :].ravel() for c in comps])
     b = np.concatenate([O.get_field(c)[:, npml:ny - npml, :].ravel() for c in comps])
     assert rel_l2(a, b) <= TOL64
-    for c in comps:
-        x, y = J.get_field(c), O.get_field(c)
-        ny_ = np.linalg.norm(y)
-        for rows in (slice(0, npml), slice(ny - npml, ny)):
-            assert np.linalg.norm((x - y)[:, rows, :]) <= 1e-7 * max(ny_, 1e-300), (c, rows)
+    # the slab rows: the state's difference there to 1e-7 of the state's
+    # norm, and each driven component's to 1e-7 of its own norm
+    fj = {c: J.get_field(c) for c in comps}
+    fo = {c: O.get_field(c) for c in comps}
+    state = math.sqrt(sum(float(np.sum(fo[c] ** 2)) for c in comps))
+    for rows in (slice(0, npml), slice(ny - npml, ny)):
+        d = math.sqrt(sum(float(np.sum((fj[c] - fo[c])[:, rows, :] ** 2)) for c in comps))
+        assert d <= 1e-7 * state, (rows, d, state)
+        for c in (abi.EX, abi.EY, abi.HZ):
+            assert np.linalg.norm((fj[c] - fo[c])[:, rows, :]) <= 1e-7 * np.linalg.norm(fo[c]), (c, rows)
     assert _dft_err(J, O, 3, live=(0, 1, 2)) <= TOL64
     for q in range(3):
         p = O.get_probe(q)
@@ -329,7 +342,7 @@ def test_core_block_shapes_give_identical_results(gpu, dim):
     ref = None
     # 3D 4..6: z-marching kernels; 7: the TMA-staged E core (FP32, core box inside the grid)
     # 3D 8: the TMA-staged E and H cores; 9: the fused step kernel (ping-pong field sets)
-    # 2D 4: the persistent step kernel (whole rings in one cooperative launch)
+    # 2D 4: the fused step kernel (ping-pong field sets, the whole grid in one launch)
     for tile in ((1, 2, 3, 4) if dim == 2 else (1, 2, 3, 4, 5, 6, 7, 8, 9)):
         J = gpu.Job(spec, tile=tile)
         assert J.tile() == tile
@@ -404,6 +417,43 @@ def test_fused_step_across_calls_rings_and_procedures(gpu):
         for x, y in zip(J.get_monitor(q), ref.get_monitor(q)):
             np.testing.assert_array_equal(x, y)
     np.testing.assert_array_equal(J.get_probe(0), ref.get_probe(0))
+
+
+def test_fused_2d_step_across_calls_and_procedures(gpu):
+    """The fused 2D step kernel alternates two sets of fields (and of the
+    stored PML part).  Calls of any length -- odd numbers of eager steps
+    around graph rings, single steps, the per-procedure entry points (which
+    keep the split kernels) in between -- must leave the state where the
+    other entry points find it: the run equals the split kernels' single
+    call bit for bit, for the fields, the spectra and a probe.  The grid has
+    gold cylinders (the dispersive-cell kernel beside the fused one), the
+    split PML on all faces, a source row and monitor rows, and its 384-cell
+    rows end in a partly filled strip of the kernel's 124-cell strips."""
+    spec, _ = problems.config_2d_tmz(precision=abi.F32, n=384, ncyl=8, nfreq=8)
+    spec.add_probe((200, 150, 0), (abi.EZ, abi.HX, abi.HY))
+    comps = (abi.EZ, abi.HX, abi.HY)
+    ref = gpu.Job(spec, tile=2)
+    ref.step(1, 400)
+    J = gpu.Job(spec, tile=4)
+    assert J.tile() == 4
+    n = 1
+    for k in (45, 1, 77, 3, 101):
+        J.step(n, k)
+        n += k
+    for n in range(n, n + 3):
+        J.step_procedures(n)
+    n += 1
+    J.step(n, 401 - n)
+    for c in comps:
+        g = J.get_field(c)
+        assert np.any(g), f"component {c} is zero"
+        np.testing.assert_array_equal(g, ref.get_field(c), err_msg=f"component {c}")
+    for q in range(len(spec.monitors)):
+        for x, y in zip(J.get_monitor(q), ref.get_monitor(q)):
+            np.testing.assert_array_equal(x, y)
+    p = J.get_probe(0)
+    assert np.any(p)
+    np.testing.assert_array_equal(p, ref.get_probe(0))
 
 
 @pytest.fixture(scope="module")
