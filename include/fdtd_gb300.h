@@ -403,8 +403,9 @@ int fdtd_load_state(fdtd_job *job, const void *buf, uint64_t bytes);
  * FDTD_ENOMEM at every allocation of set-up and stepping. */
 int fdtd_check_finite(fdtd_job *job, int64_t *count);
 int fdtd_debug_fail_alloc(int32_t after);
-/* fdtd_debug_wait_limit sets how many polls the TMA-staged 3D core kernels
- * make of a copy's mbarrier before they give up on it (rounds < 0: the
+/* fdtd_debug_wait_limit sets how many polls the TMA-staged 3D kernels (the
+ * core kernels of tiles 7 and 8, and the fused step kernel of tile 9) make of
+ * a copy's mbarrier before they give up on it (rounds < 0: the
  * default, 2^22).  With 0 every wait of the main loop gives up at once: the
  * kernel sets the job's error flag, lets the copies it issued land, and
  * returns, and the next fdtd_sync reports FDTD_ECUDA (once).  It lets a

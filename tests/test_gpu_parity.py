@@ -970,14 +970,17 @@ def test_checkpoint_from_another_job_is_refused(gpu):
     ja.close()
 
 
-def test_tma_wait_give_up_is_reported_and_recovered(gpu):
-    """The TMA cores' bounded waits, made to run out at once (a wait limit
-    of 0 polls) while every copy still lands: the kernels set the job's flag,
-    let their copies land and return; fdtd_sync reports FDTD_ECUDA once, the
-    context stays usable, and with the default limit the job then steps
-    without error, and a fresh job gives the plain cores' fields."""
+@pytest.mark.parametrize("tile", [8, 9])
+def test_tma_wait_give_up_is_reported_and_recovered(gpu, tile):
+    """The bounded waits of the TMA-staged kernels (tile 8: the E and H
+    cores; tile 9: the fused step kernel), made to run out at once (a wait
+    limit of 0 polls) while every copy still lands: the kernels set the
+    job's flag, let their copies land and return; fdtd_sync reports
+    FDTD_ECUDA once, the context stays usable, and with the default limit
+    the job then steps without error, and a fresh job gives the plain
+    cores' fields."""
     spec, _ = problems.config_3d_sphere(precision=abi.F32, n=96, nfreq=4, npml=8, radius=40.0, half=20)
-    J = gpu.Job(spec, tile=8)
+    J = gpu.Job(spec, tile=tile)
     J.debug_wait_limit(0)
     J.step(1, 3)
     with pytest.raises(gpu.FdtdError) as e:
@@ -988,7 +991,7 @@ def test_tma_wait_give_up_is_reported_and_recovered(gpu):
     J.step(4, 40)
     J.sync()
     J.close()
-    a, b = gpu.Job(spec, tile=8), gpu.Job(spec, tile=2)
+    a, b = gpu.Job(spec, tile=tile), gpu.Job(spec, tile=2)
     a.step(1, 40)
     b.step(1, 40)
     for c in (abi.EX, abi.HY):
