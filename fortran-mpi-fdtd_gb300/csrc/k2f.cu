@@ -33,10 +33,42 @@
 namespace fdtd {
 
 constexpr int kGOwn = 31;     // x-vectors a warp stores (lane 31: the neighbour's first)
-constexpr int kGRows = 4;     // rows a warp marches
+constexpr int kGRows = 8;     // rows a warp marches
 constexpr int kGWarps = 4;    // warps of a block: consecutive row groups of one strip
 constexpr int kGThreads = 32 * kGWarps;
+constexpr int kGAhead = 3;    // rows in flight beyond the row whose Ez^{n+1} is formed
+constexpr int kGSlots = kGAhead + 1;
 constexpr unsigned kFull = 0xffffffffu;
+
+// A warp's rows travel through a ring of shared-memory slots, filled by
+// asynchronous copies (cp.async) kGAhead rows ahead of their use, so that a
+// warp keeps several rows of loads in flight without holding them in
+// registers.  Each thread copies, and later reads, only its own vector.
+struct RowSlot {
+  float4 ez[32], hx[32], hy[32], ezx[32];
+  unsigned id[32];
+  float hyl, pad[3];
+};
+struct WarpRing {
+  RowSlot s[kGSlots];
+  float4 below[32];  // Hx of the row below the warp's first row
+};
+
+__device__ __forceinline__ void cp16(void *dst, const void *src, bool in) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(__cvta_generic_to_global(src)),
+               "r"(in ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp4(void *dst, const void *src, bool in) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(__cvta_generic_to_global(src)),
+               "r"(in ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// every group but the newest kGAhead - 1 has landed
+__device__ __forceinline__ void cp_wait_ahead() { asm volatile("cp.async.wait_group %0;" ::"n"(kGAhead - 1) : "memory"); }
 
 // one row of a thread's x-vector at step n, as loaded
 struct Row2 {
@@ -51,24 +83,43 @@ struct Row2 {
 
 __device__ __forceinline__ int id_of(unsigned ids, int q) { return (ids >> (8 * q)) & 0xffu; }
 
-__device__ __forceinline__ void load_row(const StepParams<float> &p, int j, int i0, int lane, Row2 &r) {
-#pragma unroll
-  for (int q = 0; q < 4; ++q) r.ez[q] = r.hx[q] = r.hy[q] = r.ezx[q] = 0.f;
-  r.hyl = 0.f;
-  r.id = 0;
-  r.rf = 0;
-  r.shell = false;
-  r.in = j < p.ny && i0 < p.nx;
-  if (!r.in) return;
-  const long long c = (long long)j * p.nx + i0;
-  vld_ro<float, 4>(p.ez + c, r.ez);
-  vld_ro<float, 4>(p.hx + c, r.hx);
-  vld_ro<float, 4>(p.hy + c, r.hy);
-  r.id = __ldg(reinterpret_cast<const unsigned *>(p.mat + c));
-  r.rf = __ldg(p.rowflag + j);
-  if (lane == 0 && i0 > 0) r.hyl = __ldg(p.hy + c - 1);
-  r.shell = p.pml_mode == 2 && (i0 < p.slo[0] || i0 + 3 > p.shi[0] || j < p.slo[1] || j > p.shi[1]);
-  if (r.shell) vld_ro<float, 4>(p.sp[0] + c, r.ezx);
+__device__ __forceinline__ bool row_in(const StepParams<float> &p, int j, int i0) { return j < p.ny && i0 < p.nx; }
+__device__ __forceinline__ bool vec_shell(const StepParams<float> &p, int j, int i0) {
+  return p.pml_mode == 2 && (i0 < p.slo[0] || i0 + 3 > p.shi[0] || j < p.slo[1] || j > p.shi[1]);
+}
+
+// queue the copies of row j of the thread's vector into a ring slot (zeros
+// for a vector outside the grid)
+__device__ __forceinline__ void issue_row(const StepParams<float> &p, RowSlot &sl, int j, int i0, int lane) {
+  const bool in = row_in(p, j, i0);
+  const long long c = in ? (long long)j * p.nx + i0 : 0;
+  cp16(&sl.ez[lane], p.ez + c, in);
+  cp16(&sl.hx[lane], p.hx + c, in);
+  cp16(&sl.hy[lane], p.hy + c, in);
+  cp4(&sl.id[lane], p.mat + c, in);
+  const bool sh = in && vec_shell(p, j, i0);
+  if (p.pml_mode == 2) cp16(&sl.ezx[lane], sh ? p.sp[0] + c : p.ez, sh);
+  if (lane == 0) cp4(&sl.hyl, in && i0 > 0 ? p.hy + c - 1 : p.hy, in && i0 > 0);
+}
+
+// row j of the thread's vector from its ring slot, once its copies landed
+__device__ __forceinline__ void read_row(const StepParams<float> &p, const RowSlot &sl, int j, int i0, int lane,
+                                         Row2 &r) {
+  const float4 ez = sl.ez[lane], hx = sl.hx[lane], hy = sl.hy[lane];
+  r.ez[0] = ez.x; r.ez[1] = ez.y; r.ez[2] = ez.z; r.ez[3] = ez.w;
+  r.hx[0] = hx.x; r.hx[1] = hx.y; r.hx[2] = hx.z; r.hx[3] = hx.w;
+  r.hy[0] = hy.x; r.hy[1] = hy.y; r.hy[2] = hy.z; r.hy[3] = hy.w;
+  r.in = row_in(p, j, i0);
+  r.shell = r.in && vec_shell(p, j, i0);
+  if (r.shell) {
+    const float4 x = sl.ezx[lane];
+    r.ezx[0] = x.x; r.ezx[1] = x.y; r.ezx[2] = x.z; r.ezx[3] = x.w;
+  } else {
+    r.ezx[0] = r.ezx[1] = r.ezx[2] = r.ezx[3] = 0.f;
+  }
+  r.id = sl.id[lane];
+  r.hyl = lane == 0 ? sl.hyl : 0.f;
+  r.rf = r.in ? __ldg(p.rowflag + j) : 0;
 }
 
 // e plus the cell's source terms
@@ -243,25 +294,40 @@ __global__ void __launch_bounds__(kGThreads) step2d_fused(const __grid_constant_
   const int i0 = (strip * kGOwn + lane) * 4;
   const bool own_x = lane < kGOwn && i0 < p.nx;
   const int n = step_n(p);
+  __shared__ __align__(16) WarpRing rings[kGWarps];
+  WarpRing &rg = rings[w];
   if (j0 < p.ny) {
-    const int jend = min(j0 + kGRows, p.ny);  // rows j0..jend-1 are stored
-    float below[4] = {};
-    if (j0 > 0 && i0 < p.nx) vld_ro<float, 4>(p.hx + (long long)(j0 - 1) * p.nx + i0, below);
-    // the row of this round, the row above (its Ez^{n+1} is formed this
-    // round) and the row after that, loaded a round ahead
-    Row2 cur, nxt, pre{};
-    load_row(p, j0, i0, lane, cur);
-    load_row(p, j0 + 1, i0, lane, nxt);
+    const int jend = min(j0 + kGRows, p.ny);  // rows j0..jend-1 are stored; row jend is the row above
+    // copy group g holds row j0 + g (group 0 also the row below j0); every
+    // round commits one group, empty past row jend, so that the count of
+    // groups in flight is the same in every round
+    cp16(&rg.below[lane], j0 > 0 && i0 < p.nx ? p.hx + (long long)(j0 - 1) * p.nx + i0 : p.hx, j0 > 0 && i0 < p.nx);
+#pragma unroll
+    for (int g = 0; g < kGAhead; ++g) {
+      if (j0 + g <= jend) issue_row(p, rg.s[g], j0 + g, i0, lane);
+      cp_commit();
+    }
+    cp_wait_ahead();
+    Row2 cur, nxt;
+    read_row(p, rg.s[0], j0, i0, lane, cur);
+    float below[4];
+    {
+      const float4 b = rg.below[lane];
+      below[0] = b.x; below[1] = b.y; below[2] = b.z; below[3] = b.w;
+    }
     float ec[4], xc[4];
     ez_new(p, cur, below, j0, i0, lane, n, ec, xc);
 #pragma unroll 1
-    for (int j = j0; j < jend; ++j) {
-      if (j + 2 <= jend) load_row(p, j + 2, i0, lane, pre);
+    for (int t = 0; j0 + t < jend; ++t) {
+      const int j = j0 + t;
+      if (j + kGAhead <= jend) issue_row(p, rg.s[(t + kGAhead) % kGSlots], j + kGAhead, i0, lane);
+      cp_commit();
+      cp_wait_ahead();  // rows up to j + 1 have landed
+      read_row(p, rg.s[(t + 1) % kGSlots], j + 1, i0, lane, nxt);
       float en[4], xn[4];
       ez_new(p, nxt, cur.hx, j + 1, i0, lane, n, en, xn);
       h_row(p, cur, ec, en, xc, j, i0, own_x, n);
       cur = nxt;
-      nxt = pre;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         ec[q] = en[q];
@@ -269,6 +335,8 @@ __global__ void __launch_bounds__(kGThreads) step2d_fused(const __grid_constant_
       }
     }
   }
+  // no copy may still be in flight into shared memory when the block exits
+  asm volatile("cp.async.wait_all;" ::: "memory");
   // complete only after e2d_ade: the kernels after this one wait for this one
   pdl_wait();
 }
