@@ -456,6 +456,24 @@ def test_fused_2d_step_across_calls_and_procedures(gpu):
     np.testing.assert_array_equal(p, ref.get_probe(0))
 
 
+def test_fused_2d_large_grid_equals_split(gpu):
+    """The fused 2D step kernel where the tuner picks it: a 4096^2 grid of
+    the bench's workload (34 strips of 124 cells, the last partly filled, 512 marches of 8 rows per
+    strip, every dispersive cell of 40 cylinders), 96 steps -- three graph
+    rings -- against the split path, bit for bit."""
+    spec, _ = problems.config_2d_tmz(precision=abi.F32, n=4096, nfreq=8)
+    a, b = gpu.Job(spec, tile=4), gpu.Job(spec, tile=2)
+    a.step(1, 96)
+    b.step(1, 96)
+    for c in (abi.EZ, abi.HX, abi.HY):
+        x = a.get_field(c)
+        assert np.any(x), f"component {c} is zero"
+        np.testing.assert_array_equal(x, b.get_field(c), err_msg=f"component {c}")
+    for q in range(len(spec.monitors)):
+        for x, y in zip(a.get_monitor(q), b.get_monitor(q)):
+            np.testing.assert_array_equal(x, y)
+
+
 @pytest.fixture(scope="module")
 def bench2d_oracle(oracle_lib):
     """The FP64 oracle on the bench's whole 2D workload: 2048^2 cells, 40
