@@ -188,6 +188,22 @@ def dft_rel_err(ja, jb, nmon):
     return math.sqrt(num / den) if den > 0 else float("nan")
 
 
+def pml_cells_by_axes(spec):
+    """Cells of a split-PML grid inside the PML of exactly one axis, and of
+    two or three."""
+    npml = (spec.pml or {}).get("npml", ((0, 0),) * 3)
+    inside, outside = [], []
+    for a in range(3):
+        n = spec.n[a]
+        lo, hi = (0, 0) if spec.periodic[a] or n == 1 else npml[a]
+        inside.append(lo + hi)
+        outside.append(n - lo - hi)
+    (ax, ay, az), (bx, by, bz) = inside, outside
+    one = ax * by * bz + bx * ay * bz + bx * by * az
+    total = spec.cells() - bx * by * bz
+    return one, total - one
+
+
 def config_runs(stream):
     """The other named configurations.  The 3D ones run their whole length
     in FP32 and in FP64 plain (timed with CUDA events on the bench stream
@@ -196,7 +212,8 @@ def config_runs(stream):
     step's ideal bytes (each field read and written once, plus the material
     id: 12w+1 per cell in 3D, 4w+1 in 1D) over the measured HBM peak; in 3D
     also the step's algorithmic bytes with the split-PML shell's stored parts
-    (12w more per shell cell in FP32, 24w in FP64) over the same peak."""
+    (in FP32 8w more per cell inside one axis's PML and 12w inside more, 24w
+    in FP64) over the same peak."""
     import torch
     from fdtd_gpu import abi, problems
     from fdtd_gpu.job import Job
@@ -220,10 +237,15 @@ def config_runs(stream):
              "step_bytes_frac_of_hbm": mc * 1e6 * per_cell(w) / (peak * 1e9)}
         if shell:
             # the split-PML shell (cells outside the interior box) also reads
-            # and writes its stored parts: 6 per cell in FP32, 12 in FP64
+            # and writes its stored parts: in FP64 12 per cell; in FP32 one per
+            # component that has a PML axis among its two curl axes, so 4 for a
+            # cell inside one axis's PML and 6 inside two or three
             nshell = spec.cells() - J.kernel_cells(abi.KERNEL_E)
-            alg = spec.cells() * per_cell(w) + nshell * (12 if w == 4 else 24) * w
+            n1, n2 = pml_cells_by_axes(spec)
+            extra = (4 * n1 + 6 * n2) * 2 * w if w == 4 else (n1 + n2) * 24 * w
+            alg = spec.cells() * per_cell(w) + extra
             r["shell_cells"] = nshell
+            r["pml_cells_one_axis"], r["pml_cells_more_axes"] = n1, n2
             r["step_alg_bytes"] = alg
             r["step_alg_bytes_frac_of_hbm"] = alg / (ms / k / 1e3) / (peak * 1e9)
         if keep:

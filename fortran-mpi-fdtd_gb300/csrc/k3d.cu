@@ -155,13 +155,24 @@ __device__ __forceinline__ void edge_e3(const StepParams<T> &p, int unit, int n)
   vld<T, V>(p.ez + c, ez);
   vld_ids<V>(p.mat + c, id);
   const int rf = __ldg(p.rowflag + (long long)k * p.ny + j);
-  // split parts Exy Eyz Ezx (and, in FP64, Exz Eyx Ezy) and the profiles
-  T s0[V], s1[V], s2[V], s6[V], s7[V], s8[V], f1x[V], f2x[V];
+  // split parts Exy Eyz Ezx (and, in FP64, Exz Eyx Ezy) and the profiles.
+  // In FP32 a component is split only where one of its two curl axes is a
+  // PML axis of the cell; with neither (Ez in a z-slab, say) both parts
+  // would take f1 = 1 and the same f2, so the component takes the plain
+  // update E += f2 * curl, and its stored part is neither read nor written.
+  // FP64 keeps the split everywhere in the shell, as the reference does.
+  bool anyx = false;
+#pragma unroll
+  for (int q = 0; q < V; ++q) anyx |= i0 + q < p.slo[0] || i0 + q > p.shi[0];
+  const bool iny = j < p.slo[1] || j > p.shi[1], inz = k < p.slo[2] || k > p.shi[2];
+  const bool need0 = kTwoParts<T> || iny || inz, need1 = kTwoParts<T> || inz || anyx,
+             need2 = kTwoParts<T> || anyx || iny;
+  T s0[V] = {}, s1[V] = {}, s2[V] = {}, s6[V], s7[V], s8[V], f1x[V], f2x[V];
   T f1y = T(0), f2y = T(0), f1z = T(0), f2z = T(0);
   if (pml) {
-    vld<T, V>(p.sp[0] + c, s0);
-    vld<T, V>(p.sp[1] + c, s1);
-    vld<T, V>(p.sp[2] + c, s2);
+    if (need0) vld<T, V>(p.sp[0] + c, s0);
+    if (need1) vld<T, V>(p.sp[1] + c, s1);
+    if (need2) vld<T, V>(p.sp[2] + c, s2);
     if (kTwoParts<T>) {
       vld<T, V>(p.sp[6] + c, s6);
       vld<T, V>(p.sp[7] + c, s7);
@@ -181,6 +192,7 @@ __device__ __forceinline__ void edge_e3(const StepParams<T> &p, int unit, int n)
     const T curlhyx = hy[q] - (q ? hy[q - 1] : hyl), curlhxy = -hx[q] + hxd[q];
     if (split && (shell_yz || i < p.slo[0] || i > p.shi[0])) {
       if (do_pml) {  // 3D/BERpmly_mod.f90:117-159 on every face
+        const bool inx = i < p.slo[0] || i > p.shi[0];
         const T exz = kTwoParts<T> ? s6[q] : ex[q] - s0[q];
         const T eyx = kTwoParts<T> ? s7[q] : ey[q] - s1[q];
         const T ezy = kTwoParts<T> ? s8[q] : ez[q] - s2[q];
@@ -192,7 +204,12 @@ __device__ __forceinline__ void edge_e3(const StepParams<T> &p, int unit, int n)
         const T nezy = f1y * ezy + f2y * curlhxy;
         s0[q] = nexy; s1[q] = neyz; s2[q] = nezx;
         s6[q] = nexz; s7[q] = neyx; s8[q] = nezy;
-        ex[q] = nexy + nexz; ey[q] = neyz + neyx; ez[q] = nezx + nezy;
+        if (kTwoParts<T> || iny || inz) ex[q] = nexy + nexz;
+        else ex[q] = ex[q] + f2y * (curlhzy + curlhyz);
+        if (kTwoParts<T> || inz || inx) ey[q] = neyz + neyx;
+        else ey[q] = ey[q] + f2z * (curlhxz + curlhzx);
+        if (kTwoParts<T> || inx || iny) ez[q] = nezx + nezy;
+        else ez[q] = ez[q] + f2x[q] * (curlhyx + curlhxy);
         wrote = true;
       }
     } else if (do_main && main_yz && i >= p.mlo[0] && i <= p.mhi[0]) {
@@ -216,9 +233,9 @@ __device__ __forceinline__ void edge_e3(const StepParams<T> &p, int unit, int n)
     st_guard3<T, V>(p.ezo + c, ez, id);
   }
   if (pml) {
-    vst<T, V>(p.sp[0] + c, s0);
-    vst<T, V>(p.sp[1] + c, s1);
-    vst<T, V>(p.sp[2] + c, s2);
+    if (need0) vst<T, V>(p.sp[0] + c, s0);
+    if (need1) vst<T, V>(p.sp[1] + c, s1);
+    if (need2) vst<T, V>(p.sp[2] + c, s2);
     if (kTwoParts<T>) {
       vst<T, V>(p.sp[6] + c, s6);
       vst<T, V>(p.sp[7] + c, s7);
@@ -249,13 +266,20 @@ __device__ __forceinline__ void edge_h3(const StepParams<T> &p, int unit) {
   vld<T, V>(p.hx + c, hx);
   vld<T, V>(p.hy + c, hy);
   vld<T, V>(p.hz + c, hz);
-  // split parts Hxy Hyz Hzx (and, in FP64, Hxz Hyx Hzy) and the profiles
-  T s3[V], s4[V], s5[V], s9[V], s10[V], s11[V], g1x[V], g2x[V];
+  // split parts Hxy Hyz Hzx (and, in FP64, Hxz Hyx Hzy) and the profiles;
+  // in FP32 only the components that need a split (as in edge_e3)
+  bool anyx = false;
+#pragma unroll
+  for (int q = 0; q < V; ++q) anyx |= i0 + q < p.slo[0] || i0 + q > p.shi[0];
+  const bool iny = j < p.slo[1] || j > p.shi[1], inz = k < p.slo[2] || k > p.shi[2];
+  const bool need3 = kTwoParts<T> || iny || inz, need4 = kTwoParts<T> || inz || anyx,
+             need5 = kTwoParts<T> || anyx || iny;
+  T s3[V] = {}, s4[V] = {}, s5[V] = {}, s9[V], s10[V], s11[V], g1x[V], g2x[V];
   T g1y = T(0), g2y = T(0), g1z = T(0), g2z = T(0);
   if (pml) {
-    vld<T, V>(p.sp[3] + c, s3);
-    vld<T, V>(p.sp[4] + c, s4);
-    vld<T, V>(p.sp[5] + c, s5);
+    if (need3) vld<T, V>(p.sp[3] + c, s3);
+    if (need4) vld<T, V>(p.sp[4] + c, s4);
+    if (need5) vld<T, V>(p.sp[5] + c, s5);
     if (kTwoParts<T>) {
       vld<T, V>(p.sp[9] + c, s9);
       vld<T, V>(p.sp[10] + c, s10);
@@ -287,7 +311,13 @@ __device__ __forceinline__ void edge_h3(const StepParams<T> &p, int unit) {
         const T nhzy = g1y * hzy + g2y * curlexy;
         s3[q] = nhxy; s4[q] = nhyz; s5[q] = nhzx;
         s9[q] = nhxz; s10[q] = nhyx; s11[q] = nhzy;
-        hx[q] = nhxy + nhxz; hy[q] = nhyz + nhyx; hz[q] = nhzx + nhzy;
+        const bool inx = i < p.slo[0] || i > p.shi[0];
+        if (kTwoParts<T> || iny || inz) hx[q] = nhxy + nhxz;
+        else hx[q] = hx[q] + g2y * (curleyz + curlezy);
+        if (kTwoParts<T> || inz || inx) hy[q] = nhyz + nhyx;
+        else hy[q] = hy[q] + g2z * (curlezx + curlexz);
+        if (kTwoParts<T> || inx || iny) hz[q] = nhzx + nhzy;
+        else hz[q] = hz[q] + g2x[q] * (curlexy + curleyx);
         wrote = true;
       }
     } else if (do_main && main_yz && i >= p.mlo[0] && i <= p.mhi[0]) {
@@ -303,9 +333,9 @@ __device__ __forceinline__ void edge_h3(const StepParams<T> &p, int unit) {
     vst<T, V>(p.hzo + c, hz);
   }
   if (pml) {
-    vst<T, V>(p.sp[3] + c, s3);
-    vst<T, V>(p.sp[4] + c, s4);
-    vst<T, V>(p.sp[5] + c, s5);
+    if (need3) vst<T, V>(p.sp[3] + c, s3);
+    if (need4) vst<T, V>(p.sp[4] + c, s4);
+    if (need5) vst<T, V>(p.sp[5] + c, s5);
     if (kTwoParts<T>) {
       vst<T, V>(p.sp[9] + c, s9);
       vst<T, V>(p.sp[10] + c, s10);
@@ -454,7 +484,7 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
 // dispersive cells.  It may be launched early, off the previous core kernel's
 // programmatic event, and then waits for that kernel here first.
 template <typename T, int V>
-__global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepParams<T> p) {
+__global__ void __launch_bounds__(256, 3) e3d_kernel(const __grid_constant__ StepParams<T> p) {
   pdl_wait();
   const int n = step_n(p);
   int b = blockIdx.x;
@@ -476,7 +506,7 @@ __global__ void __launch_bounds__(256) e3d_kernel(const __grid_constant__ StepPa
 }
 
 template <typename T, int V>
-__global__ void __launch_bounds__(256) h3d_kernel(const __grid_constant__ StepParams<T> p) {
+__global__ void __launch_bounds__(256, 3) h3d_kernel(const __grid_constant__ StepParams<T> p) {
   pdl_wait();
   int b = blockIdx.x;
   if (b < p.ntile_blocks) {
