@@ -460,6 +460,24 @@ def test_fused_2d_step_across_calls_and_procedures(gpu):
     np.testing.assert_array_equal(p, ref.get_probe(0))
 
 
+def test_fused_2d_without_dispersive_cells_equals_split(gpu):
+    """The fused 2D step kernel on a grid with no dispersive cells: no
+    dispersive-cell kernel runs before it, so the kernel waits for the
+    previous step itself.  Against the split path, bit for bit, over three
+    graph rings and an eager tail."""
+    spec, _ = problems.config_2d_tmz(precision=abi.F32, n=256, ncyl=0, nfreq=8, npml=16)
+    a, b = gpu.Job(spec, tile=4), gpu.Job(spec, tile=2)
+    a.step(1, 101)
+    b.step(1, 101)
+    for c in (abi.EZ, abi.HX, abi.HY):
+        x = a.get_field(c)
+        assert np.any(x), f"component {c} is zero"
+        np.testing.assert_array_equal(x, b.get_field(c), err_msg=f"component {c}")
+    for q in range(len(spec.monitors)):
+        for x, y in zip(a.get_monitor(q), b.get_monitor(q)):
+            np.testing.assert_array_equal(x, y)
+
+
 def test_fused_2d_large_grid_equals_split(gpu):
     """The fused 2D step kernel where the tuner picks it: a 4096^2 grid of
     the bench's workload (34 strips of 124 cells, the last partly filled, 512 marches of 8 rows per
