@@ -403,7 +403,7 @@ __device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
   const int cell = p.ade_cell[s];
   const int nx = p.nx, ny = p.ny;
   const int i = cell % nx, j = cell / nx;
-  const AdeCoef<T> a = ade_coef(p, p.ade_mat[s]);
+  const AdeCoef<T> &a = ade_coef(p, p.ade_mat[s]);
   const AdeCoef<T> *am = p.ac + (p.ade_mat[s] - kAdeId);
   if (L == 3) {
     T curl = (p.hy[cell] - ld_x(p.hy, i - 1, j, nx, p.per[0])) +

@@ -466,7 +466,7 @@ __device__ __forceinline__ void ade_e3(const StepParams<T> &p, int s, int n) {
   const int nx = p.nx, ny = p.ny;
   const int i = cell % nx, j = (cell / nx) % ny, k = cell / (nx * ny);
   F3<T> f(p);
-  const AdeCoef<T> a = ade_coef(p, p.ade_mat[s]);
+  const AdeCoef<T> &a = ade_coef(p, p.ade_mat[s]);
   const AdeCoef<T> *am = p.ac + (p.ade_mat[s] - kAdeId);
   const T hxc = p.hx[cell], hyc = p.hy[cell], hzc = p.hz[cell];
   const T curlhzy = hzc - f.ly(p.hz, i, j - 1, k), curlhyz = -hyc + f.lz(p.hy, i, j, k - 1);

@@ -418,7 +418,10 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
 
 // coefficients of a dispersive material id (>= kAdeId)
 template <typename T>
-__device__ __forceinline__ AdeCoef<T> ade_coef(const StepParams<T> &p, int id) {
+__device__ __forceinline__ const AdeCoef<T> &ade_coef(const StepParams<T> &p, int id) {
+  // a reference, not a copy: a copy would load every field of both candidate
+  // sets (the kernel parameter's and the table's) before the kind is known;
+  // read through the reference, each update loads only the fields it uses
   const int ai = id - kAdeId;
   return ai < kAdeParam ? p.acp[ai] : p.ac[ai];
 }
