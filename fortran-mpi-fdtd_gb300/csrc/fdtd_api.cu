@@ -165,6 +165,7 @@ struct fdtd_job {
   int nade = 0, ade_stride = 0, ade_nf = 0, id0 = 0;
   std::vector<double> mca_host;
   std::vector<char> ac_host;  // AdeCoef<T> table, host copy
+  int ade_kind = -1;          // the device kind of every dispersive material, or -1 (mixed)
   int *d_ade_cell = nullptr;
   uint8_t *d_ade_mat = nullptr;
   void *d_ade_state = nullptr;
@@ -951,6 +952,9 @@ int commit_impl(fdtd_job *J) {
   if ((rc = alloc_dev(J, &J->d_ac, sizeof(AdeCoef<T>) * std::max<size_t>(1, ac.size())))) return rc;
   if (!ac.empty()) CK(cudaMemcpy(J->d_ac, ac.data(), sizeof(AdeCoef<T>) * ac.size(), cudaMemcpyHostToDevice));
   J->ac_host.assign((const char *)ac.data(), (const char *)ac.data() + sizeof(AdeCoef<T>) * ac.size());
+  J->ade_kind = ac.empty() ? -1 : ac[0].kind;  // the device update all the dispersive materials share, or -1
+  for (const AdeCoef<T> &a : ac)
+    if (a.kind != J->ade_kind) J->ade_kind = -1;
   // ---- ADE slots (dispersive cells) ----
   std::vector<int> ade_cell;
   std::vector<uint8_t> ade_mat;
@@ -1367,8 +1371,9 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   p.ade_cell = J->d_ade_cell;
   p.ade_mat = J->d_ade_mat;
   p.ac = (const AdeCoef<T> *)J->d_ac;
-  for (size_t q = 0; q < J->ac_host.size() && q < (size_t)kAdeParam; ++q)
+  for (size_t q = 0; q < J->ac_host.size() / sizeof(AdeCoef<T>) && q < (size_t)kAdeParam; ++q)
     memcpy(&p.acp[q], J->ac_host.data() + q * sizeof(AdeCoef<T>), sizeof(AdeCoef<T>));
+  p.ade_kind = J->ade_kind;
   p.ade_state = (T *)J->d_ade_state;
   p.ade_stride = J->ade_stride;
   p.pml_mode = J->has_pml ? J->pml.mode : 0;

@@ -160,6 +160,7 @@ struct StepParams {
   const uint8_t *ade_mat;  // material id
   const AdeCoef<T> *ac;
   AdeCoef<T> acp[4];       // the first dispersive materials' coefficients
+  int ade_kind;            // the device kind (MatKind) of every dispersive material, or -1
   T *ade_state;            // [field][comp][slot], see AdeState
   int ade_stride;          // = padded nade
   // sources: boxes, and amp*g(t) of every step in a device table

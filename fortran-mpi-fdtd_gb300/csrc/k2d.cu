@@ -398,7 +398,9 @@ struct K2 {
 };
 
 // ---- dispersive cells ------------------------------------------------------
-template <typename T, int L>
+// KIND: the kind of every dispersive material of the job when there is one
+// (MatKind), else -1
+template <typename T, int L, int KIND = -1>
 __device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
   const int cell = p.ade_cell[s];
   const int nx = p.nx, ny = p.ny;
@@ -409,15 +411,15 @@ __device__ __forceinline__ void ade_e2(const StepParams<T> &p, int s, int n) {
     T curl = (p.hy[cell] - ld_x(p.hy, i - 1, j, nx, p.per[0])) +
              (-p.hx[cell] + ld_y(p.hx, i, j - 1, nx, ny, p.per[1]));
     T inc = p.ku * curl + src_sum<T>(p, n, 2, i, j, 0);
-    p.ezo[cell] = ade_update<T>(p, a, am, s, 0, inc, p.ez[cell]);
+    p.ezo[cell] = ade_update<T, KIND>(p, a, am, s, 0, inc, p.ez[cell]);
   } else {
     T hzc = p.hz[cell];
     T curlhx = hzc - ld_x(p.hz, i - 1, j, nx, p.per[0]);
     T curlhy = hzc - ld_y(p.hz, i, j - 1, nx, ny, p.per[1]);
     T incx = p.ku * curlhy + src_sum<T>(p, n, 0, i, j, 0);
     T incy = -(p.ku * curlhx) + src_sum<T>(p, n, 1, i, j, 0);
-    p.exo[cell] = ade_update<T>(p, a, am, s, 0, incx, p.ex[cell]);
-    p.eyo[cell] = ade_update<T>(p, a, am, s, 1, incy, p.ey[cell]);
+    p.exo[cell] = ade_update<T, KIND>(p, a, am, s, 0, incx, p.ex[cell]);
+    p.eyo[cell] = ade_update<T, KIND>(p, a, am, s, 1, incy, p.ey[cell]);
   }
 }
 
@@ -582,12 +584,25 @@ __global__ void __launch_bounds__(256) h2d_edge(const __grid_constant__ StepPara
 // The fused 2D step kernel follows this one with a programmatic dependency
 // and waits for it only where it meets a dispersive cell: it may start once
 // every block here has passed its own wait (and with it, the previous step).
-template <typename T, int L>
+template <typename T, int L, int KIND>
 __global__ void __launch_bounds__(256) e2d_ade(const __grid_constant__ StepParams<T> p) {
   pdl_wait();
   pdl_release();
   const int s = blockIdx.x * 256 + threadIdx.x;
-  if (s < p.nade) ade_e2<T, L>(p, s, step_n(p));
+  if (s < p.nade) ade_e2<T, L, KIND>(p, s, step_n(p));
+}
+
+// the dispersive-cell kernel for the job's kinds: the gold update's own
+// instance when every dispersive material runs it
+template <typename T, int L>
+void launch_ade(const StepParams<T> &p, int blocks, cudaStream_t s, bool pdl) {
+  if (p.ade_kind == MK_GOLD) {
+    if (pdl) launch_pdl(e2d_ade<T, L, MK_GOLD>, blocks, 256, s, p);
+    else launch_side(e2d_ade<T, L, MK_GOLD>, blocks, 256, s, p);
+  } else {
+    if (pdl) launch_pdl(e2d_ade<T, L, -1>, blocks, 256, s, p);
+    else launch_side(e2d_ade<T, L, -1>, blocks, 256, s, p);
+  }
 }
 
 // V: cells per unit along x; 4 (float) / 2 (double) when the row length
@@ -601,7 +616,7 @@ int launch_e2d_v(const StepParams<T> &p, int part, cudaStream_t s, cudaEvent_t e
   const int blocks = (units + 255) / 256;
   if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, true, s, ev);
   else if (part == K2D_EDGE) launch_side(e2d_edge<T, L, V>, blocks, 256, s, p);
-  else launch_side(e2d_ade<T, L>, blocks, 256, s, p);
+  else launch_ade<T, L>(p, blocks, s, false);
   return 1;
 }
 template <typename T, int L, int V>
@@ -628,8 +643,8 @@ template <typename T>
 int launch_e2d_ade_pdl(const StepParams<T> &p, void *stream) {
   if (p.nade <= 0) return 0;
   cudaStream_t s = (cudaStream_t)stream;
-  if (p.layout == 3) launch_pdl(e2d_ade<T, 3>, (p.nade + 255) / 256, 256, s, p);
-  else launch_pdl(e2d_ade<T, 2>, (p.nade + 255) / 256, 256, s, p);
+  if (p.layout == 3) launch_ade<T, 3>(p, (p.nade + 255) / 256, s, true);
+  else launch_ade<T, 2>(p, (p.nade + 255) / 256, s, true);
   return 1;
 }
 

@@ -242,14 +242,17 @@ __device__ __forceinline__ bool sample_row(const StepParams<T> &p, int j, int k)
 // component is vacuum, and the Kerr term adds lk Q E to pole 0's drive with
 //   g += -lqv g + lqs ((escale E)^2 - Q);  Q += g.
 // The components of a cell are updated in order x, y, z by one thread.
-template <typename T>
+// KIND >= 0: every cell of the launch has that kind, known at compile time,
+// so the state loads of its update need not wait for the kind's test.
+template <typename T, int KIND = -1>
 __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int comp, const AdeCoef<T> &a,
                                                const AdeCoef<T> *am, T inc, T eold) {
+  const int kind = KIND >= 0 ? KIND : a.kind;
   T *q_ = st + (0 * 3 + comp) * (long long)stride + slot;
   T *s_ = st + (1 * 3 + comp) * (long long)stride + slot;
   T *f2 = st + (2 * 3 + comp) * (long long)stride + slot;
   T *f3 = st + (3 * 3 + comp) * (long long)stride + slot;
-  if (a.kind == MK_LORENTZ) {
+  if (kind == MK_LORENTZ) {
     if (comp == a.normal) return eold + inc;  // sheet: the normal component is vacuum
     T pl[kMaxPoles], vl[kMaxPoles];
     T sv = T(0);
@@ -294,7 +297,7 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
   }
   T Q = *q_ + inc;
   T S = *s_;
-  if (a.kind == MK_GOLD) {
+  if (kind == MK_GOLD) {
     T *f4 = st + (4 * 3 + comp) * (long long)stride + slot;
     T *f5 = st + (5 * 3 + comp) * (long long)stride + slot;
     const T g1r = *f2, g1i = *f3, g2r = *f4, g2i = *f5;
@@ -312,7 +315,7 @@ __device__ __forceinline__ T ade_update_state(T *st, int stride, int slot, int c
     *f5 = p2i + a.gci[1] * e;
     return e;
   }
-  if (a.kind == MK_GRAPHENE_CP) {
+  if (kind == MK_GRAPHENE_CP) {
     // the reference's Graphene: Re[(Q + ha S + sum_p gb_p g_p) / (ga + S_R)].
     // Its coefficients are read through am, not the caller's copy a: a copy
     // of every kind's fields would stay in registers across the components.
@@ -427,10 +430,10 @@ __device__ __forceinline__ const AdeCoef<T> &ade_coef(const StepParams<T> &p, in
 }
 
 // a: the coefficients by value; am: the same set in the job's table
-template <typename T>
+template <typename T, int KIND = -1>
 __device__ __forceinline__ T ade_update(const StepParams<T> &p, const AdeCoef<T> &a, const AdeCoef<T> *am, int slot,
                                          int comp, T inc, T eold) {
-  return ade_update_state<T>(p.ade_state, p.ade_stride, slot, comp, a, am, inc, eold);
+  return ade_update_state<T, KIND>(p.ade_state, p.ade_stride, slot, comp, a, am, inc, eold);
 }
 
 // vals[c] for a component number known only at run time, by constant-index
