@@ -1598,7 +1598,7 @@ int launch_part(const fdtd_job *J, const StepParams<T> &p, int part, bool e_half
 template <typename T>
 int run_parts(fdtd_job *J, const StepParams<T> &p, const bool (&want)[3], bool e_half, bool graph) {
   static const int kind[3] = {-1, FDTD_KERNEL_EDGE, FDTD_KERNEL_ADE};
-  const int general = J->dim == 2 ? p.nedge : p.ntile_blocks + p.nslab_blocks + (e_half ? p.nade_blocks : 0);
+  const int general = J->dim == 2 ? p.nedge + (e_half ? p.nade : 0) : p.ntile_blocks + p.nslab_blocks + (e_half ? p.nade_blocks : 0);
   const int units[3] = {p.ncore, general, J->dim == 2 && e_half ? p.nade : 0};
   int use[3], nuse = 0;
   for (int q = 0; q < 3; ++q)
@@ -1759,8 +1759,7 @@ int half_e(fdtd_job *J, int n, int roles, int slot = 0, bool graph = false) {
   p.n = n;
   p.slot = slot;
   p.d_base = graph ? J->d_base : nullptr;
-  const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML | (J->dim == 3 ? ROLE_ADE : 0))) != 0,
-                         J->dim == 2 && (roles & ROLE_ADE) != 0};
+  const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML | ROLE_ADE)) != 0, false};
   int rc = run_parts<T>(J, p, parts, true, graph);
   if (!rc && J->has_tfbox && (roles & ROLE_MAIN)) rc = tfsf_part<T>(J, p, true, graph);
   return rc;

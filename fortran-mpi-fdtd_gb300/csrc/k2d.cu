@@ -15,6 +15,8 @@
 //          (2D/BERpmly_HzExEy_mod.f90).
 //   ADE  : one thread per dispersive cell (gold Drude+2CP,
 //          2D/gold_mod.f90:47-75); core and edge threads never store E there.
+//          Its blocks follow the edge units' in the E edge launch
+//          (e2d_edge_ade); the fused 2D step launches them alone (e2d_ade).
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.h"
@@ -605,16 +607,37 @@ void launch_ade(const StepParams<T> &p, int blocks, cudaStream_t s, bool pdl) {
   }
 }
 
+// The E half's side kernel when the job has dispersive cells: the edge
+// units' blocks, then the dispersive cells' blocks, in one launch beside the
+// core kernel (one branch of the step's graph instead of two)
+template <typename T, int L, int V, int KIND>
+__global__ void __launch_bounds__(256) e2d_edge_ade(const __grid_constant__ StepParams<T> p) {
+  pdl_wait();
+  const int eb = (p.nedge + 255) / 256;
+  if ((int)blockIdx.x < eb) {
+    const int t = blockIdx.x * 256 + threadIdx.x;
+    if (t < p.nedge && (p.roles & (ROLE_MAIN | ROLE_PML))) K2<T, L, V>::unit_e(p, __ldg(p.edge_units + t), step_n(p));
+    return;
+  }
+  const int s = ((int)blockIdx.x - eb) * 256 + threadIdx.x;
+  if (s < p.nade && (p.roles & ROLE_ADE)) ade_e2<T, L, KIND>(p, s, step_n(p));
+}
+
 // V: cells per unit along x; 4 (float) / 2 (double) when the row length
 // allows aligned vector access, else 1.  Returns the kernels launched (0/1).
 // `ev`: the core kernel's programmatic event (see launch_pdl), or null; side
 // kernels launch with the device's top priority
 template <typename T, int L, int V>
 int launch_e2d_v(const StepParams<T> &p, int part, cudaStream_t s, cudaEvent_t ev) {
-  const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge : p.nade;
+  const int units = part == K2D_CORE ? p.ncore : part == K2D_EDGE ? p.nedge + p.nade : p.nade;
   if (units <= 0) return 0;
   const int blocks = (units + 255) / 256;
   if (part == K2D_CORE) launch_core2_tiled<T, L, V>(p, true, s, ev);
+  else if (part == K2D_EDGE && p.nade > 0) {
+    const int b2 = (p.nedge + 255) / 256 + (p.nade + 255) / 256;
+    if (p.ade_kind == MK_GOLD) launch_side(e2d_edge_ade<T, L, V, MK_GOLD>, b2, 256, s, p);
+    else launch_side(e2d_edge_ade<T, L, V, -1>, b2, 256, s, p);
+  }
   else if (part == K2D_EDGE) launch_side(e2d_edge<T, L, V>, blocks, 256, s, p);
   else launch_ade<T, L>(p, blocks, s, false);
   return 1;

@@ -122,13 +122,15 @@ __global__ void __launch_bounds__(kFThreads, 3) step3d_fused(const __grid_consta
   load_e(kz0);
   for (int k = kz0; ok && k <= kz1; ++k) {
     const int u = k - kz0 + 1;  // load number of plane k
-    // the next plane goes into the stage the plane k - 2 held: every thread
-    // finished with it before the barrier that ended the last round
-    if (threadIdx.x == 0 && u + 1 < nload) issue(u + 1);
-    if (u + 1 < nload) issued = u + 2;
     ok = __syncthreads_and(mbar_wait(bar0 + 8 * (u % 3), (unsigned)(u / 3) & 1u, p.wait_limit));
     if (!ok) break;
     waited = u + 1;
+    // the next plane goes into the stage the plane k - 2 held, which the last
+    // round read: every thread has passed the barrier above, so every thread
+    // is done with it (and with the E rows the last round read, which this
+    // round's rows of the other parity overwrite next round)
+    if (threadIdx.x == 0 && u + 1 < nload) issue(u + 1);
+    if (u + 1 < nload) issued = u + 2;
     const float *Hx = gbase + (u % 3) * kFStage, *Hy = Hx + kFHx, *Hz = Hy + kFHy;
     const float *Hxp = gbase + ((u + 2) % 3) * kFStage, *Hyp = Hxp + kFHx, *Hzp = Hyp + kFHy;
     // ---- E^{n+1} of plane k (e3d_core's arithmetic) ----
@@ -223,7 +225,6 @@ __global__ void __launch_bounds__(kFThreads, 3) step3d_fused(const __grid_consta
       for (int q = 0; q < 4; ++q) ep[c][q] = ne[c][q];
     core_prev = core;
     if (k + 1 <= kz1) load_e(k + 1);
-    __syncthreads();
   }
   if (!ok) {
     // a wait gave up: report it, and let the copies already issued land

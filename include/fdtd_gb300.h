@@ -439,7 +439,9 @@ int fdtd_estimate_bytes(const fdtd_job *job, uint64_t *bytes);
  * (core) kernels; FDTD_KERNEL_EDGE: the 2D kernels for PML cells, the edges
  * of the main range and rows with sources, monitors or reference slabs (in
  * 3D with the fused step kernel: the general E and H kernels);
- * FDTD_KERNEL_ADE: the 2D dispersive-cell kernel; FDTD_KERNEL_STEP: the
+ * FDTD_KERNEL_ADE: the 2D dispersive-cell kernel of the fused step (the
+ * split 2D step appends the dispersive cells' blocks to its E edge kernel,
+ * timed as FDTD_KERNEL_EDGE); FDTD_KERNEL_STEP: the
  * fused step kernels (3D: E and H of the core box in one launch; 2D: E and
  * H of the whole grid, dispersive cells aside, in one launch). */
 enum { FDTD_KERNEL_E = 0, FDTD_KERNEL_H = 1, FDTD_KERNEL_DFT = 2, FDTD_KERNEL_LINE1D = 3,
