@@ -184,6 +184,15 @@ struct fdtd_job {
   void *d_stage = nullptr;
   long long stage_cap_rows = 0;
   int stage_fill = 0, stage_n0 = 1;
+  // 2D/3D: the stage buffer holds two rings.  A replayed ring writes one half
+  // while its graph folds the ring before it, from the other half, beside its
+  // first steps; the last ring's fold runs when the replays end.
+  int stage_half = 0;        // the half the current ring writes
+  bool fold_pending = false; // a replayed ring whose fold has not run yet
+  int pending_half = 0, pending_n0 = 0;
+  int *d_half = nullptr, *d_gate = nullptr;  // the ring's half and the fold's gate, on the device
+  cudaStream_t fold_stream = nullptr;
+  cudaEvent_t ev_ffork = nullptr, ev_fjoin = nullptr;
   double *d_omega = nullptr, *d_acc_re = nullptr, *d_acc_im = nullptr;
   double *d_rot = nullptr;  // per frequency and ring slot: cos, sin of w s dt
   double *d_mean_part = nullptr;   // mean monitors: partial sums per block
@@ -478,6 +487,9 @@ int make_branches(fdtd_job *J) {
     CK(cudaEventCreateWithFlags(&J->ev_prog[q], cudaEventDisableTiming));
   }
   CK(cudaEventCreateWithFlags(&J->ev_fork, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithFlags(&J->fold_stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&J->ev_ffork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&J->ev_fjoin, cudaEventDisableTiming));
   return FDTD_OK;
 }
 
@@ -1202,7 +1214,8 @@ int commit_impl(fdtd_job *J) {
   if ((rc = alloc_state(J, (void **)&J->d_acc_re, (size_t)std::max(1LL, acc) * sizeof(double), 8))) return rc;
   if ((rc = alloc_state(J, (void **)&J->d_acc_im, (size_t)std::max(1LL, acc) * sizeof(double), 8))) return rc;
   J->stage_cap_rows = J->dim == 1 ? 4096 : kStageSteps;
-  if ((rc = alloc_state(J, &J->d_stage, (size_t)std::max(1LL, base) * J->stage_cap_rows * sizeof(T)))) return rc;
+  const long long stage_rows = J->dim == 1 ? J->stage_cap_rows : 2 * kStageSteps;  // 2D/3D: two rings
+  if ((rc = alloc_state(J, &J->d_stage, (size_t)std::max(1LL, base) * stage_rows * sizeof(T)))) return rc;
   int blocks = 0;
   for (auto &m : J->mon_dev)
     blocks += ((m.ncomp * m.ncell + 255) / 256) * ((m.nfreq + 7) / 8);
@@ -1428,7 +1441,8 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
   p.nade_blocks = (J->nade + 255) / 256;
   p.nmon = (int)J->mon_dev.size();
   for (int q = 0; q < p.nmon; ++q) p.mon[q] = J->mon_dev[q];
-  p.stage = (T *)J->d_stage;
+  p.stage = (T *)J->d_stage + (size_t)J->stage_half * kStageSteps * J->stage_row;
+  p.d_half = nullptr;
   p.stage_row = J->stage_row;
   p.mean_part = J->d_mean_part;
   p.mean_ctr = J->d_mean_ctr;
@@ -1443,6 +1457,18 @@ void fill_common(fdtd_job *J, StepParams<T> &p) {
     d.n_last = P.d.n_last;
     d.buf = P.buf;
     d.cap = P.cap;
+  }
+}
+
+// Parameters of a step in a captured ring (graph) or an eager one: in a
+// ring the step number and the stage half are read on the device, so that
+// one graph serves every replay.
+template <typename T>
+void ring_params(fdtd_job *J, StepParams<T> &p, bool graph) {
+  p.d_base = graph ? J->d_base : nullptr;
+  if (graph) {
+    p.stage = (T *)J->d_stage;
+    p.d_half = J->d_half;
   }
 }
 
@@ -1548,6 +1574,37 @@ int ensure_probe_cap(fdtd_job *J, int n_max) {
   return FDTD_OK;
 }
 
+// The job's DFT fold parameters, without the ring's slots
+void fold_params(const fdtd_job *J, DftParams &d) {
+  d = DftParams{};
+  d.nmon = (int)J->mon_dev.size();
+  for (int q = 0; q < d.nmon; ++q) d.mon[q] = J->mon_dev[q];
+  d.omega = J->d_omega;
+  d.rot = (const double2 *)J->d_rot;
+  d.acc_re = J->d_acc_re;
+  d.acc_im = J->d_acc_im;
+  d.dt = J->g.dt;
+  d.stage_row = J->stage_row;
+  d.total_work_blocks = J->dft_blocks;
+}
+
+// The fold of the last replayed ring, which no later replay has run
+template <typename T>
+int flush_fold(fdtd_job *J) {
+  if (!J->fold_pending) return FDTD_OK;
+  J->fold_pending = false;
+  if (J->mon_dev.empty() || J->dft_blocks <= 0) return FDTD_OK;
+  DftParams d;
+  fold_params(J, d);
+  d.nslots = kStageSteps;
+  d.n0 = J->pending_n0;
+  launch_dft<T>(d, (const T *)J->d_stage + (size_t)J->pending_half * kStageSteps * J->stage_row, J->stream);
+  J->launches++;
+  J->prog_prev = -1;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
 template <typename T>
 int dft_fold(fdtd_job *J) {
   if (J->stage_fill == 0) return FDTD_OK;
@@ -1567,7 +1624,8 @@ int dft_fold(fdtd_job *J) {
       d.nslots = std::min(kStageSteps, J->stage_fill - r0);
       d.n0 = J->stage_n0 + r0;
       ev_record(J, FDTD_KERNEL_DFT, true);
-      launch_dft<T>(d, (const T *)J->d_stage + (size_t)r0 * J->stage_row, J->stream);
+      launch_dft<T>(d, (const T *)J->d_stage + ((size_t)J->stage_half * kStageSteps + r0) * J->stage_row,
+                    J->stream);
       ev_record(J, FDTD_KERNEL_DFT, false);
       J->launches++;
     }
@@ -1758,7 +1816,7 @@ int half_e(fdtd_job *J, int n, int roles, int slot = 0, bool graph = false) {
   p.roles = roles;
   p.n = n;
   p.slot = slot;
-  p.d_base = graph ? J->d_base : nullptr;
+  ring_params(J, p, graph);
   const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML | ROLE_ADE)) != 0, false};
   int rc = run_parts<T>(J, p, parts, true, graph);
   if (!rc && J->has_tfbox && (roles & ROLE_MAIN)) rc = tfsf_part<T>(J, p, true, graph);
@@ -1773,7 +1831,7 @@ int half_h(fdtd_job *J, int n, int roles, bool gather, int slot = -1, bool graph
   p.n = n;
   p.gather = gather ? 1 : 0;
   p.slot = slot >= 0 ? slot : J->stage_fill;
-  p.d_base = graph ? J->d_base : nullptr;
+  ring_params(J, p, graph);
   const bool parts[3] = {(roles & ROLE_MAIN) != 0, (roles & (ROLE_MAIN | ROLE_PML)) != 0, false};
   int rc = run_parts<T>(J, p, parts, false, graph);
   if (!rc && J->has_tfbox && (roles & ROLE_MAIN)) rc = tfsf_part<T>(J, p, false, graph);
@@ -1786,7 +1844,7 @@ int sample_sep(fdtd_job *J, int n, int slot = -1, bool graph = false) {
   fill_common<T>(J, p);
   p.n = n;
   p.slot = slot >= 0 ? slot : J->stage_fill;
-  p.d_base = graph ? J->d_base : nullptr;
+  ring_params(J, p, graph);
   J->launches += launch_gather<T>(p, J->stream);
   J->prog_prev = -1;
   CK(cudaGetLastError());
@@ -1824,7 +1882,7 @@ int fused_step2(fdtd_job *J, int n, int slot, bool graph) {
   p.roles = ROLE_MAIN | ROLE_PML | ROLE_ADE;
   p.n = n;
   p.slot = slot;
-  p.d_base = graph ? J->d_base : nullptr;
+  ring_params(J, p, graph);
   p.gather = 1;
   p.pp = 1;
   p.ez = A[2]; p.hx = A[3]; p.hy = A[4];
@@ -1868,7 +1926,7 @@ int fused_step(fdtd_job *J, int n, int slot, bool graph) {
     p.roles = ROLE_MAIN | ROLE_PML | ROLE_ADE;
     p.n = n;
     p.slot = slot;
-    p.d_base = graph ? J->d_base : nullptr;
+    ring_params(J, p, graph);
     p.pp = 1;
     p.ex = A[0]; p.ey = A[1]; p.ez = A[2]; p.hx = A[3]; p.hy = A[4]; p.hz = A[5];
     p.exo = B[0]; p.eyo = B[1]; p.ezo = B[2]; p.hxo = B[3]; p.hyo = B[4]; p.hzo = B[5];
@@ -1888,7 +1946,7 @@ int fused_step(fdtd_job *J, int n, int slot, bool graph) {
     g.hx = g.hxo = B[3]; g.hy = g.hyo = B[4]; g.hz = g.hzo = B[5];
     g.n = n;
     g.slot = slot;
-    g.d_base = graph ? J->d_base : nullptr;
+    ring_params(J, g, graph);
     J->launches += launch_gather<float>(g, J->stream);
     J->pp = to;
     J->prog_prev = -1;
@@ -1926,6 +1984,12 @@ int eager_step(fdtd_job *J, int n) {
 }
 
 __global__ void set_base_kernel(int *base, int v) { *base = v; }
+// a ring's step base, its half of the stage buffer and its fold's gate
+__global__ void set_ring_kernel(int *base, int v, int *half, int h, int *gate, int g) {
+  *base = v;
+  *half = h;
+  *gate = g;
+}
 
 // Capture one ring (kStageSteps steps and the DFT fold of the ring) as a CUDA
 // graph; every replay reads its first step number from d_base.
@@ -1934,11 +1998,34 @@ int ring_graph(fdtd_job *J) {
   int rc;
   if (J->graph_exec) return FDTD_OK;
   if (!J->d_base && (rc = alloc_dev(J, (void **)&J->d_base, sizeof(int)))) return rc;
+  if (!J->d_half && (rc = alloc_dev(J, (void **)&J->d_half, sizeof(int)))) return rc;
+  if (!J->d_gate && (rc = alloc_dev(J, (void **)&J->d_gate, sizeof(int)))) return rc;
   CK(cudaStreamSynchronize(J->stream));
   const long long launches0 = J->launches;
   J->prog_prev = -1;  // events recorded outside the capture cannot be waited on inside it
   CK(cudaStreamBeginCapture(J->stream, cudaStreamCaptureModeThreadLocal));
   int bad = FDTD_OK;
+  // the fold of the ring before this one (the other half of the stage
+  // buffer), on its own branch beside this ring's steps; its gate on the
+  // device is 0 when no ring came before
+  const bool fold = !J->mon_dev.empty() && J->dft_blocks > 0;
+  if (fold) {
+    bad = cudaEventRecord(J->ev_ffork, J->stream) != cudaSuccess ||
+          cudaStreamWaitEvent(J->fold_stream, J->ev_ffork, 0) != cudaSuccess;
+    if (!bad) {
+      DftParams d;
+      fold_params(J, d);
+      d.nslots = kStageSteps;
+      d.d_base = J->d_base;
+      d.d_half = J->d_half;
+      d.gate = J->d_gate;
+      d.prev = 1;
+      launch_dft<T>(d, (const T *)J->d_stage, J->fold_stream);
+      J->launches++;
+      bad = cudaEventRecord(J->ev_fjoin, J->fold_stream) != cudaSuccess;
+    }
+    if (bad) bad = set_err(FDTD_ECUDA, "fold branch of the ring graph");
+  }
   // the fused path alternates the field sets over the ring's even number of
   // steps, so a replay starts and ends with the canonical set
   for (int s = 0; s < kStageSteps && !bad; ++s) {
@@ -1950,22 +2037,8 @@ int ring_graph(fdtd_job *J) {
     if (!bad) bad = half_h<T>(J, 0, ROLE_MAIN | ROLE_PML, J->gather_fused, s, true);
     if (!bad && !J->gather_fused) bad = sample_sep<T>(J, 0, s, true);
   }
-  if (!bad && !J->mon_dev.empty() && J->dft_blocks > 0) {
-    DftParams d{};
-    d.nmon = (int)J->mon_dev.size();
-    for (int q = 0; q < d.nmon; ++q) d.mon[q] = J->mon_dev[q];
-    d.omega = J->d_omega;
-    d.rot = (const double2 *)J->d_rot;
-    d.acc_re = J->d_acc_re;
-    d.acc_im = J->d_acc_im;
-    d.dt = J->g.dt;
-    d.stage_row = J->stage_row;
-    d.total_work_blocks = J->dft_blocks;
-    d.nslots = kStageSteps;
-    d.d_base = J->d_base;
-    launch_dft<T>(d, (const T *)J->d_stage, J->stream);
-    J->launches++;
-  }
+  if (!bad && fold && cudaStreamWaitEvent(J->stream, J->ev_fjoin, 0) != cudaSuccess)
+    bad = set_err(FDTD_ECUDA, "joining the fold branch");
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(J->stream, &g);
   J->prog_prev = -1;
@@ -1983,9 +2056,14 @@ template <typename T>
 int replay_ring(fdtd_job *J, int n0) {
   int rc = ring_graph<T>(J);
   if (rc) return rc;
-  set_base_kernel<<<1, 1, 0, J->stream>>>(J->d_base, n0);
+  set_ring_kernel<<<1, 1, 0, J->stream>>>(J->d_base, n0, J->d_half, J->stage_half, J->d_gate, J->fold_pending ? 1 : 0);
   CK(cudaGetLastError());
   CK(cudaGraphLaunch(J->graph_exec, J->stream));
+  // this ring's fold runs in the next replay's graph, or in flush_fold
+  J->fold_pending = true;
+  J->pending_half = J->stage_half;
+  J->pending_n0 = n0;
+  J->stage_half ^= 1;
   J->prog_prev = -1;
   J->launches += 1 + J->graph_kernels;
   J->stage_n0 = n0 + kStageSteps;
@@ -2128,6 +2206,7 @@ int step_impl(fdtd_job *J, int n_first, int n_steps) {
       if ((rc = replay_ring<T>(J, n))) return rc;
       n += kStageSteps;
     }
+    if ((rc = flush_fold<T>(J))) return rc;
   }
   while (n < end)
     if ((rc = eager_step<T>(J, n++))) return rc;
@@ -2312,7 +2391,8 @@ int pack_capture(fdtd::Pack *P) {
     d.total_work_blocks = J->dft_blocks;
     d.nslots = kStageSteps;
     d.d_base = P->d_n0 + q;
-    launch_dft<T>(d, (const T *)J->d_stage, P->stream);
+    // the job's current half of its stage buffer, where its pack steps stage
+    launch_dft<T>(d, (const T *)J->d_stage + (size_t)J->stage_half * kStageSteps * J->stage_row, P->stream);
     ++kernels;
     bad = cudaGetLastError();
   }
@@ -2494,6 +2574,9 @@ int fdtd_destroy(fdtd_job *J) {
     if (J->ev_prog[q]) cudaEventDestroy(J->ev_prog[q]);
   }
   if (J->ev_fork) cudaEventDestroy(J->ev_fork);
+  if (J->fold_stream) cudaStreamDestroy(J->fold_stream);
+  if (J->ev_ffork) cudaEventDestroy(J->ev_ffork);
+  if (J->ev_fjoin) cudaEventDestroy(J->ev_fjoin);
   if (J->own_stream) cudaStreamDestroy(J->own_stream);
   delete J;
   return FDTD_OK;
@@ -2776,14 +2859,15 @@ int fdtd_debug_fail_alloc(int32_t after) {
 // Layout: CkptHeader, then per state buffer its size (uint64), per probe its
 // rows and components (int32 pairs), then the buffers' bytes in allocation
 // order and the probes' rows.  The unfolded part of the DFT ring is part of
-// the stage buffer, with stage_fill and stage_n0 in the header, so a resumed
-// job folds the same rings as the saved one would have.
+// the stage buffer (both halves), with stage_fill, stage_n0 and the half in
+// use in the header, so a resumed job folds the same rings as the saved one
+// would have.
 struct CkptHeader {
   char magic[8];
   uint32_t version;
   int32_t layout, precision, n[3];
   uint32_t nbuf, nprobe;
-  int32_t stage_fill, stage_n0, last_n, reserved;
+  int32_t stage_fill, stage_n0, last_n, stage_half;  // stage_half: the ring in progress's half of the stage buffer
   uint64_t total;
 };
 constexpr char kCkptMagic[8] = {'F', 'D', 'T', 'D', 'C', 'K', 'P', 'T'};
@@ -2823,6 +2907,7 @@ int fdtd_save_state(fdtd_job *J, void *buf, uint64_t bytes) {
   h.nbuf = (uint32_t)J->state.size();
   h.nprobe = (uint32_t)J->probes.size();
   h.stage_fill = J->stage_fill;
+  h.stage_half = J->stage_half;
   h.stage_n0 = J->stage_n0;
   h.last_n = J->last_n;
   h.total = need;
@@ -2908,6 +2993,8 @@ int fdtd_load_state(fdtd_job *J, const void *buf, uint64_t bytes) {
     o += b;
   }
   J->stage_fill = h.stage_fill;
+  J->stage_half = h.stage_half & 1;
+  J->fold_pending = false;
   J->stage_n0 = h.stage_n0;
   J->last_n = h.last_n;
   J->prog_prev = -1;

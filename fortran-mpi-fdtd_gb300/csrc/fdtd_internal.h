@@ -214,6 +214,9 @@ struct StepParams {
   int n;                   // step number (eager launches)
   const int *d_base;       // graph replays: step number of ring slot 0 on the
                            // device; then n = *d_base + slot
+  const int *d_half;       // graph replays: which half of the two-ring stage
+                           // buffer this ring writes, on the device (null: stage
+                           // already points at the ring's half)
   int vec;                 // cells per thread along x in the 2D tile path
   double *mean_part;       // mean monitors: FP64 partial sums per block
   unsigned *mean_ctr;      // mean monitors: blocks done per component
@@ -310,6 +313,11 @@ struct DftParams {
   int nslots;              // valid slots in this fold (0..kStageSteps)
   int n0;                  // step number of slot 0 (eager launches)
   const int *d_base;       // graph replays: slot-0 step number on the device
+  const int *d_half;       // graph replays: the ring's half of the stage buffer
+                           // on the device (null: stage points at the ring)
+  int prev;                // graph replays: fold the ring before this one (the
+                           // other half, slot 0 at *d_base - kStageSteps)
+  const int *gate;         // graph replays: 0 on the device: nothing to fold
   double dt;
   long long stage_row;
   int total_work_blocks;

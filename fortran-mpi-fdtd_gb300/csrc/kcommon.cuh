@@ -447,6 +447,13 @@ __device__ __forceinline__ T pick6(const T *vals, int c) {
   return r;
 }
 
+// Slot 0 of the stage ring this step's samples go to: a graph replay finds
+// its ring's half of the two-ring stage buffer on the device.
+template <typename T>
+__device__ __forceinline__ T *stage_ring(const StepParams<T> &p) {
+  return p.d_half ? p.stage + (long long)(*p.d_half) * kStageSteps * p.stage_row : p.stage;
+}
+
 // Fused sampling: write the monitored components of cell (i,j,k) into this
 // step's stage row, and probe samples.  vals[c] = value of component c.
 template <typename T>
@@ -456,7 +463,7 @@ __device__ __forceinline__ void gather_cell(const StepParams<T> &p, int n, int i
     if (i < m.lo[0] || i > m.hi[0] || j < m.lo[1] || j > m.hi[1] || k < m.lo[2] || k > m.hi[2]) continue;
     const int wx = m.hi[0] - m.lo[0] + 1, wy = m.hi[1] - m.lo[1] + 1;
     const long long idx = (long long)(i - m.lo[0]) + (long long)wx * ((j - m.lo[1]) + (long long)wy * (k - m.lo[2]));
-    T *row = p.stage + (long long)p.slot * p.stage_row + m.base;
+    T *row = stage_ring(p) + (long long)p.slot * p.stage_row + m.base;
     for (int u = 0; u < m.ncomp; ++u) row[(long long)u * m.ncell + idx] = pick6(vals, m.comps[u]);
   }
   for (int q = 0; q < p.nprobe; ++q) {

@@ -43,9 +43,11 @@ __global__ void __launch_bounds__(kDftThreads) dft_kernel(const __grid_constant_
     b -= sblocks * fchunks;
   }
   if (q >= d.nmon) return;
+  if (d.gate && *d.gate == 0) return;  // a replay with no ring before it to fold
   const Monitor &m = d.mon[q];
   // skip the fold when no slot of it lies in the monitor's step window
-  const int n0 = d.d_base ? *d.d_base : d.n0;
+  const int n0 = d.d_base ? *d.d_base - (d.prev ? kStageSteps : 0) : d.n0;
+  if (d.d_half) stage += (long long)(d.prev ? 1 - *d.d_half : *d.d_half) * kStageSteps * d.stage_row;
   const int nlast = n0 + d.nslots - 1;
   if (nlast < m.n_first || n0 > m.n_last) return;
   const int fc = b / sblocks, sb = b % sblocks;
@@ -139,7 +141,7 @@ __device__ __forceinline__ void gather_cells(const StepParams<T> &p, long long t
       const int k = m.lo[2] + (int)(c / ((long long)wx * wy));
       const long long cell = (long long)i + (long long)p.nx * (j + (long long)p.ny * k);
       const T *f = F[m.comps[u]];
-      p.stage[(long long)p.slot * p.stage_row + m.base + t] = f ? f[cell] : T(0);
+      stage_ring(p)[(long long)p.slot * p.stage_row + m.base + t] = f ? f[cell] : T(0);
       return;
     }
     t -= ns;
@@ -220,7 +222,7 @@ __device__ __forceinline__ void gather_mean(const StepParams<T> &p, int b) {
     __threadfence();
     double tot = 0.0;
     for (int c = 0; c < m.mchunks; ++c) tot += __ldcg(p.mean_part + slot + c);
-    p.stage[(long long)p.slot * p.stage_row + m.base + u] = T(tot / (double)m.boxcells);
+    stage_ring(p)[(long long)p.slot * p.stage_row + m.base + u] = T(tot / (double)m.boxcells);
     p.mean_ctr[slot] = 0u;
   }
 }
