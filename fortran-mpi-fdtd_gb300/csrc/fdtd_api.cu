@@ -1983,8 +1983,7 @@ int eager_step(fdtd_job *J, int n) {
   return after_sample<T>(J, n);
 }
 
-__global__ void set_base_kernel(int *base, int v) { *base = v; }
-// a ring's step base, its half of the stage buffer and its fold's gate
+// a replayed ring's step base, its half of the stage buffer and its fold's gate
 __global__ void set_ring_kernel(int *base, int v, int *half, int h, int *gate, int g) {
   *base = v;
   *half = h;
