@@ -34,6 +34,7 @@
 
 #include "fdtd_gb300.h"
 #include "fdtd_internal.h"
+#include "hostscan.h"
 
 using namespace fdtd;
 
@@ -968,11 +969,15 @@ int commit_impl(fdtd_job *J) {
   for (const AdeCoef<T> &a : ac)
     if (a.kind != J->ade_kind) J->ade_kind = -1;
   // ---- ADE slots (dispersive cells) ----
+  static_assert(kAdeId == 128, "the dispersive ids are the ids with the high bit set");
+  std::vector<long long> disp;  // ids >= kAdeId are exactly the dispersive materials
+  for_high_ids(mat.data(), N, [&](long long c) { disp.push_back(c); });
   std::vector<int> ade_cell;
   std::vector<uint8_t> ade_mat;
-  for (long long c = 0; c < N; ++c) {
+  ade_cell.reserve(disp.size());
+  ade_mat.reserve(disp.size());
+  for (const long long c : disp) {
     const uint8_t id = mat[(size_t)c];
-    if (id < kAdeId) continue;  // ids >= kAdeId are exactly the dispersive materials
     const int i = (int)(c % nx), j = (int)((c / nx) % ny), k = (int)(c / ((long long)nx * ny));
     if (in_shell(i, j, k)) continue;
     if (!(i >= J->g.main_lo[0] && i <= J->g.main_hi[0] && j >= J->g.main_lo[1] && j <= J->g.main_hi[1] &&
@@ -997,15 +1002,9 @@ int commit_impl(fdtd_job *J) {
     return rc;
   {
     // most common constant-dielectric material: its Ku/eps is a kernel parameter
-    // eight interleaved sub-histograms: runs of one id would otherwise chain
-    // every increment on the same counter
-    std::vector<long long> sub(8 * kMaxMat, 0), cnt(kMaxMat, 0);
-    long long c2 = 0;
-    for (; c2 + 8 <= N; c2 += 8)
-      for (int u = 0; u < 8; ++u) sub[u * kMaxMat + mat[(size_t)(c2 + u)]]++;
-    for (; c2 < N; ++c2) sub[mat[(size_t)c2]]++;
-    for (int u = 0; u < 8; ++u)
-      for (int t = 0; t < kMaxMat; ++t) cnt[t] += sub[u * kMaxMat + t];
+    static_assert(kMaxMat == 256, "one byte per material id");
+    long long cnt[256];
+    count_ids(mat.data(), N, cnt);
     int best = 0;
     for (int t = 1; t < kAdeId; ++t) if (cnt[t] > cnt[best]) best = t;
     J->id0 = best;

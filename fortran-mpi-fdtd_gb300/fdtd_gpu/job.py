@@ -241,10 +241,19 @@ class Job:
         a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
         check(lib().fdtd_set_field(self.h, int(comp), a.ctypes.data))
 
-    def get_monitor(self, mid):
+    def get_monitor(self, mid, out=None):
+        """The monitor's running sums (re, im), each [comp][freq][cell].
+        ``out``: an (re, im) pair of contiguous float64 arrays of that size
+        (e.g. views of pinned host memory) to download into, else new arrays."""
         nc, nf, ncell = S.monitor_shape(self.spec.monitors[mid])
-        re = np.empty(nc * nf * ncell)
-        im = np.empty_like(re)
+        if out is None:
+            re = np.empty(nc * nf * ncell)
+            im = np.empty_like(re)
+        else:
+            re, im = out
+            for a in (re, im):
+                if a.dtype != np.float64 or a.size != nc * nf * ncell or not a.flags.c_contiguous:
+                    raise ValueError(f"monitor {mid} needs contiguous float64 arrays of {nc * nf * ncell}")
         check(lib().fdtd_get_monitor(self.h, int(mid), re.ctypes.data, im.ctypes.data))
         return re.reshape(nc, nf, ncell), im.reshape(nc, nf, ncell)
 
